@@ -1,0 +1,206 @@
+/*
+ * pppm_c.h - C ABI of the GB300 (sm_103a) implementation of tatsy-pppm's
+ * probabilistic progressive photon mapping (PPM-APA) pass.
+ *
+ * The reference has no FFI: its interface is C++ methods taking
+ * `const Scene&`, `const Camera&` and `const RenderParameters&`. Every entry
+ * point below names the reference method it replaces (file:line within the
+ * tatsy-pppm project). The C++ host mirror in tatsy-pppm_gb300/host/ keeps
+ * the reference class names on top of these calls.
+ *
+ * Conventions
+ *  - Every function returns an int status: PPPM_OK (0) or a negative
+ *    PPPM_E_* code. Nothing aborts. pppm_last_error() describes the last
+ *    failure of a context.
+ *  - Array arguments may live in host memory or in device memory of the
+ *    context's GPU (detected with CUDA unified addressing). Host arrays are
+ *    staged through buffers owned by the context and are not retained after
+ *    the call returns; a call that touches any host array synchronises its
+ *    stream before returning. A call whose arrays are all on the device is
+ *    enqueued on the context stream and returns without waiting
+ *    (pppm_sync() waits and reports deferred kernel errors).
+ *  - One context per host thread; the context owns all device memory it
+ *    allocates. Calls on one context are not thread safe.
+ *  - Triangles are 9 floats (p0, p1, p2); rays are 6 floats (origin,
+ *    unit direction), vectors are xyz floats unless stated otherwise.
+ */
+#ifndef PPPM_C_H_
+#define PPPM_C_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PPPM_OK 0
+#define PPPM_E_ARG (-1)       /* invalid argument or size */
+#define PPPM_E_CUDA (-2)      /* CUDA runtime error (message in pppm_last_error) */
+#define PPPM_E_STATE (-3)     /* call out of order (no scene, no env, ...) */
+#define PPPM_E_CAPACITY (-4)  /* an output or internal buffer was too small */
+#define PPPM_E_UNDEFINED (-5) /* input whose reference behaviour is undefined */
+#define PPPM_E_TIMEOUT (-6)   /* a bounded device-side loop ran out of iterations */
+
+/* BSDF type bits (bsdf.h:19-26). */
+#define PPPM_BSDF_LAMBERTIAN 0x01
+#define PPPM_BSDF_SPECULAR 0x02
+#define PPPM_BSDF_PHONG 0x04
+#define PPPM_BSDF_REFRACTION 0x08
+#define PPPM_BSDF_BSSRDF 0x10
+
+/* Render modes. */
+#define PPPM_MODE_COMPAT 0    /* the reference's semantics, quirks included */
+#define PPPM_MODE_CANONICAL 1 /* textbook Knaus-Zwicker PPM-APA */
+
+typedef struct pppm_ctx pppm_ctx;
+
+/* One material (BSDF + optional dipole BSSRDF), replaces the factories
+ * LambertianBRDF/SpecularBRDF/PhongBRDF/RefractionBSDF::factory
+ * (brdf.cc:23-150) and DipoleBSSRDF::factory (bssrdf.cc:48-63). 56 bytes. */
+typedef struct {
+    int32_t type;       /* one PPPM_BSDF_* bit (not BSSRDF) */
+    int32_t has_bssrdf; /* 1: BSDF::setBssrdf(DipoleBSSRDF(...)) (bsdf.cc:70-73) */
+    float refl[3];      /* reflectance */
+    float phong_n;      /* Phong exponent */
+    float sigma_a[3];   /* dipole absorption */
+    float sigmap_s[3];  /* dipole reduced scattering */
+    float eta;          /* dipole relative IOR */
+    float scale;        /* dipole distance scale */
+} pppm_material;
+
+/* Pinhole camera, replaces PerspectiveCamera (perspective_camera.cc:11-46).
+ * fov is used as tan(fov*0.5) exactly like the reference (an angle in
+ * radians; the reference's own driver passes 45.0). */
+typedef struct {
+    float eye[3];
+    float dir[3];
+    float up[3];
+    float fov;
+    int32_t width;
+    int32_t height;
+} pppm_camera;
+
+/* Replaces RenderParameters (render_parameters.h:12) plus the constants of
+ * ppm_probabilistic.cc (ALPHA, radius init, bounce limits, OMP streams). */
+typedef struct {
+    int32_t mode;           /* PPPM_MODE_* */
+    int32_t num_streams;    /* RNG streams = OMP_NUM_CORE of the reference run (compat) */
+    int64_t photons;        /* photons emitted per pass (RenderParameters::photons) */
+    int32_t gather_photons; /* RenderParameters::gatherPhotons */
+    int32_t max_bounce_photon; /* tracePhotons bounceLimit (64) */
+    int32_t max_bounce_eye;    /* radiance bounceLimit (64) */
+    uint32_t seed;          /* canonical-mode RNG seed */
+    double gather_radius;   /* RenderParameters::gatherRadius */
+    double alpha;           /* ALPHA (0.7) */
+    double radius_scale;    /* r1 = radius_scale * |bbox diagonal| (0.1 in the reference) */
+    float cell_factor;      /* canonical hash-grid cell size / radius */
+    int32_t reserved;
+} pppm_params;
+
+/* Per-pass statistics written by pppm_render_pass. */
+typedef struct {
+    int64_t photons_traced;  /* emitted photon paths (num_streams * ceil(P/N) in compat) */
+    int64_t photons_stored;  /* photon records deposited (excluding phantoms) */
+    int64_t phantom_photons; /* compat: default Photon() slots entering the map */
+    int64_t photon_rays;     /* photon ray segments traced */
+    int64_t eye_rays;        /* eye ray segments traced */
+    int64_t gather_queries;  /* Lambertian hit points gathered */
+    double radius;           /* global radius used in this pass */
+    double ms_photon;        /* device time of the photon stage (ms) */
+    double ms_grid;          /* hash-grid build (ms) */
+    double ms_eye;           /* eye paths (ms) */
+    double ms_gather;        /* gather (ms) */
+} pppm_pass_stats;
+
+/* ------------------------------------------------------------- lifetime */
+/* device: CUDA ordinal. */
+int pppm_create(int device, pppm_ctx** out);
+int pppm_destroy(pppm_ctx* ctx);
+const char* pppm_last_error(const pppm_ctx* ctx);
+/* Waits for all work queued on the context stream. */
+int pppm_sync(pppm_ctx* ctx);
+/* The context's cudaStream_t, for callers that time or order work. */
+void* pppm_stream(pppm_ctx* ctx);
+
+/* ------------------------------------------------------------- scene */
+/* Replaces Scene::add<T> (scene.h:38-50) + Scene::setAccelerator
+ * (scene.cc:35-38) + QBVHAccel::construct (qbvh_accel.cc:139-203): uploads
+ * the triangle soup (tri_xyz: 9*ntri floats, host), one material id per
+ * triangle and builds the 4-wide BVH with the reference's topology. */
+int pppm_scene_set(pppm_ctx* ctx, const float* tri_xyz, int64_t ntri, const int32_t* mat_id,
+                   const pppm_material* mats, int32_t nmat);
+
+/* Replaces Envmap::Envmap(file) (envmap.cc:28-36): rgb is w*h*3 floats of
+ * the decoded equirect image (row 0 = top, as Image stores it); builds the
+ * 64x64 importance pdf/cdf (envmap.cc:88-163) in double on the host. */
+int pppm_env_set(pppm_ctx* ctx, const float* rgb, int32_t w, int32_t h);
+
+/* Envmap importance tables (envmap.cc:88-163), 4096 doubles each. */
+int pppm_env_tables(pppm_ctx* ctx, double* pdf, double* cdf);
+
+/* Decodes a Radiance RGBE file image held in memory (the reference's
+ * Image::loadHdr, image.cc:296-434) into w*h*3 floats. Call with rgb=NULL
+ * to query the size. */
+int pppm_hdr_decode(const uint8_t* bytes, int64_t nbytes, float* rgb, int64_t cap_floats, int32_t* w, int32_t* h);
+
+/* ------------------------------------------------------------- stages */
+/* Replaces QBVHAccel::intersect (qbvh_accel.cc:205-285) through
+ * Scene::intersect (scene.cc:40-47): closest hit of n rays. tri: original
+ * triangle id or -1; t: hit distance (1e20 on a miss); pos/nrm (optional,
+ * may be NULL): hit position and geometric normal (3 floats each). The
+ * traversal and triangle test reproduce the reference arithmetic, so ids
+ * and t are bit-identical for the same float rays. */
+int pppm_intersect(pppm_ctx* ctx, const float* rays, int64_t n, int32_t* tri, double* t, float* pos, float* nrm);
+
+/* Replaces HashGrid<T>::operator[] bucket selection (hash_grid_detail.h:60-72):
+ * bucket index of each point for a grid initialised with
+ * init(hash_size, scale, bbox) (hash_grid_detail.h:26-31). bbmin: 3 doubles. */
+int pppm_hash_points(pppm_ctx* ctx, const float* pts, int64_t n, int32_t hash_size, double scale,
+                     const double* bbmin, uint32_t* out);
+
+/* Replaces PhotonMap::findKNN (photon_map.cc:24-26) -> KdTree::knnSearch
+ * (kdtree_detail.h:90-132) with the reference's argument order
+ * (numTargetPhotons lands in epsilon, targetRadius in k). Results per query
+ * in the reference's order (farthest first): idx (m x cap), cnt (m). */
+int pppm_knn(pppm_ctx* ctx, const float* photon_pos, int64_t n, const float* queries, int64_t m,
+             int32_t num_target_photons, double target_radius, int32_t* idx, int32_t* cnt, int32_t cap);
+
+/* Replaces the Lambertian gather of ProgressivePhotonMappingProb::radiance
+ * (ppm_probabilistic.cc:300-335). photons: n records of 8 floats
+ * (pos xyz, flux xyz, normal packed as float bits of an int, unused);
+ * queries: m records of 12 floats (pos xyz, normal xyz, refl xyz,
+ * weight xyz = path throughput / roulette). mode COMPAT reproduces the
+ * reference (kNN with k=(int)radius, eps=gather_photons, cone filter);
+ * CANONICAL sums refl*flux/pi over photons within `radius` whose normal
+ * faces the query normal, divided by pi*radius^2. out: m x 3 radiance
+ * (weight included). phantoms: number of default Photon() records at the
+ * origin that the compat map contains (ppm_probabilistic.cc:202-207). */
+int pppm_gather(pppm_ctx* ctx, int32_t mode, const float* photons, int64_t n, int64_t phantoms,
+                const float* queries, int64_t m, double radius, int32_t gather_photons, float* out);
+
+/* ------------------------------------------------------------- render */
+/* Replaces the set-up half of ProgressivePhotonMappingProb::render
+ * (ppm_probabilistic.cc:24-79): radius init, RNG streams, zeroed buffer. */
+int pppm_render_begin(pppm_ctx* ctx, const pppm_camera* cam, const pppm_params* params);
+
+/* One pass t (1-based) of the render loop (ppm_probabilistic.cc:80-96):
+ * tracePhotons, photon map build, traceRays + gather, radius update. */
+int pppm_render_pass(pppm_ctx* ctx, int32_t t, pppm_pass_stats* stats);
+
+/* The linear accumulation buffer after the last pass (not divided by the
+ * pass count, not flipped): w*h*3 floats, row y = camera pixel row y. */
+int pppm_render_read(pppm_ctx* ctx, float* accum);
+
+/* ProgressivePhotonMappingProb::render (ppm_probabilistic.cc:24-121) minus
+ * the PNG side effects: begin + `passes` passes + read. */
+int pppm_render(pppm_ctx* ctx, const pppm_camera* cam, const pppm_params* params, int32_t passes, float* accum);
+
+/* Photon records of the last pass: n x 8 floats (pos xyz, flux xyz, packed
+ * normal, stream id as float bits of an int). Returns the count in *n. */
+int pppm_render_photons(pppm_ctx* ctx, float* out, int64_t cap, int64_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PPPM_C_H_ */

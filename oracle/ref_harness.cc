@@ -1,0 +1,433 @@
+// Test-only harness around the UNMODIFIED tatsy-pppm reference library.
+//
+// This file is part of the oracle (test infrastructure). It is linked with
+// the reference's own object files (oracle/Makefile) and is called through
+// ctypes by tests/golden/make_golden.py and by the CPU tests that pin the
+// C++ port (oracle/pppm_port.cc) against the reference. Nothing in the
+// product links or loads it.
+//
+// The stage methods of the reference are private; the harness reaches them
+// by redefining `private` before including the reference headers, so no
+// reference file is edited. Every function below calls reference code; the
+// harness adds only marshalling between flat arrays and reference objects.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <cstdint>
+#include <algorithm>
+#include <functional>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <queue>
+#include <stack>
+#include <string>
+#include <vector>
+#include <xmmintrin.h>
+#include <immintrin.h>
+#include <omp.h>
+
+#define private public
+#define protected public
+#include "renderer.h"
+#include "random.h"
+#include "random_queue.h"
+#include "sampler.h"
+#include "hash_grid.h"
+#include "kdtree.h"
+#include "subsurface_integrator.h"
+#undef private
+#undef protected
+
+// `enabler` is declared (common.h:41, size.h:6) but never defined by the
+// reference; the default template argument of clamp()/Size<> needs a symbol.
+void* enabler = nullptr;
+
+namespace {
+
+// Triangle soup geometry: lets the harness add an arbitrary triangle list
+// through the reference's own Scene::add<T> (scene.h:38-50).
+class TriSoup : public IGeometry {
+public:
+    std::vector<Triangle> tris;
+    bool intersect(const Ray&, Hitpoint*) const override { return false; }
+    double area() const override { return 0.0; }
+    IGeometry* clone() const override { return new TriSoup(*this); }
+    std::vector<Triangle> triangulate() const override { return tris; }
+};
+
+struct HarnessScene {
+    Scene scene;
+};
+
+// Material record shared with the Python side (same layout as pppm_material
+// in include/pppm_c.h).
+struct Mat {
+    int32_t type;        // BsdfType bitmask without the BSSRDF bit
+    int32_t has_bssrdf;  // 1 -> attach DipoleBSSRDF
+    float refl[3];
+    float phong_n;
+    float sigma_a[3];
+    float sigmap_s[3];
+    float eta;
+    float scale;
+};
+
+BSDF makeBsdf(const Mat& m) {
+    const Vector3D refl(m.refl[0], m.refl[1], m.refl[2]);
+    BSDF b;
+    switch (m.type) {
+    case BSDF_TYPE_LAMBERTIAN_BRDF: b = LambertianBRDF::factory(refl); break;
+    case BSDF_TYPE_SPECULAR_BRDF:   b = SpecularBRDF::factory(refl); break;
+    case BSDF_TYPE_PHONG_BRDF:      b = PhongBRDF::factory(refl, m.phong_n); break;
+    case BSDF_TYPE_REFRACTION:      b = RefractionBSDF::factory(refl); break;
+    default: std::abort();
+    }
+    if (m.has_bssrdf) {
+        BSSRDF s = DipoleBSSRDF::factory(Vector3D(m.sigma_a[0], m.sigma_a[1], m.sigma_a[2]),
+                                         Vector3D(m.sigmap_s[0], m.sigmap_s[1], m.sigmap_s[2]),
+                                         m.eta, m.scale);
+        b.setBssrdf(s);
+    }
+    return b;
+}
+
+Vector3D v3(const float* p) { return Vector3D(p[0], p[1], p[2]); }
+void put3(double* o, const Vector3D& v) { o[0] = v.x(); o[1] = v.y(); o[2] = v.z(); }
+
+}  // namespace
+
+extern "C" {
+
+int rh_num_threads() { return OMP_NUM_CORE; }
+
+// ---------------------------------------------------------------- scene
+void* rh_scene_create() { return new HarnessScene(); }
+void rh_scene_destroy(void* s) { delete static_cast<HarnessScene*>(s); }
+
+// Adds `ntri` triangles (9 floats each) sharing one material.
+void rh_scene_add(void* s, const float* v9, int ntri, const Mat* m) {
+    TriSoup soup;
+    soup.tris.reserve(ntri);
+    for (int i = 0; i < ntri; i++) {
+        soup.tris.push_back(Triangle(v3(v9 + 9 * i), v3(v9 + 9 * i + 3), v3(v9 + 9 * i + 6)));
+    }
+    static_cast<HarnessScene*>(s)->scene.add(soup, makeBsdf(*m));
+}
+
+// Adds a PLY mesh through the reference loader (trimesh.cc:139-217).
+int rh_scene_add_ply(void* s, const char* path, const Mat* m) {
+    Trimesh mesh;
+    mesh.load(path);
+    static_cast<HarnessScene*>(s)->scene.add(mesh, makeBsdf(*m));
+    return (int)mesh.numFaces();
+}
+
+void rh_scene_finalize(void* s) { static_cast<HarnessScene*>(s)->scene.setAccelerator(); }
+
+// Writes an RGB float image as Radiance HDR with the reference writer
+// (image.cc:436-482) so the env map goes through its own RGBE round trip.
+void rh_write_hdr(const char* path, const float* rgb, int w, int h) {
+    Image img(w, h);
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const float* p = rgb + 3 * (y * w + x);
+            img.pixel(x, y) = Vector3D(p[0], p[1], p[2]);
+        }
+    img.save(path);
+}
+
+// Loads an HDR with the reference loader (image.cc:296-434) into doubles.
+int rh_load_hdr(const char* path, double* rgb_out, int cap_pixels, int* w, int* h) {
+    Image img;
+    img.load(path);
+    *w = img.width();
+    *h = img.height();
+    if ((int)(img.width() * img.height()) > cap_pixels) return -1;
+    for (unsigned y = 0; y < img.height(); y++)
+        for (unsigned x = 0; x < img.width(); x++) put3(rgb_out + 3 * (y * img.width() + x), img(x, y));
+    return 0;
+}
+
+void rh_scene_set_envmap(void* s, const char* hdr_path) {
+    Envmap env(hdr_path);
+    static_cast<HarnessScene*>(s)->scene.setEnvmap(env);
+}
+
+// Envmap importance arrays (envmap.cc:88-163), 64*64 entries each.
+void rh_envmap_tables(void* s, double* pdf, double* cdf) {
+    const Envmap& e = static_cast<HarnessScene*>(s)->scene.envmap();
+    for (size_t i = 0; i < e._pdf.size(); i++) { pdf[i] = e._pdf[i]; cdf[i] = e._cdf[i]; }
+}
+
+// Envmap::sampleFromDir (envmap.cc:47-60) for unit directions.
+void rh_envmap_lookup(void* s, const double* dirs, int n, double* out) {
+    const Envmap& e = static_cast<HarnessScene*>(s)->scene.envmap();
+    for (int i = 0; i < n; i++) put3(out + 3 * i, e.sampleFromDir(Vector3D(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2])));
+}
+
+// Envmap::samplePhoton + sampler::onHemisphere on explicit random tapes
+// (ppm_probabilistic.cc:137-144). tapes: n x 5 doubles.
+void rh_emit(void* s, const double* tapes, int n, int numPhotons, double* pos, double* dir, double* flux) {
+    const Envmap& e = static_cast<HarnessScene*>(s)->scene.envmap();
+    for (int i = 0; i < n; i++) {
+        RandomSequence rseq;
+        rseq.resize(5);
+        for (int k = 0; k < 5; k++) rseq.set(k, tapes[5 * i + k]);
+        rseq.reset();
+        const Photon ph = e.samplePhoton(rseq, numPhotons);
+        Vector3D nextDir;
+        sampler::onHemisphere(ph.normal(), &nextDir, rseq.pop(), rseq.pop());
+        put3(pos + 3 * i, static_cast<Vector3D>(ph));
+        put3(dir + 3 * i, nextDir);
+        put3(flux + 3 * i, ph.flux());
+    }
+}
+
+// ---------------------------------------------------------------- geometry
+// Scene::intersect (scene.cc:40-47) for rays given as 6 floats (o, d).
+void rh_intersect(void* s, const float* rays, int n, int32_t* tri, double* t, double* pos, double* nrm) {
+    const Scene& sc = static_cast<HarnessScene*>(s)->scene;
+    for (int i = 0; i < n; i++) {
+        Ray ray(v3(rays + 6 * i), v3(rays + 6 * i + 3));
+        Intersection isect;
+        const bool hit = sc.intersect(ray, isect);
+        tri[i] = hit ? isect.objectID() : -1;
+        t[i] = isect.hitpoint().distance();
+        put3(pos + 3 * i, isect.hitpoint().position());
+        put3(nrm + 3 * i, isect.hitpoint().normal());
+    }
+}
+
+// ---------------------------------------------------------------- RNG
+void rh_xorshift(uint32_t seed, int n, uint32_t* out) {
+    XorShift x(seed);
+    for (int i = 0; i < n; i++) out[i] = x.next();
+}
+
+// Random::nextReal tape of n doubles (random.h:45-55).
+void rh_xorshift_reals(uint32_t seed, int skip, int n, double* out) {
+    XorShift x(seed);
+    for (int i = 0; i < skip; i++) x.next();
+    for (int i = 0; i < n; i++) out[i] = x.nextReal();
+}
+
+// ---------------------------------------------------------------- sampling / BSDF
+void rh_on_hemisphere(const double* normals, const double* r, int n, double* out) {
+    for (int i = 0; i < n; i++) {
+        Vector3D d;
+        sampler::onHemisphere(Vector3D(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]), &d, r[2 * i], r[2 * i + 1]);
+        put3(out + 3 * i, d);
+    }
+}
+
+// BSDF::sample for one material over n (in, normal, r1, r2) tuples.
+void rh_bsdf_sample(const Mat* m, const double* in, const double* nrm, const double* r, int n, double* out, double* pdf) {
+    BSDF b = makeBsdf(*m);
+    for (int i = 0; i < n; i++) {
+        Vector3D o;
+        double p = 1.0;
+        b.sample(Vector3D(in[3 * i], in[3 * i + 1], in[3 * i + 2]), Vector3D(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]),
+                 r[2 * i], r[2 * i + 1], &o, &p);
+        put3(out + 3 * i, o);
+        pdf[i] = p;
+    }
+}
+
+// PerspectiveCamera::getRay (perspective_camera.cc:42-46).
+void rh_camera_rays(const double* eye, const double* dir, const double* up, double fov, int w, int h,
+                    const double* pxy, int n, double* org, double* d) {
+    PerspectiveCamera cam(Vector3D(eye[0], eye[1], eye[2]), Vector3D(dir[0], dir[1], dir[2]),
+                          Vector3D(up[0], up[1], up[2]), fov, w, h, 1.0);
+    for (int i = 0; i < n; i++) {
+        Ray r = cam.getRay(pxy[2 * i], pxy[2 * i + 1]);
+        put3(org + 3 * i, r.origin());
+        put3(d + 3 * i, r.direction());
+    }
+}
+
+// ---------------------------------------------------------------- hash grid
+// HashGrid<int>::operator[] bucket index (hash_grid_detail.h:60-72).
+void rh_hash_points(int hashSize, double scale, const double* bbmin, const double* bbmax, const float* pts, int n,
+                    uint32_t* out) {
+    HashGrid<int> g;
+    g.init(hashSize, scale, BBox(Vector3D(bbmin[0], bbmin[1], bbmin[2]), Vector3D(bbmax[0], bbmax[1], bbmax[2])));
+    for (int i = 0; i < n; i++) out[i] = (uint32_t)(&g[v3(pts + 3 * i)] - &g._data[0]);
+}
+
+// HashGrid<int>::add (hash_grid_detail.h:34-52): items inserted per bucket.
+// Returns, for every bucket, the item ids in insertion order (CSR layout).
+int rh_hash_add_boxes(int hashSize, double scale, const double* bbmin, const double* bbmax, const double* boxmin,
+                      const double* boxmax, int n, int32_t* start, int32_t* items, int cap) {
+    HashGrid<int> g;
+    g.init(hashSize, scale, BBox(Vector3D(bbmin[0], bbmin[1], bbmin[2]), Vector3D(bbmax[0], bbmax[1], bbmax[2])));
+    for (int i = 0; i < n; i++)
+        g.add(i, Vector3D(boxmin[3 * i], boxmin[3 * i + 1], boxmin[3 * i + 2]),
+              Vector3D(boxmax[3 * i], boxmax[3 * i + 1], boxmax[3 * i + 2]));
+    int k = 0;
+    for (int b = 0; b < hashSize; b++) {
+        start[b] = k;
+        for (int id : g._data[b]) {
+            if (k >= cap) return -1;
+            items[k++] = id;
+        }
+    }
+    start[hashSize] = k;
+    return k;
+}
+
+// ---------------------------------------------------------------- kNN
+// PhotonMap::findKNN (photon_map.cc:24-26) with the reference's argument
+// order. Photon ids travel in the (unused by the query) direction field.
+// out_idx: m x cap ids in the reference's result order (farthest first).
+int rh_knn(const float* ppos, int n, const float* q, int m, int numTargetPhotons, double targetRadius,
+           int32_t* out_idx, int32_t* out_cnt, int cap) {
+    std::vector<Photon> photons(n);
+    for (int i = 0; i < n; i++) photons[i] = Photon(v3(ppos + 3 * i), Vector3D(), Vector3D(i, 0, 0), Vector3D());
+    PhotonMap pm;
+    pm.construct(photons);
+    int overflow = 0;
+    for (int j = 0; j < m; j++) {
+        std::vector<Photon> res;
+        pm.findKNN(Photon(v3(q + 3 * j), Vector3D(), Vector3D(), Vector3D()), &res, numTargetPhotons, targetRadius);
+        out_cnt[j] = (int)res.size();
+        for (size_t i = 0; i < res.size(); i++) {
+            if ((int)i < cap) out_idx[j * cap + i] = (int32_t)res[i].direction().x();
+            else overflow = 1;
+        }
+    }
+    return overflow ? -1 : 0;
+}
+
+// ---------------------------------------------------------------- gather
+// ProgressivePhotonMappingProb::radiance (ppm_probabilistic.cc:246-344) at
+// bounce 0 for rays hitting Lambertian surfaces, with the photon map built
+// from the given photons and the global radius forced to `radius`.
+// Photon records: pos(3) flux(3) dir(3) normal(3) floats.
+void rh_gather(void* s, const float* photons, int n, double radius, int gatherPhotons, const float* rays, int m,
+               double* out) {
+    const Scene& sc = static_cast<HarnessScene*>(s)->scene;
+    std::vector<Photon> ph(n);
+    for (int i = 0; i < n; i++) {
+        const float* p = photons + 12 * i;
+        ph[i] = Photon(v3(p), v3(p + 3), v3(p + 6), v3(p + 9));
+    }
+    ProgressivePhotonMappingProb ppm;
+    ppm._photonMap.construct(ph);
+    ppm._radius = radius;
+    RenderParameters params(1000, 1, gatherPhotons, 16.0);
+    for (int j = 0; j < m; j++) {
+        RandomSequence rseq;
+        rseq.resize(200);
+        for (int k = 0; k < 200; k++) rseq.set(k, 0.5);
+        rseq.reset();
+        Ray ray(v3(rays + 6 * j), v3(rays + 6 * j + 3));
+        put3(out + 3 * j, ppm.radiance(sc, ray, params, rseq, 0));
+    }
+}
+
+// ---------------------------------------------------------------- whole pass
+// Runs passes 1..npasses of ProgressivePhotonMappingProb::render's loop
+// (ppm_probabilistic.cc:24-121) by calling the reference's own
+// tracePhotons / traceRays and radius update, without the PNG side effects.
+// accum: w*h*3 doubles of the linear buffer after the last pass (not divided
+// by t). radii: radius used in each pass. photons_out (optional): the photon
+// multiset of the last pass read back from the kd-tree, 12 doubles each.
+struct PassJob {
+    double eye[3], dir[3], up[3];
+    double fov;
+    int w, h;
+    int photons;
+    int gatherPhotons;
+    double gatherRadius;
+    int npasses;
+};
+
+static void collectKd(const KdTree<Photon>::KdTreeNode* node, std::vector<Photon>* out) {
+    if (!node) return;
+    out->push_back(node->point);
+    collectKd(node->left, out);
+    collectKd(node->right, out);
+}
+
+int rh_render_passes(void* s, const PassJob* job, double* accum, double* radii, double* photons_out, int photon_cap,
+                     int* photon_count) {
+    const Scene& sc = static_cast<HarnessScene*>(s)->scene;
+    PerspectiveCamera cam(Vector3D(job->eye[0], job->eye[1], job->eye[2]), Vector3D(job->dir[0], job->dir[1], job->dir[2]),
+                          Vector3D(job->up[0], job->up[1], job->up[2]), job->fov, job->w, job->h, 1.0);
+    RenderParameters params(job->photons, job->npasses, job->gatherPhotons, job->gatherRadius);
+    ProgressivePhotonMappingProb ppm;
+
+    BBox bbox;
+    for (int i = 0; i < (int)sc.numTriangles(); i++) bbox.merge(sc.getTriangle(i));
+    ppm._radius = (bbox.posMax() - bbox.posMin()).norm() * 0.1;
+
+    RandomSampler* rs = new RandomSampler[OMP_NUM_CORE];
+    for (int i = 0; i < OMP_NUM_CORE; i++) rs[i] = Random::generateSampler(i);
+    Image buffer(job->w, job->h);
+    buffer.fill(Vector3D(0.0, 0.0, 0.0));
+    std::streambuf* old = std::cout.rdbuf(nullptr);  // silence progress output
+    for (int t = 1; t <= job->npasses; t++) {
+        radii[t - 1] = ppm._radius;
+        ppm.tracePhotons(sc, cam, params, rs);
+        ppm.traceRays(&buffer, sc, cam, params, rs);
+        ppm._radius = (t + 1.0) / (t + ProgressivePhotonMappingProb::ALPHA) * ppm._radius;
+    }
+    std::cout.rdbuf(old);
+    for (int y = 0; y < job->h; y++)
+        for (int x = 0; x < job->w; x++) put3(accum + 3 * (y * job->w + x), buffer(x, y));
+    if (photons_out && photon_count) {
+        std::vector<Photon> all;
+        collectKd(&ppm._photonMap._kdtree._nodes[0], &all);
+        *photon_count = (int)all.size();
+        for (int i = 0; i < (int)all.size() && i < photon_cap; i++) {
+            put3(photons_out + 12 * i, static_cast<Vector3D>(all[i]));
+            put3(photons_out + 12 * i + 3, all[i].flux());
+            put3(photons_out + 12 * i + 6, all[i].direction());
+            put3(photons_out + 12 * i + 9, all[i].normal());
+        }
+    }
+    delete[] rs;
+    return 0;
+}
+
+// ---------------------------------------------------------------- dipole
+void rh_dipole_rd(const Mat* m, const double* d2, int n, double* out) {
+    BSDF b = makeBsdf(*m);
+    for (int i = 0; i < n; i++) put3(out + 3 * i, (*b._bssrdf)(d2[i]));
+}
+
+double rh_dipole_fdr(const Mat* m) {
+    BSDF b = makeBsdf(*m);
+    return b._bssrdf->Fdr();
+}
+
+// SubsurfaceIntegrator::irradiance (subsurface_integrator.cc:234-238) over an
+// octree built (subsurface_integrator.cc:67-145) from injected irradiance
+// points: pos(3) normal(3) area(1) irad(3) doubles each.
+void rh_dipole_irradiance(const Mat* m, const double* ipts, int n, double maxError, const double* q, int nq,
+                          double* out) {
+    BSDF b = makeBsdf(*m);
+    SubsurfaceIntegrator integ;
+    integ._maxError = maxError;
+    std::vector<IrradiancePoint> pts(n);
+    for (int i = 0; i < n; i++) {
+        const double* p = ipts + 10 * i;
+        pts[i] = IrradiancePoint(Vector3D(p[0], p[1], p[2]), Vector3D(p[3], p[4], p[5]), p[6], Vector3D(p[7], p[8], p[9]));
+    }
+    integ.octree.construct(&integ, pts);
+    for (int j = 0; j < nq; j++) put3(out + 3 * j, integ.irradiance(Vector3D(q[3 * j], q[3 * j + 1], q[3 * j + 2]), b));
+}
+
+// sampler::poissonDisk (sampler.cc:36-101). Uses the reference's static RNG,
+// so only the first call in a fresh process is reproducible.
+int rh_poisson_disk(const float* v9, int ntri, double minDist, double* pts, double* nrms, int cap) {
+    std::vector<Triangle> tris;
+    for (int i = 0; i < ntri; i++) tris.push_back(Triangle(v3(v9 + 9 * i), v3(v9 + 9 * i + 3), v3(v9 + 9 * i + 6)));
+    std::vector<Vector3D> p, nn;
+    sampler::poissonDisk(tris, minDist, &p, &nn);
+    for (int i = 0; i < (int)p.size() && i < cap; i++) { put3(pts + 3 * i, p[i]); put3(nrms + 3 * i, nn[i]); }
+    return (int)p.size();
+}
+
+}  // extern "C"

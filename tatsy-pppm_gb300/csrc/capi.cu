@@ -1,0 +1,284 @@
+// C-ABI entry points: lifetime, staging, scene, env map and stage queries.
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "context.h"
+#include "host_build.h"
+
+namespace pppm {
+
+bool isDevicePtr(const void* p) {
+    if (p == nullptr) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int stageIn(pppm_ctx* c, const void* src, size_t bytes, int slot, const void** out) {
+    if (bytes == 0 || isDevicePtr(src)) {
+        *out = src;
+        return PPPM_OK;
+    }
+    PPPM_CUDA(c, c->stage[slot].ensure(bytes));
+    PPPM_CUDA(c, cudaMemcpyAsync(c->stage[slot].p, src, bytes, cudaMemcpyHostToDevice, c->stream));
+    *out = c->stage[slot].p;
+    return PPPM_OK;
+}
+
+int stageOut(pppm_ctx* c, void* dst, size_t bytes, int slot, void** out) {
+    if (dst == nullptr) {
+        *out = nullptr;
+        return PPPM_OK;
+    }
+    if (bytes == 0 || isDevicePtr(dst)) {
+        *out = dst;
+        return PPPM_OK;
+    }
+    PPPM_CUDA(c, c->stage[slot].ensure(bytes));
+    *out = c->stage[slot].p;
+    return PPPM_OK;
+}
+
+int finishOut(pppm_ctx* c, void* dst, const void* staged, size_t bytes) {
+    if (dst == nullptr || dst == staged || bytes == 0) return PPPM_OK;
+    PPPM_CUDA(c, cudaMemcpyAsync(dst, staged, bytes, cudaMemcpyDeviceToHost, c->stream));
+    return PPPM_OK;
+}
+
+static DevMaterial toDevMaterial(const pppm_material& m) {
+    DevMaterial d;
+    std::memset(&d, 0, sizeof(d));
+    d.type = m.type | (m.has_bssrdf ? PPPM_BSDF_BSSRDF : 0);
+    for (int k = 0; k < 3; k++) d.refl[k] = m.refl[k];
+    d.phong_n = m.phong_n;
+    d.roulette = std::fmax(m.refl[0], std::fmax(m.refl[1], m.refl[2]));
+    d.rr_photon = ((double)m.refl[0] + (double)m.refl[1] + (double)m.refl[2]) / 3.0;
+    if (m.has_bssrdf) {
+        // DipoleBSSRDF ctor (bssrdf.cc:48-63) and Fdr (bssrdf.cc:33-42) in double
+        const double eta = m.eta, eta2 = eta * eta, eta3 = eta2 * eta;
+        const double fdr = eta >= 1.0 ? (-1.439 + 0.7099 * eta + 0.6681 * eta2 + 0.0636 * eta3) / eta2
+                                      : (-0.4399 * eta3 + 0.7099 * eta2 - 0.3319 * eta + 0.0636) / eta3;
+        const double A = (1.0 + fdr) / (1.0 - fdr);
+        d.A = (float)A;
+        d.fdr = (float)fdr;
+        d.eta = m.eta;
+        d.scale = m.scale;
+        for (int k = 0; k < 3; k++) {
+            const double sa = m.sigma_a[k], ss = m.sigmap_s[k];
+            const double st = sa + ss;
+            d.sigma_tr[k] = (float)std::sqrt(3.0 * sa * st);
+            d.alphap[k] = (float)(ss / st);
+            d.zpos[k] = (float)(1.0 / st);
+            d.zneg[k] = (float)((1.0 / st) * (1.0 + (4.0 / 3.0) * A));
+        }
+    }
+    return d;
+}
+
+}  // namespace pppm
+
+using namespace pppm;
+
+extern "C" {
+
+int pppm_create(int device, pppm_ctx** out) {
+    if (!out) return PPPM_E_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return PPPM_E_CUDA;
+    }
+    pppm_ctx* c = new (std::nothrow) pppm_ctx();
+    if (!c) return PPPM_E_CAPACITY;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return PPPM_E_CUDA;
+    }
+    for (auto& e : c->ev) cudaEventCreate(&e);
+    *out = c;
+    return PPPM_OK;
+}
+
+int pppm_destroy(pppm_ctx* c) {
+    if (!c) return PPPM_E_ARG;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return PPPM_OK;
+}
+
+const char* pppm_last_error(const pppm_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int pppm_sync(pppm_ctx* c) {
+    if (!c) return PPPM_E_ARG;
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    PPPM_CUDA(c, cudaGetLastError());
+    return PPPM_OK;
+}
+
+void* pppm_stream(pppm_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int pppm_scene_set(pppm_ctx* c, const float* tri, int64_t ntri, const int32_t* matId, const pppm_material* mats,
+                   int32_t nmat) {
+    if (!c || ntri < 0 || (ntri > 0 && (!tri || !matId)) || nmat < 0 || (nmat > 0 && !mats))
+        return fail(c, PPPM_E_ARG, "scene_set: bad arguments");
+    if (isDevicePtr(tri) || isDevicePtr(matId) || isDevicePtr(mats))
+        return fail(c, PPPM_E_ARG, "scene_set: scene arrays must be host memory");
+    for (int i = 0; i < nmat; i++) {
+        const int t = mats[i].type;
+        if (t != PPPM_BSDF_LAMBERTIAN && t != PPPM_BSDF_SPECULAR && t != PPPM_BSDF_PHONG && t != PPPM_BSDF_REFRACTION)
+            return fail(c, PPPM_E_ARG, "scene_set: material type must be one BSDF bit");
+    }
+    for (int64_t i = 0; i < ntri; i++)
+        if (matId[i] < 0 || matId[i] >= nmat) return fail(c, PPPM_E_ARG, "scene_set: material id out of range");
+    cudaSetDevice(c->device);
+    HostBvh bvh;
+    std::string err;
+    if (!buildQbvh(tri, ntri, &bvh, &err)) return fail(c, PPPM_E_CAPACITY, "scene_set: " + err);
+    c->hasScene = false;
+    c->rs.active = false;
+    const size_t nodeBytes = bvh.nodes.size() * sizeof(QNode);
+    PPPM_CUDA(c, c->nodes.ensure(nodeBytes));
+    if (nodeBytes) {
+        std::vector<QNode> dn(bvh.nodes.size());
+        for (size_t k = 0; k < dn.size(); k++) {
+            const HostQNode& h = bvh.nodes[k];
+            for (int d = 0; d < 3; d++) {
+                dn[k].bmin[d] = make_float4(h.bmin[d][0], h.bmin[d][1], h.bmin[d][2], h.bmin[d][3]);
+                dn[k].bmax[d] = make_float4(h.bmax[d][0], h.bmax[d][1], h.bmax[d][2], h.bmax[d][3]);
+            }
+            dn[k].child = make_int4(h.child[0], h.child[1], h.child[2], h.child[3]);
+            dn[k].meta = make_int4(h.sep, 0, 0, 0);
+        }
+        PPPM_CUDA(c, cudaMemcpy(c->nodes.p, dn.data(), nodeBytes, cudaMemcpyHostToDevice));
+    }
+    PPPM_CUDA(c, c->tris.ensure(bvh.tris.size() * sizeof(float)));
+    if (!bvh.tris.empty())
+        PPPM_CUDA(c, cudaMemcpy(c->tris.p, bvh.tris.data(), bvh.tris.size() * sizeof(float), cudaMemcpyHostToDevice));
+    PPPM_CUDA(c, c->matId.ensure((size_t)ntri * 4));
+    if (ntri) PPPM_CUDA(c, cudaMemcpy(c->matId.p, matId, (size_t)ntri * 4, cudaMemcpyHostToDevice));
+    std::vector<DevMaterial> dm(nmat);
+    c->anyBssrdf = false;
+    for (int i = 0; i < nmat; i++) {
+        dm[i] = toDevMaterial(mats[i]);
+        c->anyBssrdf |= mats[i].has_bssrdf != 0;
+    }
+    PPPM_CUDA(c, c->devMats.ensure(dm.size() * sizeof(DevMaterial)));
+    if (nmat) PPPM_CUDA(c, cudaMemcpy(c->devMats.p, dm.data(), dm.size() * sizeof(DevMaterial), cudaMemcpyHostToDevice));
+    c->mats.assign(mats, mats + nmat);
+    c->lambertArea = 0.0;
+    for (int64_t i = 0; i < ntri; i++) {
+        if (mats[matId[i]].type != PPPM_BSDF_LAMBERTIAN) continue;
+        const float* p = tri + 9 * i;
+        const double e1[3] = {(double)p[3] - p[0], (double)p[4] - p[1], (double)p[5] - p[2]};
+        const double e2[3] = {(double)p[6] - p[0], (double)p[7] - p[1], (double)p[8] - p[2]};
+        const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
+        c->lambertArea += 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+    }
+    c->ntri = ntri;
+    c->rootCode = bvh.rootCode;
+    c->bvhDepth = bvh.depth;
+    // BBox over all triangles (ppm_probabilistic.cc:50-54)
+    for (int d = 0; d < 3; d++) { c->bbmin[d] = 1e20; c->bbmax[d] = -1e20; }
+    for (int64_t i = 0; i < ntri * 3; i++)
+        for (int d = 0; d < 3; d++) {
+            const double v = tri[3 * i + d];
+            c->bbmin[d] = v < c->bbmin[d] ? v : c->bbmin[d];
+            c->bbmax[d] = v > c->bbmax[d] ? v : c->bbmax[d];
+        }
+    c->hasScene = true;
+    return PPPM_OK;
+}
+
+int pppm_env_set(pppm_ctx* c, const float* rgb, int32_t w, int32_t h) {
+    if (!c || !rgb || w <= 0 || h <= 0) return fail(c, PPPM_E_ARG, "env_set: bad arguments");
+    // The 64x64 importance map divides by the texel area of each cell
+    // (envmap.cc:104-113); below 64 texels per axis that area is zero and
+    // the reference aborts.
+    if (w < 64 || h < 64) return fail(c, PPPM_E_UNDEFINED, "env_set: env map must be at least 64x64");
+    if (isDevicePtr(rgb)) return fail(c, PPPM_E_ARG, "env_set: rgb must be host memory");
+    cudaSetDevice(c->device);
+    envImportance(rgb, w, h, &c->envPdf, &c->envCdf);
+    const size_t bytes = (size_t)w * h * 3 * sizeof(float);
+    PPPM_CUDA(c, c->envRgb.ensure(bytes));
+    PPPM_CUDA(c, cudaMemcpy(c->envRgb.p, rgb, bytes, cudaMemcpyHostToDevice));
+    PPPM_CUDA(c, c->envPdfD.ensure(4096 * sizeof(double)));
+    PPPM_CUDA(c, c->envCdfD.ensure(4096 * sizeof(double)));
+    PPPM_CUDA(c, cudaMemcpy(c->envPdfD.p, c->envPdf.data(), 4096 * sizeof(double), cudaMemcpyHostToDevice));
+    PPPM_CUDA(c, cudaMemcpy(c->envCdfD.p, c->envCdf.data(), 4096 * sizeof(double), cudaMemcpyHostToDevice));
+    c->envW = w;
+    c->envH = h;
+    c->hasEnv = true;
+    return PPPM_OK;
+}
+
+int pppm_env_tables(pppm_ctx* c, double* pdf, double* cdf) {
+    if (!c || !pdf || !cdf) return fail(c, PPPM_E_ARG, "env_tables: bad arguments");
+    if (!c->hasEnv) return fail(c, PPPM_E_STATE, "env_tables: no env map");
+    std::memcpy(pdf, c->envPdf.data(), 4096 * sizeof(double));
+    std::memcpy(cdf, c->envCdf.data(), 4096 * sizeof(double));
+    return PPPM_OK;
+}
+
+int pppm_hdr_decode(const uint8_t* bytes, int64_t n, float* rgb, int64_t cap, int32_t* w, int32_t* h) {
+    if (!bytes || n <= 0 || !w || !h) return PPPM_E_ARG;
+    int ww = 0, hh = 0;
+    const int r = decodeHdr(bytes, n, rgb, cap, &ww, &hh);
+    *w = ww;
+    *h = hh;
+    if (r == -4) return PPPM_E_CAPACITY;
+    return r == 0 ? PPPM_OK : PPPM_E_ARG;
+}
+
+int pppm_intersect(pppm_ctx* c, const float* rays, int64_t n, int32_t* tri, double* t, float* pos, float* nrm) {
+    if (!c || n < 0 || (n > 0 && (!rays || !tri || !t))) return fail(c, PPPM_E_ARG, "intersect: bad arguments");
+    if (!c->hasScene) return fail(c, PPPM_E_STATE, "intersect: no scene");
+    if (n == 0) return PPPM_OK;
+    cudaSetDevice(c->device);
+    const void* dr;
+    void *dtri, *dt, *dpos, *dnrm;
+    int r;
+    if ((r = stageIn(c, rays, (size_t)n * 24, 0, &dr))) return r;
+    if ((r = stageOut(c, tri, (size_t)n * 4, 1, &dtri))) return r;
+    if ((r = stageOut(c, t, (size_t)n * 8, 2, &dt))) return r;
+    if ((r = stageOut(c, pos, (size_t)n * 12, 3, &dpos))) return r;
+    if ((r = stageOut(c, nrm, (size_t)n * 12, 4, &dnrm))) return r;
+    PPPM_CUDA(c, launchIntersect(sceneView(c), (const float*)dr, n, (int32_t*)dtri, (double*)dt, (float*)dpos,
+                                 (float*)dnrm, c->stream, true));
+    const bool host = dr != rays || dtri != tri || dt != t || (pos && dpos != pos) || (nrm && dnrm != nrm);
+    if ((r = finishOut(c, tri, dtri, (size_t)n * 4))) return r;
+    if ((r = finishOut(c, t, dt, (size_t)n * 8))) return r;
+    if ((r = finishOut(c, pos, dpos, (size_t)n * 12))) return r;
+    if ((r = finishOut(c, nrm, dnrm, (size_t)n * 12))) return r;
+    if (host) PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PPPM_OK;
+}
+
+int pppm_hash_points(pppm_ctx* c, const float* pts, int64_t n, int32_t size, double scale, const double* bbmin,
+                     uint32_t* out) {
+    if (!c || n < 0 || size <= 0 || !bbmin || (n > 0 && (!pts || !out)))
+        return fail(c, PPPM_E_ARG, "hash_points: bad arguments");
+    if (n == 0) return PPPM_OK;
+    cudaSetDevice(c->device);
+    const void* dp;
+    void* dout;
+    int r;
+    if ((r = stageIn(c, pts, (size_t)n * 12, 0, &dp))) return r;
+    if ((r = stageOut(c, out, (size_t)n * 4, 1, &dout))) return r;
+    PPPM_CUDA(c, launchHashPoints((const float*)dp, n, (uint32_t)size, scale, bbmin, (uint32_t*)dout, c->stream));
+    if ((r = finishOut(c, out, dout, (size_t)n * 4))) return r;
+    if (dp != pts || dout != out) PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PPPM_OK;
+}
+
+}  // extern "C"

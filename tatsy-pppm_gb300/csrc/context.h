@@ -1,0 +1,164 @@
+// The C-ABI context: device memory owned per context, staging of host
+// arguments, and the render state carried between passes.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/pppm_c.h"
+#include "pppm_device.cuh"
+
+namespace pppm {
+
+// Growable device allocation owned by the context.
+struct DBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes < 256 ? 256 : bytes;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    ~DBuf() { release(); }
+};
+
+struct GridBufs {
+    DBuf counts;   // uint32 per bucket (+1), becomes start offsets
+    DBuf cursor;   // uint32 per bucket
+    DBuf sorted;   // float4 x 2 per photon, bucket order
+    DBuf keys;     // uint32 bucket per photon
+    DBuf scanTmp;  // scan partials
+    uint32_t size = 0;   // buckets (power of two)
+    float cell = 0.0f;   // cell edge
+    float invCell = 0.0f;
+    float origin[3] = {0, 0, 0};
+    int64_t count = 0;   // photons in the grid
+};
+
+struct RenderState {
+    bool active = false;
+    pppm_camera cam{};
+    pppm_params par{};
+    double radius = 0.0;
+    double bboxDiag = 0.0;
+    int64_t taskPerThread = 0;  // ceil(P / N)
+    int passesDone = 0;
+    // per-stream XorShift state at the start of the next pass (compat)
+    std::vector<XorShift> streams;
+    DBuf accum;       // float3 per pixel (W*H*3 floats)
+    DBuf photons;     // 2 x float4 per stored photon (pos|normal, flux|stream)
+    DBuf photonCount; // counters (see render.cu)
+    DBuf pathA, pathB;  // wavefront path state
+    DBuf queries;     // gather queries
+    DBuf tapeStates;  // uint4 start state per photon / pixel (compat)
+    DBuf jumpMats;    // jump-ahead matrices
+    DBuf streamStatesD;  // N x uint4 per-stream state at the start of the pass
+    GridBufs grid;
+    int64_t depositCap = 0;
+    int64_t storedLast = 0;
+    int64_t phantomsLast = 0;
+};
+
+}  // namespace pppm
+
+struct pppm_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    // scene
+    bool hasScene = false;
+    int64_t ntri = 0;
+    int rootCode = 0;
+    int bvhDepth = 0;
+    double bbmin[3] = {0, 0, 0}, bbmax[3] = {0, 0, 0};
+    std::vector<pppm_material> mats;
+    bool anyBssrdf = false;
+    pppm::DBuf nodes, tris, matId, devMats;
+    double lambertArea = 0.0;  // summed area of Lambertian triangles
+    // env
+    bool hasEnv = false;
+    int envW = 0, envH = 0;
+    std::vector<double> envPdf, envCdf;
+    pppm::DBuf envRgb, envPdfD, envCdfD;
+    // staging for host arguments
+    pppm::DBuf stage[8];
+    std::vector<void*> pinned;
+    pppm::RenderState rs;
+    std::vector<uint32_t> jumpTables;  // XorShift jump-ahead matrices (host copy)
+    // scratch of the kNN / gather stage entry points
+    pppm::DBuf stageRec, stageQ, stageCount;
+    pppm::GridBufs stageGrid;
+    cudaEvent_t ev[8] = {};
+};
+
+namespace pppm {
+
+inline int fail(pppm_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+inline int cudaFail(pppm_ctx* c, cudaError_t e, const char* where) {
+    return fail(c, PPPM_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define PPPM_CUDA(ctx, call)                                   \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return ::pppm::cudaFail((ctx), e_, #call); \
+    } while (0)
+
+bool isDevicePtr(const void* p);
+
+// Returns a device pointer holding `bytes` of `src`: src itself when it is
+// device memory, else a staging copy (slot chooses the staging buffer).
+int stageIn(pppm_ctx* c, const void* src, size_t bytes, int slot, const void** out);
+// Returns where a kernel should write `bytes` destined for `dst`.
+int stageOut(pppm_ctx* c, void* dst, size_t bytes, int slot, void** out);
+// Copies staged output back to a host `dst` (no-op for device dst).
+int finishOut(pppm_ctx* c, void* dst, const void* staged, size_t bytes);
+
+// Uploads the scene device view used by kernels.
+struct SceneView {
+    const QNode* nodes;
+    const float4* tris;
+    const int* matId;
+    const DevMaterial* mats;
+    int rootCode;
+};
+inline SceneView sceneView(const pppm_ctx* c) {
+    return {c->nodes.as<QNode>(), c->tris.as<float4>(), c->matId.as<int>(), c->devMats.as<DevMaterial>(), c->rootCode};
+}
+inline EnvDev envView(const pppm_ctx* c) {
+    EnvDev e;
+    e.rgb = c->envRgb.as<float>();
+    e.cdf = c->envCdfD.as<double>();
+    e.pdf = c->envPdfD.as<double>();
+    e.w = c->envW;
+    e.h = c->envH;
+    e.area_over_p = 0.0;
+    return e;
+}
+
+// Kernel launchers (defined in the .cu files).
+cudaError_t launchIntersect(const SceneView& s, const float* rays, int64_t n, int32_t* tri, double* t, float* pos,
+                            float* nrm, cudaStream_t st, bool prefilter);
+cudaError_t launchHashPoints(const float* pts, int64_t n, uint32_t size, double scale, const double* bbmin, uint32_t* out,
+                             cudaStream_t st);
+
+}  // namespace pppm

@@ -1,0 +1,435 @@
+// Photon emission and bounce wavefront, eye paths, and the RNG tapes that
+// reproduce the reference's per-thread XorShift streams.
+#include <cstring>
+
+#include "trace.h"
+
+namespace pppm {
+
+// ------------------------------------------------------------------ jump-ahead (host)
+namespace {
+
+struct Gf2Mat {
+    uint32_t col[128][4];
+};
+
+void gf2Apply(const Gf2Mat& m, const uint32_t in[4], uint32_t out[4]) {
+    uint32_t r[4] = {0, 0, 0, 0};
+    for (int j = 0; j < 128; j++)
+        if ((in[j >> 5] >> (j & 31)) & 1u)
+            for (int w = 0; w < 4; w++) r[w] ^= m.col[j][w];
+    std::memcpy(out, r, sizeof(r));
+}
+
+void gf2Mul(const Gf2Mat& a, const Gf2Mat& b, Gf2Mat* c) {  // c = a * b (apply b first)
+    Gf2Mat t;
+    for (int j = 0; j < 128; j++) gf2Apply(a, b.col[j], t.col[j]);
+    *c = t;
+}
+
+}  // namespace
+
+void xorshiftJumpTables(std::vector<uint32_t>* tables) {
+    // one XorShift step as a 128x128 GF(2) matrix
+    Gf2Mat m;
+    for (int j = 0; j < 128; j++) {
+        XorShift x;
+        for (int w = 0; w < 4; w++) x.s[w] = 0;
+        x.s[j >> 5] = 1u << (j & 31);
+        x.next();
+        std::memcpy(m.col[j], x.s, 16);
+    }
+    // T = M^200 by square and multiply
+    Gf2Mat t, p = m;
+    bool first = true;
+    for (int e = 200; e > 0; e >>= 1) {
+        if (e & 1) {
+            if (first) { t = p; first = false; } else gf2Mul(p, t, &t);
+        }
+        if (e > 1) gf2Mul(p, p, &p);
+    }
+    tables->assign((size_t)kJumpLevels * 128 * 4, 0u);
+    Gf2Mat cur = t;
+    for (int k = 0; k < kJumpLevels; k++) {
+        std::memcpy(tables->data() + (size_t)k * 512, cur.col, sizeof(cur.col));
+        gf2Mul(cur, cur, &cur);
+    }
+}
+
+void xorshiftJumpHost(const std::vector<uint32_t>& tables, uint64_t tapes, XorShift* st) {
+    for (int k = 0; k < kJumpLevels && tapes; k++, tapes >>= 1) {
+        if (!(tapes & 1)) continue;
+        Gf2Mat const* m = reinterpret_cast<const Gf2Mat*>(tables.data() + (size_t)k * 512);
+        gf2Apply(*m, st->s, st->s);
+    }
+}
+
+namespace {
+
+unsigned blocksFor(int64_t n, int bs, int cap = 152 * 16) {
+    const int64_t want = (n + bs - 1) / bs;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, cap));
+}
+
+__device__ __forceinline__ void jumpApply(const uint32_t* __restrict__ J, uint32_t s[4]) {
+    uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+    const uint4* cols = reinterpret_cast<const uint4*>(J);
+#pragma unroll 1
+    for (int w = 0; w < 4; w++) {
+        const uint32_t word = s[w];
+#pragma unroll 8
+        for (int b = 0; b < 32; b++) {
+            const uint32_t m = 0u - ((word >> b) & 1u);
+            const uint4 c = __ldg(&cols[w * 32 + b]);
+            r0 ^= c.x & m;
+            r1 ^= c.y & m;
+            r2 ^= c.z & m;
+            r3 ^= c.w & m;
+        }
+    }
+    s[0] = r0; s[1] = r1; s[2] = r2; s[3] = r3;
+}
+
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// Canonical mode: an independent XorShift state per (seed, pass, path).
+__device__ __forceinline__ void seedCanonical(uint32_t seed, int pass, uint64_t id, XorShift& x) {
+    const uint32_t a = mix32(seed ^ 0x9e3779b9u * (uint32_t)(pass + 1));
+    const uint32_t b = mix32((uint32_t)id ^ mix32((uint32_t)(id >> 32) + a));
+    x.s[0] = mix32(a ^ b) | 1u;
+    x.s[1] = mix32(b + 0x632be59bu);
+    x.s[2] = mix32(a + 0x85157af5u + b);
+    x.s[3] = mix32(b ^ 0xa54ff53au);
+}
+
+constexpr int kRun = 32;  // tapes generated sequentially per thread
+
+// Start state of every photon tape and pixel tape of this pass. Stream s
+// (one per reference OpenMP thread) draws, in order, ceil(P/N) photon tapes
+// (ppm_probabilistic.cc:131-135) and then one tape per pixel of the rows
+// y = s, s + N, ... (ppm_probabilistic.cc:213-228).
+__global__ void kTapeStates(TraceParams tp, const uint32_t* __restrict__ streamStates, const uint32_t* __restrict__ jump,
+                            int W, int H, uint32_t* __restrict__ photonStates, uint32_t* __restrict__ pixelStates) {
+    const int N = tp.numStreams;
+    const int64_t T = tp.taskPerThread;
+    const int64_t maxRows = (H + N - 1) / N;
+    const int64_t maxItems = T + maxRows * W;
+    const int64_t runsPer = (maxItems + kRun - 1) / kRun;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < runsPer * N;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(g / runsPer);
+        const int64_t run = g % runsPer;
+        const int64_t rows = s < H ? (H - 1 - s) / N + 1 : 0;
+        const int64_t items = T + rows * W;
+        const int64_t o = run * kRun;
+        if (o >= items) continue;
+        uint32_t st[4] = {streamStates[4 * s], streamStates[4 * s + 1], streamStates[4 * s + 2], streamStates[4 * s + 3]};
+        uint64_t k = (uint64_t)o;
+        for (int lvl = 0; k; lvl++, k >>= 1)
+            if (k & 1) jumpApply(jump + (size_t)lvl * 512, st);
+        XorShift x;
+        x.s[0] = st[0]; x.s[1] = st[1]; x.s[2] = st[2]; x.s[3] = st[3];
+        const int64_t end = min(o + kRun, items);
+        for (int64_t j = o; j < end; j++) {
+            uint32_t* dst;
+            if (j < T) {
+                dst = photonStates + 4 * ((int64_t)s * T + j);
+            } else {
+                const int64_t pj = j - T;
+                const int64_t y = s + (int64_t)N * (pj / W), xx = pj % W;
+                dst = pixelStates + 4 * (y * W + xx);
+            }
+            *reinterpret_cast<uint4*>(dst) = make_uint4(x.s[0], x.s[1], x.s[2], x.s[3]);
+            for (int t = 0; t < 200; t++) x.next();
+        }
+    }
+}
+
+__global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restrict__ photonStates,
+                            PathState* __restrict__ queue, PassCounters* ctr) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < tp.numPaths;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        Tape tape;
+        tape.pos = 0;
+        if (tp.mode == PPPM_MODE_COMPAT) {
+            const uint4 s = *reinterpret_cast<const uint4*>(photonStates + 4 * g);
+            tape.x.s[0] = s.x; tape.x.s[1] = s.y; tape.x.s[2] = s.z; tape.x.s[3] = s.w;
+        } else {
+            seedCanonical(tp.seed, tp.pass, (uint64_t)g, tape.x);
+        }
+        f3 d, dir, flux;
+        const bool ok = emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux);
+        if (!ok) atomicAdd(&ctr->undefinedEmit, 1ull);
+        PathState p;
+        p.ox = 50.0 * (double)d.x;  // R * dir with R = 50 (envmap.cc:63,85)
+        p.oy = 50.0 * (double)d.y;
+        p.oz = 50.0 * (double)d.z;
+        p.dx = dir.x; p.dy = dir.y; p.dz = dir.z;
+        p.fx = ok ? flux.x : 0.f; p.fy = ok ? flux.y : 0.f; p.fz = ok ? flux.z : 0.f;
+        p.rng[0] = tape.x.s[0]; p.rng[1] = tape.x.s[1]; p.rng[2] = tape.x.s[2]; p.rng[3] = tape.x.s[3];
+        p.id = (int)g;
+        p.bounce = 0;
+        p.pad[0] = p.pad[1] = 0;
+        queue[g] = p;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctr->queue[0] = (unsigned long long)tp.numPaths;
+        ctr->queue[1] = 0;
+        ctr->queue[2] = 0;
+    }
+}
+
+__device__ __forceinline__ unsigned long long warpAppend(bool take, unsigned long long* counter) {
+    const unsigned mask = __ballot_sync(0xffffffffu, take);
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (mask) {
+        const int leader = __ffs(mask) - 1;
+        if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    return base + (unsigned long long)__popc(mask & ((1u << lane) - 1u));
+}
+
+// One bounce of every live photon path (ppm_probabilistic.cc:150-193):
+// closest hit, three draws, deposit + Russian roulette on Lambertian
+// surfaces, BSDF sampling elsewhere. Survivors are compacted into `out`
+// with one atomic per warp; queue lengths rotate through ctr->queue[b % 3].
+__global__ void __launch_bounds__(128) kPhotonBounce(TraceParams tp, SceneView sc, int bounce, const PathState* __restrict__ in,
+                                                     PathState* __restrict__ out, int64_t maxPaths,
+                                                     float4* __restrict__ dep, int64_t depCap, PassCounters* ctr) {
+    __shared__ int order[128];
+    loadOrderTable(order);
+    const int qi = bounce % 3, qo = (bounce + 1) % 3, qz = (bounce + 2) % 3;
+    const int64_t n = min((int64_t)ctr->queue[qi], maxPaths);
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr->queue[qz] = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        bool alive = false, store = false;
+        PathState p;
+        float4 da, db;
+        if (i < n) {
+            p = in[i];
+            alive = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
+        }
+        int traced = 0;
+        if (alive) {
+            double best;
+            traced = 1;
+            const int slot = traverseExact<true>(sc.nodes, sc.tris, sc.rootCode, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz,
+                                                 order, &best, nullptr, nullptr);
+            if (slot < 0) {
+                alive = false;
+            } else {
+                Tape tape;
+                tape.pos = 0;
+                tape.x.s[0] = p.rng[0]; tape.x.s[1] = p.rng[1]; tape.x.s[2] = p.rng[2]; tape.x.s[3] = p.rng[3];
+                const double r0 = tape.popd(), r1 = tape.popd(), r2 = tape.popd();
+                const float4 a = sc.tris[3 * slot], b = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
+                const int tid = __float_as_int(a.w);
+                const DevMaterial& m = sc.mats[sc.matId[tid]];
+                double hp[3];
+                hitPosition(p.ox, p.oy, p.oz, p.dx, p.dy, p.dz, best, hp);
+                const f3 nrm = triNormal(a, b, c);
+                const f3 din = {p.dx, p.dy, p.dz};
+                const f3 on = dot(nrm, din) < 0.0f ? nrm : -nrm;
+                f3 flux = {p.fx, p.fy, p.fz};
+                const f3 refl = {m.refl[0], m.refl[1], m.refl[2]};
+                f3 nd;
+                if (m.type & PPPM_BSDF_LAMBERTIAN) {
+                    store = true;
+                    da = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
+                                     __uint_as_float(packNormal(on)));
+                    db = make_float4(flux.x, flux.y, flux.z, __int_as_float(p.id));
+                    if (r0 < m.rr_photon) {
+                        bsdfSample(m, din, on, (float)r1, (float)r2, &nd);
+                        const float inv = (float)(1.0 / m.rr_photon);
+                        flux = flux * refl * inv;
+                    } else {
+                        alive = false;
+                    }
+                } else {
+                    const float pdf = bsdfSample(m, din, on, (float)r0, (float)r1, &nd);
+                    flux = flux * refl * (1.0f / pdf);
+                }
+                p.ox = hp[0]; p.oy = hp[1]; p.oz = hp[2];
+                p.dx = nd.x; p.dy = nd.y; p.dz = nd.z;
+                p.fx = flux.x; p.fy = flux.y; p.fz = flux.z;
+                p.rng[0] = tape.x.s[0]; p.rng[1] = tape.x.s[1]; p.rng[2] = tape.x.s[2]; p.rng[3] = tape.x.s[3];
+                p.bounce += 1;
+            }
+        }
+        const unsigned long long di = warpAppend(store, &ctr->deposits);
+        if (store && (int64_t)di < depCap) {
+            dep[2 * di] = da;
+            dep[2 * di + 1] = db;
+        }
+        const unsigned long long oi = warpAppend(alive, &ctr->queue[qo]);
+        if (alive) out[oi] = p;
+        const unsigned nt = __reduce_add_sync(0xffffffffu, (unsigned)traced);
+        if ((threadIdx.x & 31) == 0 && nt) atomicAdd(&ctr->photonRays, (unsigned long long)nt);
+    }
+}
+
+__device__ __forceinline__ void cameraRay(const CameraDev& c, double px, double py, f3* d) {
+    // PerspectiveCamera::getRay (perspective_camera.cc:42-46)
+    const float a = c.halfTan * c.aspect * (float)(2.0 * px / c.w - 1.0);
+    const float b = c.halfTan * (float)(2.0 * py / c.h - 1.0);
+    const f3 dir = {c.dx + a * c.ux + b * c.vx, c.dy + a * c.uy + b * c.vy, c.dz + a * c.uz + b * c.vz};
+    *d = normalized(dir);
+}
+
+// Eye paths of ProgressivePhotonMappingProb::radiance (ppm_probabilistic.cc:
+// 236-344) without BSSRDF: tail recursion through specular and refractive
+// surfaces, Russian roulette after 3 bounces, a gather query at the first
+// Lambertian hit, the env map on a miss. Environment terms go straight into
+// the accumulation buffer; queries are compacted with one atomic per warp.
+__global__ void __launch_bounds__(128) kEyeTrace(TraceParams tp, SceneView sc, EnvDev env, CameraDev cam,
+                                                 const uint32_t* __restrict__ pixelStates, float* __restrict__ accum,
+                                                 float4* __restrict__ queries, PassCounters* ctr) {
+    __shared__ int order[128];
+    loadOrderTable(order);
+    const int64_t np = (int64_t)cam.w * cam.h;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < np; base += stride) {
+        const int64_t pix = base + threadIdx.x;
+        bool query = false;
+        float4 q0, q1, q2;
+        int traced = 0;
+        if (pix < np) {
+            const int x = (int)(pix % cam.w), y = (int)(pix / cam.w);
+            Tape tape;
+            tape.pos = 0;
+            if (tp.mode == PPPM_MODE_COMPAT) {
+                const uint4 s = *reinterpret_cast<const uint4*>(pixelStates + 4 * pix);
+                tape.x.s[0] = s.x; tape.x.s[1] = s.y; tape.x.s[2] = s.z; tape.x.s[3] = s.w;
+            } else {
+                seedCanonical(tp.seed, tp.pass, (uint64_t)tp.numPaths + (uint64_t)pix, tape.x);
+            }
+            const double px = x + tape.popd() - 0.5;
+            const double py = y + tape.popd() - 0.5;
+            f3 d;
+            cameraRay(cam, px, py, &d);
+            double o[3] = {cam.ex, cam.ey, cam.ez};
+            f3 w = {1.f, 1.f, 1.f}, L = {0.f, 0.f, 0.f};
+            for (int b = 0;; b++) {
+                if (b >= tp.maxBounceEye) {
+                    L = L + w * envLookup(env, d);
+                    break;
+                }
+                double best;
+                traced++;
+                const int slot = traverseExact<true>(sc.nodes, sc.tris, sc.rootCode, o[0], o[1], o[2], d.x, d.y, d.z,
+                                                     order, &best, nullptr, nullptr);
+                if (slot < 0) {
+                    L = L + w * envLookup(env, d);
+                    break;
+                }
+                const double r0 = tape.popd(), r1 = tape.popd(), r2 = tape.popd();
+                const float4 a = sc.tris[3 * slot], bb = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
+                const DevMaterial& m = sc.mats[sc.matId[__float_as_int(a.w)]];
+                double hp[3];
+                hitPosition(o[0], o[1], o[2], d.x, d.y, d.z, best, hp);
+                const f3 nrm = triNormal(a, bb, c);
+                float roul = m.roulette;
+                if (b >= 3) {
+                    if (r0 > (double)roul) break;  // terminated path contributes nothing more
+                } else {
+                    roul = 1.0f;
+                }
+                const f3 refl = {m.refl[0], m.refl[1], m.refl[2]};
+                if (m.type & PPPM_BSDF_LAMBERTIAN) {
+                    const f3 on = dot(nrm, d) < 0.0f ? nrm : -nrm;
+                    const f3 wq = w * refl * (1.0f / roul);
+                    q0 = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
+                                     __int_as_float((int)pix));
+                    q1 = make_float4(on.x, on.y, on.z, 0.f);
+                    q2 = make_float4(wq.x, wq.y, wq.z, 0.f);
+                    query = true;
+                    break;
+                }
+                f3 nd;
+                const float pdf = bsdfSample(m, d, nrm, (float)r1, (float)r2, &nd);
+                w = w * refl * (1.0f / (pdf * roul));
+                o[0] = hp[0]; o[1] = hp[1]; o[2] = hp[2];
+                d = nd;
+            }
+            accum[3 * pix] += L.x;
+            accum[3 * pix + 1] += L.y;
+            accum[3 * pix + 2] += L.z;
+        }
+        const unsigned long long qi = warpAppend(query, &ctr->queries);
+        if (query) {
+            queries[3 * qi] = q0;
+            queries[3 * qi + 1] = q1;
+            queries[3 * qi + 2] = q2;
+        }
+        const unsigned nt = __reduce_add_sync(0xffffffffu, (unsigned)traced);
+        if ((threadIdx.x & 31) == 0 && nt) atomicAdd(&ctr->eyeRays, (unsigned long long)nt);
+    }
+}
+
+__global__ void kStreamCounts(const float4* __restrict__ dep, const unsigned long long* count, int64_t cap, int64_t tpt,
+                              int N, unsigned long long* perStream) {
+    extern __shared__ unsigned long long hist[];
+    for (int s = threadIdx.x; s < N; s += blockDim.x) hist[s] = 0;
+    __syncthreads();
+    const int64_t n = min((int64_t)*count, cap);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int id = __float_as_int(dep[2 * i + 1].w);
+        atomicAdd(&hist[min((int64_t)id / tpt, (int64_t)N - 1)], 1ull);
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < N; s += blockDim.x)
+        if (hist[s]) atomicAdd(&perStream[s], hist[s]);
+}
+
+}  // namespace
+
+cudaError_t launchTapeStates(const TraceParams& tp, const uint32_t* streamStates, const uint32_t* jump, int width,
+                             int height, uint32_t* photonStates, uint32_t* pixelStates, cudaStream_t st) {
+    const int64_t maxRows = (height + tp.numStreams - 1) / tp.numStreams;
+    const int64_t runs = ((tp.taskPerThread + maxRows * width + kRun - 1) / kRun) * tp.numStreams;
+    kTapeStates<<<blocksFor(runs, 128, 152 * 64), 128, 0, st>>>(tp, streamStates, jump, width, height, photonStates,
+                                                                pixelStates);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPhotonEmit(const TraceParams& tp, const EnvDev& env, const uint32_t* photonStates, PathState* queue,
+                             PassCounters* ctr, cudaStream_t st) {
+    kPhotonEmit<<<blocksFor(tp.numPaths, 256), 256, 0, st>>>(tp, env, photonStates, queue, ctr);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
+                               PathState* out, int64_t maxPaths, float4* deposits, int64_t depositCap,
+                               PassCounters* ctr, cudaStream_t st) {
+    kPhotonBounce<<<blocksFor(maxPaths, 128, 152 * 16), 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths, deposits,
+                                                                      depositCap, ctr);
+    return cudaGetLastError();
+}
+
+cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
+                           const uint32_t* pixelStates, float* accum, float4* queries, PassCounters* ctr,
+                           cudaStream_t st) {
+    kEyeTrace<<<blocksFor((int64_t)cam.w * cam.h, 128, 152 * 16), 128, 0, st>>>(tp, sc, env, cam, pixelStates, accum,
+                                                                                 queries, ctr);
+    return cudaGetLastError();
+}
+
+cudaError_t launchStreamCounts(const float4* deposits, const unsigned long long* count, int64_t cap, int64_t tpt,
+                               int numStreams, unsigned long long* perStream, cudaStream_t st) {
+    kStreamCounts<<<152 * 4, 256, numStreams * sizeof(unsigned long long), st>>>(deposits, count, cap, tpt, numStreams,
+                                                                                perStream);
+    return cudaGetLastError();
+}
+
+}  // namespace pppm

@@ -1,0 +1,40 @@
+// Launchers shared between the C-ABI files.
+#pragma once
+
+#include "context.h"
+#include "grid.cuh"
+
+namespace pppm {
+
+constexpr int kMaxKnn = 64;  // largest k of the compat kNN gather
+
+// Query record of the gather: q0 = (pos, pixel bits), q1 = (normal, 0),
+// q2 = (weight = path throughput * refl / roulette, 0).
+struct QueryView {
+    const float4* q;      // 3 float4 per query
+    const uint32_t* count;  // device count (nullptr: use n)
+    int64_t n;
+};
+
+cudaError_t gridLayout(GridBufs& g, const double* bbmin, const double* bbmax, double cell, int64_t nPhotons);
+GridDev gridView(const GridBufs& g, const double* bbmin, const double* bbmax);
+cudaError_t gridBuild(GridBufs& g, const GridDev& view, const float4* rec, const uint64_t* dCount, int64_t capacity,
+                      cudaStream_t st);
+
+// Canonical radius-ball gather. out: per query (accumulate=false, m x 3)
+// or accum[pixel] += (accumulate=true).
+cudaError_t launchGatherCanonical(const GridDev& g, QueryView q, float radius, float* out, bool accumulate,
+                                  cudaStream_t st);
+// Compat kNN gather (ppm_probabilistic.cc:300-335).
+cudaError_t launchGatherCompat(const GridDev& g, QueryView q, int k, float eps, float radius, int64_t phantoms,
+                               float* out, bool accumulate, cudaStream_t st);
+// kNN only (PhotonMap::findKNN): idx in farthest-first order.
+cudaError_t launchKnn(const GridDev& g, const float* queries, int64_t m, int k, float eps, int32_t* idx, int32_t* cnt,
+                      int cap, cudaStream_t st);
+
+// Photon records from plain arrays (pos xyz, flux xyz, normal bits, id).
+cudaError_t launchPackPhotons(const float* in8, int64_t n, float4* rec, uint64_t* count, cudaStream_t st);
+cudaError_t launchPackPositions(const float* pos3, int64_t n, float4* rec, uint64_t* count, cudaStream_t st);
+cudaError_t launchPackQueries(const float* in12, int64_t m, float4* q, cudaStream_t st);
+
+}  // namespace pppm

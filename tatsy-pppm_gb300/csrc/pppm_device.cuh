@@ -1,0 +1,472 @@
+// Device-side data layouts and inner routines shared by the kernels.
+//
+// Exactness policy: every step whose result decides something discrete
+// (which triangle is hit, which bucket a point falls in, Russian roulette,
+// CDF inversion) repeats the reference's own arithmetic with explicitly
+// rounded IEEE operations (no FMA contraction), in float where the
+// reference uses float and in double where it uses double. Continuous
+// shading (directions, fluxes, radiance) runs in FP32.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pppm {
+
+constexpr double kEps = 1.0e-12;    // EPS (common.h:13)
+constexpr double kInfty = 1.0e20;   // INFTY (common.h:12)
+constexpr float kPiF = 3.14159265358979323846f;
+constexpr double kPi = 3.14159265358979323846;
+constexpr int kStackSize = 64;      // traversal stack; the builder caps depth at 20
+constexpr int kMaxBvhDepth = 20;
+
+// ------------------------------------------------------------------ layouts
+// One 4-wide BVH node, 128 bytes (one L2 line). Boxes are the reference's
+// float child boxes (qbvh_accel.cc:178-191) in [x/y/z][child] order.
+// child[i] >= 0: inner node index; < 0: leaf code ~(first_slot << 2 | count).
+struct __align__(16) QNode {
+    float4 bmin[3];  // bmin[d] = (child0..3) min along axis d
+    float4 bmax[3];
+    int4 child;
+    int4 meta;  // x: sepAxes packed (sep0 | sep1 << 2 | sep2 << 4), y,z,w unused
+};
+static_assert(sizeof(QNode) == 128, "QNode must be one 128-byte line");
+
+// Leaf triangles are 3 float4 (p0,p1,p2); p0.w holds the original id bits.
+__host__ __device__ inline int leafCode(int slot, int count) { return ~((slot << 2) | count); }
+
+struct DevMaterial {
+    int type;        // BsdfType bitmask including the BSSRDF bit
+    float refl[3];
+    float phong_n;
+    float roulette;  // max(refl) (ppm_probabilistic.cc:261)
+    double rr_photon;  // (r+g+b)/3.0 in double (ppm_probabilistic.cc:177)
+    // dipole (bssrdf.cc:48-63), derived on the host in double
+    float A, eta, scale, fdr;
+    float sigma_tr[3], alphap[3], zpos[3], zneg[3];
+    float pad[2];
+};
+
+struct EnvDev {
+    const float* rgb;    // w*h*3
+    const double* cdf;   // 4096
+    const double* pdf;   // 4096
+    int w, h;
+    double area_over_p;  // area / numPhotons is applied per pass
+};
+
+// ------------------------------------------------------------------ RNG
+// XorShift128 of the reference (random.h:16-62).
+struct XorShift {
+    uint32_t s[4];
+    __host__ __device__ inline void seed(uint32_t init) {
+        uint32_t v = init;
+        for (int i = 1; i <= 4; i++) { v = 1812433253u * (v ^ (v >> 30)) + (uint32_t)i; s[i - 1] = v; }
+    }
+    __host__ __device__ inline uint32_t next() {
+        const uint32_t t = s[0] ^ (s[0] << 11);
+        s[0] = s[1]; s[1] = s[2]; s[2] = s[3];
+        s[3] = (s[3] ^ (s[3] >> 19)) ^ (t ^ (t >> 8));
+        return s[3];
+    }
+};
+
+// nextReal() = next() * (float)(1/UINT_MAX) = next() * 2^-32 exactly (random.h:45-47)
+__host__ __device__ inline double u32ToReal(uint32_t x) { return (double)x * 2.3283064365386963e-10; }
+
+// A 200-number tape consumed in order (RandomSequence, random_sequence.h).
+struct Tape {
+    XorShift x;
+    int pos;
+    __device__ inline double popd() { pos++; return u32ToReal(x.next()); }
+    __device__ inline float popf() { return (float)popd(); }
+};
+
+// ------------------------------------------------------------------ vectors
+struct f3 { float x, y, z; };
+__device__ inline f3 mk(float x, float y, float z) { return {x, y, z}; }
+__device__ inline f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ inline f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ inline f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ inline f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ inline f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ inline float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ inline f3 cross(f3 u, f3 v) { return {u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x}; }
+// Vector3D::normalized divides by (norm + EPS) (vector3d.cc:63-65)
+__device__ inline f3 normalized(f3 v) { return v * (1.0f / (sqrtf(dot(v, v)) + 1e-12f)); }
+__device__ inline f3 reflect(f3 v, f3 n) { return v - n * (2.0f * dot(n, v)); }
+__device__ inline float maxc(f3 v) { return fmaxf(v.x, fmaxf(v.y, v.z)); }
+
+// ------------------------------------------------------------------ exact geometry
+// Moller-Trumbore in double with the reference's operation order
+// (triangle.cc:53-78); every product and sum is an explicitly rounded IEEE
+// double op so the result is bit-identical to the reference.
+__device__ __forceinline__ bool triHitExact(double ox, double oy, double oz, double dx, double dy, double dz,
+                                            const float4& a, const float4& b, const float4& c, double* tOut) {
+    const double p0x = a.x, p0y = a.y, p0z = a.z;
+    const double e1x = __dsub_rn((double)b.x, p0x), e1y = __dsub_rn((double)b.y, p0y), e1z = __dsub_rn((double)b.z, p0z);
+    const double e2x = __dsub_rn((double)c.x, p0x), e2y = __dsub_rn((double)c.y, p0y), e2z = __dsub_rn((double)c.z, p0z);
+    // pVec = cross(d, e2)
+    const double px = __dsub_rn(__dmul_rn(dy, e2z), __dmul_rn(dz, e2y));
+    const double py = __dsub_rn(__dmul_rn(dz, e2x), __dmul_rn(dx, e2z));
+    const double pz = __dsub_rn(__dmul_rn(dx, e2y), __dmul_rn(dy, e2x));
+    const double det = __dadd_rn(__dadd_rn(__dmul_rn(e1x, px), __dmul_rn(e1y, py)), __dmul_rn(e1z, pz));
+    if (det > -kEps && det < kEps) return false;
+    const double invdet = __drcp_rn(det);  // == 1.0 / det, correctly rounded
+    const double tx = __dsub_rn(ox, p0x), ty = __dsub_rn(oy, p0y), tz = __dsub_rn(oz, p0z);
+    const double u = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(tx, px), __dmul_rn(ty, py)), __dmul_rn(tz, pz)), invdet);
+    if (u < 0.0 || u > 1.0) return false;
+    // qVec = cross(tVec, e1)
+    const double qx = __dsub_rn(__dmul_rn(ty, e1z), __dmul_rn(tz, e1y));
+    const double qy = __dsub_rn(__dmul_rn(tz, e1x), __dmul_rn(tx, e1z));
+    const double qz = __dsub_rn(__dmul_rn(tx, e1y), __dmul_rn(ty, e1x));
+    const double v = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, qx), __dmul_rn(dy, qy)), __dmul_rn(dz, qz)), invdet);
+    if (v < 0.0 || __dadd_rn(u, v) > 1.0) return false;
+    const double t = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(e2x, qx), __dmul_rn(e2y, qy)), __dmul_rn(e2z, qz)), invdet);
+    if (t > kEps) { *tOut = t; return true; }
+    return false;
+}
+
+// Conservative FP32 pre-test for triHitExact. Returns false only when the
+// exact double test is certain to reject the triangle or to produce a
+// distance that cannot beat `best` (the caller's current closest hit);
+// returns true when the exact test must decide. Rounding-error bounds follow
+// the standard a-priori bound |fl(x) - x| <= gamma_k * S where S is the same
+// expression evaluated on absolute values (Higham, Accuracy and Stability of
+// Numerical Algorithms, ch. 3); gamma is inflated well above the tight
+// value so the double reference's own rounding (2^-53) is covered too.
+__device__ __forceinline__ bool triMayHit(float ox, float oy, float oz, float dx, float dy, float dz,
+                                          const float4& a, const float4& b, const float4& c, float best) {
+    const float kG = 3.0e-6f;  // ~ 48 * 2^-24
+    const float e1x = b.x - a.x, e1y = b.y - a.y, e1z = b.z - a.z;
+    const float e2x = c.x - a.x, e2y = c.y - a.y, e2z = c.z - a.z;
+    const float ae1x = fabsf(e1x), ae1y = fabsf(e1y), ae1z = fabsf(e1z);
+    const float ae2x = fabsf(e2x), ae2y = fabsf(e2y), ae2z = fabsf(e2z);
+    const float adx = fabsf(dx), ady = fabsf(dy), adz = fabsf(dz);
+    const float px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
+    const float apx = ady * ae2z + adz * ae2y, apy = adz * ae2x + adx * ae2z, apz = adx * ae2y + ady * ae2x;
+    const float det = e1x * px + e1y * py + e1z * pz;
+    const float sdet = ae1x * apx + ae1y * apy + ae1z * apz;
+    const float edet = kG * sdet + 2e-12f;
+    if (fabsf(det) <= edet) return true;  // sign or EPS test undecided
+    const float tx = ox - a.x, ty = oy - a.y, tz = oz - a.z;
+    const float atx = fabsf(tx), aty = fabsf(ty), atz = fabsf(tz);
+    const float nu = tx * px + ty * py + tz * pz;
+    const float enu = kG * (atx * apx + aty * apy + atz * apz);
+    const float qx = ty * e1z - tz * e1y, qy = tz * e1x - tx * e1z, qz = tx * e1y - ty * e1x;
+    const float aqx = aty * ae1z + atz * ae1y, aqy = atz * ae1x + atx * ae1z, aqz = atx * ae1y + aty * ae1x;
+    const float nv = dx * qx + dy * qy + dz * qz;
+    const float env_ = kG * (adx * aqx + ady * aqy + adz * aqz);
+    const float nt = e2x * qx + e2y * qy + e2z * qz;
+    const float ent = kG * (ae2x * aqx + ae2y * aqy + ae2z * aqz);
+    // Work with det > 0 by flipping the numerators' signs.
+    const float s = det > 0.0f ? 1.0f : -1.0f;
+    const float D = det * s, U = nu * s, V = nv * s, T = nt * s;
+    // u < 0, v < 0, u > 1, u + v > 1, t <= 0 certain -> reject
+    if (U < -enu) return false;
+    if (V < -env_) return false;
+    if (U - D > enu + edet) return false;
+    if (U + V - D > enu + env_ + edet + kG * (fabsf(U) + fabsf(V) + D)) return false;
+    if (T < -ent) return false;
+    // t certainly not below best: cannot become the closest hit
+    const float lo = (T - ent) / (D + edet);
+    if (lo > best * (1.0f + 1e-5f)) return false;
+    return true;
+}
+
+// orderTable of qbvh_accel.cc:21-39: for each (hitMask, sepMask) the child
+// visiting order as nibbles, 0x4 terminating. Indexed [hitMask * 8 + sepMask].
+static __device__ __constant__ int kOrderTableDev[128] = {
+    0x44444, 0x44444, 0x44444, 0x44444, 0x44444, 0x44444, 0x44444, 0x44444,
+    0x44440, 0x44440, 0x44440, 0x44440, 0x44440, 0x44440, 0x44440, 0x44440,
+    0x44441, 0x44441, 0x44441, 0x44441, 0x44441, 0x44441, 0x44441, 0x44441,
+    0x44401, 0x44401, 0x44410, 0x44410, 0x44401, 0x44401, 0x44410, 0x44410,
+    0x44442, 0x44442, 0x44442, 0x44442, 0x44442, 0x44442, 0x44442, 0x44442,
+    0x44402, 0x44402, 0x44402, 0x44402, 0x44420, 0x44420, 0x44420, 0x44420,
+    0x44412, 0x44412, 0x44412, 0x44412, 0x44421, 0x44421, 0x44421, 0x44421,
+    0x44012, 0x44012, 0x44102, 0x44102, 0x44201, 0x44201, 0x44210, 0x44210,
+    0x44443, 0x44443, 0x44443, 0x44443, 0x44443, 0x44443, 0x44443, 0x44443,
+    0x44403, 0x44403, 0x44403, 0x44403, 0x44430, 0x44430, 0x44430, 0x44430,
+    0x44413, 0x44413, 0x44413, 0x44413, 0x44431, 0x44431, 0x44431, 0x44431,
+    0x44013, 0x44013, 0x44103, 0x44103, 0x44301, 0x44301, 0x44310, 0x44310,
+    0x44423, 0x44432, 0x44423, 0x44432, 0x44423, 0x44432, 0x44423, 0x44432,
+    0x44023, 0x44032, 0x44023, 0x44032, 0x44230, 0x44320, 0x44230, 0x44320,
+    0x44123, 0x44132, 0x44123, 0x44132, 0x44231, 0x44321, 0x44231, 0x44321,
+    0x40123, 0x40132, 0x41023, 0x41032, 0x42301, 0x43201, 0x42310, 0x43210,
+};
+
+__device__ __forceinline__ void loadOrderTable(int* s) {
+    for (int i = threadIdx.x; i < 128; i += blockDim.x) s[i] = kOrderTableDev[i];
+    __syncthreads();
+}
+
+
+// Closest hit over the QBVH, reproducing QBVHAccel::intersect
+// (qbvh_accel.cc:205-285): float slab test with SSE max/min semantics,
+// orderTable child order, LIFO stack, leaf triangles in stored order with a
+// strict `<` update. orderTab points at a shared-memory copy of the table.
+// Returns the triangle slot or -1 and the hit distance in *bestOut.
+template <bool kPrefilter>
+__device__ __forceinline__ int traverseExact(const QNode* __restrict__ nodes, const float4* __restrict__ tris, int rootCode,
+                                             double odx, double ody, double odz, float dx, float dy, float dz,
+                                             const int* orderTab, double* bestOut, int* nodeVisits, int* triTests) {
+    // the slab test runs on the float-rounded origin (qbvh_accel.cc:211-213),
+    // the triangle test on the double origin
+    const float ox = __double2float_rn(odx), oy = __double2float_rn(ody), oz = __double2float_rn(odz);
+    const double ddx = dx, ddy = dy, ddz = dz;
+    // idir = dir == 0 ? 1e20f : (float)(1.0 / dir)  (qbvh_accel.cc:219-221);
+    // rounding 1/d to double then to float equals a correctly rounded float
+    // reciprocal (double rounding is innocuous for p' >= 2p + 2).
+    const float idx = dx == 0.0f ? 1.0e20f : __frcp_rn(dx);
+    const float idy = dy == 0.0f ? 1.0e20f : __frcp_rn(dy);
+    const float idz = dz == 0.0f ? 1.0e20f : __frcp_rn(dz);
+    const int sx = idx > 0.0f ? 0 : 1, sy = idy > 0.0f ? 0 : 1, sz = idz > 0.0f ? 0 : 1;
+    const int sgnBits = sx | (sy << 1) | (sz << 2);
+
+    int stack[kStackSize];
+    int sp = 0;
+    stack[sp++] = rootCode;
+    double best = kInfty;
+    int hit = -1;
+    int visits = 0, tests = 0;
+    while (sp > 0) {
+        const int code = stack[--sp];
+        if (code < 0) {
+            const int lc = ~code;
+            const int first = lc >> 2, cnt = lc & 3;
+            for (int i = 0; i < cnt; i++) {
+                const float4 a = tris[3 * (first + i)], b = tris[3 * (first + i) + 1], c = tris[3 * (first + i) + 2];
+                tests++;
+                if (kPrefilter && !triMayHit(ox, oy, oz, dx, dy, dz, a, b, c, (float)best)) continue;
+                double t;
+                if (triHitExact(odx, ody, odz, ddx, ddy, ddz, a, b, c, &t) && best > t) {
+                    best = t;
+                    hit = first + i;
+                }
+            }
+            continue;
+        }
+        visits++;
+        const QNode* nd = nodes + code;
+        const float hd = __double2float_rn(best);
+        float tmin[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        float tmax[4] = {hd, hd, hd, hd};
+        const float o3[3] = {ox, oy, oz};
+        const float i3[3] = {idx, idy, idz};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const float4 lo = __ldg(&nd->bmin[d]);
+            const float4 hi = __ldg(&nd->bmax[d]);
+            const bool neg = (sgnBits >> d) & 1;
+            const float4 nearB = neg ? hi : lo;
+            const float4 farB = neg ? lo : hi;
+            const float nb[4] = {nearB.x, nearB.y, nearB.z, nearB.w};
+            const float fb[4] = {farB.x, farB.y, farB.z, farB.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float t0 = __fmul_rn(__fsub_rn(nb[k], o3[d]), i3[d]);
+                const float t1 = __fmul_rn(__fsub_rn(fb[k], o3[d]), i3[d]);
+                tmin[k] = tmin[k] > t0 ? tmin[k] : t0;  // _mm_max_ps(tMin, t0)
+                tmax[k] = tmax[k] < t1 ? tmax[k] : t1;  // _mm_min_ps(tMax, t1)
+            }
+        }
+        int hitMask = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) hitMask |= (tmax[k] >= tmin[k]) ? (1 << k) : 0;
+        if (hitMask != 0) {
+            const int4 ch = __ldg(&nd->child);
+            const int meta = __ldg(&nd->meta.x);
+            const int a0 = meta & 3, a1 = (meta >> 2) & 3, a2 = (meta >> 4) & 3;
+            const int sepMask = (((sgnBits >> a0) & 1) << 2) | (((sgnBits >> a1) & 1) << 1) | ((sgnBits >> a2) & 1);
+            int ord = orderTab[hitMask * 8 + sepMask];
+            const int c4[4] = {ch.x, ch.y, ch.z, ch.w};
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                if (ord & 0x04) break;
+                stack[sp++] = c4[ord & 0x03];
+                ord >>= 4;
+            }
+        }
+    }
+    *bestOut = best;
+    if (nodeVisits) *nodeVisits += visits;
+    if (triTests) *triTests += tests;
+    return hit;
+}
+
+// Hit record of the exact path: position o + t*d and the triangle's
+// normal cross(p1-p0, p2-p0).normalized() computed in double like
+// Triangle::normal (triangle.cc:45-47), rounded to float.
+__device__ inline void hitPosition(double ox, double oy, double oz, float dx, float dy, float dz, double t, double* p) {
+    p[0] = __dadd_rn(ox, __dmul_rn((double)dx, t));
+    p[1] = __dadd_rn(oy, __dmul_rn((double)dy, t));
+    p[2] = __dadd_rn(oz, __dmul_rn((double)dz, t));
+}
+
+__device__ inline f3 triNormal(const float4& a, const float4& b, const float4& c) {
+    const double e1x = (double)b.x - a.x, e1y = (double)b.y - a.y, e1z = (double)b.z - a.z;
+    const double e2x = (double)c.x - a.x, e2y = (double)c.y - a.y, e2z = (double)c.z - a.z;
+    const double cx = __dsub_rn(__dmul_rn(e1y, e2z), __dmul_rn(e1z, e2y));
+    const double cy = __dsub_rn(__dmul_rn(e1z, e2x), __dmul_rn(e1x, e2z));
+    const double cz = __dsub_rn(__dmul_rn(e1x, e2y), __dmul_rn(e1y, e2x));
+    const double nn = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(cx, cx), __dmul_rn(cy, cy)), __dmul_rn(cz, cz)));
+    const double inv = __drcp_rn(__dadd_rn(nn, kEps));
+    return {__double2float_rn(__dmul_rn(cx, inv)), __double2float_rn(__dmul_rn(cy, inv)), __double2float_rn(__dmul_rn(cz, inv))};
+}
+
+__device__ inline void hitRecord(double ox, double oy, double oz, float dx, float dy, float dz, double t, const float4& a,
+                                 const float4& b, const float4& c, f3* pos, f3* nrm) {
+    double p[3];
+    hitPosition(ox, oy, oz, dx, dy, dz, t, p);
+    pos->x = __double2float_rn(p[0]);
+    pos->y = __double2float_rn(p[1]);
+    pos->z = __double2float_rn(p[2]);
+    *nrm = triNormal(a, b, c);
+}
+
+// ------------------------------------------------------------------ hashing
+// HashGrid::hash (hash_grid_detail.h:60-63): 32-bit wrapping products,
+// XOR, unsigned modulo.
+__host__ __device__ inline uint32_t refHash(int ix, int iy, int iz, uint32_t size) {
+    const uint32_t h = ((uint32_t)ix * 73856093u) ^ ((uint32_t)iy * 19349663u) ^ ((uint32_t)iz * 83492791u);
+    return h % size;
+}
+
+// Octahedral normal packing (2 x 16-bit) for photon records.
+__device__ inline uint32_t packNormal(f3 n) {
+    const float l1 = fabsf(n.x) + fabsf(n.y) + fabsf(n.z) + 1e-20f;
+    float u = n.x / l1, v = n.y / l1;
+    if (n.z < 0.0f) {
+        const float pu = (1.0f - fabsf(v)) * (u >= 0.0f ? 1.0f : -1.0f);
+        const float pv = (1.0f - fabsf(u)) * (v >= 0.0f ? 1.0f : -1.0f);
+        u = pu; v = pv;
+    }
+    const uint32_t qu = (uint32_t)__float2int_rn((fminf(fmaxf(u, -1.0f), 1.0f) * 0.5f + 0.5f) * 65535.0f);
+    const uint32_t qv = (uint32_t)__float2int_rn((fminf(fmaxf(v, -1.0f), 1.0f) * 0.5f + 0.5f) * 65535.0f);
+    return qu | (qv << 16);
+}
+__device__ inline f3 unpackNormal(uint32_t p) {
+    const float u = (float)(p & 0xffffu) / 65535.0f * 2.0f - 1.0f;
+    const float v = (float)(p >> 16) / 65535.0f * 2.0f - 1.0f;
+    f3 n = {u, v, 1.0f - fabsf(u) - fabsf(v)};
+    if (n.z < 0.0f) {
+        const float ox = n.x;
+        n.x = (1.0f - fabsf(n.y)) * (ox >= 0.0f ? 1.0f : -1.0f);
+        n.y = (1.0f - fabsf(ox)) * (n.y >= 0.0f ? 1.0f : -1.0f);
+    }
+    return normalized(n);
+}
+
+// ------------------------------------------------------------------ sampling
+// sampler::onHemisphere (sampler.cc:17-32)
+__device__ inline f3 onHemisphere(f3 w, float r1, float r2) {
+    f3 u = fabsf(w.x) > 1e-12f ? cross(mk(0.f, 1.f, 0.f), w) : cross(mk(1.f, 0.f, 0.f), w);
+    u = normalized(u);
+    const f3 v = cross(w, u);
+    float st, ct;
+    sincosf(2.0f * kPiF * r1, &st, &ct);
+    const float z2s = sqrtf(r2);
+    return normalized(u * (ct * z2s) + v * (st * z2s) + w * sqrtf(1.0f - r2));
+}
+
+// BSDF::sample dispatch (brdf.cc:23-142, reflectance.h:7-34). `normal` is
+// whatever the calling reference code passes (oriented in tracePhotons,
+// geometric in radiance). Returns the pdf written by the reference (1.0
+// where it leaves the caller's initial value).
+__device__ inline float bsdfSample(const DevMaterial& m, f3 in, f3 normal, float r1, float r2, f3* out) {
+    const int t = m.type & 0x0f;
+    if (t == 0x01) {  // Lambertian
+        const f3 on = dot(in, normal) < 0.0f ? normal : -normal;
+        *out = onHemisphere(on, r1, r2);
+        return 1.0f;
+    }
+    if (t == 0x02) {  // specular
+        const f3 on = dot(in, normal) < 0.0f ? normal : -normal;
+        *out = reflect(in, on);
+        return 1.0f;
+    }
+    if (t == 0x04) {  // Phong lobe
+        const f3 on = dot(in, normal) < 0.0f ? normal : -normal;
+        const f3 w = reflect(in, on);
+        f3 u = fabsf(w.x) > 1e-12f ? cross(mk(0.f, 1.f, 0.f), w) : cross(mk(1.f, 0.f, 0.f), w);
+        u = normalized(u);
+        const f3 v = cross(w, u);
+        const float theta = acosf(powf(r1, 1.0f / (m.phong_n + 1.0f)));
+        const float phi = 2.0f * kPiF * r2;
+        float sth, cth, sph, cph;
+        sincosf(theta, &sth, &cth);
+        sincosf(phi, &sph, &cph);
+        *out = u * (sth * cph) + w * cth + v * (sth * sph);
+        return 1.0f;
+    }
+    // refraction, IOR 1.5 fixed (common.h:16)
+    bool into = true;
+    f3 on = normal;
+    if (dot(in, normal) >= 0.0f) { into = false; on = -normal; }
+    const f3 rdir = reflect(in, normal);
+    const float nnt = into ? (1.0f / 1.5f) : 1.5f;
+    const float ddn = dot(in, on);
+    const float cos2t = 1.0f - nnt * nnt * (1.0f - ddn * ddn);
+    if (cos2t < 0.0f) { *out = rdir; return 1.0f; }
+    const f3 tdir = normalized(in * nnt - normal * (into ? 1.0f : -1.0f) * (ddn * nnt + sqrtf(cos2t)));
+    const float R0 = 0.04f;  // ((1.5-1)/(1.5+1))^2
+    const float c = 1.0f - (into ? -ddn : dot(tdir, -on));
+    const float Re = R0 + (1.0f - R0) * (c * c * c * c * c);
+    const float Tr = 1.0f - Re;
+    const float p = 0.5f;  // 0.25 + 0.5 * REFLECT_PROBABILITY
+    if (r1 < p) { *out = rdir; return p / Re; }
+    *out = tdir;
+    return (1.0f - p) / Tr;
+}
+
+// Envmap::sampleFromDir (envmap.cc:11-17,47-60), nearest texel.
+__device__ inline f3 envLookup(const EnvDev& e, f3 d) {
+    const float theta = acosf(fminf(fmaxf(d.y, -1.0f), 1.0f));
+    float phi = atan2f(d.z, d.x);
+    if (phi < 0.0f) phi += 2.0f * kPiF;
+    int ix = (int)(phi / (2.0f * kPiF) * (float)e.w);
+    int iy = (int)(theta / kPiF * (float)e.h);
+    ix = min(max(ix, 0), e.w - 1);
+    iy = min(max(iy, 0), e.h - 1);
+    const float* p = e.rgb + 3 * ((size_t)iy * e.w + ix);
+    return {p[0], p[1], p[2]};
+}
+
+// Envmap::samplePhoton (envmap.cc:62-86) followed by the cosine hemisphere
+// draw of tracePhotons (ppm_probabilistic.cc:137-144). The CDF inversion is
+// std::lower_bound over the double CDF, done in double. Returns false when
+// the draw lies past the last CDF entry, where the reference indexes _pdf
+// out of bounds. emitDir: the sampled env direction (photon origin is
+// 50 * emitDir); dir: the first ray direction.
+__device__ inline bool emitPhoton(const EnvDev& e, Tape& tp, double numPhotons, f3* emitDir, f3* dir, f3* flux) {
+    const double r = tp.popd();
+    int lo = 0, hi = 4096;  // first index with cdf[i] >= r
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&e.cdf[mid]) < r) lo = mid + 1; else hi = mid;
+    }
+    const int index = lo;
+    const int ix = index % 64, iy = index / 64;
+    const float u = (float)(((double)ix + tp.popd()) / 64.0);
+    const float v = (float)(((double)iy + tp.popd()) / 64.0);
+    const float phi = u * kPiF * 2.0f;
+    const float y = (1.0f - v) * 2.0f - 1.0f;
+    const float sxz = sqrtf(fmaxf(0.0f, 1.0f - y * y));
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    const f3 d = {sxz * cp, y, sxz * sp};
+    const double area = ((double)e.w * (double)e.h) / (4.0 * kPi * 64.0 * 64.0);
+    const double pdf = __ldg(&e.pdf[min(index, 4095)]);
+    const float scale = (float)(area / (pdf * numPhotons));
+    *flux = envLookup(e, d) * scale;
+    *emitDir = d;
+    // onHemisphere(normalLight, &nextDir, rseq.pop(), rseq.pop()): the
+    // reference build evaluates these arguments right to left, so the first
+    // number drawn becomes r2 and the second r1.
+    const float r2 = tp.popf();
+    const float r1 = tp.popf();
+    *dir = onHemisphere(-d, r1, r2);
+    return index < 4096;
+}
+
+}  // namespace pppm

@@ -1,0 +1,383 @@
+// Render loop (ProgressivePhotonMappingProb::render, ppm_probabilistic.cc:
+// 24-121) and the stage entry points for kNN and gather.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "trace.h"
+
+namespace pppm {
+
+namespace {
+
+void hostBbox(const float* p, int64_t n, double* mn, double* mx) {
+    for (int d = 0; d < 3; d++) { mn[d] = 1e30; mx[d] = -1e30; }
+    for (int64_t i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) {
+            mn[d] = std::min(mn[d], (double)p[3 * i + d]);
+            mx[d] = std::max(mx[d], (double)p[3 * i + d]);
+        }
+    if (n == 0)
+        for (int d = 0; d < 3; d++) { mn[d] = 0; mx[d] = 1; }
+}
+
+// Positions (stride floats apart) to host, for the grid extent.
+int fetchPositions(pppm_ctx* c, const float* src, int64_t n, int stride, std::vector<float>* out) {
+    out->resize((size_t)n * 3);
+    if (n == 0) return PPPM_OK;
+    std::vector<float> all((size_t)n * stride);
+    if (isDevicePtr(src)) {
+        PPPM_CUDA(c, cudaMemcpyAsync(all.data(), src, all.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+        PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    } else {
+        std::memcpy(all.data(), src, all.size() * 4);
+    }
+    for (int64_t i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) (*out)[3 * i + d] = all[(size_t)i * stride + d];
+    return PPPM_OK;
+}
+
+double knnCell(const double* mn, const double* mx, int64_t n, int k) {
+    const double ex = std::max({mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2], 1e-6});
+    const double frac = std::min(1.0, (double)std::max(k, 1) / (double)std::max<int64_t>(n, 1));
+    return ex * std::cbrt(frac);
+}
+
+}  // namespace
+
+}  // namespace pppm
+
+using namespace pppm;
+
+extern "C" {
+
+int pppm_knn(pppm_ctx* c, const float* photonPos, int64_t n, const float* queries, int64_t m, int32_t numTarget,
+             double targetRadius, int32_t* idx, int32_t* cnt, int32_t cap) {
+    if (!c || n < 0 || m < 0 || cap < 0 || (n > 0 && !photonPos) || (m > 0 && (!queries || !cnt || (cap > 0 && !idx))))
+        return fail(c, PPPM_E_ARG, "knn: bad arguments");
+    // KnnQuery(type, epsilon, k) receives (numTargetPhotons, targetRadius):
+    // k = (int)targetRadius, epsilon = numTargetPhotons (photon_map.cc:25, kdtree.h:17)
+    const int k = (int)targetRadius;
+    const float eps = (float)numTarget;
+    if (k < 1) return fail(c, PPPM_E_UNDEFINED, "knn: k = (int)radius < 1 pops an empty queue in the reference");
+    if (k > kMaxKnn) return fail(c, PPPM_E_CAPACITY, "knn: k above 64");
+    if (m == 0) return PPPM_OK;
+    cudaSetDevice(c->device);
+    std::vector<float> hp;
+    int r;
+    if ((r = fetchPositions(c, photonPos, n, 3, &hp))) return r;
+    double mn[3], mx[3];
+    hostBbox(hp.data(), n, mn, mx);
+    const void *dp, *dq;
+    void *didx, *dcnt;
+    if ((r = stageIn(c, photonPos, (size_t)n * 12, 0, &dp))) return r;
+    if ((r = stageIn(c, queries, (size_t)m * 12, 1, &dq))) return r;
+    if ((r = stageOut(c, idx, (size_t)m * cap * 4, 2, &didx))) return r;
+    if ((r = stageOut(c, cnt, (size_t)m * 4, 3, &dcnt))) return r;
+    PPPM_CUDA(c, c->stageRec.ensure((size_t)std::max<int64_t>(n, 1) * 32));
+    PPPM_CUDA(c, c->stageCount.ensure(64));
+    PPPM_CUDA(c, launchPackPositions((const float*)dp, n, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), c->stream));
+    PPPM_CUDA(c, gridLayout(c->stageGrid, mn, mx, knnCell(mn, mx, n, k), n));
+    GridDev gv = gridView(c->stageGrid, mn, mx);
+    PPPM_CUDA(c, gridBuild(c->stageGrid, gv, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), n, c->stream));
+    gv = gridView(c->stageGrid, mn, mx);
+    PPPM_CUDA(c, launchKnn(gv, (const float*)dq, m, k, eps, (int32_t*)didx, (int32_t*)dcnt, cap, c->stream));
+    if ((r = finishOut(c, idx, didx, (size_t)m * cap * 4))) return r;
+    if ((r = finishOut(c, cnt, dcnt, (size_t)m * 4))) return r;
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PPPM_OK;
+}
+
+int pppm_gather(pppm_ctx* c, int32_t mode, const float* photons, int64_t n, int64_t phantoms, const float* queries,
+                int64_t m, double radius, int32_t gatherPhotons, float* out) {
+    if (!c || n < 0 || m < 0 || phantoms < 0 || (n > 0 && !photons) || (m > 0 && (!queries || !out)) ||
+        (mode != PPPM_MODE_COMPAT && mode != PPPM_MODE_CANONICAL) || !(radius > 0.0))
+        return fail(c, PPPM_E_ARG, "gather: bad arguments");
+    const int k = (int)radius;
+    if (mode == PPPM_MODE_COMPAT) {
+        if (k < 1) return fail(c, PPPM_E_UNDEFINED, "gather: k = (int)radius < 1 pops an empty queue in the reference");
+        if (k > kMaxKnn) return fail(c, PPPM_E_CAPACITY, "gather: k above 64");
+    }
+    if (m == 0) return PPPM_OK;
+    cudaSetDevice(c->device);
+    std::vector<float> hp;
+    int r;
+    if ((r = fetchPositions(c, photons, n, 8, &hp))) return r;
+    double mn[3], mx[3];
+    hostBbox(hp.data(), n, mn, mx);
+    const void *dp, *dq;
+    void* dout;
+    if ((r = stageIn(c, photons, (size_t)n * 32, 0, &dp))) return r;
+    if ((r = stageIn(c, queries, (size_t)m * 48, 1, &dq))) return r;
+    if ((r = stageOut(c, out, (size_t)m * 12, 2, &dout))) return r;
+    PPPM_CUDA(c, c->stageRec.ensure((size_t)std::max<int64_t>(n, 1) * 32));
+    PPPM_CUDA(c, c->stageQ.ensure((size_t)m * 48));
+    PPPM_CUDA(c, c->stageCount.ensure(64));
+    PPPM_CUDA(c, launchPackPhotons((const float*)dp, n, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), c->stream));
+    PPPM_CUDA(c, launchPackQueries((const float*)dq, m, c->stageQ.as<float4>(), c->stream));
+    const double cell = mode == PPPM_MODE_CANONICAL ? radius : knnCell(mn, mx, n, k);
+    PPPM_CUDA(c, gridLayout(c->stageGrid, mn, mx, cell, n));
+    GridDev gv = gridView(c->stageGrid, mn, mx);
+    PPPM_CUDA(c, gridBuild(c->stageGrid, gv, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), n, c->stream));
+    gv = gridView(c->stageGrid, mn, mx);
+    QueryView qv{c->stageQ.as<float4>(), nullptr, m};
+    if (mode == PPPM_MODE_CANONICAL)
+        PPPM_CUDA(c, launchGatherCanonical(gv, qv, (float)radius, (float*)dout, false, c->stream));
+    else
+        PPPM_CUDA(c, launchGatherCompat(gv, qv, k, (float)gatherPhotons, (float)radius, phantoms, (float*)dout, false,
+                                        c->stream));
+    if ((r = finishOut(c, out, dout, (size_t)m * 12))) return r;
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PPPM_OK;
+}
+
+int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* par) {
+    if (!c || !cam || !par) return fail(c, PPPM_E_ARG, "render_begin: null argument");
+    if (!c->hasScene) return fail(c, PPPM_E_STATE, "render_begin: no scene");
+    // The default Scene env map has no importance tables (scene.cc:11-12):
+    // photon emission would read an empty CDF.
+    if (!c->hasEnv) return fail(c, PPPM_E_STATE, "render_begin: no env map (the only light of the reference)");
+    if (c->anyBssrdf) return fail(c, PPPM_E_STATE, "render_begin: BSSRDF materials need pppm_subsurface_* first");
+    if (par->mode != PPPM_MODE_COMPAT && par->mode != PPPM_MODE_CANONICAL)
+        return fail(c, PPPM_E_ARG, "render_begin: unknown mode");
+    if (par->num_streams < 1 || par->num_streams > 4096 || par->photons < 1 || cam->width < 1 || cam->height < 1 ||
+        par->max_bounce_photon < 0 || par->max_bounce_eye < 0 || !(par->alpha > 0.0) || !(par->radius_scale > 0.0))
+        return fail(c, PPPM_E_ARG, "render_begin: bad parameters");
+    cudaSetDevice(c->device);
+    RenderState& rs = c->rs;
+    rs.active = false;
+    rs.cam = *cam;
+    rs.par = *par;
+    if (!(rs.par.cell_factor >= 1.0f)) rs.par.cell_factor = 1.0f;
+    const double dx = c->bbmax[0] - c->bbmin[0], dy = c->bbmax[1] - c->bbmin[1], dz = c->bbmax[2] - c->bbmin[2];
+    rs.bboxDiag = std::sqrt(dx * dx + dy * dy + dz * dz);
+    rs.radius = rs.bboxDiag * par->radius_scale;  // ppm_probabilistic.cc:51-55
+    const int N = par->num_streams;
+    rs.taskPerThread = par->mode == PPPM_MODE_COMPAT ? (par->photons + N - 1) / N : par->photons;
+    const int64_t paths = par->mode == PPPM_MODE_COMPAT ? rs.taskPerThread * N : par->photons;
+    const int64_t pixels = (int64_t)cam->width * cam->height;
+    rs.streams.assign(N, XorShift());
+    for (int i = 0; i < N; i++) rs.streams[i].seed((uint32_t)i);  // Random::generateSampler(i)
+    if (par->mode == PPPM_MODE_COMPAT) {
+        if (c->jumpTables.empty()) xorshiftJumpTables(&c->jumpTables);
+        PPPM_CUDA(c, rs.jumpMats.ensure(c->jumpTables.size() * 4));
+        PPPM_CUDA(c, cudaMemcpy(rs.jumpMats.p, c->jumpTables.data(), c->jumpTables.size() * 4, cudaMemcpyHostToDevice));
+        PPPM_CUDA(c, rs.tapeStates.ensure((size_t)(paths + pixels) * 16));
+    }
+    PPPM_CUDA(c, rs.accum.ensure((size_t)pixels * 12));
+    PPPM_CUDA(c, cudaMemsetAsync(rs.accum.p, 0, (size_t)pixels * 12, c->stream));
+    PPPM_CUDA(c, rs.pathA.ensure((size_t)paths * sizeof(PathState)));
+    PPPM_CUDA(c, rs.pathB.ensure((size_t)paths * sizeof(PathState)));
+    if (rs.depositCap == 0) rs.depositCap = std::max<int64_t>(2 * paths, 1 << 16);
+    PPPM_CUDA(c, rs.photons.ensure((size_t)rs.depositCap * 32));
+    PPPM_CUDA(c, rs.queries.ensure((size_t)pixels * 48));
+    PPPM_CUDA(c, rs.photonCount.ensure(sizeof(PassCounters) + 8 * (size_t)N));
+    PPPM_CUDA(c, rs.streamStatesD.ensure((size_t)N * 16));
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    rs.passesDone = 0;
+    rs.storedLast = 0;
+    rs.phantomsLast = 0;
+    rs.active = true;
+    return PPPM_OK;
+}
+
+int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
+    if (!c) return PPPM_E_ARG;
+    RenderState& rs = c->rs;
+    if (!rs.active) return fail(c, PPPM_E_STATE, "render_pass: call render_begin first");
+    if (t != rs.passesDone + 1) return fail(c, PPPM_E_STATE, "render_pass: passes must run in order 1, 2, ...");
+    cudaSetDevice(c->device);
+    const pppm_params& par = rs.par;
+    const bool compat = par.mode == PPPM_MODE_COMPAT;
+    const int N = par.num_streams;
+    const int W = rs.cam.width, H = rs.cam.height;
+    const int64_t pixels = (int64_t)W * H;
+    const int64_t T = rs.taskPerThread;
+    const int64_t paths = compat ? T * N : par.photons;
+    const int k = (int)rs.radius;
+    if (compat && k < 1) return fail(c, PPPM_E_UNDEFINED, "render_pass: k = (int)radius < 1 pops an empty queue in the reference");
+    if (compat && k > kMaxKnn) return fail(c, PPPM_E_CAPACITY, "render_pass: k = (int)radius above 64");
+
+    TraceParams tp;
+    tp.mode = par.mode;
+    tp.numStreams = N;
+    tp.taskPerThread = T;
+    tp.numPaths = paths;
+    tp.numPhotons = (double)par.photons;
+    tp.maxBouncePhoton = par.max_bounce_photon;
+    tp.maxBounceEye = par.max_bounce_eye;
+    tp.seed = par.seed;
+    tp.pass = t;
+
+    CameraDev cd;
+    {
+        const double ex = rs.cam.eye[0], ey = rs.cam.eye[1], ez = rs.cam.eye[2];
+        const double dx = rs.cam.dir[0], dy = rs.cam.dir[1], dz = rs.cam.dir[2];
+        const double ux = rs.cam.up[0], uy = rs.cam.up[1], uz = rs.cam.up[2];
+        // ICamera: unitU = cross(direction, up), unitV = cross(unitU, direction) (camera_interface.h:40-41)
+        const double Ux = dy * uz - dz * uy, Uy = dz * ux - dx * uz, Uz = dx * uy - dy * ux;
+        const double Vx = Uy * dz - Uz * dy, Vy = Uz * dx - Ux * dz, Vz = Ux * dy - Uy * dx;
+        cd.ex = ex; cd.ey = ey; cd.ez = ez;
+        cd.dx = (float)dx; cd.dy = (float)dy; cd.dz = (float)dz;
+        cd.ux = (float)Ux; cd.uy = (float)Uy; cd.uz = (float)Uz;
+        cd.vx = (float)Vx; cd.vy = (float)Vy; cd.vz = (float)Vz;
+        cd.halfTan = (float)std::tan((double)rs.cam.fov * 0.5);
+        cd.aspect = (float)((double)W / (double)H);
+        cd.w = W;
+        cd.h = H;
+    }
+    const SceneView sv = sceneView(c);
+    const EnvDev ev = envView(c);
+    PassCounters* ctr = rs.photonCount.as<PassCounters>();
+    unsigned long long* perStream = reinterpret_cast<unsigned long long*>(ctr + 1);
+    uint32_t* photonStates = compat ? rs.tapeStates.as<uint32_t>() : nullptr;
+    uint32_t* pixelStates = compat ? photonStates + 4 * paths : nullptr;
+
+    PPPM_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
+    if (compat) {
+        std::vector<uint32_t> ss((size_t)N * 4);
+        for (int s = 0; s < N; s++) std::memcpy(&ss[4 * s], rs.streams[s].s, 16);
+        PPPM_CUDA(c, cudaMemcpyAsync(rs.streamStatesD.p, ss.data(), ss.size() * 4, cudaMemcpyHostToDevice, c->stream));
+        PPPM_CUDA(c, launchTapeStates(tp, rs.streamStatesD.as<uint32_t>(), rs.jumpMats.as<uint32_t>(), W, H, photonStates,
+                                      pixelStates, c->stream));
+    }
+    PassCounters hc;
+    for (int attempt = 0;; attempt++) {
+        PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters) + 8 * (size_t)N, c->stream));
+        PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
+        for (int b = 0; b < par.max_bounce_photon; b++) {
+            PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
+            PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
+            PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, rs.photons.as<float4>(), rs.depositCap, ctr,
+                                            c->stream));
+        }
+        PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
+        PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+        if ((int64_t)hc.deposits <= rs.depositCap) break;
+        if (attempt > 0) return fail(c, PPPM_E_CAPACITY, "render_pass: photon buffer overflow");
+        // grow and trace the same photons again (the tapes are unchanged)
+        rs.depositCap = (int64_t)(hc.deposits * 1.25) + 1024;
+        PPPM_CUDA(c, rs.photons.ensure((size_t)rs.depositCap * 32));
+    }
+    const int64_t stored = (int64_t)hc.deposits;
+    int64_t phantoms = 0;
+    if (compat) {
+        // ppm_probabilistic.cc:202-207: thread i's photons are copied to slot
+        // i * ceil(P/N); unused slots keep default Photon() records.
+        PPPM_CUDA(c, launchStreamCounts(rs.photons.as<float4>(), &ctr->deposits, rs.depositCap, T, N, perStream,
+                                        c->stream));
+        std::vector<unsigned long long> ps(N);
+        PPPM_CUDA(c, cudaMemcpyAsync(ps.data(), perStream, 8 * (size_t)N, cudaMemcpyDeviceToHost, c->stream));
+        PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+        for (int s = 0; s < N; s++) {
+            if ((int64_t)ps[s] > T)
+                return fail(c, PPPM_E_UNDEFINED,
+                            "render_pass: a thread stored more photons than its ceil(P/N) slots; the reference then "
+                            "overwrites other threads' photons or writes past the photon array");
+            phantoms += T - (int64_t)ps[s];
+        }
+    }
+    PPPM_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
+
+    // photon map
+    double cell;
+    if (compat) {
+        const double area = c->lambertArea > 0.0 ? c->lambertArea : 1.0;
+        cell = par.cell_factor * std::sqrt(area * (double)std::max(k, 1) / (double)std::max<int64_t>(stored, 1));
+    } else {
+        cell = par.cell_factor * rs.radius;
+    }
+    PPPM_CUDA(c, gridLayout(rs.grid, c->bbmin, c->bbmax, cell, stored));
+    GridDev gv = gridView(rs.grid, c->bbmin, c->bbmax);
+    PPPM_CUDA(c, gridBuild(rs.grid, gv, rs.photons.as<float4>(), reinterpret_cast<const uint64_t*>(&ctr->deposits),
+                           rs.depositCap, c->stream));
+    gv = gridView(rs.grid, c->bbmin, c->bbmax);
+    PPPM_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
+
+    // eye paths and gather
+    PPPM_CUDA(c, launchEyeTrace(tp, sv, ev, cd, pixelStates, rs.accum.as<float>(), rs.queries.as<float4>(), ctr,
+                                c->stream));
+    PPPM_CUDA(c, cudaEventRecord(c->ev[3], c->stream));
+    QueryView qv{rs.queries.as<float4>(), reinterpret_cast<const uint32_t*>(&ctr->queries), pixels};
+    if (compat)
+        PPPM_CUDA(c, launchGatherCompat(gv, qv, k, (float)par.gather_photons, (float)rs.radius, phantoms,
+                                        rs.accum.as<float>(), true, c->stream));
+    else
+        PPPM_CUDA(c, launchGatherCanonical(gv, qv, (float)rs.radius, rs.accum.as<float>(), true, c->stream));
+    PPPM_CUDA(c, cudaEventRecord(c->ev[4], c->stream));
+    PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->photons_traced = paths;
+        stats->photons_stored = stored;
+        stats->phantom_photons = phantoms;
+        stats->photon_rays = (int64_t)hc.photonRays;
+        stats->eye_rays = (int64_t)hc.eyeRays;
+        stats->gather_queries = (int64_t)hc.queries;
+        stats->radius = rs.radius;
+        float ms;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+        stats->ms_photon = ms;
+        cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
+        stats->ms_grid = ms;
+        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+        stats->ms_eye = ms;
+        cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]);
+        stats->ms_gather = ms;
+    }
+    if (hc.undefinedEmit)
+        return fail(c, PPPM_E_UNDEFINED, "render_pass: a photon draw fell past the env CDF (reference reads _pdf out of bounds)");
+
+    // radius update (ppm_probabilistic.cc:94 in compat; Knaus-Zwicker
+    // r^2_{t+1} = r^2_t (t + alpha) / (t + 1) in canonical mode)
+    if (compat) rs.radius = (t + 1.0) / (t + par.alpha) * rs.radius;
+    else rs.radius = rs.radius * std::sqrt((t + par.alpha) / (t + 1.0));
+    if (compat) {
+        // each stream drew ceil(P/N) photon tapes and one tape per pixel of its rows
+        for (int s = 0; s < N; s++) {
+            const int64_t rows = s < H ? (H - 1 - s) / N + 1 : 0;
+            xorshiftJumpHost(c->jumpTables, (uint64_t)(T + rows * W), &rs.streams[s]);
+        }
+    }
+    rs.storedLast = stored;
+    rs.phantomsLast = phantoms;
+    rs.passesDone = t;
+    return PPPM_OK;
+}
+
+int pppm_render_read(pppm_ctx* c, float* accum) {
+    if (!c || !accum) return fail(c, PPPM_E_ARG, "render_read: bad arguments");
+    if (!c->rs.active) return fail(c, PPPM_E_STATE, "render_read: no render");
+    const size_t bytes = (size_t)c->rs.cam.width * c->rs.cam.height * 12;
+    PPPM_CUDA(c, cudaMemcpyAsync(accum, c->rs.accum.p, bytes, isDevicePtr(accum) ? cudaMemcpyDeviceToDevice
+                                                                                  : cudaMemcpyDeviceToHost, c->stream));
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PPPM_OK;
+}
+
+int pppm_render(pppm_ctx* c, const pppm_camera* cam, const pppm_params* par, int32_t passes, float* accum) {
+    if (passes < 0) return fail(c, PPPM_E_ARG, "render: negative pass count");
+    int r = pppm_render_begin(c, cam, par);
+    if (r) return r;
+    for (int t = 1; t <= passes; t++)
+        if ((r = pppm_render_pass(c, t, nullptr))) return r;
+    return accum ? pppm_render_read(c, accum) : PPPM_OK;
+}
+
+int pppm_render_photons(pppm_ctx* c, float* out, int64_t cap, int64_t* n) {
+    if (!c || !n || cap < 0 || (cap > 0 && !out)) return fail(c, PPPM_E_ARG, "render_photons: bad arguments");
+    if (!c->rs.active) return fail(c, PPPM_E_STATE, "render_photons: no render");
+    const int64_t cnt = std::min<int64_t>(c->rs.storedLast, c->rs.depositCap);
+    *n = cnt;
+    const int64_t m = std::min(cnt, cap);
+    if (m > 0) {
+        PPPM_CUDA(c, cudaMemcpyAsync(out, c->rs.photons.p, (size_t)m * 32,
+                                     isDevicePtr(out) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+        PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return PPPM_OK;
+}
+
+}  // extern "C"

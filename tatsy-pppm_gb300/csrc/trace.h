@@ -1,0 +1,71 @@
+// Wavefront photon tracing, eye paths and RNG tapes.
+#pragma once
+
+#include "kernels.h"
+
+namespace pppm {
+
+// One photon path in the wavefront queue (80 bytes).
+struct __align__(16) PathState {
+    double ox, oy, oz;  // origin in double, as the reference keeps hit points
+    float dx, dy, dz;   // unit direction
+    float fx, fy, fz;   // flux
+    uint32_t rng[4];    // XorShift state positioned at the next draw
+    int id;             // path id (stream = id / taskPerThread in compat mode)
+    int bounce;
+    int pad[2];
+};
+static_assert(sizeof(PathState) == 80, "PathState layout");
+
+// Device counters of one pass.
+struct PassCounters {
+    unsigned long long queue[3];      // rotating queue lengths (see launchPhotonBounce)
+    unsigned long long deposits;      // photon records written (may exceed capacity)
+    unsigned long long queries;       // gather queries written
+    unsigned long long photonRays;    // photon traversals
+    unsigned long long eyeRays;       // eye traversals
+    unsigned long long undefinedEmit; // CDF inversion past the last entry (reference reads out of bounds)
+};
+
+struct CameraDev {
+    double ex, ey, ez;
+    float dx, dy, dz;
+    float ux, uy, uz;
+    float vx, vy, vz;
+    float halfTan, aspect;
+    int w, h;
+};
+
+struct TraceParams {
+    int mode;
+    int numStreams;
+    int64_t taskPerThread;  // ceil(P / N)
+    int64_t numPaths;       // N * taskPerThread (compat) or P (canonical)
+    double numPhotons;      // flux divisor (RenderParameters::photons)
+    int maxBouncePhoton;
+    int maxBounceEye;
+    uint32_t seed;
+    int pass;
+};
+
+// Jump-ahead matrices: J[k] advances a XorShift state by 200 * 2^k draws
+// (one 200-number tape per photon or pixel). Column j of a matrix is the
+// image of state bit j; 128 columns of 4 words each.
+constexpr int kJumpLevels = 40;
+void xorshiftJumpTables(std::vector<uint32_t>* tables);
+void xorshiftJumpHost(const std::vector<uint32_t>& tables, uint64_t tapes, XorShift* st);
+
+cudaError_t launchTapeStates(const TraceParams& tp, const uint32_t* streamStates, const uint32_t* jump, int width,
+                             int height, uint32_t* photonStates, uint32_t* pixelStates, cudaStream_t st);
+cudaError_t launchPhotonEmit(const TraceParams& tp, const EnvDev& env, const uint32_t* photonStates, PathState* queue,
+                             PassCounters* ctr, cudaStream_t st);
+cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
+                               PathState* out, int64_t maxPaths, float4* deposits, int64_t depositCap,
+                               PassCounters* ctr, cudaStream_t st);
+cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
+                           const uint32_t* pixelStates, float* accum, float4* queries, PassCounters* ctr,
+                           cudaStream_t st);
+cudaError_t launchStreamCounts(const float4* deposits, const unsigned long long* count, int64_t cap, int64_t tpt,
+                               int numStreams, unsigned long long* perStream, cudaStream_t st);
+
+}  // namespace pppm

@@ -1,0 +1,277 @@
+"""Python binding of the C ABI in include/pppm_c.h (libpppm_gb300.so).
+
+Arrays may be numpy arrays (host memory) or CUDA torch tensors (device
+memory); outputs are returned in the same kind of memory as the first
+array argument. The library is required: nothing here falls back to a CPU
+implementation, and `load()` raises when the shared object is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import pathlib
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = HERE / "libpppm_gb300.so"
+
+OK = 0
+E_ARG, E_CUDA, E_STATE, E_CAPACITY, E_UNDEFINED, E_TIMEOUT = -1, -2, -3, -4, -5, -6
+MODE_COMPAT, MODE_CANONICAL = 0, 1
+
+_lib = None
+
+
+class PppmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"pppm error {code}: {msg}")
+        self.code = code
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("eye", ctypes.c_float * 3), ("dir", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("fov", ctypes.c_float), ("width", ctypes.c_int32), ("height", ctypes.c_int32)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("num_streams", ctypes.c_int32), ("photons", ctypes.c_int64),
+                ("gather_photons", ctypes.c_int32), ("max_bounce_photon", ctypes.c_int32),
+                ("max_bounce_eye", ctypes.c_int32), ("seed", ctypes.c_uint32), ("gather_radius", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("radius_scale", ctypes.c_double), ("cell_factor", ctypes.c_float),
+                ("reserved", ctypes.c_int32)]
+
+
+class PassStats(ctypes.Structure):
+    _fields_ = [("photons_traced", ctypes.c_int64), ("photons_stored", ctypes.c_int64),
+                ("phantom_photons", ctypes.c_int64), ("photon_rays", ctypes.c_int64), ("eye_rays", ctypes.c_int64),
+                ("gather_queries", ctypes.c_int64), ("radius", ctypes.c_double), ("ms_photon", ctypes.c_double),
+                ("ms_grid", ctypes.c_double), ("ms_eye", ctypes.c_double), ("ms_gather", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_VP = ctypes.c_void_p
+
+SIGNATURES = {
+    "pppm_create": ([ctypes.c_int, ctypes.POINTER(_VP)], ctypes.c_int),
+    "pppm_destroy": ([_VP], ctypes.c_int),
+    "pppm_last_error": ([_VP], ctypes.c_char_p),
+    "pppm_sync": ([_VP], ctypes.c_int),
+    "pppm_stream": ([_VP], _VP),
+    "pppm_scene_set": ([_VP, _VP, ctypes.c_int64, _VP, _VP, ctypes.c_int32], ctypes.c_int),
+    "pppm_env_set": ([_VP, _VP, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+    "pppm_env_tables": ([_VP, _VP, _VP], ctypes.c_int),
+    "pppm_hdr_decode": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
+    "pppm_intersect": ([_VP, _VP, ctypes.c_int64, _VP, _VP, _VP, _VP], ctypes.c_int),
+    "pppm_hash_points": ([_VP, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP], ctypes.c_int),
+    "pppm_knn": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
+                  ctypes.c_int32], ctypes.c_int),
+    "pppm_gather": ([_VP, ctypes.c_int32, _VP, ctypes.c_int64, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_double,
+                     ctypes.c_int32, _VP], ctypes.c_int),
+    "pppm_render_begin": ([_VP, _VP, _VP], ctypes.c_int),
+    "pppm_render_pass": ([_VP, ctypes.c_int32, _VP], ctypes.c_int),
+    "pppm_render_read": ([_VP, _VP], ctypes.c_int),
+    "pppm_render": ([_VP, _VP, _VP, ctypes.c_int32, _VP], ctypes.c_int),
+    "pppm_render_photons": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+}
+
+
+def header_symbols():
+    """Function names declared in include/pppm_c.h."""
+    import re
+
+    text = (HERE.parent / "include" / "pppm_c.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|void\*|const char\*)\s+(pppm_\w+)\s*\(", text, re.M)))
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with tatsy-pppm_gb300/build.py")
+        _lib = ctypes.CDLL(str(LIB_PATH))
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(_lib, name, None)
+            if fn is None:
+                continue
+            fn.argtypes = args
+            fn.restype = res
+    return _lib
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_torch(a):
+        assert a.is_contiguous()
+        return a.data_ptr()
+    assert a.flags["C_CONTIGUOUS"], "arrays must be C-contiguous"
+    return a.ctypes.data
+
+
+def _empty_like_kind(ref, shape, dtype):
+    if _is_torch(ref):
+        import torch
+
+        tmap = {np.float32: torch.float32, np.float64: torch.float64, np.int32: torch.int32, np.uint32: torch.int32,
+                np.int64: torch.int64}
+        return torch.empty(shape, dtype=tmap[dtype], device=ref.device)
+    return np.empty(shape, dtype)
+
+
+class Context:
+    """One pppm context (one CUDA stream, device memory owned by the context)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = _VP()
+        r = self.lib.pppm_create(device, ctypes.byref(h))
+        if r != OK:
+            raise PppmError(r, "pppm_create failed (no CUDA device?)")
+        self.h = h
+        self.scene = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pppm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, r):
+        if r != OK:
+            raise PppmError(r, self.lib.pppm_last_error(self.h).decode())
+
+    def sync(self):
+        self._check(self.lib.pppm_sync(self.h))
+
+    def stream_ptr(self):
+        return self.lib.pppm_stream(self.h)
+
+    # -------------------------------------------------------------- scene
+    def set_scene(self, scene):
+        tris = np.ascontiguousarray(scene.tris, np.float32)
+        mid = np.ascontiguousarray(scene.mat_id, np.int32)
+        mats = np.ascontiguousarray(scene.mats)
+        self._check(self.lib.pppm_scene_set(self.h, tris.ctypes.data, tris.shape[0], mid.ctypes.data, mats.ctypes.data,
+                                            mats.shape[0]))
+        if scene.env is not None:
+            self.set_env(scene.env)
+        self.scene = scene
+
+    def set_env(self, rgb):
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        self._check(self.lib.pppm_env_set(self.h, rgb.ctypes.data, rgb.shape[1], rgb.shape[0]))
+
+    def env_tables(self):
+        pdf = np.zeros(4096)
+        cdf = np.zeros(4096)
+        self._check(self.lib.pppm_env_tables(self.h, pdf.ctypes.data, cdf.ctypes.data))
+        return pdf, cdf
+
+    # -------------------------------------------------------------- stages
+    def intersect(self, rays, with_hit=True):
+        n = int(rays.shape[0])
+        tri = _empty_like_kind(rays, (n,), np.int32)
+        t = _empty_like_kind(rays, (n,), np.float64)
+        pos = _empty_like_kind(rays, (n, 3), np.float32) if with_hit else None
+        nrm = _empty_like_kind(rays, (n, 3), np.float32) if with_hit else None
+        self._check(self.lib.pppm_intersect(self.h, _ptr(rays), n, _ptr(tri), _ptr(t), _ptr(pos), _ptr(nrm)))
+        return tri, t, pos, nrm
+
+    def hash_points(self, pts, hash_size, scale, bbmin):
+        n = int(pts.shape[0])
+        out = _empty_like_kind(pts, (n,), np.uint32)
+        bmin = np.ascontiguousarray(bbmin, np.float64)
+        self._check(self.lib.pppm_hash_points(self.h, _ptr(pts), n, int(hash_size), float(scale), bmin.ctypes.data,
+                                              _ptr(out)))
+        return out
+
+    def knn(self, photon_pos, queries, num_target_photons, target_radius, cap=64):
+        n, m = int(photon_pos.shape[0]), int(queries.shape[0])
+        idx = _empty_like_kind(queries, (m, cap), np.int32)
+        cnt = _empty_like_kind(queries, (m,), np.int32)
+        self._check(self.lib.pppm_knn(self.h, _ptr(photon_pos), n, _ptr(queries), m, int(num_target_photons),
+                                      float(target_radius), _ptr(idx), _ptr(cnt), cap))
+        return idx, cnt
+
+    def gather(self, mode, photons8, queries12, radius, gather_photons=128, phantoms=0):
+        n, m = int(photons8.shape[0]), int(queries12.shape[0])
+        out = _empty_like_kind(queries12, (m, 3), np.float32)
+        self._check(self.lib.pppm_gather(self.h, int(mode), _ptr(photons8), n, int(phantoms), _ptr(queries12), m,
+                                         float(radius), int(gather_photons), _ptr(out)))
+        return out
+
+    # -------------------------------------------------------------- render
+    @staticmethod
+    def make_camera(cam):
+        c = Camera()
+        c.eye[:] = cam.eye
+        c.dir[:] = cam.dir
+        c.up[:] = cam.up
+        c.fov = cam.fov
+        c.width, c.height = cam.width, cam.height
+        return c
+
+    @staticmethod
+    def make_params(mode=MODE_COMPAT, photons=200_000, num_streams=8, gather_photons=128, gather_radius=16.0,
+                    alpha=0.7, radius_scale=0.1, max_bounce_photon=64, max_bounce_eye=64, seed=1, cell_factor=1.0):
+        p = Params()
+        p.mode = mode
+        p.num_streams = num_streams
+        p.photons = photons
+        p.gather_photons = gather_photons
+        p.max_bounce_photon = max_bounce_photon
+        p.max_bounce_eye = max_bounce_eye
+        p.seed = seed
+        p.gather_radius = gather_radius
+        p.alpha = alpha
+        p.radius_scale = radius_scale
+        p.cell_factor = cell_factor
+        return p
+
+    def render_begin(self, cam, params):
+        self._cam = self.make_camera(cam) if not isinstance(cam, Camera) else cam
+        self._par = params
+        self._check(self.lib.pppm_render_begin(self.h, ctypes.byref(self._cam), ctypes.byref(params)))
+
+    def render_pass(self, t):
+        st = PassStats()
+        self._check(self.lib.pppm_render_pass(self.h, int(t), ctypes.byref(st)))
+        return st
+
+    def render_read(self, out=None):
+        if out is None:
+            out = np.zeros((self._cam.height, self._cam.width, 3), np.float32)
+        self._check(self.lib.pppm_render_read(self.h, _ptr(out)))
+        return out
+
+    def render_photons(self, cap):
+        out = np.zeros((cap, 8), np.float32)
+        n = ctypes.c_int64()
+        self._check(self.lib.pppm_render_photons(self.h, out.ctypes.data, cap, ctypes.byref(n)))
+        return out[: n.value]
+
+
+def hdr_decode(data: bytes):
+    lib = load()
+    buf = np.frombuffer(data, np.uint8)
+    w = ctypes.c_int32()
+    h = ctypes.c_int32()
+    r = lib.pppm_hdr_decode(buf.ctypes.data, buf.size, None, 0, ctypes.byref(w), ctypes.byref(h))
+    if r != OK:
+        raise PppmError(r, "bad HDR header")
+    out = np.zeros((h.value, w.value, 3), np.float32)
+    r = lib.pppm_hdr_decode(buf.ctypes.data, buf.size, out.ctypes.data, out.size, ctypes.byref(w), ctypes.byref(h))
+    if r != OK:
+        raise PppmError(r, "bad HDR data")
+    return out

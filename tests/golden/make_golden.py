@@ -1,0 +1,242 @@
+"""Generates the golden fixtures in tests/golden/ from the UNMODIFIED reference.
+
+Run in a container that has the reference sources (it builds oracle/_ref with
+oracle/Makefile first):
+
+    python tests/golden/make_golden.py [name ...]
+
+Every fixture stores its exact float inputs next to the reference outputs, so
+the tests never regenerate inputs (numpy's transcendental functions are not
+bit-identical across machines). OMP_NUM_THREADS is pinned to 8 because the
+reference seeds one XorShift stream per OpenMP thread.
+"""
+from __future__ import annotations
+
+import os
+import pathlib
+import sys
+
+os.environ["OMP_NUM_THREADS"] = "8"
+
+import numpy as np  # noqa: E402
+
+ROOT = pathlib.Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT / "oracle"))
+sys.path.insert(0, str(ROOT / "tatsy-pppm_gb300"))
+import refharness as rh  # noqa: E402
+import scenes as S  # noqa: E402
+
+OUT = pathlib.Path(__file__).resolve().parent
+
+
+def save(name, **arrays):
+    np.savez_compressed(OUT / f"{name}.npz", **arrays)
+    print(f"wrote {name}.npz", {k: v.shape for k, v in arrays.items()})
+
+
+def scene_arrays(sc):
+    return dict(tris=sc.tris, mat_id=sc.mat_id, mats=sc.mats.view(np.uint8).reshape(len(sc.mats), -1),
+                env=sc.env if sc.env is not None else np.zeros((0, 0, 3), np.float32))
+
+
+def special_rays(tris, rng, n):
+    """Rays aimed at vertices, edge midpoints and grazing the triangle planes."""
+    t = tris.reshape(-1, 3, 3).astype(np.float64)
+    pick = rng.integers(0, t.shape[0], n)
+    kind = rng.integers(0, 4, n)
+    tgt = np.where(kind[:, None] == 0, t[pick, 0], np.where(kind[:, None] == 1, 0.5 * (t[pick, 0] + t[pick, 1]),
+                                                            t[pick].mean(1)))
+    org = tgt + rng.normal(size=(n, 3)) * 15.0
+    # grazing: start in the triangle's plane
+    e1 = t[pick, 1] - t[pick, 0]
+    e2 = t[pick, 2] - t[pick, 0]
+    graze = kind == 3
+    org[graze] = tgt[graze] - 5.0 * (e1[graze] + 0.3 * e2[graze])
+    d = tgt - org
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([org, d], 1).astype(np.float32)
+
+
+def random_rays(bbmin, bbmax, rng, n):
+    c = 0.5 * (bbmin + bbmax)
+    ext = (bbmax - bbmin)
+    org = c + (rng.uniform(-1, 1, (n, 3)) * ext * 0.9)
+    tgt = c + (rng.uniform(-0.5, 0.5, (n, 3)) * ext)
+    d = tgt - org
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([org, d], 1).astype(np.float32)
+    # axis-aligned directions (zero components -> idir = 1e20)
+    k = n // 10
+    ax = rng.integers(0, 3, k)
+    dd = np.zeros((k, 3), np.float32)
+    dd[np.arange(k), ax] = rng.choice([-1.0, 1.0], k)
+    rays[:k, 3:] = dd
+    # renormalise in float so the reference's unit-direction assertion holds
+    dn = rays[:, 3:].astype(np.float64)
+    rays[:, 3:] = (dn / np.linalg.norm(dn, axis=1, keepdims=True)).astype(np.float32)
+    return rays
+
+
+def gen_intersect():
+    sc = S.small_test_scene(seed=3, subdiv=3)
+    rng = np.random.default_rng(11)
+    bmn, bmx = sc.bbox()
+    rays = np.concatenate([random_rays(bmn, bmx, rng, 16000), special_rays(sc.tris, rng, 8000)], 0)
+    R = rh.RefScene(sc)
+    tri, t, pos, nrm = R.intersect(rays)
+    # a second, larger mesh (subdivision 5 sphere) for deeper trees
+    sc2 = S.config1a(seed=1, width=16, height=16, subdiv=5)
+    R2 = rh.RefScene(sc2)
+    bmn2, bmx2 = sc2.bbox()
+    rays2 = np.concatenate([random_rays(bmn2, bmx2, rng, 12000), special_rays(sc2.tris, rng, 6000)], 0)
+    tri2, t2, pos2, nrm2 = R2.intersect(rays2)
+    # degenerate scenes: empty, 1..3 triangles (root is a leaf), 4 (one inner node)
+    small = {}
+    for k in (1, 2, 3, 4, 5):
+        tt = sc.tris[:k].copy()
+        sk = S.Scene("tiny", tt, np.zeros(k, np.int32), sc.mats[:1], None, sc.camera)
+        rk = rh.RefScene(sk)
+        rr = special_rays(tt, rng, 400)
+        a, b, _, _ = rk.intersect(rr)
+        small[f"tiny{k}_tris"] = tt
+        small[f"tiny{k}_rays"] = rr
+        small[f"tiny{k}_tri"] = a
+        small[f"tiny{k}_t"] = b
+    save("intersect", tris=sc.tris, rays=rays, tri=tri, t=t, pos=pos, nrm=nrm, tris2=sc2.tris, rays2=rays2, tri2=tri2,
+         t2=t2, pos2=pos2, nrm2=nrm2, **small)
+
+
+def gen_hash():
+    rng = np.random.default_rng(5)
+    out = {}
+    for k, (size, scale) in enumerate([(65536, 0.5), (1000003, 1.0 / 0.37), (12345, 3.0), (256 * 256, 1.0 / 1.6)]):
+        bbmin = rng.uniform(-30, -10, 3)
+        bbmax = rng.uniform(10, 30, 3)
+        pts = rng.uniform(bbmin - 2.0, bbmax, (20000, 3)).astype(np.float32)  # some below bbmin: |(int)x| folding
+        # points exactly on cell boundaries
+        pts[:2000] = (bbmin + np.round(rng.uniform(0, 20, (2000, 3))) / scale).astype(np.float32)
+        h = rh.hash_points(size, scale, bbmin, bbmax, pts)
+        out[f"pts{k}"] = pts
+        out[f"bbmin{k}"] = bbmin
+        out[f"bbmax{k}"] = bbmax
+        out[f"size{k}"] = np.array(size)
+        out[f"scale{k}"] = np.array(scale)
+        out[f"hash{k}"] = h
+    save("hash", **out)
+
+
+def gen_rng():
+    out = {}
+    for s in (0, 1, 7, 123456789):
+        out[f"u32_{s}"] = rh.xorshift(s, 1000)
+        out[f"real_{s}"] = rh.xorshift_reals(s, 0, 1000)
+    save("xorshift", **out)
+
+
+def gen_env():
+    env = S.sky_env(256, 128, 9, sun_peak=500.0, sun_deg=4.0)
+    path = OUT / "_tmp_env.hdr"
+    rh.write_hdr(path, env)
+    data = np.frombuffer(path.read_bytes(), np.uint8).copy()
+    decoded = rh.load_hdr(path)
+    gnd = S.ground(-5.0, 20.0)
+    sc = S._assemble("env", [(gnd, 0)], [S.material(S.LAMBERTIAN, (0.5, 0.5, 0.5))], env, S.look_camera((0, 5, -30), (0, 0, 0), 0.8, 8, 8))
+    R = rh.RefScene(sc, env_path=str(path))
+    pdf, cdf = R.env_tables()
+    rng = np.random.default_rng(3)
+    d = rng.normal(size=(5000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    look = R.env_lookup(d)
+    # emission on explicit tapes (Envmap::samplePhoton + onHemisphere)
+    tapes = rng.uniform(0, 1, (5000, 5))
+    tapes = (np.floor(tapes * 2.0**32) / 2.0**32)  # values a XorShift tape can hold
+    epos, edir, eflux = R.emit(tapes, 100000)
+    path.unlink()
+    save("env", hdr_bytes=data, decoded=decoded, pdf=pdf, cdf=cdf, dirs=d, lookup=look, tapes=tapes, emit_pos=epos,
+         emit_dir=edir, emit_flux=eflux)
+
+
+GENERATORS = {"intersect": gen_intersect, "hash": gen_hash, "xorshift": gen_rng, "env": gen_env}
+
+
+def surface_photons(rng, n):
+    """Photons on a ground plane and on a sphere, like stored photon maps."""
+    m = n // 2
+    plane = np.stack([rng.uniform(-20, 20, m), np.full(m, -5.0), rng.uniform(-20, 20, m)], 1)
+    d = rng.normal(size=(n - m, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    sph = d * 4.0 + np.array([2.0, -1.0, 3.0])
+    pos = np.concatenate([plane, sph], 0).astype(np.float32)
+    flux = rng.uniform(0.0, 1.0, (n, 3)).astype(np.float32) * 1e-3
+    nrm = np.concatenate([np.tile([0.0, 1.0, 0.0], (m, 1)), d], 0).astype(np.float32)
+    return pos, flux, nrm
+
+
+def gen_knn():
+    rng = np.random.default_rng(21)
+    pos, _, _ = surface_photons(rng, 40000)
+    q = np.concatenate([pos[rng.integers(0, len(pos), 3000)] + rng.normal(size=(3000, 3)).astype(np.float32) * 0.3,
+                        rng.uniform(-20, 20, (1000, 3))], 0).astype(np.float32)
+    out = dict(pos=pos, queries=q)
+    for k, (ntp, rad) in enumerate([(128, 8.7), (128, 1.0), (3, 16.9), (128, 40.2)]):
+        idx, cnt = rh.knn(pos, q, ntp, rad, cap=64)
+        out[f"ntp{k}"] = np.array(ntp)
+        out[f"rad{k}"] = np.array(rad)
+        out[f"idx{k}"] = idx
+        out[f"cnt{k}"] = cnt
+    save("knn", **out)
+
+
+def gen_gather():
+    """radiance() at bounce 0 on a Lambertian ground plane (y = -5): rays
+    straight down from y = 10 hit at float-exact points (x, -5, z), so the
+    query positions of the reference and of the GPU are identical."""
+    rng = np.random.default_rng(31)
+    gnd = S.ground(-5.0, 30.0)
+    refl = (0.6, 0.5, 0.4)
+    sc = S._assemble("gnd", [(gnd, 0)], [S.material(S.LAMBERTIAN, refl)], None,
+                     S.look_camera((0, 5, -30), (0, 0, 0), 0.8, 8, 8))
+    R = rh.RefScene(sc)
+    pos, flux, nrm = surface_photons(rng, 30000)
+    # lift a third of the plane photons off the plane: exercises the disc filter
+    lift = rng.random(len(pos)) < 0.15
+    pos[lift, 1] += rng.uniform(-1.5, 1.5, lift.sum()).astype(np.float32)
+    ph12 = np.concatenate([pos, flux, np.zeros_like(pos), nrm], 1).astype(np.float32)
+    m = 2000
+    xz = np.round(rng.uniform(-18, 18, (m, 2)) * 64) / 64
+    rays = np.stack([xz[:, 0], np.full(m, 10.0), xz[:, 1], np.zeros(m), np.full(m, -1.0), np.zeros(m)], 1).astype(np.float32)
+    out = dict(photons=ph12, rays=rays, refl=np.array(refl, np.float32))
+    for k, rad in enumerate([6.5, 9.3, 17.2, 3.2]):
+        out[f"rad{k}"] = np.array(rad)
+        out[f"L{k}"] = R.gather(ph12, rad, 128, rays)
+    # phantom photons at the origin (zero flux): queries near the origin
+    ph_ph = np.concatenate([ph12, np.zeros((500, 12), np.float32)], 0)
+    xz2 = np.round(rng.uniform(-3, 3, (300, 2)) * 64) / 64
+    rays2 = np.stack([xz2[:, 0], np.full(300, 10.0), xz2[:, 1], np.zeros(300), np.full(300, -1.0), np.zeros(300)], 1).astype(np.float32)
+    out["photons_ph"] = ph_ph
+    out["rays_ph"] = rays2
+    out["L_ph"] = R.gather(ph_ph, 6.5, 128, rays2)
+    save("gather", **out)
+
+
+def gen_render():
+    """Whole passes of the reference render loop (compat semantics), N = 8."""
+    sc = S.small_test_scene(seed=3, subdiv=3, width=64, height=48, photons=20000)
+    R = rh.RefScene(sc)
+    res = R.render_passes(sc.camera, sc.photons, 2, photon_cap=200000)
+    a = scene_arrays(sc)
+    cam = sc.camera
+    save("render_small", **a, accum=res["accum"], radii=res["radii"], photons=res["photons"],
+         photon_count=np.array(res["photon_count"]), eye=np.array(cam.eye), dir=np.array(cam.dir), up=np.array(cam.up),
+         fov=np.array(cam.fov), wh=np.array([cam.width, cam.height]), nphotons=np.array(sc.photons),
+         threads=np.array(rh.num_threads()))
+
+
+GENERATORS.update({"knn": gen_knn, "gather": gen_gather, "render": gen_render})
+
+
+if __name__ == "__main__":
+    rh.build()
+    names = sys.argv[1:] or list(GENERATORS)
+    for n in names:
+        GENERATORS[n]()
