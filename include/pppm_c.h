@@ -138,6 +138,19 @@ int pppm_env_set(pppm_ctx* ctx, const float* rgb, int32_t w, int32_t h);
 /* Envmap importance tables (envmap.cc:88-163), 4096 doubles each. */
 int pppm_env_tables(pppm_ctx* ctx, double* pdf, double* cdf);
 
+/* Replaces Envmap::sampleFromDir (envmap.cc:47-60): nearest-texel radiance
+ * for n unit directions (3 floats each, any memory) into rgb (n x 3). */
+int pppm_env_lookup(pppm_ctx* ctx, const float* dirs, int64_t n, float* rgb);
+
+/* Replaces Envmap::samplePhoton (envmap.cc:62-86) + the cosine-hemisphere
+ * draw of tracePhotons (ppm_probabilistic.cc:137-144) on explicit random
+ * tapes: tapes is n x 5 doubles in draw order. pos: photon origin 50*dir_env,
+ * dir: first ray direction, flux: photon flux (n x 3 floats each).
+ * defined[i] = 0 where the draw lies past the last CDF entry, where the
+ * reference reads outside its pdf table. */
+int pppm_emit_photons(pppm_ctx* ctx, const double* tapes, int64_t n, int64_t num_photons, float* pos, float* dir,
+                      float* flux, int32_t* defined);
+
 /* Decodes a Radiance RGBE file image held in memory (the reference's
  * Image::loadHdr, image.cc:296-434) into w*h*3 floats. Call with rgb=NULL
  * to query the size. */

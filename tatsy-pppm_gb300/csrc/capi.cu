@@ -264,6 +264,47 @@ int pppm_intersect(pppm_ctx* c, const float* rays, int64_t n, int32_t* tri, doub
     return PPPM_OK;
 }
 
+int pppm_env_lookup(pppm_ctx* c, const float* dirs, int64_t n, float* rgb) {
+    if (!c || n < 0 || (n > 0 && (!dirs || !rgb))) return fail(c, PPPM_E_ARG, "env_lookup: bad arguments");
+    if (!c->hasEnv) return fail(c, PPPM_E_STATE, "env_lookup: no env map");
+    if (n == 0) return PPPM_OK;
+    cudaSetDevice(c->device);
+    const void* dd;
+    void* dout;
+    int r;
+    if ((r = stageIn(c, dirs, (size_t)n * 12, 0, &dd))) return r;
+    if ((r = stageOut(c, rgb, (size_t)n * 12, 1, &dout))) return r;
+    PPPM_CUDA(c, launchEnvLookup(envView(c), (const float*)dd, n, (float*)dout, c->stream));
+    if ((r = finishOut(c, rgb, dout, (size_t)n * 12))) return r;
+    if (dd != dirs || dout != rgb) PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PPPM_OK;
+}
+
+int pppm_emit_photons(pppm_ctx* c, const double* tapes, int64_t n, int64_t numPhotons, float* pos, float* dir,
+                      float* flux, int32_t* defined) {
+    if (!c || n < 0 || numPhotons < 1 || (n > 0 && (!tapes || !pos || !dir || !flux || !defined)))
+        return fail(c, PPPM_E_ARG, "emit_photons: bad arguments");
+    if (!c->hasEnv) return fail(c, PPPM_E_STATE, "emit_photons: no env map");
+    if (n == 0) return PPPM_OK;
+    cudaSetDevice(c->device);
+    const void* dt;
+    void *dp, *dd, *df, *dk;
+    int r;
+    if ((r = stageIn(c, tapes, (size_t)n * 40, 0, &dt))) return r;
+    if ((r = stageOut(c, pos, (size_t)n * 12, 1, &dp))) return r;
+    if ((r = stageOut(c, dir, (size_t)n * 12, 2, &dd))) return r;
+    if ((r = stageOut(c, flux, (size_t)n * 12, 3, &df))) return r;
+    if ((r = stageOut(c, defined, (size_t)n * 4, 4, &dk))) return r;
+    PPPM_CUDA(c, launchEmit(envView(c), (const double*)dt, n, (double)numPhotons, (float*)dp, (float*)dd, (float*)df,
+                            (int*)dk, c->stream));
+    if ((r = finishOut(c, pos, dp, (size_t)n * 12))) return r;
+    if ((r = finishOut(c, dir, dd, (size_t)n * 12))) return r;
+    if ((r = finishOut(c, flux, df, (size_t)n * 12))) return r;
+    if ((r = finishOut(c, defined, dk, (size_t)n * 4))) return r;
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PPPM_OK;
+}
+
 int pppm_hash_points(pppm_ctx* c, const float* pts, int64_t n, int32_t size, double scale, const double* bbmin,
                      uint32_t* out) {
     if (!c || n < 0 || size <= 0 || !bbmin || (n > 0 && (!pts || !out)))

@@ -158,6 +158,9 @@ inline EnvDev envView(const pppm_ctx* c) {
 // Kernel launchers (defined in the .cu files).
 cudaError_t launchIntersect(const SceneView& s, const float* rays, int64_t n, int32_t* tri, double* t, float* pos,
                             float* nrm, cudaStream_t st, bool prefilter);
+cudaError_t launchEnvLookup(const EnvDev& env, const float* dirs, int64_t n, float* out, cudaStream_t st);
+cudaError_t launchEmit(const EnvDev& env, const double* tapes, int64_t n, double numPhotons, float* pos, float* dir,
+                       float* flux, int* ok, cudaStream_t st);
 cudaError_t launchHashPoints(const float* pts, int64_t n, uint32_t size, double scale, const double* bbmin, uint32_t* out,
                              cudaStream_t st);
 

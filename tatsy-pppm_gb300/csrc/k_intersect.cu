@@ -67,3 +67,47 @@ cudaError_t launchHashPoints(const float* pts, int64_t n, uint32_t size, double 
 }
 
 }  // namespace pppm
+
+namespace pppm {
+
+__global__ void kEnvLookup(EnvDev env, const float* __restrict__ dirs, int64_t n, float* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const f3 c = envLookup(env, mk(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]));
+    out[3 * i] = c.x;
+    out[3 * i + 1] = c.y;
+    out[3 * i + 2] = c.z;
+}
+
+__global__ void kEmit(EnvDev env, const double* __restrict__ tapes, int64_t n, double numPhotons, float* __restrict__ pos,
+                      float* __restrict__ dir, float* __restrict__ flux, int* __restrict__ ok) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    ArrayTape t{tapes + 5 * i, 0};
+    f3 e, d, f;
+    ok[i] = emitPhoton(env, t, numPhotons, &e, &d, &f) ? 1 : 0;
+    pos[3 * i] = 50.0f * e.x;
+    pos[3 * i + 1] = 50.0f * e.y;
+    pos[3 * i + 2] = 50.0f * e.z;
+    dir[3 * i] = d.x;
+    dir[3 * i + 1] = d.y;
+    dir[3 * i + 2] = d.z;
+    flux[3 * i] = f.x;
+    flux[3 * i + 1] = f.y;
+    flux[3 * i + 2] = f.z;
+}
+
+cudaError_t launchEnvLookup(const EnvDev& env, const float* dirs, int64_t n, float* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    kEnvLookup<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(env, dirs, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launchEmit(const EnvDev& env, const double* tapes, int64_t n, double numPhotons, float* pos, float* dir,
+                       float* flux, int* ok, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    kEmit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(env, tapes, n, numPhotons, pos, dir, flux, ok);
+    return cudaGetLastError();
+}
+
+}  // namespace pppm

@@ -82,6 +82,14 @@ struct Tape {
     __device__ inline float popf() { return (float)popd(); }
 };
 
+// A tape given explicitly (stage tests feed the reference's own numbers).
+struct ArrayTape {
+    const double* v;
+    int pos;
+    __device__ inline double popd() { return v[pos++]; }
+    __device__ inline float popf() { return (float)popd(); }
+};
+
 // ------------------------------------------------------------------ vectors
 struct f3 { float x, y, z; };
 __device__ inline f3 mk(float x, float y, float z) { return {x, y, z}; }
@@ -438,7 +446,8 @@ __device__ inline f3 envLookup(const EnvDev& e, f3 d) {
 // the draw lies past the last CDF entry, where the reference indexes _pdf
 // out of bounds. emitDir: the sampled env direction (photon origin is
 // 50 * emitDir); dir: the first ray direction.
-__device__ inline bool emitPhoton(const EnvDev& e, Tape& tp, double numPhotons, f3* emitDir, f3* dir, f3* flux) {
+template <class TapeT>
+__device__ inline bool emitPhoton(const EnvDev& e, TapeT& tp, double numPhotons, f3* emitDir, f3* dir, f3* flux) {
     const double r = tp.popd();
     int lo = 0, hi = 4096;  // first index with cdf[i] >= r
     while (lo < hi) {

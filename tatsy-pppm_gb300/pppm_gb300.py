@@ -62,6 +62,8 @@ SIGNATURES = {
     "pppm_scene_set": ([_VP, _VP, ctypes.c_int64, _VP, _VP, ctypes.c_int32], ctypes.c_int),
     "pppm_env_set": ([_VP, _VP, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
     "pppm_env_tables": ([_VP, _VP, _VP], ctypes.c_int),
+    "pppm_env_lookup": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_emit_photons": ([_VP, _VP, ctypes.c_int64, ctypes.c_int64, _VP, _VP, _VP, _VP], ctypes.c_int),
     "pppm_hdr_decode": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
     "pppm_intersect": ([_VP, _VP, ctypes.c_int64, _VP, _VP, _VP, _VP], ctypes.c_int),
     "pppm_hash_points": ([_VP, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP], ctypes.c_int),
@@ -177,6 +179,22 @@ class Context:
         cdf = np.zeros(4096)
         self._check(self.lib.pppm_env_tables(self.h, pdf.ctypes.data, cdf.ctypes.data))
         return pdf, cdf
+
+    def env_lookup(self, dirs):
+        n = int(dirs.shape[0])
+        out = _empty_like_kind(dirs, (n, 3), np.float32)
+        self._check(self.lib.pppm_env_lookup(self.h, _ptr(dirs), n, _ptr(out)))
+        return out
+
+    def emit_photons(self, tapes, num_photons):
+        n = int(tapes.shape[0])
+        pos = _empty_like_kind(tapes, (n, 3), np.float32)
+        d = _empty_like_kind(tapes, (n, 3), np.float32)
+        flux = _empty_like_kind(tapes, (n, 3), np.float32)
+        ok = _empty_like_kind(tapes, (n,), np.int32)
+        self._check(self.lib.pppm_emit_photons(self.h, _ptr(tapes), n, int(num_photons), _ptr(pos), _ptr(d), _ptr(flux),
+                                               _ptr(ok)))
+        return pos, d, flux, ok
 
     # -------------------------------------------------------------- stages
     def intersect(self, rays, with_hit=True):

@@ -260,10 +260,13 @@ def _assemble(name, parts, mats, env, camera, **kw):
 
 
 def look_camera(eye, target, fov, w, h):
+    """Camera values are rounded to float32 so the C ABI (float fields) and
+    the reference (doubles) see identical inputs."""
     eye = np.asarray(eye, np.float64)
     d = np.asarray(target, np.float64) - eye
     d /= np.linalg.norm(d)
-    return Camera(tuple(map(float, eye)), tuple(map(float, d)), (0.0, 1.0, 0.0), fov, w, h)
+    f32 = lambda v: tuple(float(np.float32(x)) for x in v)  # noqa: E731
+    return Camera(f32(eye), f32(d), (0.0, 1.0, 0.0), float(np.float32(fov)), w, h)
 
 
 def config1a(seed=1, width=256, height=256, photons=200_000, passes=16, subdiv=5, env_w=256, env_h=128):

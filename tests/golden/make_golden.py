@@ -219,9 +219,21 @@ def gen_gather():
     save("gather", **out)
 
 
+def quantize_env(env):
+    """The env map as the reference sees it: through its own RGBE writer and
+    loader (image.cc:436-482, 296-434). Idempotent, so the quantized map
+    round-trips unchanged when the harness writes it again."""
+    path = OUT / "_tmp_q.hdr"
+    rh.write_hdr(path, env)
+    q = rh.load_hdr(path).astype(np.float32)
+    path.unlink()
+    return q
+
+
 def gen_render():
     """Whole passes of the reference render loop (compat semantics), N = 8."""
     sc = S.small_test_scene(seed=3, subdiv=3, width=64, height=48, photons=20000)
+    sc.env = quantize_env(sc.env)
     R = rh.RefScene(sc)
     res = R.render_passes(sc.camera, sc.photons, 2, photon_cap=200000)
     a = scene_arrays(sc)

@@ -1,0 +1,94 @@
+"""Whole-pass parity of the compat render loop against the reference.
+
+The fixture holds the reference's linear buffer after two passes of
+ProgressivePhotonMappingProb::render on a small mixed-material scene with
+OMP_NUM_THREADS=8, plus the photon multiset of the last pass read back from
+its kd-tree. The GPU run uses the same eight XorShift streams (jump-ahead
+per photon and pixel tape), so photon paths and eye paths follow the same
+random numbers; they differ only where FP32 shading moves a ray across a
+triangle edge, so the comparison is statistical: per-photon records must
+match for almost all photons and the image must agree to a small relMSE.
+"""
+import numpy as np
+import pytest
+
+import pppm_gb300 as P
+import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(g):
+    mats = g["mats"].reshape(-1).view(S.MATERIAL_DTYPE)
+    cam = S.Camera(tuple(g["eye"]), tuple(g["dir"]), tuple(g["up"]), float(g["fov"]), int(g["wh"][0]), int(g["wh"][1]))
+    return S.Scene("render_small", g["tris"], g["mat_id"], mats, g["env"], cam, photons=int(g["nphotons"]))
+
+
+def test_render_compat_two_passes(ctx, golden):
+    g = golden("render_small")
+    sc = _scene(g)
+    ctx.set_scene(sc)
+    par = P.Context.make_params(mode=P.MODE_COMPAT, photons=sc.photons, num_streams=int(g["threads"]))
+    ctx.render_begin(sc.camera, par)
+    st1 = ctx.render_pass(1)
+    assert st1.radius == g["radii"][0]
+    st2 = ctx.render_pass(2)
+    assert st2.radius == g["radii"][1]
+    img = ctx.render_read()
+    ref = g["accum"].astype(np.float64)
+    # photon multiset of pass 2: phantoms + stored records
+    ref_ph = g["photons"]
+    ref_phantom = np.all(ref_ph[:, :6] == 0, axis=1)
+    assert st2.phantom_photons == ref_phantom.sum()
+    assert st2.photons_stored == (~ref_phantom).sum()
+    gpu = ctx.render_photons(1 << 20)
+    from scipy.spatial import cKDTree
+
+    tree = cKDTree(ref_ph[~ref_phantom, :3])
+    dist, j = tree.query(gpu[:, :3].astype(np.float64))
+    rflux = ref_ph[~ref_phantom][j, 3:6]
+    match = (dist < 1e-3) & np.all(np.abs(gpu[:, 3:6] - rflux) <= 1e-4 * np.abs(rflux) + 1e-12, axis=1)
+    assert match.mean() > 0.98, match.mean()
+    # image: relMSE over pixels and the fraction of near-identical pixels
+    rel = np.abs(img - ref) / np.maximum(np.abs(ref), 1e-3)
+    close = np.all(rel < 1e-3, axis=2).mean()
+    relmse = np.mean((img - ref) ** 2) / np.mean(ref ** 2)
+    print(f"pixels within 1e-3: {close:.4f}, relMSE {relmse:.3e}")
+    assert close > 0.9
+    assert relmse < 1e-3
+
+
+def test_render_canonical_runs(ctx, golden):
+    g = golden("render_small")
+    sc = _scene(g)
+    ctx.set_scene(sc)
+    par = P.Context.make_params(mode=P.MODE_CANONICAL, photons=50000, radius_scale=1 / 64, seed=7)
+    ctx.render_begin(sc.camera, par)
+    r0 = None
+    for t in range(1, 5):
+        st = ctx.render_pass(t)
+        if r0 is None:
+            r0 = st.radius
+        # Knaus-Zwicker: r^2_{t+1} = r^2_t (t + alpha) / (t + 1)
+        expect = r0 ** 2
+        for s in range(1, t):
+            expect *= (s + 0.7) / (s + 1)
+        assert abs(st.radius ** 2 - expect) <= 1e-12 * expect
+    img = ctx.render_read() / 4
+    assert np.isfinite(img).all() and img.mean() > 0
+
+
+def test_render_errors(ctx, golden):
+    g = golden("render_small")
+    sc = _scene(g)
+    ctx.set_scene(sc)
+    par = P.Context.make_params(mode=P.MODE_COMPAT, photons=1000, num_streams=8)
+    ctx.render_begin(sc.camera, par)
+    with pytest.raises(P.PppmError):
+        ctx.render_pass(2)  # passes run in order
+    # k = (int)radius < 1 is undefined in the reference
+    par = P.Context.make_params(mode=P.MODE_COMPAT, photons=1000, num_streams=8, radius_scale=1e-3)
+    ctx.render_begin(sc.camera, par)
+    with pytest.raises(P.PppmError) as e:
+        ctx.render_pass(1)
+    assert e.value.code == P.E_UNDEFINED

@@ -1,0 +1,203 @@
+"""Stage parity on the GPU against the reference's own outputs (golden fixtures).
+
+Bit-exact where the stage is integer/index work or reproduces the reference's
+double arithmetic (env importance tables are built on the host in double);
+1e-5 relative in FP32 for radiance; kNN neighbour sets identical except for
+near-ties (two candidate distances within 1e-5 relative), which are counted,
+listed and bounded.
+"""
+import numpy as np
+import pytest
+
+import scenes as S
+from conftest import scene_from
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5  # FP32 radiance / flux tolerance
+
+
+def _env_ctx(ctx, golden):
+    g = golden("env")
+    ctx.set_scene(scene_from(S.ground(-5.0, 20.0).reshape(-1, 9)))
+    ctx.set_env(g["decoded"].astype(np.float32))
+    return g
+
+
+def test_env_tables(ctx, golden):
+    g = _env_ctx(ctx, golden)
+    pdf, cdf = ctx.env_tables()
+    # host double arithmetic; libm may differ in the last bit across machines
+    np.testing.assert_allclose(pdf, g["pdf"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(cdf, g["cdf"], rtol=1e-12, atol=0)
+
+
+def test_env_lookup(ctx, golden):
+    g = _env_ctx(ctx, golden)
+    out = ctx.env_lookup(g["dirs"].astype(np.float32))
+    ref = g["lookup"]
+    same = np.all(out == ref.astype(np.float32), axis=1)
+    # FP32 angles can pick the neighbouring texel when the reference's
+    # double coordinate lies within ~1e-5 texel of a texel edge
+    d = g["dirs"]
+    th = np.arccos(np.clip(d[:, 1], -1, 1))
+    ph = np.arctan2(d[:, 2], d[:, 0])
+    ph = np.where(ph < 0, ph + 2 * np.pi, ph)
+    h, w = g["decoded"].shape[:2]
+    fx, fy = ph / (2 * np.pi) * w, th / np.pi * h
+    edge = (np.abs(fx - np.round(fx)) < 1e-3) | (np.abs(fy - np.round(fy)) < 1e-3)
+    bad = ~same & ~edge
+    assert bad.sum() == 0, f"{bad.sum()} lookups differ away from texel edges"
+    assert (~same).sum() <= 0.001 * len(same)
+
+
+def test_emit_photons(ctx, golden):
+    g = _env_ctx(ctx, golden)
+    pos, d, flux, ok = ctx.emit_photons(g["tapes"], 100000)
+    assert ok.all()
+    np.testing.assert_allclose(pos, g["emit_pos"], rtol=0, atol=2e-4)  # |pos| = 50
+    np.testing.assert_allclose(d, g["emit_dir"], rtol=0, atol=2e-5)
+    rel = np.abs(flux - g["emit_flux"]) / np.maximum(np.abs(g["emit_flux"]), 1e-30)
+    good = np.all(rel < RTOL, axis=1)
+    # flux differs only where the emitted direction lands on a texel edge
+    assert good.mean() > 0.998, good.mean()
+
+
+def _ref_knn_sets(pos, q, k, eps):
+    """float64 distances of every photon, for tie classification."""
+    out = []
+    for i in range(0, len(q), 256):
+        d = np.sqrt(((q[i:i + 256, None, :].astype(np.float64) - pos[None].astype(np.float64)) ** 2).sum(-1))
+        out.append(d)
+    return np.concatenate(out, 0)
+
+
+@pytest.mark.parametrize("case", [0, 1, 2, 3])
+def test_knn_sets(ctx, golden, case):
+    g = golden("knn")
+    pos, q = g["pos"], g["queries"]
+    ntp, rad = int(g[f"ntp{case}"]), float(g[f"rad{case}"])
+    idx, cnt = ctx.knn(pos, q, ntp, rad, cap=64)
+    ref_idx, ref_cnt = g[f"idx{case}"], g[f"cnt{case}"]
+    assert np.array_equal(cnt, ref_cnt)
+    k = int(rad)
+    mism = [i for i in range(len(q)) if not np.array_equal(idx[i, :cnt[i]], ref_idx[i, :ref_cnt[i]])]
+    if not mism:
+        return
+    dist = _ref_knn_sets(pos, q[mism], k, ntp)
+    ties = []
+    for row, i in enumerate(mism):
+        a = set(idx[i, :cnt[i]].tolist())
+        b = set(ref_idx[i, :ref_cnt[i]].tolist())
+        dd = dist[row]
+        if a == b:
+            # same set, different order: only allowed among near-equal distances
+            o1 = dd[idx[i, :cnt[i]]]
+            o2 = dd[ref_idx[i, :ref_cnt[i]]]
+            assert np.allclose(o1, o2, rtol=1e-5), (i, o1, o2)
+            ties.append(i)
+            continue
+        sym = list(a ^ b)
+        kth = np.sort(dd[list(b)])[-1]
+        assert np.all(np.abs(dd[sym] - kth) <= 1e-5 * kth), (i, dd[sym], kth)
+        ties.append(i)
+    print(f"knn case {case}: {len(ties)} near-tie queries listed: {ties[:20]}")
+    assert len(ties) <= 0.002 * len(q)
+
+
+@pytest.mark.parametrize("case", [0, 1, 2, 3])
+def test_gather_compat(ctx, golden, case):
+    g = golden("gather")
+    ph12, rays = g["photons"], g["rays"]
+    rad = float(g[f"rad{case}"])
+    ref = g[f"L{case}"]
+    ph8 = np.zeros((len(ph12), 8), np.float32)
+    ph8[:, :6] = ph12[:, :6]
+    m = len(rays)
+    hit = rays[:, :3].copy()
+    hit[:, 1] = -5.0
+    q = np.zeros((m, 12), np.float32)
+    q[:, :3] = hit
+    q[:, 4] = 1.0  # plane normal; the disc filter uses |n . d|
+    q[:, 6:9] = g["refl"]
+    q[:, 9:12] = 1.0
+    out = ctx.gather(0, ph8, q, rad, 128)
+    scale = np.abs(ref).max()
+    err = np.abs(out - ref)
+    bad = np.flatnonzero(np.any(err > RTOL * np.abs(ref) + 1e-6 * scale, axis=1))
+    if bad.size:
+        # must be kNN near-ties: the k-th and (k+1)-th distances within 1e-5
+        d = _ref_knn_sets(ph12[:, :3], hit[bad], int(rad), 128)
+        k = int(rad)
+        srt = np.sort(d, axis=1)
+        gap = (srt[:, k] - srt[:, k - 1]) / srt[:, k - 1]
+        assert np.all(gap < 1e-5), (bad[gap >= 1e-5], err[bad[gap >= 1e-5]], ref[bad[gap >= 1e-5]])
+    assert bad.size <= 0.002 * m
+
+
+def test_gather_compat_phantoms(ctx, golden):
+    """Default Photon() slots (zero flux at the origin) enter the compat kNN."""
+    g = golden("gather")
+    ph12 = g["photons_ph"]
+    real = ~np.all(ph12 == 0, axis=1)
+    ph8 = np.zeros((real.sum(), 8), np.float32)
+    ph8[:, :6] = ph12[real, :6]
+    rays = g["rays_ph"]
+    m = len(rays)
+    q = np.zeros((m, 12), np.float32)
+    q[:, :3] = rays[:, :3]
+    q[:, 1] = -5.0
+    q[:, 4] = 1.0
+    q[:, 6:9] = g["refl"]
+    q[:, 9:12] = 1.0
+    out = ctx.gather(0, ph8, q, 6.5, 128, phantoms=int((~real).sum()))
+    ref = g["L_ph"]
+    scale = np.abs(ref).max()
+    ok = np.all(np.abs(out - ref) <= RTOL * np.abs(ref) + 1e-6 * scale, axis=1)
+    assert ok.mean() > 0.995, ok.mean()
+
+
+def _canonical_np(ph8, nrm, q12, r):
+    """float64 restatement of the canonical gather for checking."""
+    out = np.zeros((len(q12), 3))
+    for i in range(len(q12)):
+        d2 = ((ph8[:, :3].astype(np.float64) - q12[i, :3]) ** 2).sum(1)
+        sel = (d2 < r * r) & ((nrm @ q12[i, 3:6].astype(np.float64)) > 0)
+        s = ph8[sel, 3:6].astype(np.float64).sum(0)
+        out[i] = q12[i, 6:9] * q12[i, 9:12] * s / (np.pi * np.pi * r * r)
+    return out
+
+
+def pack_normals(n):
+    """Octahedral 2x16-bit packing used by photon records (pppm_device.cuh)."""
+    n = n / np.abs(n).sum(1, keepdims=True)
+    u, v = n[:, 0].copy(), n[:, 1].copy()
+    neg = n[:, 2] < 0
+    pu = (1 - np.abs(v)) * np.where(u >= 0, 1, -1)
+    pv = (1 - np.abs(u)) * np.where(v >= 0, 1, -1)
+    u[neg], v[neg] = pu[neg], pv[neg]
+    qu = np.rint((np.clip(u, -1, 1) * 0.5 + 0.5) * 65535).astype(np.uint32)
+    qv = np.rint((np.clip(v, -1, 1) * 0.5 + 0.5) * 65535).astype(np.uint32)
+    return (qu | (qv << 16)).view(np.float32)
+
+
+@pytest.mark.parametrize("r", [0.7, 2.3])
+def test_gather_canonical(ctx, golden, r):
+    g = golden("gather")
+    ph12 = g["photons"]
+    ph8 = np.zeros((len(ph12), 8), np.float32)
+    ph8[:, :6] = ph12[:, :6]
+    ph8[:, 6] = pack_normals(ph12[:, 9:12].astype(np.float64))
+    rng = np.random.default_rng(4)
+    m = 600
+    qp = ph12[rng.integers(0, len(ph12), m), :3] + rng.normal(size=(m, 3)).astype(np.float32) * 0.2
+    qn = rng.normal(size=(m, 3))
+    qn[: m // 2] = [0, 1, 0]
+    qn /= np.linalg.norm(qn, axis=1, keepdims=True)
+    q = np.concatenate([qp, qn, rng.uniform(0.2, 0.9, (m, 3)), rng.uniform(0.5, 2, (m, 3))], 1).astype(np.float32)
+    out = ctx.gather(1, ph8, q, r)
+    ref = _canonical_np(ph8, ph12[:, 9:12].astype(np.float64), q, r)
+    scale = np.abs(ref).max()
+    ok = np.all(np.abs(out - ref) <= RTOL * np.abs(ref) + 1e-6 * scale, axis=1)
+    # boundary photons (|d - r| < 1e-5 r) or normals within the packing error of perpendicular may flip
+    assert ok.mean() > 0.99, ok.mean()
