@@ -93,9 +93,12 @@ typedef struct {
     double gather_radius;   /* RenderParameters::gatherRadius */
     double alpha;           /* ALPHA (0.7) */
     double radius_scale;    /* r1 = radius_scale * |bbox diagonal| (0.1 in the reference) */
-    float cell_factor;      /* canonical hash-grid cell size / radius */
-    int32_t reserved;
+    float cell_factor;      /* hash-grid cell size: canonical = cell_factor * radius (>= 1) */
+    int32_t flags;          /* PPPM_FLAG_* */
 } pppm_params;
+
+/* pppm_params.flags */
+#define PPPM_FLAG_COUNT_TRAVERSAL 0x1 /* count BVH nodes visited / triangles tested */
 
 /* Per-pass statistics written by pppm_render_pass. */
 typedef struct {
@@ -110,6 +113,12 @@ typedef struct {
     double ms_grid;          /* hash-grid build (ms) */
     double ms_eye;           /* eye paths (ms) */
     double ms_gather;        /* gather (ms) */
+    double ms_bounce;        /* photon bounce kernels only (ms) */
+    int64_t kernel_launches; /* kernels launched by the pass */
+    int64_t node_visits;     /* BVH nodes visited (PPPM_FLAG_COUNT_TRAVERSAL) */
+    int64_t tri_tests;       /* triangles tested (PPPM_FLAG_COUNT_TRAVERSAL) */
+    int64_t photon_node_visits; /* of which by photon rays */
+    int64_t photon_tri_tests;
 } pppm_pass_stats;
 
 /* ------------------------------------------------------------- lifetime */

@@ -69,6 +69,12 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> pathlib.Path:
                 logs.append(out)
     if jobs or not LIB.exists():
         _run([nvcc, *ARCH, "-shared", "-Xcompiler", "-fopenmp", "-o", str(LIB), *map(str, objs)])
+    demo = HERE / "appmain_gpu"
+    src = HERE / "host" / "appmain_gpu.cc"
+    if not demo.exists() or demo.stat().st_mtime < max(LIB.stat().st_mtime, src.stat().st_mtime,
+                                                       (HERE / "host" / "pppm.hpp").stat().st_mtime):
+        _run(["g++", "-std=c++17", "-O2", str(src), "-o", str(demo), f"-L{HERE}", "-lpppm_gb300",
+              f"-Wl,-rpath,{HERE}"])
     if verbose or ptxas_info:
         for s in logs:
             if s.strip():

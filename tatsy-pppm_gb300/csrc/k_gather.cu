@@ -316,3 +316,27 @@ cudaError_t launchPackQueries(const float* in12, int64_t m, float4* q, cudaStrea
 }
 
 }  // namespace pppm
+
+namespace pppm {
+
+namespace {
+// Photon records (pos|normal, flux|id) -> 8 floats (pos, flux, normal, id),
+// the layout of pppm_gather's photon input.
+__global__ void kUnpackRecords(const float4* __restrict__ rec, int64_t n, float* __restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 a = rec[2 * i], b = rec[2 * i + 1];
+        float* o = out + 8 * i;
+        o[0] = a.x; o[1] = a.y; o[2] = a.z;
+        o[3] = b.x; o[4] = b.y; o[5] = b.z;
+        o[6] = a.w; o[7] = b.w;
+    }
+}
+}  // namespace
+
+cudaError_t launchUnpackRecords(const float4* rec, int64_t n, float* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    kUnpackRecords<<<blocksFor(n, 256), 256, 0, st>>>(rec, n, out);
+    return cudaGetLastError();
+}
+
+}  // namespace pppm

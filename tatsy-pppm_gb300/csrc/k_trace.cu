@@ -220,12 +220,12 @@ __global__ void __launch_bounds__(128) kPhotonBounce(TraceParams tp, SceneView s
             p = in[i];
             alive = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
         }
-        int traced = 0;
+        int traced = 0, visits = 0, tests = 0;
         if (alive) {
             double best;
             traced = 1;
             const int slot = traverseExact<true>(sc.nodes, sc.tris, sc.rootCode, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz,
-                                                 order, &best, nullptr, nullptr);
+                                                 order, &best, &visits, &tests);
             if (slot < 0) {
                 alive = false;
             } else {
@@ -276,6 +276,14 @@ __global__ void __launch_bounds__(128) kPhotonBounce(TraceParams tp, SceneView s
         if (alive) out[oi] = p;
         const unsigned nt = __reduce_add_sync(0xffffffffu, (unsigned)traced);
         if ((threadIdx.x & 31) == 0 && nt) atomicAdd(&ctr->photonRays, (unsigned long long)nt);
+        if (tp.countTraversal) {
+            const unsigned nv = __reduce_add_sync(0xffffffffu, (unsigned)visits);
+            const unsigned nx = __reduce_add_sync(0xffffffffu, (unsigned)tests);
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(&ctr->nodeVisits[0], (unsigned long long)nv);
+                atomicAdd(&ctr->triTests[0], (unsigned long long)nx);
+            }
+        }
     }
 }
 
@@ -303,7 +311,7 @@ __global__ void __launch_bounds__(128) kEyeTrace(TraceParams tp, SceneView sc, E
         const int64_t pix = base + threadIdx.x;
         bool query = false;
         float4 q0, q1, q2;
-        int traced = 0;
+        int traced = 0, visits = 0, tests = 0;
         if (pix < np) {
             const int x = (int)(pix % cam.w), y = (int)(pix / cam.w);
             Tape tape;
@@ -328,7 +336,7 @@ __global__ void __launch_bounds__(128) kEyeTrace(TraceParams tp, SceneView sc, E
                 double best;
                 traced++;
                 const int slot = traverseExact<true>(sc.nodes, sc.tris, sc.rootCode, o[0], o[1], o[2], d.x, d.y, d.z,
-                                                     order, &best, nullptr, nullptr);
+                                                     order, &best, &visits, &tests);
                 if (slot < 0) {
                     L = L + w * envLookup(env, d);
                     break;
@@ -374,6 +382,14 @@ __global__ void __launch_bounds__(128) kEyeTrace(TraceParams tp, SceneView sc, E
         }
         const unsigned nt = __reduce_add_sync(0xffffffffu, (unsigned)traced);
         if ((threadIdx.x & 31) == 0 && nt) atomicAdd(&ctr->eyeRays, (unsigned long long)nt);
+        if (tp.countTraversal) {
+            const unsigned nv = __reduce_add_sync(0xffffffffu, (unsigned)visits);
+            const unsigned nx = __reduce_add_sync(0xffffffffu, (unsigned)tests);
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(&ctr->nodeVisits[1], (unsigned long long)nv);
+                atomicAdd(&ctr->triTests[1], (unsigned long long)nx);
+            }
+        }
     }
 }
 

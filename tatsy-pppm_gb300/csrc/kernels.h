@@ -36,5 +36,6 @@ cudaError_t launchKnn(const GridDev& g, const float* queries, int64_t m, int k, 
 cudaError_t launchPackPhotons(const float* in8, int64_t n, float4* rec, uint64_t* count, cudaStream_t st);
 cudaError_t launchPackPositions(const float* pos3, int64_t n, float4* rec, uint64_t* count, cudaStream_t st);
 cudaError_t launchPackQueries(const float* in12, int64_t m, float4* q, cudaStream_t st);
+cudaError_t launchUnpackRecords(const float4* rec, int64_t n, float* out, cudaStream_t st);
 
 }  // namespace pppm

@@ -208,6 +208,8 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     tp.maxBounceEye = par.max_bounce_eye;
     tp.seed = par.seed;
     tp.pass = t;
+    tp.countTraversal = (par.flags & PPPM_FLAG_COUNT_TRAVERSAL) ? 1 : 0;
+    int64_t launches = 0;
 
     CameraDev cd;
     {
@@ -240,17 +242,21 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         PPPM_CUDA(c, cudaMemcpyAsync(rs.streamStatesD.p, ss.data(), ss.size() * 4, cudaMemcpyHostToDevice, c->stream));
         PPPM_CUDA(c, launchTapeStates(tp, rs.streamStatesD.as<uint32_t>(), rs.jumpMats.as<uint32_t>(), W, H, photonStates,
                                       pixelStates, c->stream));
+        launches += 1;
     }
     PassCounters hc;
     for (int attempt = 0;; attempt++) {
         PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters) + 8 * (size_t)N, c->stream));
         PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
+        PPPM_CUDA(c, cudaEventRecord(c->ev[5], c->stream));
+        launches += 1 + par.max_bounce_photon;
         for (int b = 0; b < par.max_bounce_photon; b++) {
             PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
             PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
             PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, rs.photons.as<float4>(), rs.depositCap, ctr,
                                             c->stream));
         }
+        PPPM_CUDA(c, cudaEventRecord(c->ev[6], c->stream));
         PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
         PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
         if ((int64_t)hc.deposits <= rs.depositCap) break;
@@ -266,6 +272,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         // i * ceil(P/N); unused slots keep default Photon() records.
         PPPM_CUDA(c, launchStreamCounts(rs.photons.as<float4>(), &ctr->deposits, rs.depositCap, T, N, perStream,
                                         c->stream));
+        launches += 1;
         std::vector<unsigned long long> ps(N);
         PPPM_CUDA(c, cudaMemcpyAsync(ps.data(), perStream, 8 * (size_t)N, cudaMemcpyDeviceToHost, c->stream));
         PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -292,6 +299,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     PPPM_CUDA(c, gridBuild(rs.grid, gv, rs.photons.as<float4>(), reinterpret_cast<const uint64_t*>(&ctr->deposits),
                            rs.depositCap, c->stream));
     gv = gridView(rs.grid, c->bbmin, c->bbmax);
+    launches += 5;
     PPPM_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
 
     // eye paths and gather
@@ -304,6 +312,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
                                         rs.accum.as<float>(), true, c->stream));
     else
         PPPM_CUDA(c, launchGatherCanonical(gv, qv, (float)rs.radius, rs.accum.as<float>(), true, c->stream));
+    launches += 2;
     PPPM_CUDA(c, cudaEventRecord(c->ev[4], c->stream));
     PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -326,6 +335,13 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         stats->ms_eye = ms;
         cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]);
         stats->ms_gather = ms;
+        cudaEventElapsedTime(&ms, c->ev[5], c->ev[6]);
+        stats->ms_bounce = ms;
+        stats->kernel_launches = launches;
+        stats->node_visits = (int64_t)(hc.nodeVisits[0] + hc.nodeVisits[1]);
+        stats->tri_tests = (int64_t)(hc.triTests[0] + hc.triTests[1]);
+        stats->photon_node_visits = (int64_t)hc.nodeVisits[0];
+        stats->photon_tri_tests = (int64_t)hc.triTests[0];
     }
     if (hc.undefinedEmit)
         return fail(c, PPPM_E_UNDEFINED, "render_pass: a photon draw fell past the env CDF (reference reads _pdf out of bounds)");
@@ -373,8 +389,11 @@ int pppm_render_photons(pppm_ctx* c, float* out, int64_t cap, int64_t* n) {
     *n = cnt;
     const int64_t m = std::min(cnt, cap);
     if (m > 0) {
-        PPPM_CUDA(c, cudaMemcpyAsync(out, c->rs.photons.p, (size_t)m * 32,
-                                     isDevicePtr(out) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+        void* dout;
+        int r;
+        if ((r = stageOut(c, out, (size_t)m * 32, 0, &dout))) return r;
+        PPPM_CUDA(c, launchUnpackRecords(c->rs.photons.as<float4>(), m, (float*)dout, c->stream));
+        if ((r = finishOut(c, out, dout, (size_t)m * 32))) return r;
         PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     return PPPM_OK;

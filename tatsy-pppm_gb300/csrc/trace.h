@@ -25,6 +25,8 @@ struct PassCounters {
     unsigned long long photonRays;    // photon traversals
     unsigned long long eyeRays;       // eye traversals
     unsigned long long undefinedEmit; // CDF inversion past the last entry (reference reads out of bounds)
+    unsigned long long nodeVisits[2]; // [photon, eye] BVH nodes visited (counting flag)
+    unsigned long long triTests[2];   // [photon, eye] triangles tested (counting flag)
 };
 
 struct CameraDev {
@@ -46,6 +48,7 @@ struct TraceParams {
     int maxBounceEye;
     uint32_t seed;
     int pass;
+    int countTraversal;
 };
 
 // Jump-ahead matrices: J[k] advances a XorShift state by 200 * 2^k draws

@@ -1,0 +1,439 @@
+// C++ host mirror of the tatsy-pppm interface over the GB300 C ABI.
+//
+// Same class names and argument meanings as the reference, so a driver
+// written against the reference (appmain.cc:11-26 shape) switches to the GPU
+// by including this header instead of renderer.h and linking
+// libpppm_gb300.so:
+//
+//   Scene scene;                      scene.h:23-56
+//   scene.add(mesh, LambertianBRDF::factory(Vector3D(0.7, 0.3, 0.3)));
+//   scene.setEnvmap(Envmap("sky.hdr"));
+//   scene.setAccelerator();
+//   Camera camera(eye, dir, up, 45.0, w, h, 1.0);
+//   RenderParameters params(2000000, spp, 128, 16.0);
+//   ProgressivePhotonMappingProb ppm;
+//   ppm.render(scene, camera, params);
+//
+// Where the reference aborts (Assertion, common.h:24-35) the mirror throws
+// pppm::Error carrying the C ABI status and message; uncaught, it ends the
+// program as the reference's abort does. Header-only.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <fstream>
+#include <iterator>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/pppm_c.h"
+
+namespace pppm {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void check(int r, const pppm_ctx* c, const char* what) {
+    if (r != PPPM_OK) throw Error(r, std::string(what) + ": " + (c ? pppm_last_error(c) : "no context"));
+}
+
+// One context per thread of the calling program; created on first use.
+inline pppm_ctx* context() {
+    thread_local std::unique_ptr<pppm_ctx, int (*)(pppm_ctx*)> ctx(nullptr, pppm_destroy);
+    if (!ctx) {
+        pppm_ctx* c = nullptr;
+        check(pppm_create(0, &c), nullptr, "pppm_create");
+        ctx.reset(c);
+    }
+    return ctx.get();
+}
+
+}  // namespace pppm
+
+// --------------------------------------------------------------- math
+class Vector3D {  // vector3d.h:21-98 (double x3)
+    double v_[3];
+
+public:
+    Vector3D() : v_{0, 0, 0} {}
+    Vector3D(double x, double y, double z) : v_{x, y, z} {}
+    double x() const { return v_[0]; }
+    double y() const { return v_[1]; }
+    double z() const { return v_[2]; }
+    double operator[](int d) const { return v_[d]; }
+    double norm() const { return std::sqrt(dot(*this, *this)); }
+    Vector3D normalized() const { return *this / (norm() + 1e-12); }
+    static double dot(const Vector3D& a, const Vector3D& b) { return a.x() * b.x() + a.y() * b.y() + a.z() * b.z(); }
+    static Vector3D cross(const Vector3D& u, const Vector3D& v) {
+        return Vector3D(u.y() * v.z() - u.z() * v.y(), u.z() * v.x() - u.x() * v.z(), u.x() * v.y() - u.y() * v.x());
+    }
+    friend Vector3D operator+(const Vector3D& a, const Vector3D& b) { return Vector3D(a.x() + b.x(), a.y() + b.y(), a.z() + b.z()); }
+    friend Vector3D operator-(const Vector3D& a, const Vector3D& b) { return Vector3D(a.x() - b.x(), a.y() - b.y(), a.z() - b.z()); }
+    friend Vector3D operator*(const Vector3D& a, double s) { return Vector3D(a.x() * s, a.y() * s, a.z() * s); }
+    friend Vector3D operator*(double s, const Vector3D& a) { return a * s; }
+    friend Vector3D operator/(const Vector3D& a, double s) { return a * (1.0 / s); }
+    Vector3D operator-() const { return Vector3D(-v_[0], -v_[1], -v_[2]); }
+};
+
+// --------------------------------------------------------------- geometry
+class Triangle {  // triangle.h:16-45
+    Vector3D p_[3];
+
+public:
+    Triangle() = default;
+    Triangle(const Vector3D& a, const Vector3D& b, const Vector3D& c) : p_{a, b, c} {}
+    Vector3D p(int i) const { return p_[i]; }
+    std::vector<Triangle> triangulate() const { return {*this}; }
+};
+
+class Trimesh {  // trimesh.h:68-166: binary little-endian PLY (float xyz, uchar + 3 int faces)
+    std::vector<Vector3D> verts_;
+    std::vector<int> faces_;
+
+public:
+    Trimesh() = default;
+    explicit Trimesh(const std::string& filename) { load(filename); }
+    Trimesh(const std::vector<Vector3D>& v, const std::vector<int>& f) : verts_(v), faces_(f) {}
+    void load(const std::string& filename) {  // trimesh.cc:125-217
+        std::ifstream in(filename, std::ios::binary);
+        if (!in) throw pppm::Error(PPPM_E_ARG, "Failed to open mesh file: " + filename);
+        std::string line;
+        size_t nv = 0, nf = 0;
+        std::getline(in, line);
+        if (line.rfind("ply", 0) != 0) throw pppm::Error(PPPM_E_ARG, "Invalid format identifier");
+        while (std::getline(in, line)) {
+            if (line.rfind("format", 0) == 0 && line.find("binary_little_endian") == std::string::npos)
+                throw pppm::Error(PPPM_E_ARG, "PLY must be binary little endian format!");
+            if (line.rfind("element vertex", 0) == 0) nv = std::stoull(line.substr(15));
+            if (line.rfind("element face", 0) == 0) nf = std::stoull(line.substr(13));
+            if (line.rfind("end_header", 0) == 0) break;
+        }
+        if (nv == 0 || nf == 0) throw pppm::Error(PPPM_E_ARG, "numVerts and numFaces must be positive");
+        verts_.resize(nv);
+        for (auto& v : verts_) {
+            float f[3];
+            in.read(reinterpret_cast<char*>(f), 12);
+            v = Vector3D(f[0], f[1], f[2]);
+        }
+        faces_.resize(3 * nf);
+        for (size_t i = 0; i < nf; i++) {
+            unsigned char n;
+            in.read(reinterpret_cast<char*>(&n), 1);
+            if (n != 3) throw pppm::Error(PPPM_E_ARG, "mesh contains non-triangle polygon");
+            in.read(reinterpret_cast<char*>(&faces_[3 * i]), 12);
+        }
+        if (!in) throw pppm::Error(PPPM_E_ARG, "truncated PLY body");
+    }
+    size_t numVerts() const { return verts_.size(); }
+    size_t numFaces() const { return faces_.size() / 3; }
+    std::vector<Triangle> triangulate() const {
+        std::vector<Triangle> out;
+        out.reserve(numFaces());
+        for (size_t i = 0; i < numFaces(); i++)
+            out.emplace_back(verts_.at(faces_[3 * i]), verts_.at(faces_[3 * i + 1]), verts_.at(faces_[3 * i + 2]));
+        return out;
+    }
+};
+
+// --------------------------------------------------------------- materials
+enum BsdfType {  // bsdf.h:19-26
+    BSDF_TYPE_NONE = 0x00,
+    BSDF_TYPE_LAMBERTIAN_BRDF = PPPM_BSDF_LAMBERTIAN,
+    BSDF_TYPE_SPECULAR_BRDF = PPPM_BSDF_SPECULAR,
+    BSDF_TYPE_PHONG_BRDF = PPPM_BSDF_PHONG,
+    BSDF_TYPE_REFRACTION = PPPM_BSDF_REFRACTION,
+    BSDF_TYPE_BSSRDF = PPPM_BSDF_BSSRDF
+};
+
+class BSSRDF {
+public:
+    pppm_material dipole{};
+};
+
+class DipoleBSSRDF {  // bssrdf.h:47-66
+public:
+    static BSSRDF factory(const Vector3D& sigma_a, const Vector3D& sigmap_s, double eta = 1.3, double scale = 1.0) {
+        BSSRDF b;
+        for (int k = 0; k < 3; k++) {
+            b.dipole.sigma_a[k] = (float)sigma_a[k];
+            b.dipole.sigmap_s[k] = (float)sigmap_s[k];
+        }
+        b.dipole.eta = (float)eta;
+        b.dipole.scale = (float)scale;
+        return b;
+    }
+};
+
+class BSDF {  // bsdf.h:32-59
+public:
+    pppm_material m{};
+    BsdfType type() const { return (BsdfType)(m.type | (m.has_bssrdf ? PPPM_BSDF_BSSRDF : 0)); }
+    Vector3D reflectance() const { return Vector3D(m.refl[0], m.refl[1], m.refl[2]); }
+    void setBssrdf(const BSSRDF& b) {
+        m.has_bssrdf = 1;
+        for (int k = 0; k < 3; k++) {
+            m.sigma_a[k] = b.dipole.sigma_a[k];
+            m.sigmap_s[k] = b.dipole.sigmap_s[k];
+        }
+        m.eta = b.dipole.eta;
+        m.scale = b.dipole.scale;
+    }
+    static BSDF make(int type, const Vector3D& r, double n = 0.0) {
+        BSDF b;
+        b.m.type = type;
+        for (int k = 0; k < 3; k++) b.m.refl[k] = (float)r[k];
+        b.m.phong_n = (float)n;
+        return b;
+    }
+};
+
+struct LambertianBRDF {
+    static BSDF factory(const Vector3D& r) { return BSDF::make(PPPM_BSDF_LAMBERTIAN, r); }
+};
+struct SpecularBRDF {
+    static BSDF factory(const Vector3D& r) { return BSDF::make(PPPM_BSDF_SPECULAR, r); }
+};
+struct PhongBRDF {
+    static BSDF factory(const Vector3D& r, double n) { return BSDF::make(PPPM_BSDF_PHONG, r, n); }
+};
+struct RefractionBSDF {
+    static BSDF factory(const Vector3D& r) { return BSDF::make(PPPM_BSDF_REFRACTION, r); }
+};
+
+// --------------------------------------------------------------- env map
+class Envmap {  // envmap.h:21-47
+public:
+    int width = 0, height = 0;
+    std::vector<float> rgb;  // row 0 = top, as Image stores it
+    Envmap() = default;
+    explicit Envmap(const std::string& filename) {  // Radiance HDR via Image::loadHdr semantics
+        std::ifstream in(filename, std::ios::binary);
+        if (!in) throw pppm::Error(PPPM_E_ARG, "Failed to load file \"" + filename + "\"");
+        std::vector<uint8_t> bytes((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+        int32_t w = 0, h = 0;
+        pppm::check(pppm_hdr_decode(bytes.data(), (int64_t)bytes.size(), nullptr, 0, &w, &h), nullptr, "Envmap");
+        rgb.resize((size_t)w * h * 3);
+        pppm::check(pppm_hdr_decode(bytes.data(), (int64_t)bytes.size(), rgb.data(), (int64_t)rgb.size(), &w, &h),
+                    nullptr, "Envmap");
+        width = w;
+        height = h;
+    }
+    Envmap(int w, int h, std::vector<float> data) : width(w), height(h), rgb(std::move(data)) {}
+};
+
+// --------------------------------------------------------------- rays / scene
+class Ray {  // ray.h:20-38
+    Vector3D o_, d_;
+
+public:
+    Ray(const Vector3D& o, const Vector3D& d) : o_(o), d_(d) {}
+    Vector3D origin() const { return o_; }
+    Vector3D direction() const { return d_; }
+};
+
+class Hitpoint {  // ray.h:40-60
+public:
+    double distance_ = 1e20;
+    Vector3D position_, normal_;
+    double distance() const { return distance_; }
+    Vector3D position() const { return position_; }
+    Vector3D normal() const { return normal_; }
+};
+
+class Intersection {  // ray.h:62-80
+public:
+    Hitpoint hp;
+    int id = -1;
+    int objectID() const { return id; }
+    const Hitpoint& hitpoint() const { return hp; }
+};
+
+class Scene {  // scene.h:23-56, scene.cc
+    std::vector<float> tris_;
+    std::vector<int32_t> matId_;
+    std::vector<pppm_material> mats_;
+    Envmap env_;
+    bool accel_ = false;
+
+public:
+    template <class T>
+    void add(const T& geom, const BSDF& bsdf) {
+        const int id = (int)mats_.size();
+        mats_.push_back(bsdf.m);
+        for (const Triangle& t : geom.triangulate()) {
+            for (int k = 0; k < 3; k++)
+                for (int d = 0; d < 3; d++) tris_.push_back((float)t.p(k)[d]);
+            matId_.push_back(id);
+        }
+        accel_ = false;
+    }
+    void setEnvmap(const Envmap& e) { env_ = e; }
+    void setAccelerator() {
+        pppm_ctx* c = pppm::context();
+        pppm::check(pppm_scene_set(c, tris_.data(), (int64_t)matId_.size(), matId_.data(), mats_.data(),
+                                   (int32_t)mats_.size()), c, "Scene::setAccelerator");
+        if (!env_.rgb.empty())
+            pppm::check(pppm_env_set(c, env_.rgb.data(), env_.width, env_.height), c, "Scene::setEnvmap");
+        accel_ = true;
+    }
+    size_t numTriangles() const { return matId_.size(); }
+    // Scene::intersect -> QBVHAccel::intersect (scene.cc:40-47)
+    bool intersect(const Ray& ray, Intersection& isect) const {
+        if (!accel_) throw pppm::Error(PPPM_E_STATE, "Scene::intersect before setAccelerator");
+        const float r[6] = {(float)ray.origin().x(), (float)ray.origin().y(), (float)ray.origin().z(),
+                            (float)ray.direction().x(), (float)ray.direction().y(), (float)ray.direction().z()};
+        int32_t tri;
+        double t;
+        float pos[3], nrm[3];
+        pppm_ctx* c = pppm::context();
+        pppm::check(pppm_intersect(c, r, 1, &tri, &t, pos, nrm), c, "Scene::intersect");
+        isect.id = tri;
+        isect.hp.distance_ = t;
+        isect.hp.position_ = Vector3D(pos[0], pos[1], pos[2]);
+        isect.hp.normal_ = Vector3D(nrm[0], nrm[1], nrm[2]);
+        return tri != -1;
+    }
+};
+
+// --------------------------------------------------------------- camera / params
+class PerspectiveCamera {  // perspective_camera.h:16-32
+public:
+    pppm_camera c{};
+    PerspectiveCamera() = default;
+    PerspectiveCamera(const Vector3D& center, const Vector3D& direction, const Vector3D& up, double fov, int w, int h,
+                      double /*sensitivity*/) {
+        for (int d = 0; d < 3; d++) {
+            c.eye[d] = (float)center[d];
+            c.dir[d] = (float)direction[d];
+            c.up[d] = (float)up[d];
+        }
+        c.fov = (float)fov;
+        c.width = w;
+        c.height = h;
+    }
+};
+typedef PerspectiveCamera Camera;
+
+class RenderParameters {  // render_parameters.h:4-37
+    int photons_, spp_, gatherPhotons_;
+    double gatherRadius_;
+
+public:
+    explicit RenderParameters(int photons = 1000000, int spp = 16, int gatherPhotons = 16, double gatherRadius = 16.0)
+        : photons_(photons), spp_(spp), gatherPhotons_(gatherPhotons), gatherRadius_(gatherRadius) {}
+    int photons() const { return photons_; }
+    int spp() const { return spp_; }
+    int gatherPhotons() const { return gatherPhotons_; }
+    double gatherRadius() const { return gatherRadius_; }
+};
+
+// --------------------------------------------------------------- integrator
+class ProgressivePhotonMappingProb {  // ppm_probabilistic.h:23-42
+    std::vector<float> result_;
+    int w_ = 0, h_ = 0, passes_ = 0;
+
+public:
+    // Reference semantics by default; `mode` selects PPPM_MODE_CANONICAL.
+    // numStreams is the reference's OMP_NUM_CORE (its RNG stream count).
+    int mode = PPPM_MODE_COMPAT;
+    int numStreams = 8;
+
+    // ProgressivePhotonMappingProb::render (ppm_probabilistic.cc:24-121): the
+    // reference writes a PNG per pass; here the linear buffer stays on the
+    // GPU and result() returns buffer / passes after the call.
+    void render(const Scene& /*scene*/, const Camera& camera, const RenderParameters& params) {
+        pppm_ctx* ctx = pppm::context();
+        pppm_params p{};
+        p.mode = mode;
+        p.num_streams = numStreams;
+        p.photons = params.photons();
+        p.gather_photons = params.gatherPhotons();
+        p.gather_radius = params.gatherRadius();
+        p.max_bounce_photon = 64;
+        p.max_bounce_eye = 64;
+        p.alpha = 0.7;
+        p.radius_scale = mode == PPPM_MODE_COMPAT ? 0.1 : 1.0 / 64.0;
+        p.cell_factor = 1.0f;
+        p.seed = 1;
+        pppm::check(pppm_render_begin(ctx, &camera.c, &p), ctx, "render");
+        for (int t = 1; t <= params.spp(); t++) pppm::check(pppm_render_pass(ctx, t, nullptr), ctx, "render");
+        w_ = camera.c.width;
+        h_ = camera.c.height;
+        passes_ = params.spp();
+        result_.assign((size_t)w_ * h_ * 3, 0.0f);
+        pppm::check(pppm_render_read(ctx, result_.data()), ctx, "render");
+    }
+    // Linear radiance per pixel (row y = camera row y, not flipped), divided
+    // by the pass count like the reference's per-pass image (:97-100).
+    std::vector<float> result() const {
+        std::vector<float> r(result_);
+        for (auto& v : r) v /= (float)(passes_ > 0 ? passes_ : 1);
+        return r;
+    }
+    int width() const { return w_; }
+    int height() const { return h_; }
+};
+
+// --------------------------------------------------------------- photon map / hash grid
+class Photon : public Vector3D {  // photon.h:6-44
+public:
+    Vector3D flux_;
+    using Vector3D::Vector3D;
+    Photon(const Vector3D& p, const Vector3D& flux) : Vector3D(p), flux_(flux) {}
+    Vector3D flux() const { return flux_; }
+};
+
+class PhotonMap {  // photon_map.h:18-29
+    std::vector<Photon> photons_;
+    std::vector<float> pos_;
+
+public:
+    void construct(const std::vector<Photon>& photons) {
+        photons_ = photons;
+        pos_.clear();
+        for (const Photon& p : photons)
+            for (int d = 0; d < 3; d++) pos_.push_back((float)p[d]);
+    }
+    // PhotonMap::findKNN (photon_map.cc:24-26), reference argument order and
+    // result order (farthest first).
+    void findKNN(const Photon& query, std::vector<Photon>* out, int numTargetPhotons, double targetRadius) const {
+        const float q[3] = {(float)query.x(), (float)query.y(), (float)query.z()};
+        const int cap = 64;
+        std::vector<int32_t> idx(cap);
+        int32_t cnt = 0;
+        pppm_ctx* c = pppm::context();
+        pppm::check(pppm_knn(c, pos_.data(), (int64_t)photons_.size(), q, 1, numTargetPhotons, targetRadius,
+                             idx.data(), &cnt, cap), c, "PhotonMap::findKNN");
+        for (int i = 0; i < cnt && i < cap; i++) out->push_back(photons_[idx[i]]);
+    }
+};
+
+template <class T>
+class HashGrid {  // hash_grid.h:8-37: bucket selection on the GPU
+    int size_ = -1;
+    double scale_ = 0.0;
+    double bbmin_[3] = {0, 0, 0};
+
+public:
+    void init(int hashSize, double hashScale, const Vector3D& bbMin) {
+        size_ = hashSize;
+        scale_ = hashScale;
+        for (int d = 0; d < 3; d++) bbmin_[d] = bbMin[d];
+    }
+    // bucket index of HashGrid::operator[] for each point
+    std::vector<uint32_t> buckets(const std::vector<Vector3D>& pts) const {
+        std::vector<float> p;
+        for (const auto& v : pts)
+            for (int d = 0; d < 3; d++) p.push_back((float)v[d]);
+        std::vector<uint32_t> out(pts.size());
+        pppm_ctx* c = pppm::context();
+        pppm::check(pppm_hash_points(c, p.data(), (int64_t)pts.size(), size_, scale_, bbmin_, out.data()), c,
+                    "HashGrid");
+        return out;
+    }
+};

@@ -18,6 +18,7 @@ LIB_PATH = HERE / "libpppm_gb300.so"
 OK = 0
 E_ARG, E_CUDA, E_STATE, E_CAPACITY, E_UNDEFINED, E_TIMEOUT = -1, -2, -3, -4, -5, -6
 MODE_COMPAT, MODE_CANONICAL = 0, 1
+FLAG_COUNT_TRAVERSAL = 0x1
 
 _lib = None
 
@@ -38,14 +39,17 @@ class Params(ctypes.Structure):
                 ("gather_photons", ctypes.c_int32), ("max_bounce_photon", ctypes.c_int32),
                 ("max_bounce_eye", ctypes.c_int32), ("seed", ctypes.c_uint32), ("gather_radius", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("radius_scale", ctypes.c_double), ("cell_factor", ctypes.c_float),
-                ("reserved", ctypes.c_int32)]
+                ("flags", ctypes.c_int32)]
 
 
 class PassStats(ctypes.Structure):
     _fields_ = [("photons_traced", ctypes.c_int64), ("photons_stored", ctypes.c_int64),
                 ("phantom_photons", ctypes.c_int64), ("photon_rays", ctypes.c_int64), ("eye_rays", ctypes.c_int64),
                 ("gather_queries", ctypes.c_int64), ("radius", ctypes.c_double), ("ms_photon", ctypes.c_double),
-                ("ms_grid", ctypes.c_double), ("ms_eye", ctypes.c_double), ("ms_gather", ctypes.c_double)]
+                ("ms_grid", ctypes.c_double), ("ms_eye", ctypes.c_double), ("ms_gather", ctypes.c_double),
+                ("ms_bounce", ctypes.c_double), ("kernel_launches", ctypes.c_int64), ("node_visits", ctypes.c_int64),
+                ("tri_tests", ctypes.c_int64), ("photon_node_visits", ctypes.c_int64),
+                ("photon_tri_tests", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -242,7 +246,8 @@ class Context:
 
     @staticmethod
     def make_params(mode=MODE_COMPAT, photons=200_000, num_streams=8, gather_photons=128, gather_radius=16.0,
-                    alpha=0.7, radius_scale=0.1, max_bounce_photon=64, max_bounce_eye=64, seed=1, cell_factor=1.0):
+                    alpha=0.7, radius_scale=0.1, max_bounce_photon=64, max_bounce_eye=64, seed=1, cell_factor=1.0,
+                    flags=0):
         p = Params()
         p.mode = mode
         p.num_streams = num_streams
@@ -255,6 +260,7 @@ class Context:
         p.alpha = alpha
         p.radius_scale = radius_scale
         p.cell_factor = cell_factor
+        p.flags = flags
         return p
 
     def render_begin(self, cam, params):

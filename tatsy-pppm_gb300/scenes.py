@@ -330,3 +330,48 @@ def small_test_scene(seed=3, subdiv=3, width=64, height=48, photons=20_000):
     cam = look_camera((0.0, 4.0, -30.0), (0.0, -1.0, 0.0), 0.8, width, height)
     return _assemble("small", [(gnd, 0), (s1, 1), (s2, 2), (s3, 3), (s4, 4)], mats, env, cam, photons=photons,
                      passes=4, max_depth=64)
+
+
+# --------------------------------------------------------------------- files
+def write_ply(path, tris):
+    """Binary little-endian PLY in the layout Trimesh::loadPly reads
+    (trimesh.cc:139-217): float x/y/z vertices, faces as uchar count + 3 int."""
+    t = np.ascontiguousarray(tris, np.float32).reshape(-1, 3, 3)
+    n = t.shape[0]
+    verts = t.reshape(-1, 3)
+    faces = np.zeros(n, np.dtype([("n", "u1"), ("i", "<i4", (3,))]))
+    faces["n"] = 3
+    faces["i"] = np.arange(3 * n, dtype=np.int32).reshape(n, 3)
+    head = (f"ply\nformat binary_little_endian 1.0\nelement vertex {3 * n}\nproperty float x\nproperty float y\n"
+            f"property float z\nelement face {n}\nproperty list uchar int vertex_indices\nend_header\n")
+    with open(path, "wb") as f:
+        f.write(head.encode())
+        f.write(verts.astype("<f4").tobytes())
+        f.write(faces.tobytes())
+
+
+def write_hdr(path, rgb):
+    """Radiance RGBE file with the layout of Image::saveHdr (image.cc:436-482):
+    -Y H +X W, every scanline new-style RLE with literal runs of <= 127."""
+    rgb = np.asarray(rgb, np.float64)
+    h, w = rgb.shape[:2]
+    m = rgb.max(2)
+    e = np.zeros((h, w), np.int64)
+    mant, ex = np.frexp(np.where(m > 1e-32, m, 1.0))
+    e = np.where(m > 1e-32, ex, 0)
+    scale = np.where(m > 1e-32, mant * 256.0 / np.where(m > 1e-32, m, 1.0), 0.0)
+    px = np.zeros((h, w, 4), np.uint8)
+    px[..., :3] = np.where(m[..., None] > 1e-32, np.floor(rgb * scale[..., None]), 0).astype(np.uint8)
+    px[..., 3] = np.where(m > 1e-32, e + 128, 0).astype(np.uint8)
+    out = bytearray(b"#?RADIANCE\n# synthetic\nFORMAT=32-bit_rle_rgbe\nEXPOSURE=1.0000000000000\n\n")
+    out += f"-Y {h} +X {w}\n".encode()
+    for y in range(h):
+        out += bytes([2, 2, (w >> 8) & 0xFF, w & 0xFF])
+        for c in range(4):
+            row = px[y, :, c]
+            for s in range(0, w, 127):
+                chunk = row[s:s + 127]
+                out.append(len(chunk))
+                out += chunk.tobytes()
+    with open(path, "wb") as f:
+        f.write(bytes(out))
