@@ -299,7 +299,9 @@ def run_gb300(args):
                 "per_pass": {"photon_rays": cnt.photon_rays, "eye_rays": cnt.eye_rays,
                              "stored": int(stats[-1]["photons_stored"]), "queries": int(stats[-1]["gather_queries"]),
                              "node_visits_per_photon_ray": cnt.photon_node_visits / max(cnt.photon_rays, 1),
-                             "tri_tests_per_photon_ray": cnt.photon_tri_tests / max(cnt.photon_rays, 1)}}
+                             "tri_tests_per_photon_ray": cnt.photon_tri_tests / max(cnt.photon_rays, 1),
+                             "gather_pairs_per_query": cnt.gather_pairs / max(cnt.gather_queries, 1),
+                             "gather_inside_per_query": cnt.gather_inside / max(cnt.gather_queries, 1)}}
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(scene)
         print(json.dumps(line), flush=True)

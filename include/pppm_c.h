@@ -119,6 +119,8 @@ typedef struct {
     int64_t tri_tests;       /* triangles tested (PPPM_FLAG_COUNT_TRAVERSAL) */
     int64_t photon_node_visits; /* of which by photon rays */
     int64_t photon_tri_tests;
+    int64_t gather_pairs;    /* canonical: photon-query pairs tested (PPPM_FLAG_COUNT_TRAVERSAL) */
+    int64_t gather_inside;   /* canonical: pairs within the radius (PPPM_FLAG_COUNT_TRAVERSAL) */
 } pppm_pass_stats;
 
 /* ------------------------------------------------------------- lifetime */

@@ -20,6 +20,8 @@ CSRC = HERE / "csrc"
 OUT = HERE / "_build"
 LIB = HERE / "libpppm_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# extra nvcc flags for tuning builds (e.g. -DPPPM_TRACE_MINBLOCKS=4)
+EXTRA = os.environ.get("PPPM_NVCC_EXTRA", "").split()
 
 
 def _nvcc():
@@ -43,6 +45,13 @@ def _stale(src: pathlib.Path, obj: pathlib.Path, deps):
 
 def build(verbose: bool = False, ptxas_info: bool = False) -> pathlib.Path:
     OUT.mkdir(exist_ok=True)
+    # rebuild everything when the extra flags change
+    stamp = OUT / "flags.txt"
+    flags = " ".join(EXTRA)
+    if not stamp.exists() or stamp.read_text() != flags:
+        for o in OUT.glob("*.o"):
+            o.unlink()
+        stamp.write_text(flags)
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "pppm_c.h"]
     jobs = []
     objs = []
@@ -52,7 +61,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> pathlib.Path:
         objs.append(obj)
         if _stale(src, obj, headers) or ptxas_info:
             cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                   "--expt-relaxed-constexpr", "-c", str(src), "-o", str(obj)]
+                   "--expt-relaxed-constexpr", *EXTRA, "-c", str(src), "-o", str(obj)]
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

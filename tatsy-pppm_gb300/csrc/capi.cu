@@ -57,6 +57,10 @@ static DevMaterial toDevMaterial(const pppm_material& m) {
     d.phong_n = m.phong_n;
     d.roulette = std::fmax(m.refl[0], std::fmax(m.refl[1], m.refl[2]));
     d.rr_photon = ((double)m.refl[0] + (double)m.refl[1] + (double)m.refl[2]) / 3.0;
+    // integer forms of the draw comparisons (x * 2^-32 is exact in double)
+    d.rrCeil = (unsigned long long)std::ceil(d.rr_photon * 4294967296.0);
+    d.roulFloor = (unsigned long long)std::floor((double)d.roulette * 4294967296.0);
+    d.invRr = (float)(1.0 / d.rr_photon);
     if (m.has_bssrdf) {
         // DipoleBSSRDF ctor (bssrdf.cc:48-63) and Fdr (bssrdf.cc:33-42) in double
         const double eta = m.eta, eta2 = eta * eta, eta3 = eta2 * eta;
@@ -77,6 +81,17 @@ static DevMaterial toDevMaterial(const pppm_material& m) {
         }
     }
     return d;
+}
+
+int envFluxScale(pppm_ctx* c, double numPhotons) {
+    if (c->envScaleFor == numPhotons) return PPPM_OK;
+    // Envmap::samplePhoton: area / (pdf * numPhotons) (envmap.cc:80-83)
+    const double area = ((double)((unsigned)c->envW * (unsigned)c->envH)) / (4.0 * 3.14159265358979323846 * 64 * 64);
+    std::vector<float> s(4096);
+    for (int i = 0; i < 4096; i++) s[i] = (float)(area / (c->envPdf[i] * numPhotons));
+    PPPM_CUDA(c, cudaMemcpy(c->envScaleD.p, s.data(), 4096 * 4, cudaMemcpyHostToDevice));
+    c->envScaleFor = numPhotons;
+    return PPPM_OK;
 }
 
 }  // namespace pppm
@@ -187,6 +202,7 @@ int pppm_scene_set(pppm_ctx* c, const float* tri, int64_t ntri, const int32_t* m
     }
     c->ntri = ntri;
     c->rootCode = bvh.rootCode;
+    c->numNodes = (int)bvh.nodes.size();
     c->bvhDepth = bvh.depth;
     // BBox over all triangles (ppm_probabilistic.cc:50-54)
     for (int d = 0; d < 3; d++) { c->bbmin[d] = 1e20; c->bbmax[d] = -1e20; }
@@ -216,6 +232,15 @@ int pppm_env_set(pppm_ctx* c, const float* rgb, int32_t w, int32_t h) {
     PPPM_CUDA(c, c->envCdfD.ensure(4096 * sizeof(double)));
     PPPM_CUDA(c, cudaMemcpy(c->envPdfD.p, c->envPdf.data(), 4096 * sizeof(double), cudaMemcpyHostToDevice));
     PPPM_CUDA(c, cudaMemcpy(c->envCdfD.p, c->envCdf.data(), 4096 * sizeof(double), cudaMemcpyHostToDevice));
+    {
+        // lower_bound(cdf, x * 2^-32) == first i with x <= floor(cdf[i] * 2^32)
+        std::vector<unsigned long long> u(4096);
+        for (int i = 0; i < 4096; i++) u[i] = (unsigned long long)std::floor(c->envCdf[i] * 4294967296.0);
+        PPPM_CUDA(c, c->envUcdfD.ensure(4096 * 8));
+        PPPM_CUDA(c, cudaMemcpy(c->envUcdfD.p, u.data(), 4096 * 8, cudaMemcpyHostToDevice));
+    }
+    PPPM_CUDA(c, c->envScaleD.ensure(4096 * 4));
+    c->envScaleFor = -1.0;
     c->envW = w;
     c->envH = h;
     c->hasEnv = true;
@@ -295,6 +320,8 @@ int pppm_emit_photons(pppm_ctx* c, const double* tapes, int64_t n, int64_t numPh
     if ((r = stageOut(c, dir, (size_t)n * 12, 2, &dd))) return r;
     if ((r = stageOut(c, flux, (size_t)n * 12, 3, &df))) return r;
     if ((r = stageOut(c, defined, (size_t)n * 4, 4, &dk))) return r;
+    int rs_;
+    if ((rs_ = envFluxScale(c, (double)numPhotons))) return rs_;
     PPPM_CUDA(c, launchEmit(envView(c), (const double*)dt, n, (double)numPhotons, (float*)dp, (float*)dd, (float*)df,
                             (int*)dk, c->stream));
     if ((r = finishOut(c, pos, dp, (size_t)n * 12))) return r;

@@ -50,6 +50,12 @@ struct GridBufs {
     int64_t count = 0;   // photons in the grid
 };
 
+// Counting sort of gather queries by grid cell (tiled gather).
+struct QuerySortBufs {
+    DBuf hist, cursor, tmp, keys, sorted;
+    uint32_t size = 0;
+};
+
 struct RenderState {
     bool active = false;
     pppm_camera cam{};
@@ -69,6 +75,8 @@ struct RenderState {
     DBuf jumpMats;    // jump-ahead matrices
     DBuf streamStatesD;  // N x uint4 per-stream state at the start of the pass
     GridBufs grid;
+    QuerySortBufs qsort;
+    DBuf gatherWork;  // 2 counters: photon pairs tested, pairs within the radius
     int64_t depositCap = 0;
     int64_t storedLast = 0;
     int64_t phantomsLast = 0;
@@ -85,6 +93,7 @@ struct pppm_ctx {
     int64_t ntri = 0;
     int rootCode = 0;
     int bvhDepth = 0;
+    int numNodes = 0;
     double bbmin[3] = {0, 0, 0}, bbmax[3] = {0, 0, 0};
     std::vector<pppm_material> mats;
     bool anyBssrdf = false;
@@ -94,7 +103,8 @@ struct pppm_ctx {
     bool hasEnv = false;
     int envW = 0, envH = 0;
     std::vector<double> envPdf, envCdf;
-    pppm::DBuf envRgb, envPdfD, envCdfD;
+    pppm::DBuf envRgb, envPdfD, envCdfD, envUcdfD, envScaleD;
+    double envScaleFor = -1.0;  // numPhotons the flux-scale table was built for
     // staging for host arguments
     pppm::DBuf stage[8];
     std::vector<void*> pinned;
@@ -103,6 +113,7 @@ struct pppm_ctx {
     // scratch of the kNN / gather stage entry points
     pppm::DBuf stageRec, stageQ, stageCount;
     pppm::GridBufs stageGrid;
+    pppm::QuerySortBufs stageQsort;
     cudaEvent_t ev[8] = {};
 };
 
@@ -140,20 +151,25 @@ struct SceneView {
     const int* matId;
     const DevMaterial* mats;
     int rootCode;
+    int numNodes;
 };
 inline SceneView sceneView(const pppm_ctx* c) {
-    return {c->nodes.as<QNode>(), c->tris.as<float4>(), c->matId.as<int>(), c->devMats.as<DevMaterial>(), c->rootCode};
+    return {c->nodes.as<QNode>(), c->tris.as<float4>(), c->matId.as<int>(), c->devMats.as<DevMaterial>(), c->rootCode,
+            c->numNodes};
 }
 inline EnvDev envView(const pppm_ctx* c) {
     EnvDev e;
     e.rgb = c->envRgb.as<float>();
     e.cdf = c->envCdfD.as<double>();
     e.pdf = c->envPdfD.as<double>();
+    e.ucdf = c->envUcdfD.as<unsigned long long>();
+    e.fluxScale = c->envScaleD.as<float>();
     e.w = c->envW;
     e.h = c->envH;
-    e.area_over_p = 0.0;
     return e;
 }
+// Fills the per-CDF-cell photon flux scale for numPhotons.
+int envFluxScale(pppm_ctx* c, double numPhotons);
 
 // Kernel launchers (defined in the .cu files).
 cudaError_t launchIntersect(const SceneView& s, const float* rays, int64_t n, int32_t* tri, double* t, float* pos,

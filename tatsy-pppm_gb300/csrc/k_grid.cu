@@ -129,6 +129,18 @@ unsigned gridFor(int64_t n, int bs) {
 
 }  // namespace
 
+// In-place exclusive prefix sum of data[0..n); data[n] receives the total and
+// cursor[0..n) a copy of the offsets. tmp holds ceil(n / 2048) + 1 words.
+cudaError_t exclusiveScan(uint32_t* data, int64_t n, uint32_t* cursor, uint32_t* tmp, cudaStream_t st) {
+    const int64_t chunks = (n + kScanChunk - 1) / kScanChunk;
+    kScanChunks<<<(unsigned)chunks, kScanThreads, 0, st>>>(data, data, tmp, n);
+    kScanSums<<<1, kScanThreads, 0, st>>>(tmp, chunks, data + n);
+    kAddChunkBase<<<gridFor(n, 256), 256, 0, st>>>(data, tmp, n, cursor);
+    return cudaGetLastError();
+}
+
+int64_t scanTmpWords(int64_t n) { return (n + kScanChunk - 1) / kScanChunk + 1; }
+
 cudaError_t gridLayout(GridBufs& g, const double* bbmin, const double* bbmax, double cell, int64_t nPhotons) {
     // bucket table: next power of two >= 2 * photons, within [2^12, 2^26]
     uint32_t size = 1u << 12;
@@ -176,12 +188,8 @@ cudaError_t gridBuild(GridBufs& g, const GridDev& view, const float4* rec, const
     GridDev v = view;
     const int bs = 256;
     kKeys<<<gridFor(capacity, bs), bs, 0, st>>>(rec, dCount, capacity, v, g.keys.as<uint32_t>(), hist);
-    const int64_t n = (int64_t)g.size;
-    const int64_t chunks = (n + kScanChunk - 1) / kScanChunk;
-    uint32_t* chunkSums = g.scanTmp.as<uint32_t>();
-    kScanChunks<<<(unsigned)chunks, kScanThreads, 0, st>>>(hist, hist, chunkSums, n);
-    kScanSums<<<1, kScanThreads, 0, st>>>(chunkSums, chunks, hist + n);
-    kAddChunkBase<<<gridFor(n, bs), bs, 0, st>>>(hist, chunkSums, n, g.cursor.as<uint32_t>());
+    cudaError_t se = exclusiveScan(hist, (int64_t)g.size, g.cursor.as<uint32_t>(), g.scanTmp.as<uint32_t>(), st);
+    if (se != cudaSuccess) return se;
     kScatter<<<gridFor(capacity, bs), bs, 0, st>>>(rec, dCount, capacity, g.keys.as<uint32_t>(), g.cursor.as<uint32_t>(),
                                                    g.sorted.as<float4>());
     return cudaGetLastError();

@@ -8,7 +8,9 @@ __global__ void __launch_bounds__(128) kIntersect(SceneView sc, const float* __r
                                                    int32_t* __restrict__ triOut, double* __restrict__ tOut,
                                                    float* __restrict__ posOut, float* __restrict__ nrmOut) {
     __shared__ int order[128];
+    __shared__ QNode sTop[kTopNodes];
     loadOrderTable(order);
+    loadTopNodes(sTop, sc.nodes, sc.numNodes);
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* r = rays + 6 * i;
@@ -16,7 +18,7 @@ __global__ void __launch_bounds__(128) kIntersect(SceneView sc, const float* __r
     const float dx = r[3], dy = r[4], dz = r[5];
     double best;
     const int slot = traverseExact<kPrefilter>(sc.nodes, sc.tris, sc.rootCode, ox, oy, oz, dx, dy, dz, order, &best,
-                                               nullptr, nullptr);
+                                               nullptr, nullptr, sTop);
     int id = -1;
     if (slot >= 0) {
         const float4 a = sc.tris[3 * slot], b = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];

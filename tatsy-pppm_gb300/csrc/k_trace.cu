@@ -4,6 +4,12 @@
 
 #include "trace.h"
 
+// Minimum resident blocks per SM for the traversal kernels (register cap
+// 65536 / (128 * n)); overridable at build time.
+#ifndef PPPM_TRACE_MINBLOCKS
+#define PPPM_TRACE_MINBLOCKS 6
+#endif
+
 namespace pppm {
 
 // ------------------------------------------------------------------ jump-ahead (host)
@@ -202,11 +208,13 @@ __device__ __forceinline__ unsigned long long warpAppend(bool take, unsigned lon
 // closest hit, three draws, deposit + Russian roulette on Lambertian
 // surfaces, BSDF sampling elsewhere. Survivors are compacted into `out`
 // with one atomic per warp; queue lengths rotate through ctr->queue[b % 3].
-__global__ void __launch_bounds__(128) kPhotonBounce(TraceParams tp, SceneView sc, int bounce, const PathState* __restrict__ in,
+__global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(TraceParams tp, SceneView sc, int bounce, const PathState* __restrict__ in,
                                                      PathState* __restrict__ out, int64_t maxPaths,
                                                      float4* __restrict__ dep, int64_t depCap, PassCounters* ctr) {
     __shared__ int order[128];
+    __shared__ QNode sTop[kTopNodes];
     loadOrderTable(order);
+    loadTopNodes(sTop, sc.nodes, sc.numNodes);
     const int qi = bounce % 3, qo = (bounce + 1) % 3, qz = (bounce + 2) % 3;
     const int64_t n = min((int64_t)ctr->queue[qi], maxPaths);
     if (blockIdx.x == 0 && threadIdx.x == 0) ctr->queue[qz] = 0;
@@ -225,20 +233,21 @@ __global__ void __launch_bounds__(128) kPhotonBounce(TraceParams tp, SceneView s
             double best;
             traced = 1;
             const int slot = traverseExact<true>(sc.nodes, sc.tris, sc.rootCode, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz,
-                                                 order, &best, &visits, &tests);
+                                                 order, &best, &visits, &tests, sTop);
             if (slot < 0) {
                 alive = false;
             } else {
                 Tape tape;
                 tape.pos = 0;
                 tape.x.s[0] = p.rng[0]; tape.x.s[1] = p.rng[1]; tape.x.s[2] = p.rng[2]; tape.x.s[3] = p.rng[3];
-                const double r0 = tape.popd(), r1 = tape.popd(), r2 = tape.popd();
+                const uint32_t r0 = tape.popu();
+                const float r1 = tape.popf(), r2 = tape.popf();
                 const float4 a = sc.tris[3 * slot], b = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
                 const int tid = __float_as_int(a.w);
                 const DevMaterial& m = sc.mats[sc.matId[tid]];
                 double hp[3];
                 hitPosition(p.ox, p.oy, p.oz, p.dx, p.dy, p.dz, best, hp);
-                const f3 nrm = triNormal(a, b, c);
+                const f3 nrm = triNormalF(a, b, c);
                 const f3 din = {p.dx, p.dy, p.dz};
                 const f3 on = dot(nrm, din) < 0.0f ? nrm : -nrm;
                 f3 flux = {p.fx, p.fy, p.fz};
@@ -249,15 +258,14 @@ __global__ void __launch_bounds__(128) kPhotonBounce(TraceParams tp, SceneView s
                     da = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
                                      __uint_as_float(packNormal(on)));
                     db = make_float4(flux.x, flux.y, flux.z, __int_as_float(p.id));
-                    if (r0 < m.rr_photon) {
-                        bsdfSample(m, din, on, (float)r1, (float)r2, &nd);
-                        const float inv = (float)(1.0 / m.rr_photon);
-                        flux = flux * refl * inv;
+                    if ((unsigned long long)r0 < m.rrCeil) {  // rands[0] < probability
+                        bsdfSample(m, din, on, r1, r2, &nd);
+                        flux = flux * refl * m.invRr;
                     } else {
                         alive = false;
                     }
                 } else {
-                    const float pdf = bsdfSample(m, din, on, (float)r0, (float)r1, &nd);
+                    const float pdf = bsdfSample(m, din, on, u32ToFloat(r0), r1, &nd);
                     flux = flux * refl * (1.0f / pdf);
                 }
                 p.ox = hp[0]; p.oy = hp[1]; p.oz = hp[2];
@@ -287,10 +295,10 @@ __global__ void __launch_bounds__(128) kPhotonBounce(TraceParams tp, SceneView s
     }
 }
 
-__device__ __forceinline__ void cameraRay(const CameraDev& c, double px, double py, f3* d) {
+__device__ __forceinline__ void cameraRay(const CameraDev& c, float px, float py, f3* d) {
     // PerspectiveCamera::getRay (perspective_camera.cc:42-46)
-    const float a = c.halfTan * c.aspect * (float)(2.0 * px / c.w - 1.0);
-    const float b = c.halfTan * (float)(2.0 * py / c.h - 1.0);
+    const float a = c.halfTan * c.aspect * (2.0f * px / (float)c.w - 1.0f);
+    const float b = c.halfTan * (2.0f * py / (float)c.h - 1.0f);
     const f3 dir = {c.dx + a * c.ux + b * c.vx, c.dy + a * c.uy + b * c.vy, c.dz + a * c.uz + b * c.vz};
     *d = normalized(dir);
 }
@@ -300,11 +308,13 @@ __device__ __forceinline__ void cameraRay(const CameraDev& c, double px, double 
 // surfaces, Russian roulette after 3 bounces, a gather query at the first
 // Lambertian hit, the env map on a miss. Environment terms go straight into
 // the accumulation buffer; queries are compacted with one atomic per warp.
-__global__ void __launch_bounds__(128) kEyeTrace(TraceParams tp, SceneView sc, EnvDev env, CameraDev cam,
+__global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TraceParams tp, SceneView sc, EnvDev env, CameraDev cam,
                                                  const uint32_t* __restrict__ pixelStates, float* __restrict__ accum,
                                                  float4* __restrict__ queries, PassCounters* ctr) {
     __shared__ int order[128];
+    __shared__ QNode sTop[kTopNodes];
     loadOrderTable(order);
+    loadTopNodes(sTop, sc.nodes, sc.numNodes);
     const int64_t np = (int64_t)cam.w * cam.h;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < np; base += stride) {
@@ -322,8 +332,8 @@ __global__ void __launch_bounds__(128) kEyeTrace(TraceParams tp, SceneView sc, E
             } else {
                 seedCanonical(tp.seed, tp.pass, (uint64_t)tp.numPaths + (uint64_t)pix, tape.x);
             }
-            const double px = x + tape.popd() - 0.5;
-            const double py = y + tape.popd() - 0.5;
+            const float px = (float)x + tape.popf() - 0.5f;
+            const float py = (float)y + tape.popf() - 0.5f;
             f3 d;
             cameraRay(cam, px, py, &d);
             double o[3] = {cam.ex, cam.ey, cam.ez};
@@ -336,20 +346,22 @@ __global__ void __launch_bounds__(128) kEyeTrace(TraceParams tp, SceneView sc, E
                 double best;
                 traced++;
                 const int slot = traverseExact<true>(sc.nodes, sc.tris, sc.rootCode, o[0], o[1], o[2], d.x, d.y, d.z,
-                                                     order, &best, &visits, &tests);
+                                                     order, &best, &visits, &tests, sTop);
                 if (slot < 0) {
                     L = L + w * envLookup(env, d);
                     break;
                 }
-                const double r0 = tape.popd(), r1 = tape.popd(), r2 = tape.popd();
+                const uint32_t r0 = tape.popu();
+                const float r1 = tape.popf(), r2 = tape.popf();
                 const float4 a = sc.tris[3 * slot], bb = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
                 const DevMaterial& m = sc.mats[sc.matId[__float_as_int(a.w)]];
                 double hp[3];
                 hitPosition(o[0], o[1], o[2], d.x, d.y, d.z, best, hp);
-                const f3 nrm = triNormal(a, bb, c);
+                const f3 nrm = triNormalF(a, bb, c);
                 float roul = m.roulette;
                 if (b >= 3) {
-                    if (r0 > (double)roul) break;  // terminated path contributes nothing more
+                    // rands[0] > roulette: the path ends and contributes nothing more
+                    if ((unsigned long long)r0 > m.roulFloor) break;
                 } else {
                     roul = 1.0f;
                 }
@@ -365,7 +377,7 @@ __global__ void __launch_bounds__(128) kEyeTrace(TraceParams tp, SceneView sc, E
                     break;
                 }
                 f3 nd;
-                const float pdf = bsdfSample(m, d, nrm, (float)r1, (float)r2, &nd);
+                const float pdf = bsdfSample(m, d, nrm, r1, r2, &nd);
                 w = w * refl * (1.0f / (pdf * roul));
                 o[0] = hp[0]; o[1] = hp[1]; o[2] = hp[2];
                 d = nd;

@@ -16,6 +16,8 @@ struct QueryView {
     int64_t n;
 };
 
+cudaError_t exclusiveScan(uint32_t* data, int64_t n, uint32_t* cursor, uint32_t* tmp, cudaStream_t st);
+int64_t scanTmpWords(int64_t n);
 cudaError_t gridLayout(GridBufs& g, const double* bbmin, const double* bbmax, double cell, int64_t nPhotons);
 GridDev gridView(const GridBufs& g, const double* bbmin, const double* bbmax);
 cudaError_t gridBuild(GridBufs& g, const GridDev& view, const float4* rec, const uint64_t* dCount, int64_t capacity,
@@ -25,6 +27,11 @@ cudaError_t gridBuild(GridBufs& g, const GridDev& view, const float4* rec, const
 // or accum[pixel] += (accumulate=true).
 cudaError_t launchGatherCanonical(const GridDev& g, QueryView q, float radius, float* out, bool accumulate,
                                   cudaStream_t st);
+// Canonical gather with shared-memory staging of cell neighbourhoods
+// (queries counting-sorted by cell first). work: optional 2 counters.
+cudaError_t querySortLayout(QuerySortBufs& qs, int64_t maxQueries);
+cudaError_t launchGatherTiled(const GridDev& g, QueryView q, QuerySortBufs& qs, float radius, float* out,
+                              bool accumulate, unsigned long long* work, cudaStream_t st);
 // Compat kNN gather (ppm_probabilistic.cc:300-335).
 cudaError_t launchGatherCompat(const GridDev& g, QueryView q, int k, float eps, float radius, int64_t phantoms,
                                float* out, bool accumulate, cudaStream_t st);

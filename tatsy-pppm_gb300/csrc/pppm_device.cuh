@@ -41,6 +41,13 @@ struct DevMaterial {
     float phong_n;
     float roulette;  // max(refl) (ppm_probabilistic.cc:261)
     double rr_photon;  // (r+g+b)/3.0 in double (ppm_probabilistic.cc:177)
+    // The reference compares draws x * 2^-32 (x a 32-bit integer) with these
+    // doubles; the same decisions as integer compares:
+    //   x * 2^-32 <  rr_photon  <=>  x <  rrCeil   = ceil(rr_photon * 2^32)
+    //   x * 2^-32 >  roulette   <=>  x >  roulFloor = floor(roulette * 2^32)
+    unsigned long long rrCeil;
+    unsigned long long roulFloor;
+    float invRr;     // 1 / rr_photon for the flux update
     // dipole (bssrdf.cc:48-63), derived on the host in double
     float A, eta, scale, fdr;
     float sigma_tr[3], alphap[3], zpos[3], zneg[3];
@@ -51,8 +58,13 @@ struct EnvDev {
     const float* rgb;    // w*h*3
     const double* cdf;   // 4096
     const double* pdf;   // 4096
+    // lower_bound(cdf, x * 2^-32) as an integer search: the first i with
+    // x <= ucdf[i] = floor(cdf[i] * 2^32)
+    const unsigned long long* ucdf;
+    // per CDF cell: (float)(area / (pdf * numPhotons)) (envmap.cc:80-83),
+    // filled per render because numPhotons is a render parameter
+    const float* fluxScale;
     int w, h;
-    double area_over_p;  // area / numPhotons is applied per pass
 };
 
 // ------------------------------------------------------------------ RNG
@@ -74,12 +86,17 @@ struct XorShift {
 // nextReal() = next() * (float)(1/UINT_MAX) = next() * 2^-32 exactly (random.h:45-47)
 __host__ __device__ inline double u32ToReal(uint32_t x) { return (double)x * 2.3283064365386963e-10; }
 
+// nextReal() rounded to float without FP64: (float)(x * 2^-32) equals
+// rn(x) * 2^-32 because scaling by a power of two commutes with rounding.
+__device__ __forceinline__ float u32ToFloat(uint32_t x) { return __uint2float_rn(x) * 2.3283064365386963e-10f; }
+
 // A 200-number tape consumed in order (RandomSequence, random_sequence.h).
 struct Tape {
     XorShift x;
     int pos;
     __device__ inline double popd() { pos++; return u32ToReal(x.next()); }
-    __device__ inline float popf() { return (float)popd(); }
+    __device__ inline float popf() { pos++; return u32ToFloat(x.next()); }
+    __device__ inline uint32_t popu() { pos++; return x.next(); }
 };
 
 // A tape given explicitly (stage tests feed the reference's own numbers).
@@ -88,6 +105,8 @@ struct ArrayTape {
     int pos;
     __device__ inline double popd() { return v[pos++]; }
     __device__ inline float popf() { return (float)popd(); }
+    // tape values are x * 2^-32 with x < 2^32, so this is exact
+    __device__ inline uint32_t popu() { return (uint32_t)(v[pos++] * 4294967296.0); }
 };
 
 // ------------------------------------------------------------------ vectors
@@ -214,10 +233,23 @@ __device__ __forceinline__ void loadOrderTable(int* s) {
 // orderTable child order, LIFO stack, leaf triangles in stored order with a
 // strict `<` update. orderTab points at a shared-memory copy of the table.
 // Returns the triangle slot or -1 and the hit distance in *bestOut.
+constexpr int kTopNodes = 85;  // BFS levels 0-3 of the QBVH (1 + 4 + 16 + 64), staged in shared memory
+
+// Cooperative copy of the top BVH levels into shared memory; nodes are in
+// BFS order so the first kTopNodes are levels 0-3.
+__device__ __forceinline__ void loadTopNodes(QNode* sTop, const QNode* __restrict__ nodes, int numNodes) {
+    const int n = min(numNodes, kTopNodes) * (int)(sizeof(QNode) / sizeof(float4));
+    const float4* src = reinterpret_cast<const float4*>(nodes);
+    float4* dst = reinterpret_cast<float4*>(sTop);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = __ldg(&src[i]);
+    __syncthreads();
+}
+
 template <bool kPrefilter>
 __device__ __forceinline__ int traverseExact(const QNode* __restrict__ nodes, const float4* __restrict__ tris, int rootCode,
                                              double odx, double ody, double odz, float dx, float dy, float dz,
-                                             const int* orderTab, double* bestOut, int* nodeVisits, int* triTests) {
+                                             const int* orderTab, double* bestOut, int* nodeVisits, int* triTests,
+                                             const QNode* sTop = nullptr) {
     // the slab test runs on the float-rounded origin (qbvh_accel.cc:211-213),
     // the triangle test on the double origin
     const float ox = __double2float_rn(odx), oy = __double2float_rn(ody), oz = __double2float_rn(odz);
@@ -235,6 +267,7 @@ __device__ __forceinline__ int traverseExact(const QNode* __restrict__ nodes, co
     int sp = 0;
     stack[sp++] = rootCode;
     double best = kInfty;
+    float bestf = 1.0e20f;  // (float)best, refreshed whenever best changes
     int hit = -1;
     int visits = 0, tests = 0;
     while (sp > 0) {
@@ -245,26 +278,28 @@ __device__ __forceinline__ int traverseExact(const QNode* __restrict__ nodes, co
             for (int i = 0; i < cnt; i++) {
                 const float4 a = tris[3 * (first + i)], b = tris[3 * (first + i) + 1], c = tris[3 * (first + i) + 2];
                 tests++;
-                if (kPrefilter && !triMayHit(ox, oy, oz, dx, dy, dz, a, b, c, (float)best)) continue;
+                if (kPrefilter && !triMayHit(ox, oy, oz, dx, dy, dz, a, b, c, bestf)) continue;
                 double t;
                 if (triHitExact(odx, ody, odz, ddx, ddy, ddz, a, b, c, &t) && best > t) {
                     best = t;
+                    bestf = __double2float_rn(t);
                     hit = first + i;
                 }
             }
             continue;
         }
         visits++;
-        const QNode* nd = nodes + code;
-        const float hd = __double2float_rn(best);
+        // levels 0-3 come from shared memory, deeper nodes from L2/HBM
+        const QNode* nd = (sTop != nullptr && code < kTopNodes) ? sTop + code : nodes + code;
+        const float hd = bestf;
         float tmin[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         float tmax[4] = {hd, hd, hd, hd};
         const float o3[3] = {ox, oy, oz};
         const float i3[3] = {idx, idy, idz};
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            const float4 lo = __ldg(&nd->bmin[d]);
-            const float4 hi = __ldg(&nd->bmax[d]);
+            const float4 lo = nd->bmin[d];
+            const float4 hi = nd->bmax[d];
             const bool neg = (sgnBits >> d) & 1;
             const float4 nearB = neg ? hi : lo;
             const float4 farB = neg ? lo : hi;
@@ -282,8 +317,8 @@ __device__ __forceinline__ int traverseExact(const QNode* __restrict__ nodes, co
 #pragma unroll
         for (int k = 0; k < 4; k++) hitMask |= (tmax[k] >= tmin[k]) ? (1 << k) : 0;
         if (hitMask != 0) {
-            const int4 ch = __ldg(&nd->child);
-            const int meta = __ldg(&nd->meta.x);
+            const int4 ch = nd->child;
+            const int meta = nd->meta.x;
             const int a0 = meta & 3, a1 = (meta >> 2) & 3, a2 = (meta >> 4) & 3;
             const int sepMask = (((sgnBits >> a0) & 1) << 2) | (((sgnBits >> a1) & 1) << 1) | ((sgnBits >> a2) & 1);
             int ord = orderTab[hitMask * 8 + sepMask];
@@ -320,6 +355,13 @@ __device__ inline f3 triNormal(const float4& a, const float4& b, const float4& c
     const double nn = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(cx, cx), __dmul_rn(cy, cy)), __dmul_rn(cz, cz)));
     const double inv = __drcp_rn(__dadd_rn(nn, kEps));
     return {__double2float_rn(__dmul_rn(cx, inv)), __double2float_rn(__dmul_rn(cy, inv)), __double2float_rn(__dmul_rn(cz, inv))};
+}
+
+// The same normal in FP32 for the shading kernels (direction sampling and
+// orientation only; pppm_intersect reports the double-derived normal).
+__device__ inline f3 triNormalF(const float4& a, const float4& b, const float4& c) {
+    const f3 e1 = {b.x - a.x, b.y - a.y, b.z - a.z}, e2 = {c.x - a.x, c.y - a.y, c.z - a.z};
+    return normalized(cross(e1, e2));
 }
 
 __device__ inline void hitRecord(double ox, double oy, double oz, float dx, float dy, float dz, double t, const float4& a,
@@ -448,26 +490,23 @@ __device__ inline f3 envLookup(const EnvDev& e, f3 d) {
 // 50 * emitDir); dir: the first ray direction.
 template <class TapeT>
 __device__ inline bool emitPhoton(const EnvDev& e, TapeT& tp, double numPhotons, f3* emitDir, f3* dir, f3* flux) {
-    const double r = tp.popd();
-    int lo = 0, hi = 4096;  // first index with cdf[i] >= r
+    const unsigned long long r = tp.popu();
+    int lo = 0, hi = 4096;  // first index with cdf[i] >= r * 2^-32
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (__ldg(&e.cdf[mid]) < r) lo = mid + 1; else hi = mid;
+        if (__ldg(&e.ucdf[mid]) < r) lo = mid + 1; else hi = mid;
     }
     const int index = lo;
     const int ix = index % 64, iy = index / 64;
-    const float u = (float)(((double)ix + tp.popd()) / 64.0);
-    const float v = (float)(((double)iy + tp.popd()) / 64.0);
+    const float u = ((float)ix + tp.popf()) * (1.0f / 64.0f);
+    const float v = ((float)iy + tp.popf()) * (1.0f / 64.0f);
     const float phi = u * kPiF * 2.0f;
     const float y = (1.0f - v) * 2.0f - 1.0f;
     const float sxz = sqrtf(fmaxf(0.0f, 1.0f - y * y));
     float sp, cp;
     sincosf(phi, &sp, &cp);
     const f3 d = {sxz * cp, y, sxz * sp};
-    const double area = ((double)e.w * (double)e.h) / (4.0 * kPi * 64.0 * 64.0);
-    const double pdf = __ldg(&e.pdf[min(index, 4095)]);
-    const float scale = (float)(area / (pdf * numPhotons));
-    *flux = envLookup(e, d) * scale;
+    *flux = envLookup(e, d) * __ldg(&e.fluxScale[min(index, 4095)]);
     *emitDir = d;
     // onHemisphere(normalLight, &nextDir, rseq.pop(), rseq.pop()): the
     // reference build evaluates these arguments right to left, so the first
@@ -475,6 +514,7 @@ __device__ inline bool emitPhoton(const EnvDev& e, TapeT& tp, double numPhotons,
     const float r2 = tp.popf();
     const float r1 = tp.popf();
     *dir = onHemisphere(-d, r1, r2);
+    (void)numPhotons;
     return index < 4096;
 }
 

@@ -121,8 +121,10 @@ int pppm_gather(pppm_ctx* c, int32_t mode, const float* photons, int64_t n, int6
     PPPM_CUDA(c, gridBuild(c->stageGrid, gv, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), n, c->stream));
     gv = gridView(c->stageGrid, mn, mx);
     QueryView qv{c->stageQ.as<float4>(), nullptr, m};
-    if (mode == PPPM_MODE_CANONICAL)
-        PPPM_CUDA(c, launchGatherCanonical(gv, qv, (float)radius, (float*)dout, false, c->stream));
+    if (mode == PPPM_MODE_CANONICAL) {
+        PPPM_CUDA(c, querySortLayout(c->stageQsort, m));
+        PPPM_CUDA(c, launchGatherTiled(gv, qv, c->stageQsort, (float)radius, (float*)dout, false, nullptr, c->stream));
+    }
     else
         PPPM_CUDA(c, launchGatherCompat(gv, qv, k, (float)gatherPhotons, (float)radius, phantoms, (float*)dout, false,
                                         c->stream));
@@ -173,6 +175,12 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     PPPM_CUDA(c, rs.queries.ensure((size_t)pixels * 48));
     PPPM_CUDA(c, rs.photonCount.ensure(sizeof(PassCounters) + 8 * (size_t)N));
     PPPM_CUDA(c, rs.streamStatesD.ensure((size_t)N * 16));
+    PPPM_CUDA(c, querySortLayout(rs.qsort, pixels));
+    PPPM_CUDA(c, rs.gatherWork.ensure(16));
+    {
+        const int e = envFluxScale(c, (double)par->photons);
+        if (e) return e;
+    }
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
     rs.passesDone = 0;
     rs.storedLast = 0;
@@ -247,6 +255,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     PassCounters hc;
     for (int attempt = 0;; attempt++) {
         PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters) + 8 * (size_t)N, c->stream));
+    PPPM_CUDA(c, cudaMemsetAsync(rs.gatherWork.p, 0, 16, c->stream));
         PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
         PPPM_CUDA(c, cudaEventRecord(c->ev[5], c->stream));
         launches += 1 + par.max_bounce_photon;
@@ -311,8 +320,10 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         PPPM_CUDA(c, launchGatherCompat(gv, qv, k, (float)par.gather_photons, (float)rs.radius, phantoms,
                                         rs.accum.as<float>(), true, c->stream));
     else
-        PPPM_CUDA(c, launchGatherCanonical(gv, qv, (float)rs.radius, rs.accum.as<float>(), true, c->stream));
-    launches += 2;
+        PPPM_CUDA(c, launchGatherTiled(gv, qv, rs.qsort, (float)rs.radius, rs.accum.as<float>(), true,
+                                       tp.countTraversal ? rs.gatherWork.as<unsigned long long>() : nullptr,
+                                       c->stream));
+    launches += compat ? 2 : 8;
     PPPM_CUDA(c, cudaEventRecord(c->ev[4], c->stream));
     PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -342,6 +353,10 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         stats->tri_tests = (int64_t)(hc.triTests[0] + hc.triTests[1]);
         stats->photon_node_visits = (int64_t)hc.nodeVisits[0];
         stats->photon_tri_tests = (int64_t)hc.triTests[0];
+        unsigned long long gw[2] = {0, 0};
+        if (tp.countTraversal) PPPM_CUDA(c, cudaMemcpy(gw, rs.gatherWork.p, 16, cudaMemcpyDeviceToHost));
+        stats->gather_pairs = (int64_t)gw[0];
+        stats->gather_inside = (int64_t)gw[1];
     }
     if (hc.undefinedEmit)
         return fail(c, PPPM_E_UNDEFINED, "render_pass: a photon draw fell past the env CDF (reference reads _pdf out of bounds)");

@@ -49,7 +49,8 @@ class PassStats(ctypes.Structure):
                 ("ms_grid", ctypes.c_double), ("ms_eye", ctypes.c_double), ("ms_gather", ctypes.c_double),
                 ("ms_bounce", ctypes.c_double), ("kernel_launches", ctypes.c_int64), ("node_visits", ctypes.c_int64),
                 ("tri_tests", ctypes.c_int64), ("photon_node_visits", ctypes.c_int64),
-                ("photon_tri_tests", ctypes.c_int64)]
+                ("photon_tri_tests", ctypes.c_int64), ("gather_pairs", ctypes.c_int64),
+                ("gather_inside", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
