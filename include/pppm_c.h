@@ -202,6 +202,23 @@ int pppm_knn(pppm_ctx* ctx, const float* photon_pos, int64_t n, const float* que
 int pppm_gather(pppm_ctx* ctx, int32_t mode, const float* photons, int64_t n, int64_t phantoms,
                 const float* queries, int64_t m, double radius, int32_t gather_photons, float* out);
 
+/* Allocation-free variant of pppm_knn (same arguments and results) for
+ * callers that cannot let a library allocate GPU memory: programs that own
+ * all device memory under a fixed budget, frame loops that must not stall on
+ * cudaMalloc, or code that must not create a pppm context. It needs no
+ * context and calls no cudaMalloc/cudaFree or allocating library routine.
+ * Every array must already be device (or managed) memory; work runs on
+ * `stream` (a cudaStream_t, NULL = the default stream) and the call waits
+ * for it before returning. Scratch lives in one fixed device array of about
+ * 6.6 MB that every GPU loading the library holds until exit; n above
+ * PPPM_NOALLOC_MAX_PHOTONS returns PPPM_E_CAPACITY. The first call on a
+ * device looks up that array's address (issue it before any stream
+ * capture). Calls share the array, so calls that overlap on the GPU race.
+ * No counterpart in the reference. */
+#define PPPM_NOALLOC_MAX_PHOTONS (1 << 17)
+int pppm_knn_noalloc(const float* photon_pos, int64_t n, const float* queries, int64_t m, int32_t num_target_photons,
+                     double target_radius, int32_t* idx, int32_t* cnt, int32_t cap, void* stream);
+
 /* ------------------------------------------------------------- render */
 /* Replaces the set-up half of ProgressivePhotonMappingProb::render
  * (ppm_probabilistic.cc:24-79): radius init, RNG streams, zeroed buffer. */

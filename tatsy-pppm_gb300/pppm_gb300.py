@@ -19,6 +19,7 @@ OK = 0
 E_ARG, E_CUDA, E_STATE, E_CAPACITY, E_UNDEFINED, E_TIMEOUT = -1, -2, -3, -4, -5, -6
 MODE_COMPAT, MODE_CANONICAL = 0, 1
 FLAG_COUNT_TRAVERSAL = 0x1
+NOALLOC_MAX_PHOTONS = 1 << 17  # PPPM_NOALLOC_MAX_PHOTONS
 
 _lib = None
 
@@ -74,6 +75,8 @@ SIGNATURES = {
     "pppm_hash_points": ([_VP, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP], ctypes.c_int),
     "pppm_knn": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
                   ctypes.c_int32], ctypes.c_int),
+    "pppm_knn_noalloc": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
+                          ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_gather": ([_VP, ctypes.c_int32, _VP, ctypes.c_int64, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_double,
                      ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_render_begin": ([_VP, _VP, _VP], ctypes.c_int),
@@ -285,6 +288,15 @@ class Context:
         n = ctypes.c_int64()
         self._check(self.lib.pppm_render_photons(self.h, out.ctypes.data, cap, ctypes.byref(n)))
         return out[: n.value]
+
+
+def knn_noalloc(photon_pos, queries, num_target_photons, target_radius, idx, cnt, stream=None):
+    """pppm_knn_noalloc on CUDA torch tensors (outputs passed in, nothing is
+    allocated by the library). Returns the status code."""
+    lib = load()
+    return lib.pppm_knn_noalloc(_ptr(photon_pos), int(photon_pos.shape[0]), _ptr(queries), int(queries.shape[0]),
+                                int(num_target_photons), float(target_radius), _ptr(idx), _ptr(cnt),
+                                int(idx.shape[1]), stream)
 
 
 def hdr_decode(data: bytes):
