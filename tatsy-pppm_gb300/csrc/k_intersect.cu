@@ -12,13 +12,21 @@ __global__ void __launch_bounds__(128) kIntersect(SceneView sc, const float* __r
     loadOrderTable(order);
     loadTopNodes(sTop, sc.nodes, sc.numNodes);
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float* r = rays + 6 * i;
+    const bool valid = i < n;  // all lanes traverse together (warp-cooperative)
+    const float* r = rays + 6 * (valid ? i : 0);
     const double ox = r[0], oy = r[1], oz = r[2];
     const float dx = r[3], dy = r[4], dz = r[5];
     double best;
-    const int slot = traverseExact<kPrefilter>(sc.nodes, sc.tris, sc.rootCode, ox, oy, oz, dx, dy, dz, order, &best,
-                                               nullptr, nullptr, sTop);
+    int slot;
+    if (kPrefilter) {
+        slot = traverseExactWarp(sc.nodes, sc.tris, sc.rootCode, valid, ox, oy, oz, dx, dy, dz, order, sTop, &best,
+                                 nullptr, nullptr);
+    } else {
+        if (!valid) return;
+        slot = traverseExact<false>(sc.nodes, sc.tris, sc.rootCode, ox, oy, oz, dx, dy, dz, order, &best, nullptr,
+                                    nullptr, sTop);
+    }
+    if (!valid) return;
     int id = -1;
     if (slot >= 0) {
         const float4 a = sc.tris[3 * slot], b = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];

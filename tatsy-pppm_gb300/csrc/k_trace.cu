@@ -223,17 +223,20 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
         const int64_t i = base + threadIdx.x;
         bool alive = false, store = false;
         PathState p;
+        p.ox = p.oy = p.oz = 0.0;
+        p.dx = p.dy = 0.f;
+        p.dz = 1.f;
         float4 da, db;
         if (i < n) {
             p = in[i];
             alive = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
         }
         int traced = 0, visits = 0, tests = 0;
+        double best;
+        const int slot = traverseExactWarp(sc.nodes, sc.tris, sc.rootCode, alive, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz,
+                                           order, sTop, &best, &visits, &tests);
         if (alive) {
-            double best;
             traced = 1;
-            const int slot = traverseExact<true>(sc.nodes, sc.tris, sc.rootCode, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz,
-                                                 order, &best, &visits, &tests, sTop);
             if (slot < 0) {
                 alive = false;
             } else {
@@ -322,10 +325,17 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
         bool query = false;
         float4 q0, q1, q2;
         int traced = 0, visits = 0, tests = 0;
-        if (pix < np) {
+        // every lane of the warp stays in the bounce loop until all paths end
+        // (the traversal is warp-cooperative)
+        bool alive = pix < np;
+        Tape tape;
+        tape.pos = 0;
+        tape.x.s[0] = tape.x.s[1] = tape.x.s[2] = tape.x.s[3] = 1u;
+        f3 d = {0.f, 0.f, 1.f};
+        double o[3] = {cam.ex, cam.ey, cam.ez};
+        f3 w = {1.f, 1.f, 1.f}, L = {0.f, 0.f, 0.f};
+        if (alive) {
             const int x = (int)(pix % cam.w), y = (int)(pix / cam.w);
-            Tape tape;
-            tape.pos = 0;
             if (tp.mode == PPPM_MODE_COMPAT) {
                 const uint4 s = *reinterpret_cast<const uint4*>(pixelStates + 4 * pix);
                 tape.x.s[0] = s.x; tape.x.s[1] = s.y; tape.x.s[2] = s.z; tape.x.s[3] = s.w;
@@ -334,54 +344,61 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
             }
             const float px = (float)x + tape.popf() - 0.5f;
             const float py = (float)y + tape.popf() - 0.5f;
-            f3 d;
             cameraRay(cam, px, py, &d);
-            double o[3] = {cam.ex, cam.ey, cam.ez};
-            f3 w = {1.f, 1.f, 1.f}, L = {0.f, 0.f, 0.f};
-            for (int b = 0;; b++) {
-                if (b >= tp.maxBounceEye) {
-                    L = L + w * envLookup(env, d);
-                    break;
-                }
-                double best;
-                traced++;
-                const int slot = traverseExact<true>(sc.nodes, sc.tris, sc.rootCode, o[0], o[1], o[2], d.x, d.y, d.z,
-                                                     order, &best, &visits, &tests, sTop);
-                if (slot < 0) {
-                    L = L + w * envLookup(env, d);
-                    break;
-                }
-                const uint32_t r0 = tape.popu();
-                const float r1 = tape.popf(), r2 = tape.popf();
-                const float4 a = sc.tris[3 * slot], bb = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
-                const DevMaterial& m = sc.mats[sc.matId[__float_as_int(a.w)]];
-                double hp[3];
-                hitPosition(o[0], o[1], o[2], d.x, d.y, d.z, best, hp);
-                const f3 nrm = triNormalF(a, bb, c);
-                float roul = m.roulette;
-                if (b >= 3) {
-                    // rands[0] > roulette: the path ends and contributes nothing more
-                    if ((unsigned long long)r0 > m.roulFloor) break;
-                } else {
-                    roul = 1.0f;
-                }
-                const f3 refl = {m.refl[0], m.refl[1], m.refl[2]};
-                if (m.type & PPPM_BSDF_LAMBERTIAN) {
-                    const f3 on = dot(nrm, d) < 0.0f ? nrm : -nrm;
-                    const f3 wq = w * refl * (1.0f / roul);
-                    q0 = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
-                                     __int_as_float((int)pix));
-                    q1 = make_float4(on.x, on.y, on.z, 0.f);
-                    q2 = make_float4(wq.x, wq.y, wq.z, 0.f);
-                    query = true;
-                    break;
-                }
-                f3 nd;
-                const float pdf = bsdfSample(m, d, nrm, r1, r2, &nd);
-                w = w * refl * (1.0f / (pdf * roul));
-                o[0] = hp[0]; o[1] = hp[1]; o[2] = hp[2];
-                d = nd;
+        }
+        const bool onImage = alive;
+        for (int b = 0; __any_sync(0xffffffffu, alive); b++) {
+            const bool doTrace = alive && b < tp.maxBounceEye;
+            if (alive && !doTrace) {
+                L = L + w * envLookup(env, d);
+                alive = false;
             }
+            double best;
+            const int slot = traverseExactWarp(sc.nodes, sc.tris, sc.rootCode, doTrace, o[0], o[1], o[2], d.x, d.y,
+                                               d.z, order, sTop, &best, &visits, &tests);
+            if (!doTrace) continue;
+            traced++;
+            if (slot < 0) {
+                L = L + w * envLookup(env, d);
+                alive = false;
+                continue;
+            }
+            const uint32_t r0 = tape.popu();
+            const float r1 = tape.popf(), r2 = tape.popf();
+            const float4 a = sc.tris[3 * slot], bb = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
+            const DevMaterial& m = sc.mats[sc.matId[__float_as_int(a.w)]];
+            double hp[3];
+            hitPosition(o[0], o[1], o[2], d.x, d.y, d.z, best, hp);
+            const f3 nrm = triNormalF(a, bb, c);
+            float roul = m.roulette;
+            if (b >= 3) {
+                // rands[0] > roulette: the path ends and contributes nothing more
+                if ((unsigned long long)r0 > m.roulFloor) {
+                    alive = false;
+                    continue;
+                }
+            } else {
+                roul = 1.0f;
+            }
+            const f3 refl = {m.refl[0], m.refl[1], m.refl[2]};
+            if (m.type & PPPM_BSDF_LAMBERTIAN) {
+                const f3 on = dot(nrm, d) < 0.0f ? nrm : -nrm;
+                const f3 wq = w * refl * (1.0f / roul);
+                q0 = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
+                                 __int_as_float((int)pix));
+                q1 = make_float4(on.x, on.y, on.z, 0.f);
+                q2 = make_float4(wq.x, wq.y, wq.z, 0.f);
+                query = true;
+                alive = false;
+                continue;
+            }
+            f3 nd;
+            const float pdf = bsdfSample(m, d, nrm, r1, r2, &nd);
+            w = w * refl * (1.0f / (pdf * roul));
+            o[0] = hp[0]; o[1] = hp[1]; o[2] = hp[2];
+            d = nd;
+        }
+        if (onImage) {
             accum[3 * pix] += L.x;
             accum[3 * pix + 1] += L.y;
             accum[3 * pix + 2] += L.z;

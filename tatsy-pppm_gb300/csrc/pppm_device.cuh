@@ -337,6 +337,122 @@ __device__ __forceinline__ int traverseExact(const QNode* __restrict__ nodes, co
     return hit;
 }
 
+// Warp-cooperative form of traverseExact with the same results. The double
+// triangle test costs a warp ~50 FP64 instructions at 1/64 of the FP32 rate
+// whenever any lane needs it, and lanes reach their leaves at different
+// iterations. Here a lane whose FP32 pre-test passes records the leaf's
+// candidate triangles (in leaf order) and pauses; the warp runs the double
+// tests for all paused lanes together once kBatch lanes wait or no lane can
+// advance. A paused lane does nothing else until its tests are done, so each
+// lane performs the reference's operations in the reference's order: the
+// same box tests against the same (float)best, the same strict updates.
+// All 32 lanes of the warp must call it (inactive lanes pass active=false).
+constexpr int kExactBatch = 8;
+
+__device__ __forceinline__ int traverseExactWarp(const QNode* __restrict__ nodes, const float4* __restrict__ tris,
+                                                 int rootCode, bool active, double odx, double ody, double odz,
+                                                 float dx, float dy, float dz, const int* orderTab,
+                                                 const QNode* sTop, double* bestOut, int* nodeVisits,
+                                                 int* triTests) {
+    const float ox = __double2float_rn(odx), oy = __double2float_rn(ody), oz = __double2float_rn(odz);
+    const float idx = dx == 0.0f ? 1.0e20f : __frcp_rn(dx);
+    const float idy = dy == 0.0f ? 1.0e20f : __frcp_rn(dy);
+    const float idz = dz == 0.0f ? 1.0e20f : __frcp_rn(dz);
+    const int sx = idx > 0.0f ? 0 : 1, sy = idy > 0.0f ? 0 : 1, sz = idz > 0.0f ? 0 : 1;
+    const int sgnBits = sx | (sy << 1) | (sz << 2);
+    int stack[kStackSize];
+    int sp = 0;
+    if (active) stack[sp++] = rootCode;
+    double best = kInfty;
+    float bestf = 1.0e20f;
+    int hit = -1;
+    int visits = 0, tests = 0;
+    int cand0 = -1, cand1 = -1, cand2 = -1, ncand = 0;  // pending exact tests, leaf order
+    for (;;) {
+        const bool canRun = sp > 0 && ncand == 0;
+        const unsigned runMask = __ballot_sync(0xffffffffu, canRun);
+        const unsigned pendMask = __ballot_sync(0xffffffffu, ncand > 0);
+        if ((runMask | pendMask) == 0) break;
+        if (pendMask != 0 && (__popc(pendMask) >= kExactBatch || runMask == 0)) {
+            if (ncand > 0) {
+                const double ddx = dx, ddy = dy, ddz = dz;
+                for (int c = 0; c < ncand; c++) {
+                    const int slot = c == 0 ? cand0 : (c == 1 ? cand1 : cand2);
+                    const float4 a = tris[3 * slot], b = tris[3 * slot + 1], cc = tris[3 * slot + 2];
+                    double t;
+                    if (triHitExact(odx, ody, odz, ddx, ddy, ddz, a, b, cc, &t) && best > t) {
+                        best = t;
+                        bestf = __double2float_rn(t);
+                        hit = slot;
+                    }
+                }
+                ncand = 0;
+            }
+            continue;
+        }
+        if (!canRun) continue;
+        const int code = stack[--sp];
+        if (code < 0) {
+            const int lc = ~code;
+            const int first = lc >> 2, cnt = lc & 3;
+            for (int i = 0; i < cnt; i++) {
+                const int slot = first + i;
+                const float4 a = tris[3 * slot], b = tris[3 * slot + 1], c = tris[3 * slot + 2];
+                tests++;
+                if (!triMayHit(ox, oy, oz, dx, dy, dz, a, b, c, bestf)) continue;
+                if (ncand == 0) cand0 = slot; else if (ncand == 1) cand1 = slot; else cand2 = slot;
+                ncand++;
+            }
+            continue;
+        }
+        visits++;
+        const QNode* nd = (sTop != nullptr && code < kTopNodes) ? sTop + code : nodes + code;
+        const float hd = bestf;
+        float tmin[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        float tmax[4] = {hd, hd, hd, hd};
+        const float o3[3] = {ox, oy, oz};
+        const float i3[3] = {idx, idy, idz};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const float4 lo = nd->bmin[d];
+            const float4 hi = nd->bmax[d];
+            const bool neg = (sgnBits >> d) & 1;
+            const float4 nearB = neg ? hi : lo;
+            const float4 farB = neg ? lo : hi;
+            const float nb[4] = {nearB.x, nearB.y, nearB.z, nearB.w};
+            const float fb[4] = {farB.x, farB.y, farB.z, farB.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float t0 = __fmul_rn(__fsub_rn(nb[k], o3[d]), i3[d]);
+                const float t1 = __fmul_rn(__fsub_rn(fb[k], o3[d]), i3[d]);
+                tmin[k] = tmin[k] > t0 ? tmin[k] : t0;
+                tmax[k] = tmax[k] < t1 ? tmax[k] : t1;
+            }
+        }
+        int hitMask = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) hitMask |= (tmax[k] >= tmin[k]) ? (1 << k) : 0;
+        if (hitMask != 0) {
+            const int4 ch = nd->child;
+            const int meta = nd->meta.x;
+            const int a0 = meta & 3, a1 = (meta >> 2) & 3, a2 = (meta >> 4) & 3;
+            const int sepMask = (((sgnBits >> a0) & 1) << 2) | (((sgnBits >> a1) & 1) << 1) | ((sgnBits >> a2) & 1);
+            int ord = orderTab[hitMask * 8 + sepMask];
+            const int c4[4] = {ch.x, ch.y, ch.z, ch.w};
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                if (ord & 0x04) break;
+                stack[sp++] = c4[ord & 0x03];
+                ord >>= 4;
+            }
+        }
+    }
+    *bestOut = best;
+    if (nodeVisits) *nodeVisits += visits;
+    if (triTests) *triTests += tests;
+    return hit;
+}
+
 // Hit record of the exact path: position o + t*d and the triangle's
 // normal cross(p1-p0, p2-p0).normalized() computed in double like
 // Triangle::normal (triangle.cc:45-47), rounded to float.
