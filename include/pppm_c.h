@@ -202,6 +202,21 @@ int pppm_knn(pppm_ctx* ctx, const float* photon_pos, int64_t n, const float* que
 int pppm_gather(pppm_ctx* ctx, int32_t mode, const float* photons, int64_t n, int64_t phantoms,
                 const float* queries, int64_t m, double radius, int32_t gather_photons, float* out);
 
+/* Replaces DipoleBSSRDF::operator() (bssrdf.cc:92-104): Rd(d^2) per colour
+ * channel for the dipole parameters of `mat` (sigma_a, sigmap_s, eta,
+ * scale), including the reference's fast_exp approximation
+ * (vector3d.cc:11-16). d2: n floats, rgb: n x 3. */
+int pppm_dipole_rd(pppm_ctx* ctx, const pppm_material* mat, const float* d2, int64_t n, float* rgb);
+
+/* Replaces SubsurfaceIntegrator::irradiance (subsurface_integrator.cc:234-238)
+ * over an octree built like Octree::construct (subsurface_integrator.cc:67-145)
+ * from n irradiance points of 10 floats (pos xyz, normal xyz, area,
+ * irradiance rgb): (1/pi)(1 - Fdr) * sum of Rd(d^2) * E * A over the nodes
+ * accepted with threshold max_error. queries: m x 3, rgb: m x 3. Repeated
+ * points return PPPM_E_UNDEFINED (the reference's recursion never ends). */
+int pppm_dipole_irradiance(pppm_ctx* ctx, const pppm_material* mat, const float* ipts, int64_t n, double max_error,
+                           const float* queries, int64_t m, float* rgb);
+
 /* Allocation-free variant of pppm_knn (same arguments and results) for
  * callers that cannot let a library allocate GPU memory: programs that own
  * all device memory under a fixed budget, frame loops that must not stall on

@@ -75,6 +75,9 @@ SIGNATURES = {
     "pppm_hash_points": ([_VP, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP], ctypes.c_int),
     "pppm_knn": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
                   ctypes.c_int32], ctypes.c_int),
+    "pppm_dipole_rd": ([_VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_dipole_irradiance": ([_VP, _VP, _VP, ctypes.c_int64, ctypes.c_double, _VP, ctypes.c_int64, _VP],
+                               ctypes.c_int),
     "pppm_knn_noalloc": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
                           ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_gather": ([_VP, ctypes.c_int32, _VP, ctypes.c_int64, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_double,
@@ -235,6 +238,22 @@ class Context:
         out = _empty_like_kind(queries12, (m, 3), np.float32)
         self._check(self.lib.pppm_gather(self.h, int(mode), _ptr(photons8), n, int(phantoms), _ptr(queries12), m,
                                          float(radius), int(gather_photons), _ptr(out)))
+        return out
+
+    def dipole_rd(self, mat, d2):
+        d2 = np.ascontiguousarray(d2, np.float32)
+        m = np.ascontiguousarray(mat)
+        out = np.zeros((d2.size, 3), np.float32)
+        self._check(self.lib.pppm_dipole_rd(self.h, m.ctypes.data, d2.ctypes.data, d2.size, out.ctypes.data))
+        return out
+
+    def dipole_irradiance(self, mat, ipts10, max_error, queries):
+        ip = np.ascontiguousarray(ipts10, np.float32).reshape(-1, 10)
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 3)
+        m = np.ascontiguousarray(mat)
+        out = np.zeros((len(q), 3), np.float32)
+        self._check(self.lib.pppm_dipole_irradiance(self.h, m.ctypes.data, ip.ctypes.data, len(ip), float(max_error),
+                                                    q.ctypes.data, len(q), out.ctypes.data))
         return out
 
     # -------------------------------------------------------------- render

@@ -244,7 +244,42 @@ def gen_render():
          threads=np.array(rh.num_threads()))
 
 
-GENERATORS.update({"knn": gen_knn, "gather": gen_gather, "render": gen_render})
+def gen_dipole():
+    """DipoleBSSRDF::operator() tables and SubsurfaceIntegrator::irradiance
+    over injected irradiance points (the reference's own photon pass for them
+    is seeded with time(NULL), so points are injected, not traced)."""
+    rng = np.random.default_rng(41)
+    mats = [S.material(S.REFRACTION, (0.99, 0.99, 0.99), sigma_a=(0.0021, 0.0041, 0.0071), sigmap_s=(2.19, 2.62, 3.00),
+                       eta=1.5, scale=1.0, bssrdf=True),
+            S.material(S.LAMBERTIAN, (0.8, 0.8, 0.8), sigma_a=(0.013, 0.070, 0.145), sigmap_s=(1.09, 1.59, 1.79),
+                       eta=1.3, scale=0.7, bssrdf=True),
+            S.material(S.REFRACTION, (0.9, 0.9, 0.9), sigma_a=(0.02, 0.01, 0.04), sigmap_s=(0.6, 2.9, 1.4),
+                       eta=0.8, scale=2.0, bssrdf=True)]
+    d2 = np.concatenate([np.linspace(0, 4, 500), rng.uniform(0, 200, 1500) ** 2 / 100]).astype(np.float32)
+    out = {"d2": d2}
+    for k, m in enumerate(mats):
+        out[f"mat{k}"] = np.ascontiguousarray(m).view(np.uint8).copy()
+        out[f"rd{k}"] = rh.dipole_rd(m, d2.astype(np.float64))
+        out[f"fdr{k}"] = np.array(rh.dipole_fdr(m))
+    # irradiance points on a displaced sphere, spacing ~ Poisson disc radius
+    sph = S.displace_sphere(S.geodesic_sphere(24), 5.0, 0.05, 3)
+    pts = sph.mean(1)
+    nrm = np.cross(sph[:, 1] - sph[:, 0], sph[:, 2] - sph[:, 0])
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    n = len(pts)
+    area = np.full(n, np.pi * 0.25 ** 2)
+    irad = rng.lognormal(0.0, 1.0, (n, 3)) * np.array([1.0, 0.8, 0.6])
+    ip = np.concatenate([pts, nrm, area[:, None], irad], 1).astype(np.float32).astype(np.float64)
+    q = (pts[rng.integers(0, n, 3000)] + rng.normal(size=(3000, 3)) * 0.05).astype(np.float32).astype(np.float64)
+    out["ipts"] = ip
+    out["queries"] = q
+    for k, m in enumerate(mats):
+        for e, me in enumerate((0.05, 0.5)):
+            out[f"irr{k}_{e}"] = rh.dipole_irradiance(m, ip, me, q)
+    save("dipole", **out)
+
+
+GENERATORS.update({"knn": gen_knn, "gather": gen_gather, "render": gen_render, "dipole": gen_dipole})
 
 
 if __name__ == "__main__":
