@@ -95,6 +95,9 @@ typedef struct {
     double radius_scale;    /* r1 = radius_scale * |bbox diagonal| (0.1 in the reference) */
     float cell_factor;      /* hash-grid cell size: canonical = cell_factor * radius (>= 1) */
     int32_t flags;          /* PPPM_FLAG_* */
+    uint32_t sss_time;      /* compat, scenes with a BSSRDF: the value time(NULL) returns when pass 1
+                               seeds its subsurface photon streams (subsurface_integrator.cc:248);
+                               pass t uses sss_time + t - 1 */
 } pppm_params;
 
 /* pppm_params.flags */
@@ -121,6 +124,10 @@ typedef struct {
     int64_t photon_tri_tests;
     int64_t gather_pairs;    /* canonical: photon-query pairs tested (PPPM_FLAG_COUNT_TRAVERSAL) */
     int64_t gather_inside;   /* canonical: pairs within the radius (PPPM_FLAG_COUNT_TRAVERSAL) */
+    int64_t sss_points;      /* subsurface irradiance points (Poisson-disc samples) of this pass */
+    int64_t sss_photons;     /* subsurface photons stored */
+    double ms_subsurface;    /* subsurface stage before the photon pass (ms, includes host sampling) */
+    double ms_subsurface_host; /* of which host Poisson sampling + octree build (ms) */
 } pppm_pass_stats;
 
 /* ------------------------------------------------------------- lifetime */
@@ -216,6 +223,28 @@ int pppm_dipole_rd(pppm_ctx* ctx, const pppm_material* mat, const float* d2, int
  * points return PPPM_E_UNDEFINED (the reference's recursion never ends). */
 int pppm_dipole_irradiance(pppm_ctx* ctx, const pppm_material* mat, const float* ipts, int64_t n, double max_error,
                            const float* queries, int64_t m, float* rgb);
+
+/* Replaces sampler::poissonDisk (sampler.cc:36-101): dart throwing over the
+ * triangle soup (9 floats each, host) with minimum distance min_dist. The
+ * candidate draws come from the XorShift state rng_state (4 words, advanced
+ * in place; the reference uses a process-wide XorShift seeded 0, whose
+ * initial state is XorShift(0)); the acceptance order follows the
+ * reference's RandomQueue seeded -1 and its hash grid. Writes up to cap
+ * points and triangle normals (3 floats each) and the total count. Host-only:
+ * needs no context or GPU. */
+int pppm_poisson_disk(const float* tri_xyz, int64_t ntri, double min_dist, uint32_t* rng_state, float* pts,
+                      float* nrm, int64_t cap, int64_t* count);
+
+/* Replaces SubsurfaceIntegrator::irradianceWithPM (subsurface_integrator.cc:
+ * 329-365) over an injected photon map: photons are n records of 8 floats
+ * (pos xyz, flux xyz, 2 unused), points m records of 6 floats (pos xyz,
+ * normal xyz). As in the reference, findKNN receives (num_photons,
+ * gather_radius), so k = (int)gather_radius nearest photons within distance
+ * num_photons; the normal filter is |n.(p-q)|/|p-q| < gather_photons^2 *
+ * 0.01; the cone-filtered flux weights the unfiltered list's photon i with
+ * the i-th kept distance. out: m x 3 irradiance. */
+int pppm_subsurface_photon_irradiance(pppm_ctx* ctx, const float* photons, int64_t n, const float* points, int64_t m,
+                                      int64_t num_photons, double gather_radius, int32_t gather_photons, float* out);
 
 /* Allocation-free variant of pppm_knn (same arguments and results) for
  * callers that cannot let a library allocate GPU memory: programs that own

@@ -43,6 +43,13 @@
 // reference; the default template argument of clamp()/Size<> needs a symbol.
 void* enabler = nullptr;
 
+// time(NULL) as seen by subsurface_integrator.cc (oracle/fake_time.h).
+static time_t gFakeTime = 0;
+extern "C" time_t rh_fake_time(time_t* t) {
+    if (t) *t = gFakeTime;
+    return gFakeTime;
+}
+
 namespace {
 
 // Triangle soup geometry: lets the harness add an arbitrary triangle list
@@ -341,6 +348,7 @@ struct PassJob {
     int gatherPhotons;
     double gatherRadius;
     int npasses;
+    unsigned int sssTime;  // time(NULL) seen by pass t's subsurface photon map: sssTime + t - 1
 };
 
 static void collectKd(const KdTree<Photon>::KdTreeNode* node, std::vector<Photon>* out) {
@@ -362,6 +370,22 @@ int rh_render_passes(void* s, const PassJob* job, double* accum, double* radii, 
     for (int i = 0; i < (int)sc.numTriangles(); i++) bbox.merge(sc.getTriangle(i));
     ppm._radius = (bbox.posMax() - bbox.posMin()).norm() * 0.1;
 
+    // subsurface set-up as render() does it (ppm_probabilistic.cc:33-47)
+    bool enableBssrdf = false;
+    double avgArea = 0.0;
+    for (int i = 0; i < sc.numTriangles(); i++) {
+        if (sc.getBsdf(i).type() & BSDF_TYPE_BSSRDF) {
+            enableBssrdf = true;
+            avgArea += sc.getTriangle(i).area();
+        }
+    }
+    avgArea /= sc.numTriangles();
+    double areaRadius = 0.0;
+    if (enableBssrdf) {
+        areaRadius = sqrt(avgArea) * 1.0;
+        ppm._integrator = new SubsurfaceIntegrator();
+    }
+
     RandomSampler* rs = new RandomSampler[OMP_NUM_CORE];
     for (int i = 0; i < OMP_NUM_CORE; i++) rs[i] = Random::generateSampler(i);
     Image buffer(job->w, job->h);
@@ -369,6 +393,10 @@ int rh_render_passes(void* s, const PassJob* job, double* accum, double* radii, 
     std::streambuf* old = std::cout.rdbuf(nullptr);  // silence progress output
     for (int t = 1; t <= job->npasses; t++) {
         radii[t - 1] = ppm._radius;
+        if (enableBssrdf) {
+            gFakeTime = (time_t)(job->sssTime + (unsigned int)(t - 1));
+            ppm._integrator->initialize(sc, params, areaRadius, 0.05);
+        }
         ppm.tracePhotons(sc, cam, params, rs);
         ppm.traceRays(&buffer, sc, cam, params, rs);
         ppm._radius = (t + 1.0) / (t + ProgressivePhotonMappingProb::ALPHA) * ppm._radius;
@@ -417,6 +445,26 @@ void rh_dipole_irradiance(const Mat* m, const double* ipts, int n, double maxErr
     }
     integ.octree.construct(&integ, pts);
     for (int j = 0; j < nq; j++) put3(out + 3 * j, integ.irradiance(Vector3D(q[3 * j], q[3 * j + 1], q[3 * j + 2]), b));
+}
+
+// SubsurfaceIntegrator::irradianceWithPM (subsurface_integrator.cc:329-365)
+// over an injected photon map: photons are 8 doubles each (pos, flux, 2
+// unused), points 6 doubles each (pos, normal).
+void rh_irradiance_pm(const double* photons, int n, const double* points, int m, int numPhotons, int gatherPhotons,
+                      double gatherRadius, double* out) {
+    SubsurfaceIntegrator integ;
+    std::vector<Photon> ph;
+    ph.reserve(n);
+    for (int i = 0; i < n; i++) {
+        const double* p = photons + 8 * i;
+        ph.push_back(Photon(Vector3D(p[0], p[1], p[2]), Vector3D(p[3], p[4], p[5]), Vector3D(), Vector3D()));
+    }
+    integ.photonMap.construct(ph);
+    RenderParameters params(numPhotons, 1, gatherPhotons, gatherRadius);
+    for (int j = 0; j < m; j++) {
+        const double* q = points + 6 * j;
+        put3(out + 3 * j, integ.irradianceWithPM(Vector3D(q[0], q[1], q[2]), Vector3D(q[3], q[4], q[5]), params));
+    }
 }
 
 // sampler::poissonDisk (sampler.cc:36-101). Uses the reference's static RNG,

@@ -79,6 +79,8 @@ def lib():
         _lib.rh_dipole_irradiance.argtypes = [ctypes.c_void_p, _D, ctypes.c_int, ctypes.c_double, _D, ctypes.c_int, _D]
         _lib.rh_poisson_disk.argtypes = [_F, ctypes.c_int, ctypes.c_double, _D, _D, ctypes.c_int]
         _lib.rh_poisson_disk.restype = ctypes.c_int
+        _lib.rh_irradiance_pm.argtypes = [_D, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_double, _D]
     return _lib
 
 
@@ -166,7 +168,12 @@ class RefScene:
                         rays.shape[0], _p(out, _D))
         return out
 
-    def render_passes(self, camera, photons, npasses, gather_photons=128, gather_radius=16.0, photon_cap=0):
+    def render_passes(self, camera, photons, npasses, gather_photons=128, gather_radius=16.0, photon_cap=0,
+                      sss_time=0):
+        """Passes 1..npasses of ProgressivePhotonMappingProb::render. With a
+        BSSRDF in the scene, pass t seeds its subsurface photon streams with
+        time(NULL) = sss_time + t - 1 and the Poisson sampler continues the
+        process-wide RNG (reproducible in a fresh process only)."""
         job = _PassJob()
         job.eye[:] = camera.eye
         job.dir[:] = camera.dir
@@ -177,6 +184,7 @@ class RefScene:
         job.gatherPhotons = gather_photons
         job.gatherRadius = gather_radius
         job.npasses = npasses
+        job.sssTime = int(sss_time)
         accum = np.zeros((camera.height, camera.width, 3))
         radii = np.zeros(npasses)
         cnt = np.zeros(1, np.int32)
@@ -193,7 +201,8 @@ class RefScene:
 class _PassJob(ctypes.Structure):
     _fields_ = [("eye", ctypes.c_double * 3), ("dir", ctypes.c_double * 3), ("up", ctypes.c_double * 3),
                 ("fov", ctypes.c_double), ("w", ctypes.c_int), ("h", ctypes.c_int), ("photons", ctypes.c_int),
-                ("gatherPhotons", ctypes.c_int), ("gatherRadius", ctypes.c_double), ("npasses", ctypes.c_int)]
+                ("gatherPhotons", ctypes.c_int), ("gatherRadius", ctypes.c_double), ("npasses", ctypes.c_int),
+                ("sssTime", ctypes.c_uint)]
 
 
 def write_hdr(path, rgb):
@@ -310,6 +319,15 @@ def dipole_irradiance(mat, ipts10, max_error, queries):
     m = np.ascontiguousarray(mat)
     lib().rh_dipole_irradiance(m.ctypes.data, _p(ipts, _D), ipts.shape[0], float(max_error), _p(q, _D), q.shape[0],
                                _p(out, _D))
+    return out
+
+
+def irradiance_pm(photons8, points6, num_photons, gather_photons, gather_radius):
+    ph = np.ascontiguousarray(photons8, np.float64).reshape(-1, 8)
+    pt = np.ascontiguousarray(points6, np.float64).reshape(-1, 6)
+    out = np.zeros((pt.shape[0], 3))
+    lib().rh_irradiance_pm(_p(ph, _D), ph.shape[0], _p(pt, _D), pt.shape[0], int(num_photons), int(gather_photons),
+                           float(gather_radius), _p(out, _D))
     return out
 
 

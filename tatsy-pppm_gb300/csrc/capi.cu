@@ -49,6 +49,28 @@ int finishOut(pppm_ctx* c, void* dst, const void* staged, size_t bytes) {
     return PPPM_OK;
 }
 
+DipoleDev dipoleFrom(const pppm_material& mat) {
+    DipoleDev d;
+    std::memset(&d, 0, sizeof(d));
+    // BSSRDFBase::Fdr (bssrdf.cc:33-42) and the DipoleBSSRDF ctor
+    // (bssrdf.cc:48-63) in double
+    const double eta = mat.eta, eta2 = eta * eta, eta3 = eta2 * eta;
+    const double fdr = eta >= 1.0 ? (-1.439 + 0.7099 * eta + 0.6681 * eta2 + 0.0636 * eta3) / eta2
+                                  : (-0.4399 * eta3 + 0.7099 * eta2 - 0.3319 * eta + 0.0636) / eta3;
+    const double A = (1.0 + fdr) / (1.0 - fdr);
+    for (int k = 0; k < 3; k++) {
+        const double sa = mat.sigma_a[k], ss = mat.sigmap_s[k], st = sa + ss;
+        d.sigma_tr[k] = (float)std::sqrt(3.0 * sa * st);
+        d.alphap[k] = (float)(ss / st);
+        const double zp = 1.0 / st;
+        d.zpos[k] = (float)zp;
+        d.zneg[k] = (float)(zp * (1.0 + (4.0 / 3.0) * A));
+    }
+    d.scale = mat.scale;
+    d.coeff = (float)((1.0 / 3.14159265358979323846) * (1.0 - fdr));
+    return d;
+}
+
 static DevMaterial toDevMaterial(const pppm_material& m) {
     DevMaterial d;
     std::memset(&d, 0, sizeof(d));
@@ -61,25 +83,7 @@ static DevMaterial toDevMaterial(const pppm_material& m) {
     d.rrCeil = (unsigned long long)std::ceil(d.rr_photon * 4294967296.0);
     d.roulFloor = (unsigned long long)std::floor((double)d.roulette * 4294967296.0);
     d.invRr = (float)(1.0 / d.rr_photon);
-    if (m.has_bssrdf) {
-        // DipoleBSSRDF ctor (bssrdf.cc:48-63) and Fdr (bssrdf.cc:33-42) in double
-        const double eta = m.eta, eta2 = eta * eta, eta3 = eta2 * eta;
-        const double fdr = eta >= 1.0 ? (-1.439 + 0.7099 * eta + 0.6681 * eta2 + 0.0636 * eta3) / eta2
-                                      : (-0.4399 * eta3 + 0.7099 * eta2 - 0.3319 * eta + 0.0636) / eta3;
-        const double A = (1.0 + fdr) / (1.0 - fdr);
-        d.A = (float)A;
-        d.fdr = (float)fdr;
-        d.eta = m.eta;
-        d.scale = m.scale;
-        for (int k = 0; k < 3; k++) {
-            const double sa = m.sigma_a[k], ss = m.sigmap_s[k];
-            const double st = sa + ss;
-            d.sigma_tr[k] = (float)std::sqrt(3.0 * sa * st);
-            d.alphap[k] = (float)(ss / st);
-            d.zpos[k] = (float)(1.0 / st);
-            d.zneg[k] = (float)((1.0 / st) * (1.0 + (4.0 / 3.0) * A));
-        }
-    }
+    if (m.has_bssrdf) d.dip = dipoleFrom(m);
     return d;
 }
 
@@ -117,6 +121,13 @@ int pppm_create(int device, pppm_ctx** out) {
         return PPPM_E_CUDA;
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
+    cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&c->rs.sss.done, cudaEventDisableTiming);
+    {
+        XorShift x;
+        x.seed(0u);
+        for (int k = 0; k < 4; k++) c->poissonRng[k] = x.s[k];
+    }
     *out = c;
     return PPPM_OK;
 }
@@ -127,6 +138,8 @@ int pppm_destroy(pppm_ctx* c) {
     cudaStreamSynchronize(c->stream);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
+    if (c->rs.sss.done) cudaEventDestroy(c->rs.sss.done);
+    if (c->aux) cudaStreamDestroy(c->aux);
     cudaStreamDestroy(c->stream);
     delete c;
     return PPPM_OK;
@@ -199,6 +212,19 @@ int pppm_scene_set(pppm_ctx* c, const float* tri, int64_t ntri, const int32_t* m
         const double e2[3] = {(double)p[6] - p[0], (double)p[7] - p[1], (double)p[8] - p[2]};
         const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
         c->lambertArea += 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+    }
+    c->hostTri.assign(tri, tri + 9 * ntri);
+    c->bssrdfTris.clear();
+    c->bssrdfArea = 0.0;
+    for (int64_t i = 0; i < ntri; i++) {
+        if (!mats[matId[i]].has_bssrdf) continue;
+        c->bssrdfTris.push_back(i);
+        // Triangle::area: 0.5 |(p1 - p0) x (p2 - p1)| (triangle.cc:80-84)
+        const float* p = tri + 9 * i;
+        const double e1[3] = {(double)p[3] - p[0], (double)p[4] - p[1], (double)p[5] - p[2]};
+        const double e2[3] = {(double)p[6] - p[3], (double)p[7] - p[4], (double)p[8] - p[5]};
+        const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
+        c->bssrdfArea += 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
     }
     c->ntri = ntri;
     c->rootCode = bvh.rootCode;

@@ -56,6 +56,47 @@ struct QuerySortBufs {
     uint32_t size = 0;
 };
 
+// Pinned host buffer (grown on demand).
+struct HostPinned {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMallocHost(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+    ~HostPinned() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+// Subsurface stage of a render (SubsurfaceIntegrator, rebuilt every pass).
+struct SssState {
+    bool enabled = false;
+    double areaRadius = 0.0;  // sqrt(BSSRDF area / all triangles) (ppm_probabilistic.cc:35-46)
+    double dA = 0.0;          // irradiance point area (subsurface_integrator.cc:202)
+    int k = 0;                // (int)gatherRadius: kNN count of irradianceWithPM
+    DBuf photons;             // 2 x float4 per stored subsurface photon
+    int64_t cap = 0;
+    GridBufs grid;
+    DBuf points;              // 3 x float4 per irradiance point (gather query layout)
+    DBuf irad;                // float3 per point
+    DBuf octree;              // OctNodeDev per node
+    int octNodes = 0;
+    HostPinned iradHost;
+    std::vector<float> pts, nrm;     // this pass's Poisson points and normals
+    std::vector<float4> query;       // packed queries
+    int64_t stored = 0;
+    double msHost = 0.0;      // host time of Poisson sampling and octree build
+    cudaEvent_t done = nullptr;  // irradiance of the points computed
+};
+
 struct RenderState {
     bool active = false;
     pppm_camera cam{};
@@ -80,6 +121,7 @@ struct RenderState {
     int64_t depositCap = 0;
     int64_t storedLast = 0;
     int64_t phantomsLast = 0;
+    SssState sss;
 };
 
 }  // namespace pppm
@@ -99,6 +141,13 @@ struct pppm_ctx {
     bool anyBssrdf = false;
     pppm::DBuf nodes, tris, matId, devMats;
     double lambertArea = 0.0;  // summed area of Lambertian triangles
+    std::vector<float> hostTri;        // triangle soup (9 floats each), for the Poisson sampler
+    std::vector<int64_t> bssrdfTris;   // triangles with a BSSRDF, in scene order
+    double bssrdfArea = 0.0;           // their summed Triangle::area, in scene order
+    // sampler.cc's static Random (seeded 0) of the Poisson-disc sampler; it
+    // lives as long as the process there and as long as the context here
+    uint32_t poissonRng[4] = {0, 0, 0, 0};
+    cudaStream_t aux = nullptr;        // readbacks that overlap the main stream
     // env
     bool hasEnv = false;
     int envW = 0, envH = 0;
@@ -135,6 +184,9 @@ inline int cudaFail(pppm_ctx* c, cudaError_t e, const char* where) {
     } while (0)
 
 bool isDevicePtr(const void* p);
+
+// Dipole constants of a material (capi.cu).
+DipoleDev dipoleFrom(const pppm_material& mat);
 
 // Returns a device pointer holding `bytes` of `src`: src itself when it is
 // device memory, else a staging copy (slot chooses the staging buffer).

@@ -281,11 +281,9 @@ cudaError_t launchGatherCanonical(const GridDev& g, QueryView q, float radius, f
     return cudaGetLastError();
 }
 
-cudaError_t launchGatherCompat(const GridDev& g, QueryView q, int k, float eps, float radius, int64_t phantoms,
+cudaError_t launchGatherCompat(const GridDev& g, QueryView q, int k, float eps, float rlim, int64_t phantoms,
                                float* out, bool accumulate, cudaStream_t st) {
     const int bs = 128;
-    // disc filter threshold _radius * _radius * 0.01 (ppm_probabilistic.cc:314)
-    const float rlim = (float)((double)radius * (double)radius * 0.01);
     if (accumulate) kGatherCompat<true><<<blocksFor(q.n, bs), bs, 0, st>>>(g, q, k, eps, rlim, phantoms, out);
     else kGatherCompat<false><<<blocksFor(q.n, bs), bs, 0, st>>>(g, q, k, eps, rlim, phantoms, out);
     return cudaGetLastError();

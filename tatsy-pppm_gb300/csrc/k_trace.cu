@@ -116,6 +116,7 @@ __device__ __forceinline__ void seedCanonical(uint32_t seed, int pass, uint64_t 
 }
 
 constexpr int kRun = 32;  // tapes generated sequentially per thread
+constexpr int kMaxEyeSegments = 4096;  // eye path segments before a path is cut (subsurface scenes)
 
 // Start state of every photon tape and pixel tape of this pass. Stream s
 // (one per reference OpenMP thread) draws, in order, ceil(P/N) photon tapes
@@ -171,7 +172,7 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
             seedCanonical(tp.seed, tp.pass, (uint64_t)g, tape.x);
         }
         f3 d, dir, flux;
-        const bool ok = emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux);
+        const bool ok = emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux, tp.sssPass != 0);
         if (!ok) atomicAdd(&ctr->undefinedEmit, 1ull);
         PathState p;
         p.ox = 50.0 * (double)d.x;  // R * dir with R = 50 (envmap.cc:63,85)
@@ -208,6 +209,11 @@ __device__ __forceinline__ unsigned long long warpAppend(bool take, unsigned lon
 // closest hit, three draws, deposit + Russian roulette on Lambertian
 // surfaces, BSDF sampling elsewhere. Survivors are compacted into `out`
 // with one atomic per warp; queue lengths rotate through ctr->queue[b % 3].
+// kSss: the photon pass of SubsurfaceIntegrator::buildPhotonMap
+// (subsurface_integrator.cc:240-327) instead: records only on BSSRDF
+// surfaces, Russian roulette there on the mean flux, and every BSDF sampled
+// with the geometric normal and draws 1, 2.
+template <bool kSss>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(TraceParams tp, SceneView sc, int bounce, const PathState* __restrict__ in,
                                                      PathState* __restrict__ out, int64_t maxPaths,
                                                      float4* __restrict__ dep, int64_t depCap, PassCounters* ctr) {
@@ -243,8 +249,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
                 Tape tape;
                 tape.pos = 0;
                 tape.x.s[0] = p.rng[0]; tape.x.s[1] = p.rng[1]; tape.x.s[2] = p.rng[2]; tape.x.s[3] = p.rng[3];
-                const uint32_t r0 = tape.popu();
-                const float r1 = tape.popf(), r2 = tape.popf();
+                const uint32_t r0 = tape.popu(), r1 = tape.popu(), r2 = tape.popu();
                 const float4 a = sc.tris[3 * slot], b = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
                 const int tid = __float_as_int(a.w);
                 const DevMaterial& m = sc.mats[sc.matId[tid]];
@@ -256,7 +261,20 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
                 f3 flux = {p.fx, p.fy, p.fz};
                 const f3 refl = {m.refl[0], m.refl[1], m.refl[2]};
                 f3 nd;
-                if (m.type & PPPM_BSDF_LAMBERTIAN) {
+                if (kSss) {
+                    if (kSss && (m.type & PPPM_BSDF_BSSRDF)) {
+                        store = true;
+                        da = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
+                                         __uint_as_float(packNormal(on)));
+                        db = make_float4(flux.x, flux.y, flux.z, __int_as_float(p.id));
+                        const float prob = (flux.x + flux.y + flux.z) / 3.0f;
+                        if (!(u32ToFloat(r0) < prob)) alive = false;  // rands[0] >= probability: break
+                    }
+                    if (alive) {
+                        const float pdf = bsdfSample(m, din, nrm, r1, r2, &nd);
+                        flux = flux * refl * (1.0f / pdf);
+                    }
+                } else if (m.type & PPPM_BSDF_LAMBERTIAN) {
                     store = true;
                     da = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
                                      __uint_as_float(packNormal(on)));
@@ -268,7 +286,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
                         alive = false;
                     }
                 } else {
-                    const float pdf = bsdfSample(m, din, on, u32ToFloat(r0), r1, &nd);
+                    const float pdf = bsdfSample(m, din, on, r0, r1, &nd);
                     flux = flux * refl * (1.0f / pdf);
                 }
                 p.ox = hp[0]; p.oy = hp[1]; p.oz = hp[2];
@@ -311,9 +329,13 @@ __device__ __forceinline__ void cameraRay(const CameraDev& c, float px, float py
 // surfaces, Russian roulette after 3 bounces, a gather query at the first
 // Lambertian hit, the env map on a miss. Environment terms go straight into
 // the accumulation buffer; queries are compacted with one atomic per warp.
+// kSss: the scene has BSSRDF materials (the subsurface branches of radiance
+// are compiled in only then).
+template <bool kSss>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TraceParams tp, SceneView sc, EnvDev env, CameraDev cam,
-                                                 const uint32_t* __restrict__ pixelStates, float* __restrict__ accum,
-                                                 float4* __restrict__ queries, PassCounters* ctr) {
+                                                 OctView oct, const uint32_t* __restrict__ pixelStates,
+                                                 float* __restrict__ accum, float4* __restrict__ queries,
+                                                 PassCounters* ctr) {
     __shared__ int order[128];
     __shared__ QNode sTop[kTopNodes];
     loadOrderTable(order);
@@ -347,8 +369,18 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
             cameraRay(cam, px, py, &d);
         }
         const bool onImage = alive;
-        for (int b = 0; __any_sync(0xffffffffu, alive); b++) {
-            const bool doTrace = alive && b < tp.maxBounceEye;
+        // bnc: the reference's `bounces` argument, which the Fresnel
+        // reflection of a refractive BSSRDF surface passes on unchanged
+        int bnc = 0;
+        int iter = 0;
+        while (__any_sync(0xffffffffu, alive)) {
+            // Fresnel reflections that keep `bnc` draw 3 numbers each, so a
+            // compat tape ends them after 66; the cap bounds canonical paths
+            if (kSss && alive && ++iter > kMaxEyeSegments) {
+                atomicAdd(&ctr->undefinedEye, 1ull);
+                alive = false;
+            }
+            const bool doTrace = alive && bnc < tp.maxBounceEye;
             if (alive && !doTrace) {
                 L = L + w * envLookup(env, d);
                 alive = false;
@@ -363,15 +395,14 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
                 alive = false;
                 continue;
             }
-            const uint32_t r0 = tape.popu();
-            const float r1 = tape.popf(), r2 = tape.popf();
+            const uint32_t r0 = tape.popu(), r1 = tape.popu(), r2 = tape.popu();
             const float4 a = sc.tris[3 * slot], bb = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
             const DevMaterial& m = sc.mats[sc.matId[__float_as_int(a.w)]];
             double hp[3];
             hitPosition(o[0], o[1], o[2], d.x, d.y, d.z, best, hp);
             const f3 nrm = triNormalF(a, bb, c);
             float roul = m.roulette;
-            if (b >= 3) {
+            if (bnc >= 3) {
                 // rands[0] > roulette: the path ends and contributes nothing more
                 if ((unsigned long long)r0 > m.roulFloor) {
                     alive = false;
@@ -381,6 +412,28 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
                 roul = 1.0f;
             }
             const f3 refl = {m.refl[0], m.refl[1], m.refl[2]};
+            if (kSss && (m.type & PPPM_BSDF_BSSRDF)) {
+                // ppm_probabilistic.cc:273-298; reflect probability 0.25 + 0.5 * 0.5
+                const float hx = __double2float_rn(hp[0]), hy = __double2float_rn(hp[1]), hz = __double2float_rn(hp[2]);
+                if (m.type & PPPM_BSDF_REFRACTION) {
+                    const FresnelSplit s = fresnelSplit(d, nrm, dot(nrm, d) < 0.0f);
+                    o[0] = hp[0]; o[1] = hp[1]; o[2] = hp[2];
+                    if (s.total) {
+                        d = s.rdir;
+                        bnc++;
+                    } else if (r1 < 0x80000000u) {  // rands[1] < 0.5: reflect, same bounce count
+                        w = w * refl * (s.Re / 0.5f);
+                        d = s.rdir;
+                    } else {  // transmit: diffuse subsurface radiance
+                        const f3 irr = subsurfaceIrradiance(oct, m.dip, hx, hy, hz, nullptr);
+                        L = L + w * irr * (s.Tr / 0.5f);
+                        alive = false;
+                    }
+                    continue;
+                }
+                const f3 irr = subsurfaceIrradiance(oct, m.dip, hx, hy, hz, nullptr);
+                L = L + w * irr * 0.5f;
+            }
             if (m.type & PPPM_BSDF_LAMBERTIAN) {
                 const f3 on = dot(nrm, d) < 0.0f ? nrm : -nrm;
                 const f3 wq = w * refl * (1.0f / roul);
@@ -397,7 +450,11 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
             w = w * refl * (1.0f / (pdf * roul));
             o[0] = hp[0]; o[1] = hp[1]; o[2] = hp[2];
             d = nd;
+            bnc++;
         }
+        // a compat tape holds 200 numbers (ppm_probabilistic.cc:222); the
+        // reference aborts when a path pops more
+        if (tp.mode == PPPM_MODE_COMPAT && tape.pos > 200) atomicAdd(&ctr->undefinedEye, 1ull);
         if (onImage) {
             accum[3 * pix] += L.x;
             accum[3 * pix + 1] += L.y;
@@ -457,16 +514,23 @@ cudaError_t launchPhotonEmit(const TraceParams& tp, const EnvDev& env, const uin
 cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
                                PathState* out, int64_t maxPaths, float4* deposits, int64_t depositCap,
                                PassCounters* ctr, cudaStream_t st) {
-    kPhotonBounce<<<blocksFor(maxPaths, 128, 152 * 16), 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths, deposits,
-                                                                      depositCap, ctr);
+    if (tp.sssPass)
+        kPhotonBounce<true><<<blocksFor(maxPaths, 128, 152 * 16), 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths,
+                                                                            deposits, depositCap, ctr);
+    else
+        kPhotonBounce<false><<<blocksFor(maxPaths, 128, 152 * 16), 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths,
+                                                                             deposits, depositCap, ctr);
     return cudaGetLastError();
 }
 
 cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
-                           const uint32_t* pixelStates, float* accum, float4* queries, PassCounters* ctr,
-                           cudaStream_t st) {
-    kEyeTrace<<<blocksFor((int64_t)cam.w * cam.h, 128, 152 * 16), 128, 0, st>>>(tp, sc, env, cam, pixelStates, accum,
-                                                                                 queries, ctr);
+                           const OctView& oct, const uint32_t* pixelStates, float* accum, float4* queries,
+                           PassCounters* ctr, cudaStream_t st) {
+    const unsigned blocks = blocksFor((int64_t)cam.w * cam.h, 128, 152 * 16);
+    if (oct.numNodes > 0 || tp.hasSss)
+        kEyeTrace<true><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, ctr);
+    else
+        kEyeTrace<false><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, ctr);
     return cudaGetLastError();
 }
 

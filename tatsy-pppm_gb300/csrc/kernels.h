@@ -32,8 +32,10 @@ cudaError_t launchGatherCanonical(const GridDev& g, QueryView q, float radius, f
 cudaError_t querySortLayout(QuerySortBufs& qs, int64_t maxQueries);
 cudaError_t launchGatherTiled(const GridDev& g, QueryView q, QuerySortBufs& qs, float radius, float* out,
                               bool accumulate, unsigned long long* work, cudaStream_t st);
-// Compat kNN gather (ppm_probabilistic.cc:300-335).
-cudaError_t launchGatherCompat(const GridDev& g, QueryView q, int k, float eps, float radius, int64_t phantoms,
+// Compat kNN gather (ppm_probabilistic.cc:300-335; irradianceWithPM,
+// subsurface_integrator.cc:329-365): k nearest within eps, normal filter
+// |n.(q-p)|/|q-p| < rlim, cone filter, output scaled by the query weight.
+cudaError_t launchGatherCompat(const GridDev& g, QueryView q, int k, float eps, float rlim, int64_t phantoms,
                                float* out, bool accumulate, cudaStream_t st);
 // kNN only (PhotonMap::findKNN): idx in farthest-first order.
 cudaError_t launchKnn(const GridDev& g, const float* queries, int64_t m, int k, float eps, int32_t* idx, int32_t* cnt,

@@ -35,6 +35,14 @@ static_assert(sizeof(QNode) == 128, "QNode must be one 128-byte line");
 // Leaf triangles are 3 float4 (p0,p1,p2); p0.w holds the original id bits.
 __host__ __device__ inline int leafCode(int slot, int count) { return ~((slot << 2) | count); }
 
+// Dipole BSSRDF constants (DipoleBSSRDF ctor, bssrdf.cc:48-63), derived on
+// the host in double and rounded once.
+struct DipoleDev {
+    float sigma_tr[3], alphap[3], zpos[3], zneg[3];
+    float scale;
+    float coeff;  // (1/pi) * (1 - Fdr) (subsurface_integrator.cc:236-237)
+};
+
 struct DevMaterial {
     int type;        // BsdfType bitmask including the BSSRDF bit
     float refl[3];
@@ -48,10 +56,8 @@ struct DevMaterial {
     unsigned long long rrCeil;
     unsigned long long roulFloor;
     float invRr;     // 1 / rr_photon for the flux update
-    // dipole (bssrdf.cc:48-63), derived on the host in double
-    float A, eta, scale, fdr;
-    float sigma_tr[3], alphap[3], zpos[3], zneg[3];
-    float pad[2];
+    float pad0;
+    DipoleDev dip;   // valid when type has the BSSRDF bit
 };
 
 struct EnvDev {
@@ -535,12 +541,43 @@ __device__ inline f3 onHemisphere(f3 w, float r1, float r2) {
     return normalized(u * (ct * z2s) + v * (st * z2s) + w * sqrtf(1.0f - r2));
 }
 
+// checkTotalReflection (reflectance.h:7-34) with the fixed IOR 1.5
+// (common.h:16); the caller decides `into` as its reference code does.
+struct FresnelSplit {
+    f3 rdir, tdir;
+    float Re, Tr;
+    bool total;
+};
+__device__ inline FresnelSplit fresnelSplit(f3 in, f3 normal, bool into) {
+    FresnelSplit s;
+    const f3 on = into ? normal : -normal;
+    s.rdir = reflect(in, normal);
+    const float nnt = into ? (1.0f / 1.5f) : 1.5f;
+    const float ddn = dot(in, on);
+    const float cos2t = 1.0f - nnt * nnt * (1.0f - ddn * ddn);
+    s.total = cos2t < 0.0f;
+    if (s.total) {
+        s.tdir = {0.f, 0.f, 0.f};
+        s.Re = 1.0f;
+        s.Tr = 0.0f;
+        return s;
+    }
+    s.tdir = normalized(in * nnt - normal * (into ? 1.0f : -1.0f) * (ddn * nnt + sqrtf(cos2t)));
+    const float R0 = 0.04f;  // ((1.5-1)/(1.5+1))^2
+    const float c = 1.0f - (into ? -ddn : dot(s.tdir, -on));
+    s.Re = R0 + (1.0f - R0) * (c * c * c * c * c);
+    s.Tr = 1.0f - s.Re;
+    return s;
+}
+
 // BSDF::sample dispatch (brdf.cc:23-142, reflectance.h:7-34). `normal` is
 // whatever the calling reference code passes (oriented in tracePhotons,
-// geometric in radiance). Returns the pdf written by the reference (1.0
-// where it leaves the caller's initial value).
-__device__ inline float bsdfSample(const DevMaterial& m, f3 in, f3 normal, float r1, float r2, f3* out) {
+// geometric in radiance). u1, u2 are the two draws as 32-bit integers
+// (rand = u * 2^-32). Returns the pdf written by the reference (1.0 where it
+// leaves the caller's initial value).
+__device__ inline float bsdfSample(const DevMaterial& m, f3 in, f3 normal, uint32_t u1, uint32_t u2, f3* out) {
     const int t = m.type & 0x0f;
+    const float r1 = u32ToFloat(u1), r2 = u32ToFloat(u2);
     if (t == 0x01) {  // Lambertian
         const f3 on = dot(in, normal) < 0.0f ? normal : -normal;
         *out = onHemisphere(on, r1, r2);
@@ -565,24 +602,14 @@ __device__ inline float bsdfSample(const DevMaterial& m, f3 in, f3 normal, float
         *out = u * (sth * cph) + w * cth + v * (sth * sph);
         return 1.0f;
     }
-    // refraction, IOR 1.5 fixed (common.h:16)
-    bool into = true;
-    f3 on = normal;
-    if (dot(in, normal) >= 0.0f) { into = false; on = -normal; }
-    const f3 rdir = reflect(in, normal);
-    const float nnt = into ? (1.0f / 1.5f) : 1.5f;
-    const float ddn = dot(in, on);
-    const float cos2t = 1.0f - nnt * nnt * (1.0f - ddn * ddn);
-    if (cos2t < 0.0f) { *out = rdir; return 1.0f; }
-    const f3 tdir = normalized(in * nnt - normal * (into ? 1.0f : -1.0f) * (ddn * nnt + sqrtf(cos2t)));
-    const float R0 = 0.04f;  // ((1.5-1)/(1.5+1))^2
-    const float c = 1.0f - (into ? -ddn : dot(tdir, -on));
-    const float Re = R0 + (1.0f - R0) * (c * c * c * c * c);
-    const float Tr = 1.0f - Re;
-    const float p = 0.5f;  // 0.25 + 0.5 * REFLECT_PROBABILITY
-    if (r1 < p) { *out = rdir; return p / Re; }
-    *out = tdir;
-    return (1.0f - p) / Tr;
+    // refraction (brdf.cc:110-142): reflect with probability 0.25 + 0.5 *
+    // REFLECT_PROBABILITY = 0.5, pdf p / Re or (1 - p) / Tr
+    const FresnelSplit s = fresnelSplit(in, normal, !(dot(in, normal) >= 0.0f));
+    if (s.total) { *out = s.rdir; return 1.0f; }
+    const float p = 0.5f;
+    if (u1 < 0x80000000u) { *out = s.rdir; return p / s.Re; }  // rand1 < 0.5, decided on the integer draw
+    *out = s.tdir;
+    return (1.0f - p) / s.Tr;
 }
 
 // Envmap::sampleFromDir (envmap.cc:11-17,47-60), nearest texel.
@@ -605,7 +632,8 @@ __device__ inline f3 envLookup(const EnvDev& e, f3 d) {
 // out of bounds. emitDir: the sampled env direction (photon origin is
 // 50 * emitDir); dir: the first ray direction.
 template <class TapeT>
-__device__ inline bool emitPhoton(const EnvDev& e, TapeT& tp, double numPhotons, f3* emitDir, f3* dir, f3* flux) {
+__device__ inline bool emitPhoton(const EnvDev& e, TapeT& tp, double numPhotons, f3* emitDir, f3* dir, f3* flux,
+                                  bool inOrder = false) {
     const unsigned long long r = tp.popu();
     int lo = 0, hi = 4096;  // first index with cdf[i] >= r * 2^-32
     while (lo < hi) {
@@ -624,12 +652,13 @@ __device__ inline bool emitPhoton(const EnvDev& e, TapeT& tp, double numPhotons,
     const f3 d = {sxz * cp, y, sxz * sp};
     *flux = envLookup(e, d) * __ldg(&e.fluxScale[min(index, 4095)]);
     *emitDir = d;
-    // onHemisphere(normalLight, &nextDir, rseq.pop(), rseq.pop()): the
-    // reference build evaluates these arguments right to left, so the first
-    // number drawn becomes r2 and the second r1.
-    const float r2 = tp.popf();
-    const float r1 = tp.popf();
-    *dir = onHemisphere(-d, r1, r2);
+    // onHemisphere(normalLight, &nextDir, rseq.pop(), rseq.pop()) in
+    // tracePhotons: the reference build evaluates these arguments right to
+    // left, so the first number drawn becomes r2 and the second r1. The
+    // subsurface photon pass draws r1 then r2 in separate statements.
+    const float a0 = tp.popf();
+    const float a1 = tp.popf();
+    *dir = inOrder ? onHemisphere(-d, a0, a1) : onHemisphere(-d, a1, a0);
     (void)numPhotons;
     return index < 4096;
 }

@@ -37,6 +37,9 @@ int fetchPositions(pppm_ctx* c, const float* src, int64_t n, int stride, std::ve
     return PPPM_OK;
 }
 
+// disc filter threshold _radius * _radius * 0.01 (ppm_probabilistic.cc:314)
+float compatDiscLimit(double radius) { return (float)(radius * radius * 0.01); }
+
 double knnCell(const double* mn, const double* mx, int64_t n, int k) {
     const double ex = std::max({mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2], 1e-6});
     const double frac = std::min(1.0, (double)std::max(k, 1) / (double)std::max<int64_t>(n, 1));
@@ -126,8 +129,8 @@ int pppm_gather(pppm_ctx* c, int32_t mode, const float* photons, int64_t n, int6
         PPPM_CUDA(c, launchGatherTiled(gv, qv, c->stageQsort, (float)radius, (float*)dout, false, nullptr, c->stream));
     }
     else
-        PPPM_CUDA(c, launchGatherCompat(gv, qv, k, (float)gatherPhotons, (float)radius, phantoms, (float*)dout, false,
-                                        c->stream));
+        PPPM_CUDA(c, launchGatherCompat(gv, qv, k, (float)gatherPhotons, compatDiscLimit(radius), phantoms,
+                                        (float*)dout, false, c->stream));
     if ((r = finishOut(c, out, dout, (size_t)m * 12))) return r;
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
     return PPPM_OK;
@@ -139,7 +142,6 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     // The default Scene env map has no importance tables (scene.cc:11-12):
     // photon emission would read an empty CDF.
     if (!c->hasEnv) return fail(c, PPPM_E_STATE, "render_begin: no env map (the only light of the reference)");
-    if (c->anyBssrdf) return fail(c, PPPM_E_STATE, "render_begin: BSSRDF materials need pppm_subsurface_* first");
     if (par->mode != PPPM_MODE_COMPAT && par->mode != PPPM_MODE_CANONICAL)
         return fail(c, PPPM_E_ARG, "render_begin: unknown mode");
     if (par->num_streams < 1 || par->num_streams > 4096 || par->photons < 1 || cam->width < 1 || cam->height < 1 ||
@@ -181,6 +183,10 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
         const int e = envFluxScale(c, (double)par->photons);
         if (e) return e;
     }
+    {
+        const int e = sssBegin(c);
+        if (e) return e;
+    }
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
     rs.passesDone = 0;
     rs.storedLast = 0;
@@ -217,6 +223,8 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     tp.seed = par.seed;
     tp.pass = t;
     tp.countTraversal = (par.flags & PPPM_FLAG_COUNT_TRAVERSAL) ? 1 : 0;
+    tp.sssPass = 0;
+    tp.hasSss = rs.sss.enabled ? 1 : 0;
     int64_t launches = 0;
 
     CameraDev cd;
@@ -244,6 +252,12 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     uint32_t* pixelStates = compat ? photonStates + 4 * paths : nullptr;
 
     PPPM_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
+    if (rs.sss.enabled) {
+        // SubsurfaceIntegrator::initialize before tracePhotons (ppm_probabilistic.cc:83-88)
+        const int e = sssPrepare(c, t, tp, sv, ev, &launches);
+        if (e) return e;
+    }
+    PPPM_CUDA(c, cudaEventRecord(c->ev[7], c->stream));
     if (compat) {
         std::vector<uint32_t> ss((size_t)N * 4);
         for (int s = 0; s < N; s++) std::memcpy(&ss[4 * s], rs.streams[s].s, 16);
@@ -266,6 +280,11 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
                                             c->stream));
         }
         PPPM_CUDA(c, cudaEventRecord(c->ev[6], c->stream));
+        if (attempt == 0 && rs.sss.enabled) {
+            // octree on the host while the GPU traces this pass's photons
+            const int e = sssFinish(c);
+            if (e) return e;
+        }
         PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
         PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
         if ((int64_t)hc.deposits <= rs.depositCap) break;
@@ -312,12 +331,12 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     PPPM_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
 
     // eye paths and gather
-    PPPM_CUDA(c, launchEyeTrace(tp, sv, ev, cd, pixelStates, rs.accum.as<float>(), rs.queries.as<float4>(), ctr,
-                                c->stream));
+    PPPM_CUDA(c, launchEyeTrace(tp, sv, ev, cd, sssView(c), pixelStates, rs.accum.as<float>(),
+                                rs.queries.as<float4>(), ctr, c->stream));
     PPPM_CUDA(c, cudaEventRecord(c->ev[3], c->stream));
     QueryView qv{rs.queries.as<float4>(), reinterpret_cast<const uint32_t*>(&ctr->queries), pixels};
     if (compat)
-        PPPM_CUDA(c, launchGatherCompat(gv, qv, k, (float)par.gather_photons, (float)rs.radius, phantoms,
+        PPPM_CUDA(c, launchGatherCompat(gv, qv, k, (float)par.gather_photons, compatDiscLimit(rs.radius), phantoms,
                                         rs.accum.as<float>(), true, c->stream));
     else
         PPPM_CUDA(c, launchGatherTiled(gv, qv, rs.qsort, (float)rs.radius, rs.accum.as<float>(), true,
@@ -338,8 +357,13 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         stats->gather_queries = (int64_t)hc.queries;
         stats->radius = rs.radius;
         float ms;
-        cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&ms, c->ev[7], c->ev[1]);
         stats->ms_photon = ms;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[7]);
+        stats->ms_subsurface = rs.sss.enabled ? ms : 0.0;
+        stats->ms_subsurface_host = rs.sss.enabled ? rs.sss.msHost : 0.0;
+        stats->sss_points = rs.sss.enabled ? (int64_t)rs.sss.pts.size() / 3 : 0;
+        stats->sss_photons = rs.sss.enabled ? rs.sss.stored : 0;
         cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
         stats->ms_grid = ms;
         cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
@@ -360,6 +384,10 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     }
     if (hc.undefinedEmit)
         return fail(c, PPPM_E_UNDEFINED, "render_pass: a photon draw fell past the env CDF (reference reads _pdf out of bounds)");
+    if (hc.undefinedEye)
+        return fail(c, compat ? PPPM_E_UNDEFINED : PPPM_E_CAPACITY,
+                    compat ? "render_pass: an eye path drew more than its 200 random numbers (the reference aborts)"
+                           : "render_pass: an eye path exceeded 4096 segments");
 
     // radius update (ppm_probabilistic.cc:94 in compat; Knaus-Zwicker
     // r^2_{t+1} = r^2_t (t + alpha) / (t + 1) in canonical mode)

@@ -1,0 +1,312 @@
+// Subsurface stage of the render: SubsurfaceIntegrator::initialize
+// (subsurface_integrator.cc:180-210), run before every pass's photon pass
+// (ppm_probabilistic.cc:83-85), and its stage entry points.
+//
+//   1. subsurface photon map: the photon pass of buildPhotonMap
+//      (subsurface_integrator.cc:240-327) on the wavefront kernels, with the
+//      reference's per-pass streams XorShift(time + i);
+//   2. Poisson-disc points on the BSSRDF triangles (host, sequential dart
+//      throwing exactly as sampler::poissonDisk) while the GPU traces 1;
+//   3. irradiance at the points: irradianceWithPM (subsurface_integrator.cc:
+//      329-365), the compat kNN gather with k = (int)gatherRadius,
+//      epsilon = #photons and the normal filter gatherPhotons^2 * 0.01;
+//   4. octree over the points (host, constructRec's splits) while the GPU
+//      traces the pass's main photons; uploaded before the eye pass.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "context.h"
+#include "host_build.h"
+#include "trace.h"
+
+namespace pppm {
+
+namespace {
+
+constexpr double kPiD = 3.14159265358979323846;  // 4 atan(1) (common.h:14)
+constexpr int kSssBounceLimit = 64;             // buildPhotonMap(scene, photons, 64)
+
+double msSince(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// Poisson points -> gather queries (pos | index, normal, unit weight).
+void packPointQueries(const std::vector<float>& p, const std::vector<float>& n, std::vector<float4>* q) {
+    const size_t m = p.size() / 3;
+    q->resize(3 * m);
+    for (size_t i = 0; i < m; i++) {
+        const int id = (int)i;
+        float idBits;
+        std::memcpy(&idBits, &id, 4);
+        (*q)[3 * i] = make_float4(p[3 * i], p[3 * i + 1], p[3 * i + 2], idBits);
+        (*q)[3 * i + 1] = make_float4(n[3 * i], n[3 * i + 1], n[3 * i + 2], 0.0f);
+        (*q)[3 * i + 2] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    }
+}
+
+double sssCell(const pppm_ctx* c, int k, int64_t stored) {
+    const double area = c->bssrdfArea > 0.0 ? c->bssrdfArea : 1.0;
+    const double f = c->rs.par.cell_factor >= 1.0f ? c->rs.par.cell_factor : 1.0;
+    return f * std::sqrt(area * (double)std::max(k, 1) / (double)std::max<int64_t>(stored, 1));
+}
+
+}  // namespace
+
+int sssBegin(pppm_ctx* c) {
+    SssState& s = c->rs.sss;
+    s.enabled = c->anyBssrdf && !c->bssrdfTris.empty();
+    s.octNodes = 0;
+    if (!s.enabled) return PPPM_OK;
+    // ppm_probabilistic.cc:35-46: the BSSRDF area is averaged over ALL triangles
+    const double avgArea = c->bssrdfArea / (double)c->ntri;
+    s.areaRadius = std::sqrt(avgArea) * 1.0;
+    s.dA = (0.5 * s.areaRadius) * (0.5 * s.areaRadius) * kPiD;
+    s.k = (int)c->rs.par.gather_radius;
+    if (s.k < 1)
+        return fail(c, PPPM_E_UNDEFINED,
+                    "render_begin: subsurface kNN count (int)gather_radius < 1 pops an empty queue in the reference");
+    if (s.k > kMaxKnn) return fail(c, PPPM_E_CAPACITY, "render_begin: subsurface kNN count (int)gather_radius above 64");
+    if (!(s.areaRadius > 0.0)) return fail(c, PPPM_E_UNDEFINED, "render_begin: BSSRDF triangles have zero area");
+    return PPPM_OK;
+}
+
+int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv, const EnvDev& ev, int64_t* launches) {
+    SssState& s = c->rs.sss;
+    RenderState& rs = c->rs;
+    const pppm_params& par = rs.par;
+    const bool compat = par.mode == PPPM_MODE_COMPAT;
+    const int N = par.num_streams;
+    const int64_t paths = base.numPaths;
+
+    TraceParams tp = base;
+    tp.sssPass = 1;
+    tp.maxBouncePhoton = kSssBounceLimit;
+    // canonical mode: an independent counter-based key for this photon set
+    tp.seed = base.seed ^ 0x5bd1e995u;
+    uint32_t* photonStates = compat ? rs.tapeStates.as<uint32_t>() : nullptr;
+    if (compat) {
+        // Random::generateSampler((unsigned long)time(NULL) + i) per thread
+        // (subsurface_integrator.cc:246-249); time is par.sss_time + t - 1
+        std::vector<uint32_t> ss((size_t)N * 4);
+        for (int i = 0; i < N; i++) {
+            XorShift x;
+            x.seed((uint32_t)((unsigned long)(par.sss_time + (uint32_t)(t - 1)) + (unsigned long)i));
+            std::memcpy(&ss[4 * (size_t)i], x.s, 16);
+        }
+        PPPM_CUDA(c, cudaMemcpyAsync(rs.streamStatesD.p, ss.data(), ss.size() * 4, cudaMemcpyHostToDevice, c->stream));
+        PPPM_CUDA(c, launchTapeStates(tp, rs.streamStatesD.as<uint32_t>(), rs.jumpMats.as<uint32_t>(), 0, 0,
+                                      photonStates, nullptr, c->stream));
+        *launches += 1;
+    }
+    PassCounters* ctr = rs.photonCount.as<PassCounters>();
+    if (s.cap == 0) s.cap = std::max<int64_t>(paths, 1 << 16);
+    PPPM_CUDA(c, s.photons.ensure((size_t)s.cap * 32));
+
+    // the photon pass is enqueued first; the host samples the points meanwhile
+    PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
+    PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
+    for (int b = 0; b < kSssBounceLimit; b++) {
+        PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
+        PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
+        PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, s.photons.as<float4>(), s.cap, ctr, c->stream));
+    }
+    *launches += 1 + kSssBounceLimit;
+
+    const auto t0 = std::chrono::steady_clock::now();
+    poissonDisk(c->hostTri.data(), c->bssrdfTris, s.areaRadius, c->poissonRng, &s.pts, &s.nrm);
+    packPointQueries(s.pts, s.nrm, &s.query);
+    s.msHost = msSince(t0);
+    const int64_t m = (int64_t)s.pts.size() / 3;
+
+    // (a pageable readback blocks until the stream drains: issued after the sampling)
+    PassCounters hc;
+    PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (hc.undefinedEmit)
+        return fail(c, PPPM_E_UNDEFINED,
+                    "render_pass: a subsurface photon draw fell past the env CDF (reference reads _pdf out of bounds)");
+    if ((int64_t)hc.deposits > s.cap) {
+        // grow and trace the same photons again (tapes and keys are unchanged)
+        s.cap = (int64_t)(hc.deposits * 1.25) + 1024;
+        PPPM_CUDA(c, s.photons.ensure((size_t)s.cap * 32));
+        PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
+        PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
+        for (int b = 0; b < kSssBounceLimit; b++) {
+            PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
+            PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
+            PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, s.photons.as<float4>(), s.cap, ctr, c->stream));
+        }
+        *launches += 1 + kSssBounceLimit;
+        PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
+        PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+        if ((int64_t)hc.deposits > s.cap) return fail(c, PPPM_E_CAPACITY, "render_pass: subsurface photon overflow");
+    }
+    s.stored = (int64_t)hc.deposits;
+
+    // irradiance at the points
+    PPPM_CUDA(c, s.irad.ensure((size_t)std::max<int64_t>(m, 1) * 12));
+    if (m > 0) {
+        PPPM_CUDA(c, s.points.ensure((size_t)m * 48));
+        PPPM_CUDA(c, cudaMemcpyAsync(s.points.p, s.query.data(), (size_t)m * 48, cudaMemcpyHostToDevice, c->stream));
+        if (s.stored == 0) {
+            // empty photon map: findKNN returns nothing, maxdist stays 0
+            PPPM_CUDA(c, cudaMemsetAsync(s.irad.p, 0, (size_t)m * 12, c->stream));
+        } else {
+            PPPM_CUDA(c, gridLayout(s.grid, c->bbmin, c->bbmax, sssCell(c, s.k, s.stored), s.stored));
+            GridDev gv = gridView(s.grid, c->bbmin, c->bbmax);
+            PPPM_CUDA(c, gridBuild(s.grid, gv, s.photons.as<float4>(), reinterpret_cast<const uint64_t*>(&ctr->deposits),
+                                   s.cap, c->stream));
+            gv = gridView(s.grid, c->bbmin, c->bbmax);
+            QueryView qv{s.points.as<float4>(), nullptr, m};
+            const int gp = par.gather_photons;
+            const float rlim = (float)((double)gp * (double)gp * 0.01);  // subsurface_integrator.cc:343
+            PPPM_CUDA(c, launchGatherCompat(gv, qv, s.k, (float)par.photons, rlim, 0, s.irad.as<float>(), false,
+                                            c->stream));
+            *launches += 6;
+        }
+    }
+    PPPM_CUDA(c, cudaEventRecord(s.done, c->stream));
+    return PPPM_OK;
+}
+
+int sssFinish(pppm_ctx* c) {
+    SssState& s = c->rs.sss;
+    const int64_t m = (int64_t)s.pts.size() / 3;
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<HostOctNode> nodes;
+    if (m > 0) {
+        PPPM_CUDA(c, s.iradHost.ensure((size_t)m * 12));
+        PPPM_CUDA(c, cudaStreamWaitEvent(c->aux, s.done, 0));
+        PPPM_CUDA(c, cudaMemcpyAsync(s.iradHost.p, s.irad.p, (size_t)m * 12, cudaMemcpyDeviceToHost, c->aux));
+        PPPM_CUDA(c, cudaStreamSynchronize(c->aux));
+        // IrradiancePoint {pos, normal, dA, irad} (subsurface_integrator.cc:224-230)
+        std::vector<double> ip((size_t)m * 10);
+        const float* irad = s.iradHost.as<float>();
+        for (int64_t i = 0; i < m; i++) {
+            double* q = &ip[(size_t)i * 10];
+            for (int d = 0; d < 3; d++) {
+                q[d] = s.pts[3 * i + d];
+                q[3 + d] = s.nrm[3 * i + d];
+                q[7 + d] = irad[3 * i + d];
+            }
+            q[6] = s.dA;
+        }
+        std::string err;
+        if (!buildOctree(ip.data(), m, &nodes, &err)) return fail(c, PPPM_E_UNDEFINED, "render_pass: " + err);
+    }
+    s.octNodes = (int)nodes.size();
+    if (!nodes.empty()) {
+        PPPM_CUDA(c, s.octree.ensure(nodes.size() * sizeof(OctNodeDev)));
+        PPPM_CUDA(c, cudaMemcpyAsync(s.octree.p, nodes.data(), nodes.size() * sizeof(OctNodeDev), cudaMemcpyHostToDevice,
+                                     c->stream));
+        // the pageable source is consumed before the call returns
+    }
+    s.msHost += msSince(t0);
+    return PPPM_OK;
+}
+
+OctView sssView(const pppm_ctx* c) {
+    const SssState& s = c->rs.sss;
+    return {s.octNodes > 0 ? s.octree.as<OctNodeDev>() : nullptr, s.octNodes, 0.05f};
+}
+
+}  // namespace pppm
+
+using namespace pppm;
+
+extern "C" {
+
+int pppm_poisson_disk(const float* tri_xyz, int64_t ntri, double min_dist, uint32_t* rng_state, float* pts,
+                      float* nrm, int64_t cap, int64_t* count) {
+    if (ntri < 0 || (ntri > 0 && !tri_xyz) || !rng_state || !count || cap < 0 || (cap > 0 && (!pts || !nrm)) ||
+        !(min_dist > 0.0))
+        return PPPM_E_ARG;
+    std::vector<int64_t> tris((size_t)ntri);
+    for (int64_t i = 0; i < ntri; i++) tris[i] = i;
+    std::vector<float> p, n;
+    poissonDisk(tri_xyz, tris, min_dist, rng_state, &p, &n);
+    const int64_t m = (int64_t)p.size() / 3;
+    *count = m;
+    const int64_t w = std::min(m, cap);
+    if (w > 0) {
+        std::memcpy(pts, p.data(), (size_t)w * 12);
+        std::memcpy(nrm, n.data(), (size_t)w * 12);
+    }
+    return PPPM_OK;
+}
+
+}  // extern "C"
+
+extern "C" int pppm_subsurface_photon_irradiance(pppm_ctx* c, const float* photons, int64_t n, const float* points,
+                                                 int64_t m, int64_t num_photons, double gather_radius,
+                                                 int32_t gather_photons, float* out) {
+    if (!c || n < 0 || m < 0 || (n > 0 && !photons) || (m > 0 && (!points || !out)))
+        return fail(c, PPPM_E_ARG, "subsurface_photon_irradiance: bad arguments");
+    // findKNN(query, &photons, params.photons(), params.gatherRadius()):
+    // epsilon = #photons, k = (int)gatherRadius (kdtree.h:17, photon_map.cc:25)
+    const int k = (int)gather_radius;
+    if (k < 1) return fail(c, PPPM_E_UNDEFINED, "subsurface_photon_irradiance: k = (int)gather_radius < 1");
+    if (k > kMaxKnn) return fail(c, PPPM_E_CAPACITY, "subsurface_photon_irradiance: k above 64");
+    if (m == 0) return PPPM_OK;
+    cudaSetDevice(c->device);
+    std::vector<float> ph((size_t)n * 8), pq((size_t)m * 6);
+    if (n > 0) {
+        if (isDevicePtr(photons)) PPPM_CUDA(c, cudaMemcpy(ph.data(), photons, ph.size() * 4, cudaMemcpyDeviceToHost));
+        else std::memcpy(ph.data(), photons, ph.size() * 4);
+    }
+    if (isDevicePtr(points)) PPPM_CUDA(c, cudaMemcpy(pq.data(), points, pq.size() * 4, cudaMemcpyDeviceToHost));
+    else std::memcpy(pq.data(), points, pq.size() * 4);
+    double mn[3] = {1e30, 1e30, 1e30}, mx[3] = {-1e30, -1e30, -1e30};
+    for (int64_t i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) {
+            mn[d] = std::min(mn[d], (double)ph[8 * i + d]);
+            mx[d] = std::max(mx[d], (double)ph[8 * i + d]);
+        }
+    if (n == 0)
+        for (int d = 0; d < 3; d++) { mn[d] = 0.0; mx[d] = 1.0; }
+    std::vector<float4> rec((size_t)std::max<int64_t>(n, 1) * 2);
+    for (int64_t i = 0; i < n; i++) {
+        const float* p = &ph[8 * i];
+        const int id = (int)i;
+        float idBits;
+        std::memcpy(&idBits, &id, 4);
+        rec[2 * i] = make_float4(p[0], p[1], p[2], 0.0f);
+        rec[2 * i + 1] = make_float4(p[3], p[4], p[5], idBits);
+    }
+    std::vector<float> pts((size_t)m * 3), nrm((size_t)m * 3);
+    for (int64_t i = 0; i < m; i++)
+        for (int d = 0; d < 3; d++) {
+            pts[3 * i + d] = pq[6 * i + d];
+            nrm[3 * i + d] = pq[6 * i + 3 + d];
+        }
+    std::vector<float4> q;
+    packPointQueries(pts, nrm, &q);
+    PPPM_CUDA(c, c->stageRec.ensure(rec.size() * 16));
+    PPPM_CUDA(c, c->stageQ.ensure(q.size() * 16));
+    PPPM_CUDA(c, c->stageCount.ensure(64));
+    PPPM_CUDA(c, cudaMemcpyAsync(c->stageRec.p, rec.data(), rec.size() * 16, cudaMemcpyHostToDevice, c->stream));
+    PPPM_CUDA(c, cudaMemcpyAsync(c->stageQ.p, q.data(), q.size() * 16, cudaMemcpyHostToDevice, c->stream));
+    const uint64_t cnt = (uint64_t)n;
+    PPPM_CUDA(c, cudaMemcpyAsync(c->stageCount.p, &cnt, 8, cudaMemcpyHostToDevice, c->stream));
+    void* dout;
+    int r;
+    if ((r = stageOut(c, out, (size_t)m * 12, 2, &dout))) return r;
+    if (n == 0) {
+        PPPM_CUDA(c, cudaMemsetAsync(dout, 0, (size_t)m * 12, c->stream));
+    } else {
+        const double ex = std::max({mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2], 1e-6});
+        const double cell = ex * std::cbrt(std::min(1.0, (double)k / (double)n));
+        PPPM_CUDA(c, gridLayout(c->stageGrid, mn, mx, cell, n));
+        GridDev gv = gridView(c->stageGrid, mn, mx);
+        PPPM_CUDA(c, gridBuild(c->stageGrid, gv, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), n, c->stream));
+        gv = gridView(c->stageGrid, mn, mx);
+        QueryView qv{c->stageQ.as<float4>(), nullptr, m};
+        const float rlim = (float)((double)gather_photons * (double)gather_photons * 0.01);
+        PPPM_CUDA(c, launchGatherCompat(gv, qv, k, (float)num_photons, rlim, 0, (float*)dout, false, c->stream));
+    }
+    if ((r = finishOut(c, out, dout, (size_t)m * 12))) return r;
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PPPM_OK;
+}

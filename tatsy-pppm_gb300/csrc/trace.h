@@ -1,6 +1,7 @@
 // Wavefront photon tracing, eye paths and RNG tapes.
 #pragma once
 
+#include "dipole.cuh"
 #include "kernels.h"
 
 namespace pppm {
@@ -27,6 +28,7 @@ struct PassCounters {
     unsigned long long undefinedEmit; // CDF inversion past the last entry (reference reads out of bounds)
     unsigned long long nodeVisits[2]; // [photon, eye] BVH nodes visited (counting flag)
     unsigned long long triTests[2];   // [photon, eye] triangles tested (counting flag)
+    unsigned long long undefinedEye;  // eye paths past their 200-number tape (compat) or the segment cap
 };
 
 struct CameraDev {
@@ -49,6 +51,8 @@ struct TraceParams {
     uint32_t seed;
     int pass;
     int countTraversal;
+    int sssPass;  // 1: the subsurface photon pass (buildPhotonMap semantics)
+    int hasSss;   // 1: the scene has BSSRDF materials
 };
 
 // Jump-ahead matrices: J[k] advances a XorShift state by 200 * 2^k draws
@@ -66,8 +70,15 @@ cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int b
                                PathState* out, int64_t maxPaths, float4* deposits, int64_t depositCap,
                                PassCounters* ctr, cudaStream_t st);
 cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
-                           const uint32_t* pixelStates, float* accum, float4* queries, PassCounters* ctr,
-                           cudaStream_t st);
+                           const OctView& oct, const uint32_t* pixelStates, float* accum, float4* queries,
+                           PassCounters* ctr, cudaStream_t st);
+// Subsurface stage of a render (sss.cu): per-render setup, the per-pass
+// photon map + points + irradiance (enqueued), and the octree upload.
+int sssBegin(pppm_ctx* c);
+int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv, const EnvDev& ev, int64_t* launches);
+int sssFinish(pppm_ctx* c);
+OctView sssView(const pppm_ctx* c);
+
 cudaError_t launchStreamCounts(const float4* deposits, const unsigned long long* count, int64_t cap, int64_t tpt,
                                int numStreams, unsigned long long* perStream, cudaStream_t st);
 

@@ -40,7 +40,7 @@ class Params(ctypes.Structure):
                 ("gather_photons", ctypes.c_int32), ("max_bounce_photon", ctypes.c_int32),
                 ("max_bounce_eye", ctypes.c_int32), ("seed", ctypes.c_uint32), ("gather_radius", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("radius_scale", ctypes.c_double), ("cell_factor", ctypes.c_float),
-                ("flags", ctypes.c_int32)]
+                ("flags", ctypes.c_int32), ("sss_time", ctypes.c_uint32)]
 
 
 class PassStats(ctypes.Structure):
@@ -51,7 +51,8 @@ class PassStats(ctypes.Structure):
                 ("ms_bounce", ctypes.c_double), ("kernel_launches", ctypes.c_int64), ("node_visits", ctypes.c_int64),
                 ("tri_tests", ctypes.c_int64), ("photon_node_visits", ctypes.c_int64),
                 ("photon_tri_tests", ctypes.c_int64), ("gather_pairs", ctypes.c_int64),
-                ("gather_inside", ctypes.c_int64)]
+                ("gather_inside", ctypes.c_int64), ("sss_points", ctypes.c_int64), ("sss_photons", ctypes.c_int64),
+                ("ms_subsurface", ctypes.c_double), ("ms_subsurface_host", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -78,6 +79,9 @@ SIGNATURES = {
     "pppm_dipole_rd": ([_VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_dipole_irradiance": ([_VP, _VP, _VP, ctypes.c_int64, ctypes.c_double, _VP, ctypes.c_int64, _VP],
                                ctypes.c_int),
+    "pppm_poisson_disk": ([_VP, ctypes.c_int64, ctypes.c_double, _VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_subsurface_photon_irradiance": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int64,
+                                           ctypes.c_double, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_knn_noalloc": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
                           ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_gather": ([_VP, ctypes.c_int32, _VP, ctypes.c_int64, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_double,
@@ -240,6 +244,15 @@ class Context:
                                          float(radius), int(gather_photons), _ptr(out)))
         return out
 
+    def subsurface_photon_irradiance(self, photons8, points6, num_photons, gather_radius, gather_photons):
+        ph = np.ascontiguousarray(photons8, np.float32).reshape(-1, 8)
+        pt = np.ascontiguousarray(points6, np.float32).reshape(-1, 6)
+        out = np.zeros((pt.shape[0], 3), np.float32)
+        self._check(self.lib.pppm_subsurface_photon_irradiance(self.h, ph.ctypes.data, ph.shape[0], pt.ctypes.data,
+                                                               pt.shape[0], int(num_photons), float(gather_radius),
+                                                               int(gather_photons), out.ctypes.data))
+        return out
+
     def dipole_rd(self, mat, d2):
         d2 = np.ascontiguousarray(d2, np.float32)
         m = np.ascontiguousarray(mat)
@@ -270,7 +283,7 @@ class Context:
     @staticmethod
     def make_params(mode=MODE_COMPAT, photons=200_000, num_streams=8, gather_photons=128, gather_radius=16.0,
                     alpha=0.7, radius_scale=0.1, max_bounce_photon=64, max_bounce_eye=64, seed=1, cell_factor=1.0,
-                    flags=0):
+                    flags=0, sss_time=0):
         p = Params()
         p.mode = mode
         p.num_streams = num_streams
@@ -284,6 +297,7 @@ class Context:
         p.radius_scale = radius_scale
         p.cell_factor = cell_factor
         p.flags = flags
+        p.sss_time = sss_time
         return p
 
     def render_begin(self, cam, params):
@@ -316,6 +330,41 @@ def knn_noalloc(photon_pos, queries, num_target_photons, target_radius, idx, cnt
     return lib.pppm_knn_noalloc(_ptr(photon_pos), int(photon_pos.shape[0]), _ptr(queries), int(queries.shape[0]),
                                 int(num_target_photons), float(target_radius), _ptr(idx), _ptr(cnt),
                                 int(idx.shape[1]), stream)
+
+
+def poisson_disk(tri_xyz, min_dist, rng_state=None):
+    """pppm_poisson_disk (sampler::poissonDisk) on a triangle soup. rng_state:
+    4 uint32 XorShift words advanced in place (default: XorShift(0), the
+    reference's static sampler RNG at program start). Returns (points,
+    normals, rng_state)."""
+    lib = load()
+    tri = np.ascontiguousarray(tri_xyz, np.float32).reshape(-1, 9)
+    if rng_state is None:
+        rng_state = xorshift_state(0)
+    st = np.ascontiguousarray(rng_state, np.uint32).copy()
+    # at most one point per candidate: ceil(4 A / d^2) per triangle (sampler.cc:44)
+    t64 = tri.astype(np.float64).reshape(-1, 3, 3)
+    area = 0.5 * np.linalg.norm(np.cross(t64[:, 1] - t64[:, 0], t64[:, 2] - t64[:, 1]), axis=1)
+    cap = int(np.ceil(4.0 * area / (min_dist * min_dist)).sum()) + tri.shape[0] + 16
+    pts = np.zeros((cap, 3), np.float32)
+    nrm = np.zeros((cap, 3), np.float32)
+    n = ctypes.c_int64()
+    r = lib.pppm_poisson_disk(tri.ctypes.data, tri.shape[0], float(min_dist), st.ctypes.data, pts.ctypes.data,
+                              nrm.ctypes.data, cap, ctypes.byref(n))
+    if r != OK:
+        raise PppmError(r, "poisson_disk: bad arguments")
+    assert n.value <= cap
+    return pts[: n.value], nrm[: n.value], st
+
+
+def xorshift_state(seed):
+    """The four state words of the reference's XorShift(seed) (random.h:23-31)."""
+    s = int(seed) & 0xFFFFFFFF
+    out = []
+    for i in range(1, 5):
+        s = (1812433253 * (s ^ (s >> 30)) + i) & 0xFFFFFFFF
+        out.append(s)
+    return np.array(out, np.uint32)
 
 
 def hdr_decode(data: bytes):

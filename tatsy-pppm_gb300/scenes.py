@@ -17,7 +17,7 @@ import math
 
 import numpy as np
 
-# pppm_material (include/pppm_c.h), 64 bytes.
+# pppm_material (include/pppm_c.h), 56 bytes.
 MATERIAL_DTYPE = np.dtype(
     [
         ("type", "<i4"),
@@ -330,6 +330,41 @@ def small_test_scene(seed=3, subdiv=3, width=64, height=48, photons=20_000):
     cam = look_camera((0.0, 4.0, -30.0), (0.0, -1.0, 0.0), 0.8, width, height)
     return _assemble("small", [(gnd, 0), (s1, 1), (s2, 2), (s3, 3), (s4, 4)], mats, env, cam, photons=photons,
                      passes=4, max_depth=64)
+
+
+def config3(seed=3, width=1280, height=720, photons=2_000_000, passes=32, nu=500, nv=200, env_w=1024, env_h=512):
+    """Subsurface scattering: a noise-displaced torus of 2*nu*nv triangles
+    (500 x 200 -> 200,000) with a refractive surface and a dipole BSSRDF
+    (sigma_a ~ U[0.001, 0.05], sigma_s' ~ U[0.5, 3.0] per mm, eta 1.3; scene
+    units are mm) on a Lambertian ground, sky-lit."""
+    rng = np.random.default_rng(seed)
+    tor = torus(10.0, 4.0, nu, nv, 0.05, seed, center=(0.0, 0.0, 0.0))
+    gnd = ground(-4.5, 30.0)
+    sa = rng.uniform(0.001, 0.05, 3)
+    ss = rng.uniform(0.5, 3.0, 3)
+    mats = [material(LAMBERTIAN, (0.7, 0.7, 0.7)),
+            material(REFRACTION, (0.99, 0.99, 0.99), sigma_a=sa, sigmap_s=ss, eta=1.3, scale=1.0, bssrdf=True)]
+    env = sky_env(env_w, env_h, seed, sun_peak=2.0e3, sun_deg=2.0)
+    cam = look_camera((0.0, 14.0, -30.0), (0.0, -1.0, 0.0), 0.75, width, height)
+    return _assemble("config3", [(gnd, 0), (tor, 1)], mats, env, cam, photons=photons, passes=passes, max_depth=12)
+
+
+def small_sss_scene(seed=5, width=64, height=48, photons=20_000, nu=48, nv=24):
+    """Small subsurface scene for parity tests: a refractive BSSRDF torus, a
+    Lambertian BSSRDF sphere and a Lambertian ground."""
+    rng = np.random.default_rng(seed)
+    gnd = ground(-6.0, 20.0)
+    tor = torus(6.0, 2.5, nu, nv, 0.05, seed, center=(-3.0, -3.0, 0.0))
+    sph = displace_sphere(geodesic_sphere(6), 2.5, 0.05, seed + 1, center=(6.0, -3.5, -2.0))
+    mats = [material(LAMBERTIAN, (0.75, 0.7, 0.6)),
+            material(REFRACTION, (0.99, 0.99, 0.99), sigma_a=rng.uniform(0.001, 0.05, 3),
+                     sigmap_s=rng.uniform(0.5, 3.0, 3), eta=1.3, scale=1.0, bssrdf=True),
+            material(LAMBERTIAN, rng.uniform(0.3, 0.8, 3), sigma_a=rng.uniform(0.001, 0.05, 3),
+                     sigmap_s=rng.uniform(0.5, 3.0, 3), eta=1.3, scale=1.0, bssrdf=True)]
+    env = sky_env(128, 64, seed, sun_peak=200.0, sun_deg=6.0)
+    cam = look_camera((0.0, 6.0, -28.0), (0.0, -2.0, 0.0), 0.8, width, height)
+    return _assemble("small_sss", [(gnd, 0), (tor, 1), (sph, 2)], mats, env, cam, photons=photons, passes=4,
+                     max_depth=64)
 
 
 # --------------------------------------------------------------------- files

@@ -279,11 +279,88 @@ def gen_dipole():
     save("dipole", **out)
 
 
-GENERATORS.update({"knn": gen_knn, "gather": gen_gather, "render": gen_render, "dipole": gen_dipole})
+def _sss_min_dist(sc):
+    """areaRadius of render(): sqrt(sum of BSSRDF Triangle::area / all
+    triangles) (ppm_probabilistic.cc:35-46)."""
+    t = sc.tris.reshape(-1, 3, 3).astype(np.float64)
+    area = 0.5 * np.linalg.norm(np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 1]), axis=1)
+    bss = sc.mats["has_bssrdf"][sc.mat_id] != 0
+    return float(np.sqrt(area[bss].sum() / len(t))), bss
+
+
+def gen_poisson():
+    """sampler::poissonDisk twice in a fresh process: the candidate draws come
+    from a process-wide XorShift seeded 0, so the second call continues the
+    first one's stream."""
+    sc = S.small_sss_scene()
+    d, bss = _sss_min_dist(sc)
+    tris = sc.tris[bss]
+    tor = tris[sc.mat_id[bss] == 1]
+    sph = tris[sc.mat_id[bss] == 2]
+    p1, n1 = rh.poisson_disk(tor, d)
+    p2, n2 = rh.poisson_disk(sph, 0.7 * d)
+    save("poisson", tor=tor, sph=sph, min_dist=np.array([d, 0.7 * d]), pts1=p1, nrm1=n1, pts2=p2, nrm2=n2)
+
+
+def gen_sss_irradiance():
+    """SubsurfaceIntegrator::irradianceWithPM over injected photon maps for
+    three parameter sets: the reference driver's (photons 2e6, gatherPhotons
+    128, gatherRadius 16: normal filter always true) and two with an active
+    normal filter and other k."""
+    rng = np.random.default_rng(43)
+    sph = S.displace_sphere(S.geodesic_sphere(16), 5.0, 0.05, 7)
+    n = 40000
+    pick = rng.integers(0, len(sph), n)
+    u = rng.uniform(size=(n, 2))
+    flip = u.sum(1) > 1
+    u[flip] = 1 - u[flip]
+    t = sph[pick]
+    pos = t[:, 0] + u[:, :1] * (t[:, 1] - t[:, 0]) + u[:, 1:] * (t[:, 2] - t[:, 0])
+    flux = rng.lognormal(0.0, 0.7, (n, 3)) * 1e-3
+    photons = np.concatenate([pos, flux, np.zeros((n, 2))], 1).astype(np.float32).astype(np.float64)
+    cent = sph.mean(1)
+    nrm = np.cross(sph[:, 1] - sph[:, 0], sph[:, 2] - sph[:, 0])
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    q = rng.integers(0, len(sph), 4000)
+    points = np.concatenate([cent[q], nrm[q]], 1).astype(np.float32).astype(np.float64)
+    sets = [(2_000_000, 128, 16.0), (100_000, 8, 8.0), (50_000, 5, 23.5)]
+    out = dict(photons=photons, points=points, sets=np.array(sets, np.float64))
+    for i, (P, gp, gr) in enumerate(sets):
+        out[f"irr{i}"] = rh.irradiance_pm(photons, points, P, gp, gr)
+    save("sss_irradiance", **out)
+
+
+def gen_sss_render():
+    """Two whole passes with subsurface scattering (compat semantics, N = 8),
+    in a fresh process (the Poisson sampler's RNG is process-wide) and with
+    time(NULL) fixed at 1234567 + t - 1 for pass t's subsurface photons."""
+    sc = S.small_sss_scene()
+    sc.env = quantize_env(sc.env)
+    R = rh.RefScene(sc)
+    res = R.render_passes(sc.camera, sc.photons, 2, sss_time=1234567)
+    a = scene_arrays(sc)
+    cam = sc.camera
+    save("render_sss", **a, accum=res["accum"], radii=res["radii"], eye=np.array(cam.eye), dir=np.array(cam.dir),
+         up=np.array(cam.up), fov=np.array(cam.fov), wh=np.array([cam.width, cam.height]),
+         nphotons=np.array(sc.photons), threads=np.array(rh.num_threads()), sss_time=np.array(1234567))
+
+
+GENERATORS.update({"knn": gen_knn, "gather": gen_gather, "render": gen_render, "dipole": gen_dipole,
+                   "sss_irradiance": gen_sss_irradiance})
+# generators that need a fresh process (process-wide reference RNG state)
+FRESH = {"poisson": gen_poisson, "render_sss": gen_sss_render}
 
 
 if __name__ == "__main__":
+    import subprocess
+
+    if sys.argv[1:2] == ["--fresh"]:
+        FRESH[sys.argv[2]]()
+        sys.exit(0)
     rh.build()
-    names = sys.argv[1:] or list(GENERATORS)
+    names = sys.argv[1:] or list(GENERATORS) + list(FRESH)
     for n in names:
-        GENERATORS[n]()
+        if n in FRESH:
+            subprocess.run([sys.executable, __file__, "--fresh", n], check=True)
+        else:
+            GENERATORS[n]()

@@ -1,0 +1,103 @@
+"""Subsurface scattering stages and whole passes against the reference.
+
+Fixtures: irradianceWithPM over injected photon maps (three parameter sets),
+and two passes of ProgressivePhotonMappingProb::render on a scene with a
+refractive BSSRDF torus and a Lambertian BSSRDF sphere, generated with
+time(NULL) fixed for the subsurface photon streams and in a fresh process
+(the Poisson sampler's RNG is process-wide).
+"""
+import numpy as np
+import pytest
+
+import pppm_gb300 as P
+import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+
+
+def _knn_dists(photons, pts):
+    d = np.sqrt(((pts[:, None, :] - photons[None, :, :]) ** 2).sum(-1))
+    return np.sort(d, axis=1)
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_subsurface_photon_irradiance(ctx, golden, case):
+    g = golden("sss_irradiance")
+    P_, gp, gr = g["sets"][case]
+    ref = g[f"irr{case}"]
+    out = ctx.subsurface_photon_irradiance(g["photons"], g["points"], int(P_), gr, int(gp))
+    scale = np.abs(ref).max()
+    err = np.abs(out - ref)
+    bad = np.flatnonzero(np.any(err > RTOL * np.abs(ref) + 1e-6 * scale, axis=1))
+    if bad.size:
+        # only kNN near-ties may differ: k-th and (k+1)-th distances within 1e-5
+        k = int(gr)
+        srt = _knn_dists(g["photons"][:, :3], g["points"][bad, :3])
+        gap = (srt[:, k] - srt[:, k - 1]) / srt[:, k - 1]
+        assert np.all(gap < 1e-5), (bad[gap >= 1e-5], err[bad[gap >= 1e-5]])
+    assert bad.size <= 0.002 * len(ref)
+
+
+def _scene(g):
+    mats = g["mats"].reshape(-1).view(S.MATERIAL_DTYPE)
+    cam = S.Camera(tuple(g["eye"]), tuple(g["dir"]), tuple(g["up"]), float(g["fov"]), int(g["wh"][0]), int(g["wh"][1]))
+    return S.Scene("render_sss", g["tris"], g["mat_id"], mats, g["env"], cam, photons=int(g["nphotons"]))
+
+
+def test_render_sss_compat_two_passes(golden):
+    """A fresh context: the Poisson sampler's RNG starts at XorShift(0) as in
+    the fresh reference process."""
+    g = golden("render_sss")
+    sc = _scene(g)
+    c = P.Context(0)
+    try:
+        c.set_scene(sc)
+        par = P.Context.make_params(mode=P.MODE_COMPAT, photons=sc.photons, num_streams=int(g["threads"]),
+                                    sss_time=int(g["sss_time"]))
+        c.render_begin(sc.camera, par)
+        st1 = c.render_pass(1)
+        assert st1.radius == g["radii"][0]
+        assert st1.sss_points > 0 and st1.sss_photons > 0
+        st2 = c.render_pass(2)
+        assert st2.radius == g["radii"][1]
+        img = c.render_read()
+    finally:
+        c.close()
+    ref = g["accum"].astype(np.float64)
+    rel = np.abs(img - ref) / np.maximum(np.abs(ref), 1e-3)
+    close = np.all(rel < 1e-3, axis=2).mean()
+    relmse = np.mean((img - ref) ** 2) / np.mean(ref ** 2)
+    print(f"pixels within 1e-3: {close:.4f}, relMSE {relmse:.3e}, points {st1.sss_points}/{st2.sss_points}")
+    assert close > 0.9
+    assert relmse < 1e-3
+
+
+def test_render_sss_canonical_runs():
+    sc = S.small_sss_scene(photons=30000)
+    c = P.Context(0)
+    try:
+        c.set_scene(sc)
+        par = P.Context.make_params(mode=P.MODE_CANONICAL, photons=sc.photons, radius_scale=1 / 64, seed=11)
+        c.render_begin(sc.camera, par)
+        for t in range(1, 4):
+            st = c.render_pass(t)
+            assert st.sss_points > 0 and st.sss_photons > 0
+        img = c.render_read() / 3
+    finally:
+        c.close()
+    assert np.isfinite(img).all() and img.mean() > 0
+
+
+def test_render_sss_rejects_small_gather_radius():
+    sc = S.small_sss_scene()
+    c = P.Context(0)
+    try:
+        c.set_scene(sc)
+        par = P.Context.make_params(mode=P.MODE_COMPAT, photons=1000, gather_radius=0.5)
+        with pytest.raises(P.PppmError) as e:
+            c.render_begin(sc.camera, par)
+        assert e.value.code == P.E_UNDEFINED
+    finally:
+        c.close()
