@@ -42,8 +42,18 @@ sys.path.insert(0, str(ROOT / "oracle"))
 
 METRIC = "Mphotons/s + equal-time relMSE, learned vs plain PPM-APA, 1080p, 1 GB300"
 UNIT = "Mphotons/s"
-PHOTONS = 4_000_000
-DEPTH = 12
+# the headline workload and the subsurface one (measured on request)
+WORKLOADS = {
+    "config2": dict(photons=4_000_000, depth=12, width=1920, height=1080, triangles=873_622,
+                    desc="ppm-apa pass, 1920x1080, displaced icosphere 873,620 tris + ground, 2048x1024 sky env, "
+                         "4M photons/pass, depth 12"),
+    "config3": dict(photons=2_000_000, depth=12, width=1280, height=720, triangles=200_002,
+                    desc="ppm-apa pass with dipole subsurface scattering, 1280x720, displaced torus 200,000 tris "
+                         "(refractive + BSSRDF) + ground, 1024x512 sky env, 2M photons/pass, depth 12, Poisson "
+                         "irradiance points + octree rebuilt every pass"),
+}
+PHOTONS = WORKLOADS["config2"]["photons"]
+DEPTH = WORKLOADS["config2"]["depth"]
 
 
 def parse():
@@ -55,7 +65,12 @@ def parse():
     ap.add_argument("--mode", default="canonical", choices=["canonical", "compat"])
     ap.add_argument("--cell-factor", type=float, default=1.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
+    args = ap.parse_args()
+    global PHOTONS, DEPTH
+    PHOTONS = WORKLOADS[args.workload]["photons"]
+    DEPTH = WORKLOADS[args.workload]["depth"]
+    return args
 
 
 def dist_env():
@@ -65,12 +80,12 @@ def dist_env():
     return rank, world, local
 
 
-def workload_config(mode, cell_factor):
-    return {"workload": "ppm-apa pass, 1920x1080, displaced icosphere 873,620 tris + ground, 2048x1024 sky env, "
-                        "4M photons/pass, depth 12",
-            "mode": mode, "width": 1920, "height": 1080, "triangles": 873_622, "photons_per_pass": PHOTONS,
-            "max_depth": DEPTH, "alpha": 0.7, "radius_scale": (1 / 64) if mode == "canonical" else 0.1,
-            "cell_factor": cell_factor, "parallelism": "replicas",
+def workload_config(mode, cell_factor, workload="config2"):
+    w = WORKLOADS[workload]
+    return {"workload": w["desc"], "mode": mode, "width": w["width"], "height": w["height"],
+            "triangles": w["triangles"], "photons_per_pass": w["photons"], "max_depth": w["depth"], "alpha": 0.7,
+            "radius_scale": (1 / 64) if mode == "canonical" else 0.1, "cell_factor": cell_factor,
+            "parallelism": "replicas",
             "l2": "inputs larger than L2 (photon map, path queues and BVH ~1.5 GB per pass)"}
 
 
@@ -128,10 +143,10 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def build_scene():
+def build_scene(workload="config2"):
     import scenes as S
 
-    return S.config2()
+    return S.config3() if workload == "config3" else S.config2()
 
 
 def measured_peak():
@@ -208,7 +223,7 @@ def run_gb300(args):
 
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    scene = build_scene()
+    scene = build_scene(args.workload)
     ctx = P.Context(local)
     ctx.set_scene(scene)
     compat = args.mode == "compat"
@@ -280,10 +295,11 @@ def run_gb300(args):
 
     line = None
     if rank == 0:
-        cfg = workload_config(args.mode, args.cell_factor)
+        cfg = workload_config(args.mode, args.cell_factor, args.workload)
         clocks = clk.summary()
         per = {k: statistics.mean(s[k] for s in stats) for k in ("ms_photon", "ms_bounce", "ms_grid", "ms_eye",
-                                                                   "ms_gather")}
+                                                                   "ms_gather", "ms_subsurface",
+                                                                   "ms_subsurface_host")}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32 (f64 triangle test, exact)", "data": "synthetic (seeded)",
@@ -301,8 +317,9 @@ def run_gb300(args):
                              "node_visits_per_photon_ray": cnt.photon_node_visits / max(cnt.photon_rays, 1),
                              "tri_tests_per_photon_ray": cnt.photon_tri_tests / max(cnt.photon_rays, 1),
                              "gather_pairs_per_query": cnt.gather_pairs / max(cnt.gather_queries, 1),
-                             "gather_inside_per_query": cnt.gather_inside / max(cnt.gather_queries, 1)}}
-        if world == 1 and not args.no_cpu_baseline:
+                             "gather_inside_per_query": cnt.gather_inside / max(cnt.gather_queries, 1),
+                             "sss_points": int(stats[-1]["sss_points"]), "sss_photons": int(stats[-1]["sss_photons"])}}
+        if world == 1 and not args.no_cpu_baseline and args.workload == "config2":
             line["cpu_baseline"] = cpu_baseline(scene)
         print(json.dumps(line), flush=True)
     ctx.close()

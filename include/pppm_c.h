@@ -225,15 +225,15 @@ int pppm_dipole_irradiance(pppm_ctx* ctx, const pppm_material* mat, const float*
                            const float* queries, int64_t m, float* rgb);
 
 /* Replaces sampler::poissonDisk (sampler.cc:36-101): dart throwing over the
- * triangle soup (9 floats each, host) with minimum distance min_dist. The
- * candidate draws come from the XorShift state rng_state (4 words, advanced
- * in place; the reference uses a process-wide XorShift seeded 0, whose
- * initial state is XorShift(0)); the acceptance order follows the
- * reference's RandomQueue seeded -1 and its hash grid. Writes up to cap
- * points and triangle normals (3 floats each) and the total count. Host-only:
- * needs no context or GPU. */
-int pppm_poisson_disk(const float* tri_xyz, int64_t ntri, double min_dist, uint32_t* rng_state, float* pts,
-                      float* nrm, int64_t cap, int64_t* count);
+ * triangle soup (9 floats each, host) with minimum distance min_dist, on the
+ * GPU with the reference's exact result. The candidate draws come from the
+ * XorShift state rng_state (4 words, advanced in place; the reference uses a
+ * process-wide XorShift seeded 0, whose initial state is XorShift(0)); the
+ * acceptance order follows the reference's RandomQueue seeded -1 and its
+ * hash grid. Writes up to cap points and triangle normals (3 floats each,
+ * host) and the total count. */
+int pppm_poisson_disk(pppm_ctx* ctx, const float* tri_xyz, int64_t ntri, double min_dist, uint32_t* rng_state,
+                      float* pts, float* nrm, int64_t cap, int64_t* count);
 
 /* Replaces SubsurfaceIntegrator::irradianceWithPM (subsurface_integrator.cc:
  * 329-365) over an injected photon map: photons are n records of 8 floats

@@ -76,6 +76,20 @@ struct HostPinned {
     }
 };
 
+// GPU Poisson-disc sampler of the BSSRDF triangles (k_poisson.cu): per-render
+// triangle tables and the candidate pop order, per-pass candidate buffers.
+struct PoissonGpu {
+    bool ready = false;
+    int64_t ntri = 0;
+    int64_t n = 0;       // candidates per pass
+    int64_t rounds = 0;  // decision rounds of the last run
+    double minDist = 0.0;
+    std::vector<uint32_t> jumpHost;  // XorShift jump matrices for 2^k draws
+    DBuf jump, tri, offs, triNrm, scanCursor, scanTmp, rank, pos, rec, triOf, own, box, state, conf, list, byPop,
+        flag, cursor, tmp, bbox, misc;
+    GridBufs grid;
+};
+
 // Subsurface stage of a render (SubsurfaceIntegrator, rebuilt every pass).
 struct SssState {
     bool enabled = false;
@@ -85,13 +99,14 @@ struct SssState {
     DBuf photons;             // 2 x float4 per stored subsurface photon
     int64_t cap = 0;
     GridBufs grid;
+    PoissonGpu poisson;
     DBuf points;              // 3 x float4 per irradiance point (gather query layout)
+    DBuf ptsD, nrmD;          // float3 per point
     DBuf irad;                // float3 per point
     DBuf octree;              // OctNodeDev per node
     int octNodes = 0;
-    HostPinned iradHost;
-    std::vector<float> pts, nrm;     // this pass's Poisson points and normals
-    std::vector<float4> query;       // packed queries
+    HostPinned hostBuf;       // points, normals and irradiance read back for the octree
+    int64_t numPoints = 0;
     int64_t stored = 0;
     double msHost = 0.0;      // host time of Poisson sampling and octree build
     cudaEvent_t done = nullptr;  // irradiance of the points computed
@@ -163,6 +178,7 @@ struct pppm_ctx {
     pppm::DBuf stageRec, stageQ, stageCount;
     pppm::GridBufs stageGrid;
     pppm::QuerySortBufs stageQsort;
+    pppm::PoissonGpu stagePoisson;
     cudaEvent_t ev[8] = {};
 };
 

@@ -55,12 +55,5 @@ struct HostOctNode {
 // exactly (the reference then recurses without end).
 bool buildOctree(const double* pts10, int64_t n, std::vector<HostOctNode>* out, std::string* err);
 
-// sampler::poissonDisk (sampler.cc:36-101) over the triangles `tris` of the
-// soup tri9, with the candidate draws taken from the XorShift state rng
-// (advanced in place). Writes the accepted points and their triangles'
-// normals, 3 floats each, in the reference's output order; returns their
-// count.
-int64_t poissonDisk(const float* tri9, const std::vector<int64_t>& tris, double minDist, uint32_t rng[4],
-                    std::vector<float>* points, std::vector<float>* normals);
 
 }  // namespace pppm

@@ -35,7 +35,7 @@ void gf2Mul(const Gf2Mat& a, const Gf2Mat& b, Gf2Mat* c) {  // c = a * b (apply 
 
 }  // namespace
 
-void xorshiftJumpTables(std::vector<uint32_t>* tables) {
+void xorshiftJumpTables(std::vector<uint32_t>* tables, uint32_t stride) {
     // one XorShift step as a 128x128 GF(2) matrix
     Gf2Mat m;
     for (int j = 0; j < 128; j++) {
@@ -45,10 +45,10 @@ void xorshiftJumpTables(std::vector<uint32_t>* tables) {
         x.next();
         std::memcpy(m.col[j], x.s, 16);
     }
-    // T = M^200 by square and multiply
+    // T = M^stride by square and multiply
     Gf2Mat t, p = m;
     bool first = true;
-    for (int e = 200; e > 0; e >>= 1) {
+    for (uint32_t e = stride; e > 0; e >>= 1) {
         if (e & 1) {
             if (first) { t = p; first = false; } else gf2Mul(p, t, &t);
         }
@@ -75,25 +75,6 @@ namespace {
 unsigned blocksFor(int64_t n, int bs, int cap = 152 * 16) {
     const int64_t want = (n + bs - 1) / bs;
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, cap));
-}
-
-__device__ __forceinline__ void jumpApply(const uint32_t* __restrict__ J, uint32_t s[4]) {
-    uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
-    const uint4* cols = reinterpret_cast<const uint4*>(J);
-#pragma unroll 1
-    for (int w = 0; w < 4; w++) {
-        const uint32_t word = s[w];
-#pragma unroll 8
-        for (int b = 0; b < 32; b++) {
-            const uint32_t m = 0u - ((word >> b) & 1u);
-            const uint4 c = __ldg(&cols[w * 32 + b]);
-            r0 ^= c.x & m;
-            r1 ^= c.y & m;
-            r2 ^= c.z & m;
-            r3 ^= c.w & m;
-        }
-    }
-    s[0] = r0; s[1] = r1; s[2] = r2; s[3] = r3;
 }
 
 __device__ __forceinline__ uint32_t mix32(uint32_t x) {

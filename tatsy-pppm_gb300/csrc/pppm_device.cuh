@@ -89,6 +89,26 @@ struct XorShift {
     }
 };
 
+// s <- J s for one 128x128 GF(2) jump matrix J (128 columns of 4 words).
+__device__ __forceinline__ void jumpApply(const uint32_t* __restrict__ J, uint32_t s[4]) {
+    uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+    const uint4* cols = reinterpret_cast<const uint4*>(J);
+#pragma unroll 1
+    for (int w = 0; w < 4; w++) {
+        const uint32_t word = s[w];
+#pragma unroll 8
+        for (int b = 0; b < 32; b++) {
+            const uint32_t m = 0u - ((word >> b) & 1u);
+            const uint4 c = __ldg(&cols[w * 32 + b]);
+            r0 ^= c.x & m;
+            r1 ^= c.y & m;
+            r2 ^= c.z & m;
+            r3 ^= c.w & m;
+        }
+    }
+    s[0] = r0; s[1] = r1; s[2] = r2; s[3] = r3;
+}
+
 // nextReal() = next() * (float)(1/UINT_MAX) = next() * 2^-32 exactly (random.h:45-47)
 __host__ __device__ inline double u32ToReal(uint32_t x) { return (double)x * 2.3283064365386963e-10; }
 

@@ -362,7 +362,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         cudaEventElapsedTime(&ms, c->ev[0], c->ev[7]);
         stats->ms_subsurface = rs.sss.enabled ? ms : 0.0;
         stats->ms_subsurface_host = rs.sss.enabled ? rs.sss.msHost : 0.0;
-        stats->sss_points = rs.sss.enabled ? (int64_t)rs.sss.pts.size() / 3 : 0;
+        stats->sss_points = rs.sss.enabled ? rs.sss.numPoints : 0;
         stats->sss_photons = rs.sss.enabled ? rs.sss.stored : 0;
         cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
         stats->ms_grid = ms;

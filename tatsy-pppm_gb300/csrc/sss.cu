@@ -5,8 +5,8 @@
 //   1. subsurface photon map: the photon pass of buildPhotonMap
 //      (subsurface_integrator.cc:240-327) on the wavefront kernels, with the
 //      reference's per-pass streams XorShift(time + i);
-//   2. Poisson-disc points on the BSSRDF triangles (host, sequential dart
-//      throwing exactly as sampler::poissonDisk) while the GPU traces 1;
+//   2. Poisson-disc points on the BSSRDF triangles (k_poisson.cu: the
+//      reference's sequential dart throwing, reproduced exactly in parallel);
 //   3. irradiance at the points: irradianceWithPM (subsurface_integrator.cc:
 //      329-365), the compat kNN gather with k = (int)gatherRadius,
 //      epsilon = #photons and the normal filter gatherPhotons^2 * 0.01;
@@ -58,6 +58,7 @@ int sssBegin(pppm_ctx* c) {
     SssState& s = c->rs.sss;
     s.enabled = c->anyBssrdf && !c->bssrdfTris.empty();
     s.octNodes = 0;
+    s.numPoints = 0;
     if (!s.enabled) return PPPM_OK;
     // ppm_probabilistic.cc:35-46: the BSSRDF area is averaged over ALL triangles
     const double avgArea = c->bssrdfArea / (double)c->ntri;
@@ -69,6 +70,20 @@ int sssBegin(pppm_ctx* c) {
                     "render_begin: subsurface kNN count (int)gather_radius < 1 pops an empty queue in the reference");
     if (s.k > kMaxKnn) return fail(c, PPPM_E_CAPACITY, "render_begin: subsurface kNN count (int)gather_radius above 64");
     if (!(s.areaRadius > 0.0)) return fail(c, PPPM_E_UNDEFINED, "render_begin: BSSRDF triangles have zero area");
+    // the BSSRDF triangles in scene order (ppm_probabilistic.cc via
+    // SubsurfaceIntegrator::initialize, subsurface_integrator.cc:189-195)
+    std::vector<float> tri(c->bssrdfTris.size() * 9);
+    for (size_t i = 0; i < c->bssrdfTris.size(); i++)
+        std::memcpy(&tri[9 * i], &c->hostTri[9 * (size_t)c->bssrdfTris[i]], 36);
+    {
+        const int e = poissonBegin(c, s.poisson, tri.data(), (int64_t)c->bssrdfTris.size(), s.areaRadius);
+        if (e) return e;
+    }
+    const size_t cand = (size_t)std::max<int64_t>(s.poisson.n, 1);
+    PPPM_CUDA(c, s.points.ensure(cand * 48));
+    PPPM_CUDA(c, s.ptsD.ensure(cand * 12));
+    PPPM_CUDA(c, s.nrmD.ensure(cand * 12));
+    PPPM_CUDA(c, s.irad.ensure(cand * 12));
     return PPPM_OK;
 }
 
@@ -104,7 +119,7 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
     if (s.cap == 0) s.cap = std::max<int64_t>(paths, 1 << 16);
     PPPM_CUDA(c, s.photons.ensure((size_t)s.cap * 32));
 
-    // the photon pass is enqueued first; the host samples the points meanwhile
+    // the subsurface photon pass
     PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
     PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
     for (int b = 0; b < kSssBounceLimit; b++) {
@@ -114,11 +129,15 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
     }
     *launches += 1 + kSssBounceLimit;
 
-    const auto t0 = std::chrono::steady_clock::now();
-    poissonDisk(c->hostTri.data(), c->bssrdfTris, s.areaRadius, c->poissonRng, &s.pts, &s.nrm);
-    packPointQueries(s.pts, s.nrm, &s.query);
-    s.msHost = msSince(t0);
-    const int64_t m = (int64_t)s.pts.size() / 3;
+    // points on the GPU after the photon pass
+    int64_t m = 0;
+    {
+        const int e = poissonRun(c, s.poisson, c->poissonRng, s.points.as<float4>(), s.ptsD.as<float>(),
+                                 s.nrmD.as<float>(), std::max<int64_t>(s.poisson.n, 1), &m);
+        if (e) return e;
+    }
+    s.numPoints = m;
+    s.msHost = 0.0;
 
     // (a pageable readback blocks until the stream drains: issued after the sampling)
     PassCounters hc;
@@ -146,10 +165,7 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
     s.stored = (int64_t)hc.deposits;
 
     // irradiance at the points
-    PPPM_CUDA(c, s.irad.ensure((size_t)std::max<int64_t>(m, 1) * 12));
     if (m > 0) {
-        PPPM_CUDA(c, s.points.ensure((size_t)m * 48));
-        PPPM_CUDA(c, cudaMemcpyAsync(s.points.p, s.query.data(), (size_t)m * 48, cudaMemcpyHostToDevice, c->stream));
         if (s.stored == 0) {
             // empty photon map: findKNN returns nothing, maxdist stays 0
             PPPM_CUDA(c, cudaMemsetAsync(s.irad.p, 0, (size_t)m * 12, c->stream));
@@ -173,23 +189,25 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
 
 int sssFinish(pppm_ctx* c) {
     SssState& s = c->rs.sss;
-    const int64_t m = (int64_t)s.pts.size() / 3;
+    const int64_t m = s.numPoints;
     const auto t0 = std::chrono::steady_clock::now();
     std::vector<HostOctNode> nodes;
     if (m > 0) {
-        PPPM_CUDA(c, s.iradHost.ensure((size_t)m * 12));
+        PPPM_CUDA(c, s.hostBuf.ensure((size_t)m * 36));
+        float* hp = s.hostBuf.as<float>();
         PPPM_CUDA(c, cudaStreamWaitEvent(c->aux, s.done, 0));
-        PPPM_CUDA(c, cudaMemcpyAsync(s.iradHost.p, s.irad.p, (size_t)m * 12, cudaMemcpyDeviceToHost, c->aux));
+        PPPM_CUDA(c, cudaMemcpyAsync(hp, s.ptsD.p, (size_t)m * 12, cudaMemcpyDeviceToHost, c->aux));
+        PPPM_CUDA(c, cudaMemcpyAsync(hp + 3 * m, s.nrmD.p, (size_t)m * 12, cudaMemcpyDeviceToHost, c->aux));
+        PPPM_CUDA(c, cudaMemcpyAsync(hp + 6 * m, s.irad.p, (size_t)m * 12, cudaMemcpyDeviceToHost, c->aux));
         PPPM_CUDA(c, cudaStreamSynchronize(c->aux));
         // IrradiancePoint {pos, normal, dA, irad} (subsurface_integrator.cc:224-230)
         std::vector<double> ip((size_t)m * 10);
-        const float* irad = s.iradHost.as<float>();
         for (int64_t i = 0; i < m; i++) {
             double* q = &ip[(size_t)i * 10];
             for (int d = 0; d < 3; d++) {
-                q[d] = s.pts[3 * i + d];
-                q[3 + d] = s.nrm[3 * i + d];
-                q[7 + d] = irad[3 * i + d];
+                q[d] = hp[3 * i + d];
+                q[3 + d] = hp[3 * m + 3 * i + d];
+                q[7 + d] = hp[6 * m + 3 * i + d];
             }
             q[6] = s.dA;
         }
@@ -218,22 +236,32 @@ using namespace pppm;
 
 extern "C" {
 
-int pppm_poisson_disk(const float* tri_xyz, int64_t ntri, double min_dist, uint32_t* rng_state, float* pts,
-                      float* nrm, int64_t cap, int64_t* count) {
-    if (ntri < 0 || (ntri > 0 && !tri_xyz) || !rng_state || !count || cap < 0 || (cap > 0 && (!pts || !nrm)) ||
+int pppm_poisson_disk(pppm_ctx* c, const float* tri_xyz, int64_t ntri, double min_dist, uint32_t* rng_state,
+                      float* pts, float* nrm, int64_t cap, int64_t* count) {
+    if (!c || ntri < 0 || (ntri > 0 && !tri_xyz) || !rng_state || !count || cap < 0 || (cap > 0 && (!pts || !nrm)) ||
         !(min_dist > 0.0))
-        return PPPM_E_ARG;
-    std::vector<int64_t> tris((size_t)ntri);
-    for (int64_t i = 0; i < ntri; i++) tris[i] = i;
-    std::vector<float> p, n;
-    poissonDisk(tri_xyz, tris, min_dist, rng_state, &p, &n);
-    const int64_t m = (int64_t)p.size() / 3;
+        return fail(c, PPPM_E_ARG, "poisson_disk: bad arguments");
+    if (isDevicePtr(tri_xyz) || isDevicePtr(pts) || isDevicePtr(nrm))
+        return fail(c, PPPM_E_ARG, "poisson_disk: arrays must be host memory");
+    cudaSetDevice(c->device);
+    PoissonGpu& g = c->stagePoisson;
+    int r;
+    if ((r = poissonBegin(c, g, tri_xyz, ntri, min_dist))) return r;
+    const size_t cand = (size_t)std::max<int64_t>(g.n, 1);
+    PPPM_CUDA(c, c->stageQ.ensure(cand * 48));
+    PPPM_CUDA(c, c->stage[0].ensure(cand * 12));
+    PPPM_CUDA(c, c->stage[1].ensure(cand * 12));
+    int64_t m = 0;
+    if ((r = poissonRun(c, g, rng_state, c->stageQ.as<float4>(), c->stage[0].as<float>(), c->stage[1].as<float>(),
+                        (int64_t)cand, &m)))
+        return r;
     *count = m;
     const int64_t w = std::min(m, cap);
     if (w > 0) {
-        std::memcpy(pts, p.data(), (size_t)w * 12);
-        std::memcpy(nrm, n.data(), (size_t)w * 12);
+        PPPM_CUDA(c, cudaMemcpyAsync(pts, c->stage[0].p, (size_t)w * 12, cudaMemcpyDeviceToHost, c->stream));
+        PPPM_CUDA(c, cudaMemcpyAsync(nrm, c->stage[1].p, (size_t)w * 12, cudaMemcpyDeviceToHost, c->stream));
     }
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
     return PPPM_OK;
 }
 

@@ -55,11 +55,11 @@ struct TraceParams {
     int hasSss;   // 1: the scene has BSSRDF materials
 };
 
-// Jump-ahead matrices: J[k] advances a XorShift state by 200 * 2^k draws
-// (one 200-number tape per photon or pixel). Column j of a matrix is the
+// Jump-ahead matrices: J[k] advances a XorShift state by stride * 2^k draws
+// (stride 200: one tape per photon or pixel). Column j of a matrix is the
 // image of state bit j; 128 columns of 4 words each.
 constexpr int kJumpLevels = 40;
-void xorshiftJumpTables(std::vector<uint32_t>* tables);
+void xorshiftJumpTables(std::vector<uint32_t>* tables, uint32_t stride = 200);
 void xorshiftJumpHost(const std::vector<uint32_t>& tables, uint64_t tapes, XorShift* st);
 
 cudaError_t launchTapeStates(const TraceParams& tp, const uint32_t* streamStates, const uint32_t* jump, int width,
@@ -72,6 +72,13 @@ cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int b
 cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
                            const OctView& oct, const uint32_t* pixelStates, float* accum, float4* queries,
                            PassCounters* ctr, cudaStream_t st);
+// GPU Poisson-disc sampling (k_poisson.cu). popOrder: RandomQueue(-1) pop
+// positions of n pushes (false where the reference's nextInt is undefined).
+bool popOrder(int64_t n, std::vector<int>* rank);
+int poissonBegin(pppm_ctx* c, PoissonGpu& g, const float* tri9, int64_t ntri, double minDist);
+int poissonRun(pppm_ctx* c, PoissonGpu& g, uint32_t rng[4], float4* queries, float* pts, float* nrm, int64_t cap,
+               int64_t* count);
+
 // Subsurface stage of a render (sss.cu): per-render setup, the per-pass
 // photon map + points + irradiance (enqueued), and the octree upload.
 int sssBegin(pppm_ctx* c);

@@ -79,7 +79,8 @@ SIGNATURES = {
     "pppm_dipole_rd": ([_VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_dipole_irradiance": ([_VP, _VP, _VP, ctypes.c_int64, ctypes.c_double, _VP, ctypes.c_int64, _VP],
                                ctypes.c_int),
-    "pppm_poisson_disk": ([_VP, ctypes.c_int64, ctypes.c_double, _VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_poisson_disk": ([_VP, _VP, ctypes.c_int64, ctypes.c_double, _VP, _VP, _VP, ctypes.c_int64, _VP],
+                          ctypes.c_int),
     "pppm_subsurface_photon_irradiance": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int64,
                                            ctypes.c_double, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_knn_noalloc": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
@@ -244,6 +245,24 @@ class Context:
                                          float(radius), int(gather_photons), _ptr(out)))
         return out
 
+    def poisson_disk(self, tri_xyz, min_dist, rng_state=None):
+        """pppm_poisson_disk (sampler::poissonDisk) on a triangle soup. rng_state:
+        4 uint32 XorShift words (default: XorShift(0), the reference's static
+        sampler RNG at program start). Returns (points, normals, next state)."""
+        tri = np.ascontiguousarray(tri_xyz, np.float32).reshape(-1, 9)
+        st = np.ascontiguousarray(xorshift_state(0) if rng_state is None else rng_state, np.uint32).copy()
+        # at most one point per candidate: ceil(4 A / d^2) per triangle (sampler.cc:44)
+        t64 = tri.astype(np.float64).reshape(-1, 3, 3)
+        area = 0.5 * np.linalg.norm(np.cross(t64[:, 1] - t64[:, 0], t64[:, 2] - t64[:, 1]), axis=1)
+        cap = int(np.ceil(4.0 * area / (min_dist * min_dist)).sum()) + tri.shape[0] + 16
+        pts = np.zeros((cap, 3), np.float32)
+        nrm = np.zeros((cap, 3), np.float32)
+        n = ctypes.c_int64()
+        self._check(self.lib.pppm_poisson_disk(self.h, tri.ctypes.data, tri.shape[0], float(min_dist), st.ctypes.data,
+                                               pts.ctypes.data, nrm.ctypes.data, cap, ctypes.byref(n)))
+        assert n.value <= cap
+        return pts[: n.value], nrm[: n.value], st
+
     def subsurface_photon_irradiance(self, photons8, points6, num_photons, gather_radius, gather_photons):
         ph = np.ascontiguousarray(photons8, np.float32).reshape(-1, 8)
         pt = np.ascontiguousarray(points6, np.float32).reshape(-1, 6)
@@ -330,31 +349,6 @@ def knn_noalloc(photon_pos, queries, num_target_photons, target_radius, idx, cnt
     return lib.pppm_knn_noalloc(_ptr(photon_pos), int(photon_pos.shape[0]), _ptr(queries), int(queries.shape[0]),
                                 int(num_target_photons), float(target_radius), _ptr(idx), _ptr(cnt),
                                 int(idx.shape[1]), stream)
-
-
-def poisson_disk(tri_xyz, min_dist, rng_state=None):
-    """pppm_poisson_disk (sampler::poissonDisk) on a triangle soup. rng_state:
-    4 uint32 XorShift words advanced in place (default: XorShift(0), the
-    reference's static sampler RNG at program start). Returns (points,
-    normals, rng_state)."""
-    lib = load()
-    tri = np.ascontiguousarray(tri_xyz, np.float32).reshape(-1, 9)
-    if rng_state is None:
-        rng_state = xorshift_state(0)
-    st = np.ascontiguousarray(rng_state, np.uint32).copy()
-    # at most one point per candidate: ceil(4 A / d^2) per triangle (sampler.cc:44)
-    t64 = tri.astype(np.float64).reshape(-1, 3, 3)
-    area = 0.5 * np.linalg.norm(np.cross(t64[:, 1] - t64[:, 0], t64[:, 2] - t64[:, 1]), axis=1)
-    cap = int(np.ceil(4.0 * area / (min_dist * min_dist)).sum()) + tri.shape[0] + 16
-    pts = np.zeros((cap, 3), np.float32)
-    nrm = np.zeros((cap, 3), np.float32)
-    n = ctypes.c_int64()
-    r = lib.pppm_poisson_disk(tri.ctypes.data, tri.shape[0], float(min_dist), st.ctypes.data, pts.ctypes.data,
-                              nrm.ctypes.data, cap, ctypes.byref(n))
-    if r != OK:
-        raise PppmError(r, "poisson_disk: bad arguments")
-    assert n.value <= cap
-    return pts[: n.value], nrm[: n.value], st
 
 
 def xorshift_state(seed):
