@@ -105,6 +105,8 @@ struct SssState {
     DBuf irad;                // float3 per point
     DBuf octree;              // OctNodeDev per node
     int octNodes = 0;
+    DBuf queue;               // eye-pass subsurface queries: 2 float4 each
+    int64_t queueCap = 0;
     HostPinned hostBuf;       // points, normals and irradiance read back for the octree
     int64_t numPoints = 0;
     int64_t stored = 0;

@@ -291,9 +291,13 @@ struct OctBuilder {
     std::vector<Acc> acc;  // double node values, parallel to `nodes`
     bool degenerate = false;
 
-    // returns the node index or -1 for an empty set
-    int rec(std::vector<int64_t>& idx, const double* bmin, const double* bmax, int depth) {
-        if (idx.empty()) return -1;
+    std::vector<int64_t> idx, tmp;  // point indices, partitioned in place per node
+
+    // Node over idx[lo, hi); returns its index or -1 for an empty set. The
+    // child sets are those of the reference (membership only matters: the
+    // boxes are min/max and a leaf holds one point).
+    int rec(int64_t lo, int64_t hi, const double* bmin, const double* bmax, int depth) {
+        if (lo == hi) return -1;
         const int self = (int)nodes.size();
         nodes.push_back(HostOctNode());
         acc.push_back(Acc());
@@ -301,8 +305,8 @@ struct OctBuilder {
             nodes[self].bmin[d] = (float)bmin[d];
             nodes[self].bmax[d] = (float)bmax[d];
         }
-        if (idx.size() == 1) {
-            const double* p = P + 10 * idx[0];
+        if (hi - lo == 1) {
+            const double* p = P + 10 * idx[lo];
             Acc& a = acc[self];
             for (int d = 0; d < 3; d++) {
                 a.pos[d] = p[d];
@@ -321,24 +325,33 @@ struct OctBuilder {
             return self;
         }
         const double mid[3] = {(bmin[0] + bmax[0]) * 0.5, (bmin[1] + bmax[1]) * 0.5, (bmin[2] + bmax[2]) * 0.5};
-        std::vector<int64_t> child[8];
-        for (int64_t i : idx) {
-            const double* v = P + 10 * i;
+        // 8-way partition into child ranges, each with its tight box
+        int64_t cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        double cmn[8][3], cmx[8][3];
+        for (int c = 0; c < 8; c++)
+            for (int d = 0; d < 3; d++) { cmn[c][d] = 1e20; cmx[c][d] = -1e20; }  // BBox() then merge
+        for (int64_t k = lo; k < hi; k++) {
+            const double* v = P + 10 * idx[k];
             const int id = (v[0] < mid[0] ? 0 : 4) + (v[1] < mid[1] ? 0 : 2) + (v[2] < mid[2] ? 0 : 1);
-            child[id].push_back(i);
+            cnt[id]++;
+            for (int d = 0; d < 3; d++) {
+                cmn[id][d] = std::min(cmn[id][d], v[d]);
+                cmx[id][d] = std::max(cmx[id][d], v[d]);
+            }
         }
-        idx.clear();
-        idx.shrink_to_fit();
+        int64_t start[9];
+        start[0] = lo;
+        for (int c = 0; c < 8; c++) start[c + 1] = start[c] + cnt[c];
+        int64_t cur[8];
+        for (int c = 0; c < 8; c++) cur[c] = start[c];
+        for (int64_t k = lo; k < hi; k++) {
+            const double* v = P + 10 * idx[k];
+            const int id = (v[0] < mid[0] ? 0 : 4) + (v[1] < mid[1] ? 0 : 2) + (v[2] < mid[2] ? 0 : 1);
+            tmp[cur[id]++] = idx[k];
+        }
+        std::copy(tmp.begin() + lo, tmp.begin() + hi, idx.begin() + lo);
         int ch[8];
-        for (int c = 0; c < 8; c++) {
-            double cmn[3] = {1e20, 1e20, 1e20}, cmx[3] = {-1e20, -1e20, -1e20};  // BBox() then merge
-            for (int64_t i : child[c])
-                for (int d = 0; d < 3; d++) {
-                    cmn[d] = std::min(cmn[d], P[10 * i + d]);
-                    cmx[d] = std::max(cmx[d], P[10 * i + d]);
-                }
-            ch[c] = rec(child[c], cmn, cmx, depth + 1);
-        }
+        for (int c = 0; c < 8; c++) ch[c] = rec(start[c], start[c + 1], cmn[c], cmx[c], depth + 1);
         // accumulation of the children (subsurface_integrator.cc:123-144)
         Acc a;
         std::memset(&a, 0, sizeof(a));
@@ -380,16 +393,19 @@ struct OctBuilder {
 bool buildOctree(const double* pts10, int64_t n, std::vector<HostOctNode>* out, std::string* err) {
     OctBuilder b;
     b.P = pts10;
-    std::vector<int64_t> idx((size_t)n);
+    b.idx.resize((size_t)n);
+    b.tmp.resize((size_t)n);
+    b.nodes.reserve((size_t)(2 * n + 1));
+    b.acc.reserve((size_t)(2 * n + 1));
     double mn[3] = {1e20, 1e20, 1e20}, mx[3] = {-1e20, -1e20, -1e20};
     for (int64_t i = 0; i < n; i++) {
-        idx[i] = i;
+        b.idx[i] = i;
         for (int d = 0; d < 3; d++) {
             mn[d] = std::min(mn[d], pts10[10 * i + d]);
             mx[d] = std::max(mx[d], pts10[10 * i + d]);
         }
     }
-    b.rec(idx, mn, mx, 0);
+    b.rec(0, n, mn, mx, 0);
     if (b.degenerate) {
         *err = "octree: repeated irradiance points (the reference recursion does not terminate)";
         return false;

@@ -316,7 +316,7 @@ template <bool kSss>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TraceParams tp, SceneView sc, EnvDev env, CameraDev cam,
                                                  OctView oct, const uint32_t* __restrict__ pixelStates,
                                                  float* __restrict__ accum, float4* __restrict__ queries,
-                                                 PassCounters* ctr) {
+                                                 float4* __restrict__ sssQ, int64_t sssCap, PassCounters* ctr) {
     __shared__ int order[128];
     __shared__ QNode sTop[kTopNodes];
     loadOrderTable(order);
@@ -396,6 +396,8 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
             if (kSss && (m.type & PPPM_BSDF_BSSRDF)) {
                 // ppm_probabilistic.cc:273-298; reflect probability 0.25 + 0.5 * 0.5
                 const float hx = __double2float_rn(hp[0]), hy = __double2float_rn(hp[1]), hz = __double2float_rn(hp[2]);
+                bool sss = false;
+                f3 sssAdd;
                 if (m.type & PPPM_BSDF_REFRACTION) {
                     const FresnelSplit s = fresnelSplit(d, nrm, dot(nrm, d) < 0.0f);
                     o[0] = hp[0]; o[1] = hp[1]; o[2] = hp[2];
@@ -406,14 +408,28 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
                         w = w * refl * (s.Re / 0.5f);
                         d = s.rdir;
                     } else {  // transmit: diffuse subsurface radiance
-                        const f3 irr = subsurfaceIrradiance(oct, m.dip, hx, hy, hz, nullptr);
-                        L = L + w * irr * (s.Tr / 0.5f);
+                        sssAdd = w * (s.Tr / 0.5f);
+                        sss = true;
                         alive = false;
                     }
-                    continue;
+                } else {
+                    sssAdd = w * 0.5f;
+                    sss = true;
                 }
-                const f3 irr = subsurfaceIrradiance(oct, m.dip, hx, hy, hz, nullptr);
-                L = L + w * irr * 0.5f;
+                if (sss) {
+                    // deferred to kSubsurfaceGather (one coherent pass over the
+                    // octree); evaluated here only when the queue is full
+                    const unsigned long long si = atomicAdd(&ctr->sssQueries, 1ull);
+                    if ((int64_t)si < sssCap) {
+                        sssQ[2 * si] = make_float4(hx, hy, hz, __int_as_float((int)pix));
+                        sssQ[2 * si + 1] = make_float4(sssAdd.x, sssAdd.y, sssAdd.z,
+                                                       __int_as_float(sc.matId[__float_as_int(a.w)]));
+                    } else {
+                        L = L + sssAdd * subsurfaceIrradiance(oct, m.dip, hx, hy, hz, nullptr);
+                    }
+                    sss = false;
+                }
+                if (m.type & PPPM_BSDF_REFRACTION) continue;
             }
             if (m.type & PPPM_BSDF_LAMBERTIAN) {
                 const f3 on = dot(nrm, d) < 0.0f ? nrm : -nrm;
@@ -457,6 +473,29 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
                 atomicAdd(&ctr->triTests[1], (unsigned long long)nx);
             }
         }
+    }
+}
+
+// The subsurface radiance queued by the eye pass: SubsurfaceIntegrator::
+// irradiance at each query times its path weight, added to the pixel.
+__global__ void __launch_bounds__(128) kSubsurfaceGather(OctView oct, const DevMaterial* __restrict__ mats,
+                                                         const float4* __restrict__ q, const unsigned long long* count,
+                                                         int64_t cap, float* __restrict__ accum,
+                                                         unsigned long long* visits) {
+    const int64_t n = min((int64_t)*count, cap);
+    int v = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 a = q[2 * i], b = q[2 * i + 1];
+        const DipoleDev& dip = mats[__float_as_int(b.w)].dip;
+        const f3 irr = subsurfaceIrradiance(oct, dip, a.x, a.y, a.z, visits ? &v : nullptr);
+        const int64_t px = __float_as_int(a.w);
+        atomicAdd(&accum[3 * px], b.x * irr.x);
+        atomicAdd(&accum[3 * px + 1], b.y * irr.y);
+        atomicAdd(&accum[3 * px + 2], b.z * irr.z);
+    }
+    if (visits) {
+        const unsigned t = __reduce_add_sync(0xffffffffu, (unsigned)v);
+        if ((threadIdx.x & 31) == 0 && t) atomicAdd(visits, (unsigned long long)t);
     }
 }
 
@@ -506,12 +545,19 @@ cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int b
 
 cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
                            const OctView& oct, const uint32_t* pixelStates, float* accum, float4* queries,
-                           PassCounters* ctr, cudaStream_t st) {
+                           float4* sssQ, int64_t sssCap, PassCounters* ctr, cudaStream_t st) {
     const unsigned blocks = blocksFor((int64_t)cam.w * cam.h, 128, 152 * 16);
     if (oct.numNodes > 0 || tp.hasSss)
-        kEyeTrace<true><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, ctr);
+        kEyeTrace<true><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap, ctr);
     else
-        kEyeTrace<false><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, ctr);
+        kEyeTrace<false><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap, ctr);
+    return cudaGetLastError();
+}
+
+cudaError_t launchSubsurfaceGather(const OctView& oct, const DevMaterial* mats, const float4* q,
+                                   const unsigned long long* count, int64_t cap, float* accum,
+                                   unsigned long long* visits, cudaStream_t st) {
+    kSubsurfaceGather<<<blocksFor(cap, 128, 152 * 16), 128, 0, st>>>(oct, mats, q, count, cap, accum, visits);
     return cudaGetLastError();
 }
 

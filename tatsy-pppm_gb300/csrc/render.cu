@@ -332,7 +332,13 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
 
     // eye paths and gather
     PPPM_CUDA(c, launchEyeTrace(tp, sv, ev, cd, sssView(c), pixelStates, rs.accum.as<float>(),
-                                rs.queries.as<float4>(), ctr, c->stream));
+                                rs.queries.as<float4>(), rs.sss.queue.as<float4>(), rs.sss.queueCap, ctr, c->stream));
+    if (rs.sss.enabled) {
+        PPPM_CUDA(c, launchSubsurfaceGather(sssView(c), sv.mats, rs.sss.queue.as<float4>(), &ctr->sssQueries,
+                                            rs.sss.queueCap, rs.accum.as<float>(),
+                                            tp.countTraversal ? &ctr->sssVisits : nullptr, c->stream));
+        launches += 1;
+    }
     PPPM_CUDA(c, cudaEventRecord(c->ev[3], c->stream));
     QueryView qv{rs.queries.as<float4>(), reinterpret_cast<const uint32_t*>(&ctr->queries), pixels};
     if (compat)

@@ -84,6 +84,9 @@ int sssBegin(pppm_ctx* c) {
     PPPM_CUDA(c, s.ptsD.ensure(cand * 12));
     PPPM_CUDA(c, s.nrmD.ensure(cand * 12));
     PPPM_CUDA(c, s.irad.ensure(cand * 12));
+    // eye-pass subsurface queries: two per pixel before the inline fallback
+    s.queueCap = 2 * (int64_t)c->rs.cam.width * c->rs.cam.height;
+    PPPM_CUDA(c, s.queue.ensure((size_t)s.queueCap * 32));
     return PPPM_OK;
 }
 

@@ -29,6 +29,8 @@ struct PassCounters {
     unsigned long long nodeVisits[2]; // [photon, eye] BVH nodes visited (counting flag)
     unsigned long long triTests[2];   // [photon, eye] triangles tested (counting flag)
     unsigned long long undefinedEye;  // eye paths past their 200-number tape (compat) or the segment cap
+    unsigned long long sssQueries;    // subsurface radiance queries queued by the eye pass
+    unsigned long long sssVisits;     // octree nodes visited by them (counting flag)
 };
 
 struct CameraDev {
@@ -71,7 +73,10 @@ cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int b
                                PassCounters* ctr, cudaStream_t st);
 cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
                            const OctView& oct, const uint32_t* pixelStates, float* accum, float4* queries,
-                           PassCounters* ctr, cudaStream_t st);
+                           float4* sssQ, int64_t sssCap, PassCounters* ctr, cudaStream_t st);
+cudaError_t launchSubsurfaceGather(const OctView& oct, const DevMaterial* mats, const float4* q,
+                                   const unsigned long long* count, int64_t cap, float* accum,
+                                   unsigned long long* visits, cudaStream_t st);
 // GPU Poisson-disc sampling (k_poisson.cu). popOrder: RandomQueue(-1) pop
 // positions of n pushes (false where the reference's nextInt is undefined).
 bool popOrder(int64_t n, std::vector<int>* rank);
