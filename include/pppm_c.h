@@ -246,6 +246,16 @@ int pppm_poisson_disk(pppm_ctx* ctx, const float* tri_xyz, int64_t ntri, double 
 int pppm_subsurface_photon_irradiance(pppm_ctx* ctx, const float* photons, int64_t n, const float* points, int64_t m,
                                       int64_t num_photons, double gather_radius, int32_t gather_photons, float* out);
 
+/* Forward pass of the learned photon proposal network (no counterpart in
+ * the reference): params is the flat FP32 parameter vector (W1[64][80] b1[64]
+ * W2[64][64] b2 W3[64][64] b3 W4[40][64] b4[40], PPPM_MLP_PARAMS floats),
+ * pos/nrm n x 3 floats, bbox 6 doubles (min xyz, max xyz) normalising the
+ * positions of the input encoding. out: n x 40 raw outputs (8 lobes x weight
+ * logit, mean xyz, log kappa). FP16 tensor-core GEMMs, FP32 accumulation. */
+#define PPPM_MLP_PARAMS 16104
+int pppm_mlp_forward(pppm_ctx* ctx, const float* params, const float* pos, const float* nrm, int64_t n,
+                     const double* bbox, float* out);
+
 /* Allocation-free variant of pppm_knn (same arguments and results) for
  * callers that cannot let a library allocate GPU memory: programs that own
  * all device memory under a fixed budget, frame loops that must not stall on

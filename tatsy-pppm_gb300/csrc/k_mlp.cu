@@ -1,0 +1,264 @@
+// Fused forward pass of the proposal network on the 5th-generation tensor
+// cores: one CTA of 128 threads holds the FP16 weights of all four layers in
+// shared memory (canonical no-swizzle K-major layout), computes the input
+// encoding of 128 rows, and runs the four GEMMs as tcgen05.mma (M=128,
+// N=64/48, K=16 steps) with the FP32 accumulator in TMEM. After each layer
+// the four warps read their 32 rows back with tcgen05.ld, add the bias,
+// apply ReLU, and write the FP16 activations as the next A operand. Every
+// mbarrier wait is bounded; on a timeout the CTA records an error, waits for
+// its MMAs to drain and frees its TMEM.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "context.h"
+#include "mlp.cuh"
+#include "mlp_dev.cuh"
+
+namespace pppm {
+
+namespace {
+
+constexpr int kSmemW = kMlpTilesBytes;        // 32768
+constexpr int kSmemBias = 1024;               // 240 floats, padded
+constexpr int kSmemA = kMlpRows * kMlpIn * 2;  // 20480
+constexpr int kSmemTotal = kSmemW + kSmemBias + kSmemA + 64 + 1024;  // + barrier/slot + alignment slack
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// tcgen05 shared-memory matrix descriptor, no swizzle, K-major.
+__device__ __forceinline__ uint64_t umDesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+    return d;                // base offset 0, layout type 0 (no swizzle)
+}
+
+// Instruction descriptor, kind::f16: F16 A and B (K-major), F32 D.
+__host__ __device__ constexpr uint32_t umIdesc(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void umCommit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbarWait(uint32_t mbar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tcFenceBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tcFenceAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void asyncProxyFence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmemLd16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmemWaitLd() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// 8 FP32 values -> 8 FP16 at a 16-byte canonical chunk.
+__device__ __forceinline__ void storeChunk(uint8_t* base, int off, const float* v) {
+    __half2 h[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) h[i] = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
+    *reinterpret_cast<uint4*>(base + off) = *reinterpret_cast<uint4*>(h);
+}
+
+__global__ void __launch_bounds__(128) kMlpForward(MlpInputs in, const uint8_t* __restrict__ blob, int64_t n,
+                                                   float* __restrict__ out, int* __restrict__ err) {
+    extern __shared__ uint8_t smemRaw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~(uintptr_t)1023);
+    uint8_t* sW = smem;
+    float* sBias = reinterpret_cast<float*>(smem + kSmemW);
+    uint8_t* sA = smem + kSmemW + kSmemBias;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sA + kSmemA);
+    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(mbar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    for (int i = tid; i < (kSmemW + kMlpBiasFloats * 4) / 16; i += blockDim.x)
+        reinterpret_cast<uint4*>(smem)[i] = __ldg(reinterpret_cast<const uint4*>(blob) + i);
+    const uint32_t mb = smemAddr(mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(tmemSlot)),
+                     "r"(64));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asyncProxyFence();
+    tcFenceBefore();
+    __syncthreads();
+    tcFenceAfter();
+    const uint32_t tmem = *tmemSlot;
+    const uint32_t aBase = smemAddr(sA), wBase = smemAddr(sW);
+    uint32_t phase = 0;
+    bool ok = true;
+
+    for (int64_t tile = blockIdx.x; ok && tile * kMlpRows < n; tile += gridDim.x) {
+        const int64_t row = tile * kMlpRows + tid;
+        {
+            float f[kMlpIn];
+            mlpFeatures(in, row < n ? row : -1, f);
+#pragma unroll
+            for (int c = 0; c < kMlpIn / 8; c++) storeChunk(sA, mlpCanon(tid, 8 * c, kMlpIn), f + 8 * c);
+        }
+        asyncProxyFence();
+        tcFenceBefore();
+        __syncthreads();
+#pragma unroll
+        for (int l = 0; l < kMlpLayers; l++) {
+            const int K = mlpK(l), N = mlpN(l);
+            if (tid == 0) {
+                tcFenceAfter();
+                const uint32_t idesc = umIdesc(kMlpRows, N);
+                const uint32_t sbo = (uint32_t)(K / 8) * 128u;
+#pragma unroll
+                for (int kk = 0; kk < K / 16; kk++) {
+                    const uint64_t a = umDesc(aBase + kk * 256, 128, sbo);
+                    const uint64_t b = umDesc(wBase + mlpTileOffset(l) + kk * 256, 128, sbo);
+                    umma(tmem, a, b, idesc, kk > 0 ? 1u : 0u);
+                }
+                umCommit(mb);
+            }
+            const bool got = mbarWait(mb, phase);
+            phase ^= 1u;
+            ok = !__syncthreads_or(!got);
+            if (!ok) break;
+            tcFenceAfter();
+            float v[kMlpHidden];
+            const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+            for (int c = 0; c < N / 16; c++) tmemLd16(lane + c * 16, v + 16 * c);
+            tmemWaitLd();
+            const float* bias = sBias + l * kMlpHidden;
+            if (l < kMlpLayers - 1) {
+#pragma unroll
+                for (int j = 0; j < kMlpHidden; j++) v[j] = fmaxf(v[j] + bias[j], 0.0f);
+#pragma unroll
+                for (int c = 0; c < kMlpHidden / 8; c++) storeChunk(sA, mlpCanon(tid, 8 * c, kMlpHidden), v + 8 * c);
+                asyncProxyFence();
+                tcFenceBefore();
+                __syncthreads();
+            } else if (row < n) {
+                float* o = out + row * kMlpOut;
+#pragma unroll
+                for (int j = 0; j < kMlpOut; j++) o[j] = v[j] + bias[j];
+            }
+        }
+        tcFenceBefore();
+        __syncthreads();
+    }
+    if (!ok && tid == 0) {
+        atomicExch(err, 1);
+        // the last commit may still be outstanding: wait (bounded) before freeing TMEM
+        mbarWait(mb, phase);
+    }
+    tcFenceBefore();
+    __syncthreads();
+    if (warp == 0) {
+        tcFenceAfter();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64));
+    }
+}
+
+}  // namespace
+
+void packMlp(const float* params, std::vector<uint8_t>* blob) {
+    blob->assign(kMlpBlobBytes, 0);
+    const float* p = params;
+    float* bias = reinterpret_cast<float*>(blob->data() + kMlpTilesBytes);
+    for (int l = 0; l < kMlpLayers; l++) {
+        const int K = mlpK(l), Nr = mlpNReal(l);
+        __half* tile = reinterpret_cast<__half*>(blob->data() + mlpTileOffset(l));
+        for (int nn = 0; nn < Nr; nn++)
+            for (int k = 0; k < K; k++) tile[mlpCanon(nn, k, K) / 2] = __float2half_rn(p[nn * K + k]);
+        p += Nr * K;
+        for (int nn = 0; nn < Nr; nn++) bias[l * kMlpHidden + nn] = p[nn];
+        p += Nr;
+    }
+}
+
+cudaError_t launchMlpForward(const MlpInputs& in, const uint8_t* blob, int64_t n, float* out, int* err,
+                             cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(kMlpForward, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTotal);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    if (n <= 0) return cudaSuccess;
+    const int64_t tiles = (n + kMlpRows - 1) / kMlpRows;
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, 152 * 3);
+    kMlpForward<<<grid, 128, kSmemTotal, st>>>(in, blob, n, out, err);
+    return cudaGetLastError();
+}
+
+}  // namespace pppm
+
+using namespace pppm;
+
+extern "C" int pppm_mlp_forward(pppm_ctx* c, const float* params, const float* pos, const float* nrm, int64_t n,
+                                const double* bbox, float* out) {
+    if (!c || !params || !bbox || n < 0 || (n > 0 && (!pos || !nrm || !out)))
+        return fail(c, PPPM_E_ARG, "mlp_forward: bad arguments");
+    if (n == 0) return PPPM_OK;
+    cudaSetDevice(c->device);
+    std::vector<float> hp(kMlpParams);
+    if (isDevicePtr(params)) PPPM_CUDA(c, cudaMemcpy(hp.data(), params, hp.size() * 4, cudaMemcpyDeviceToHost));
+    else std::memcpy(hp.data(), params, hp.size() * 4);
+    std::vector<uint8_t> blob;
+    packMlp(hp.data(), &blob);
+    PPPM_CUDA(c, c->stageRec.ensure(blob.size()));
+    PPPM_CUDA(c, cudaMemcpyAsync(c->stageRec.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, c->stream));
+    const void *dp, *dn;
+    void* dout;
+    int r;
+    if ((r = stageIn(c, pos, (size_t)n * 12, 0, &dp))) return r;
+    if ((r = stageIn(c, nrm, (size_t)n * 12, 1, &dn))) return r;
+    if ((r = stageOut(c, out, (size_t)n * kMlpOut * 4, 2, &dout))) return r;
+    PPPM_CUDA(c, c->stageCount.ensure(64));
+    PPPM_CUDA(c, cudaMemsetAsync(c->stageCount.p, 0, 4, c->stream));
+    MlpInputs in = mlpInputs(bbox, (const float*)dp, (const float*)dn);
+    PPPM_CUDA(c, launchMlpForward(in, c->stageRec.as<uint8_t>(), n, (float*)dout, c->stageCount.as<int>(), c->stream));
+    if ((r = finishOut(c, out, dout, (size_t)n * kMlpOut * 4))) return r;
+    int err = 0;
+    PPPM_CUDA(c, cudaMemcpyAsync(&err, c->stageCount.p, 4, cudaMemcpyDeviceToHost, c->stream));
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (err) return fail(c, PPPM_E_CUDA, "mlp_forward: a tensor-core wait timed out");
+    return PPPM_OK;
+}

@@ -20,6 +20,7 @@ E_ARG, E_CUDA, E_STATE, E_CAPACITY, E_UNDEFINED, E_TIMEOUT = -1, -2, -3, -4, -5,
 MODE_COMPAT, MODE_CANONICAL = 0, 1
 FLAG_COUNT_TRAVERSAL = 0x1
 NOALLOC_MAX_PHOTONS = 1 << 17  # PPPM_NOALLOC_MAX_PHOTONS
+MLP_PARAMS = 16104  # PPPM_MLP_PARAMS
 
 _lib = None
 
@@ -83,6 +84,7 @@ SIGNATURES = {
                           ctypes.c_int),
     "pppm_subsurface_photon_irradiance": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int64,
                                            ctypes.c_double, ctypes.c_int32, _VP], ctypes.c_int),
+    "pppm_mlp_forward": ([_VP, _VP, _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
     "pppm_knn_noalloc": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
                           ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_gather": ([_VP, ctypes.c_int32, _VP, ctypes.c_int64, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_double,
@@ -262,6 +264,18 @@ class Context:
                                                pts.ctypes.data, nrm.ctypes.data, cap, ctypes.byref(n)))
         assert n.value <= cap
         return pts[: n.value], nrm[: n.value], st
+
+    def mlp_forward(self, params, pos, nrm, bbox):
+        """pppm_mlp_forward: the proposal network's 40 raw outputs per row."""
+        prm = np.ascontiguousarray(params, np.float32).reshape(-1)
+        assert prm.size == MLP_PARAMS
+        p = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        n = np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+        bb = np.ascontiguousarray(bbox, np.float64).reshape(6)
+        out = np.zeros((p.shape[0], 40), np.float32)
+        self._check(self.lib.pppm_mlp_forward(self.h, prm.ctypes.data, p.ctypes.data, n.ctypes.data, p.shape[0],
+                                              bb.ctypes.data, out.ctypes.data))
+        return out
 
     def subsurface_photon_irradiance(self, photons8, points6, num_photons, gather_radius, gather_photons):
         ph = np.ascontiguousarray(photons8, np.float32).reshape(-1, 8)
