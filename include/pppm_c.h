@@ -256,6 +256,15 @@ int pppm_subsurface_photon_irradiance(pppm_ctx* ctx, const float* photons, int64
 int pppm_mlp_forward(pppm_ctx* ctx, const float* params, const float* pos, const float* nrm, int64_t n,
                      const double* bbox, float* out);
 
+/* Loss and gradient of the proposal network on n training records (10
+ * floats each: pos xyz, normal xyz, unit direction xyz, weight w >= 0): the
+ * weighted negative log-likelihood  -sum_i w_i log q(d_i | x_i) / sum_i w_i
+ * of the directions under the vMF mixture, back-propagated with FP16 tensor-
+ * core GEMMs and FP32 accumulation. grad: PPPM_MLP_PARAMS floats (same
+ * layout as params); loss: one float. No counterpart in the reference. */
+int pppm_mlp_grad(pppm_ctx* ctx, const float* params, const float* records, int64_t n, const double* bbox,
+                  float* grad, float* loss);
+
 /* Allocation-free variant of pppm_knn (same arguments and results) for
  * callers that cannot let a library allocate GPU memory: programs that own
  * all device memory under a fixed budget, frame loops that must not stall on

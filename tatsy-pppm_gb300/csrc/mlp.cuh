@@ -36,7 +36,28 @@ __host__ __device__ constexpr int mlpTileOffset(int l) {
 }
 constexpr int kMlpTilesBytes = mlpTileOffset(4);  // 10240 + 8192 + 8192 + 6144
 constexpr int kMlpBiasFloats = 64 + 64 + 64 + kMlpOutPad;
-constexpr int kMlpBlobBytes = kMlpTilesBytes + kMlpBiasFloats * 4;
+constexpr int kMlpBiasBytes = 1024;  // biases, padded
+// Transposed tiles for the backward pass: W_l^T as [in = N][out = K] for
+// layers 2..4 (K = 64, 64, 48).
+__host__ __device__ constexpr int mlpTKOut(int l) { return l == 3 ? kMlpOutPad : kMlpHidden; }
+__host__ __device__ constexpr int mlpTTileOffset(int l) { return (l - 1) * kMlpHidden * kMlpHidden * 2; }
+constexpr int kMlpTTilesBytes = 2 * 8192 + 6144;
+// blob: [forward tiles][biases][transposed tiles]
+constexpr int kMlpBlobBytes = kMlpTilesBytes + kMlpBiasBytes + kMlpTTilesBytes;
+
+// Offsets of W_l and b_l in the flat parameter vector.
+__host__ __device__ constexpr int mlpWOffset(int l) {
+    return l == 0 ? 0 : mlpWOffset(l - 1) + mlpNReal(l - 1) * mlpK(l - 1) + mlpNReal(l - 1);
+}
+__host__ __device__ constexpr int mlpBOffset(int l) { return mlpWOffset(l) + mlpNReal(l) * mlpK(l); }
+static_assert(mlpBOffset(3) + kMlpOut == kMlpParams, "parameter layout");
+
+// One training record: position, normal, direction, weight.
+struct MlpRecord {
+    float px, py, pz, w;
+    float nx, ny, nz, pad0;
+    float dx, dy, dz, pad1;
+};
 
 // Offset of element (row r, column k) of a [rows x K] FP16 operand in the
 // no-swizzle K-major canonical layout: 8x8 core matrices of 128 contiguous

@@ -2,6 +2,8 @@
 // Mises-Fisher mixture it outputs (pdf and sampling).
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <algorithm>
 
 #include "mlp.cuh"
@@ -64,5 +66,12 @@ __device__ __forceinline__ void mlpFeatures(const MlpInputs& in, int64_t row, fl
     const float* n = in.nrm + 3 * row;
     mlpEncode((p[0] - in.ox) * in.sx, (p[1] - in.oy) * in.sy, (p[2] - in.oz) * in.sz, n[0], n[1], n[2], f);
 }
+
+cudaError_t launchMlpPack(const float* params, uint8_t* blob, cudaStream_t st);
+cudaError_t launchMlpForward(const MlpInputs& in, const uint8_t* blob, int64_t n, float* out, int* err,
+                             cudaStream_t st);
+cudaError_t launchMlpTrain(const MlpRecord* rec, int64_t n, const float* invSumW, const MlpInputs& box,
+                           const uint8_t* blob, float* grad, float* loss, int* err, cudaStream_t st);
+cudaError_t launchMlpAdam(float* params, const float* grad, float* m, float* v, int step, float lr, cudaStream_t st);
 
 }  // namespace pppm

@@ -85,6 +85,7 @@ SIGNATURES = {
     "pppm_subsurface_photon_irradiance": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int64,
                                            ctypes.c_double, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_mlp_forward": ([_VP, _VP, _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
+    "pppm_mlp_grad": ([_VP, _VP, _VP, ctypes.c_int64, _VP, _VP, _VP], ctypes.c_int),
     "pppm_knn_noalloc": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
                           ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_gather": ([_VP, ctypes.c_int32, _VP, ctypes.c_int64, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_double,
@@ -276,6 +277,18 @@ class Context:
         self._check(self.lib.pppm_mlp_forward(self.h, prm.ctypes.data, p.ctypes.data, n.ctypes.data, p.shape[0],
                                               bb.ctypes.data, out.ctypes.data))
         return out
+
+    def mlp_grad(self, params, records10, bbox):
+        """pppm_mlp_grad: (loss, gradient) of the proposal's training loss."""
+        prm = np.ascontiguousarray(params, np.float32).reshape(-1)
+        assert prm.size == MLP_PARAMS
+        rec = np.ascontiguousarray(records10, np.float32).reshape(-1, 10)
+        bb = np.ascontiguousarray(bbox, np.float64).reshape(6)
+        grad = np.zeros(MLP_PARAMS, np.float32)
+        loss = ctypes.c_float()
+        self._check(self.lib.pppm_mlp_grad(self.h, prm.ctypes.data, rec.ctypes.data, rec.shape[0], bb.ctypes.data,
+                                           grad.ctypes.data, ctypes.byref(loss)))
+        return loss.value, grad
 
     def subsurface_photon_irradiance(self, photons8, points6, num_photons, gather_radius, gather_photons):
         ph = np.ascontiguousarray(photons8, np.float32).reshape(-1, 8)

@@ -35,3 +35,28 @@ def test_mlp_forward_matches_oracle(ctx, n):
     exact = L.forward(params, feats, fp16=False)
     rel = np.abs(out - exact).mean() / np.abs(exact).mean()
     assert rel < 2e-2, rel
+
+
+@pytest.mark.parametrize("n", [1000, 70_000])
+def test_mlp_grad_matches_oracle(ctx, n):
+    """Loss and parameter gradient of the tensor-core training kernel against
+    float64 autograd on the CPU (the GPU keeps FP16 weights and activations,
+    so the comparison is at the 1e-2 level)."""
+    pos, nrm, bbox = _inputs(n, 7)
+    rng = np.random.default_rng(8)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    w = rng.lognormal(0.0, 1.0, n)
+    w[rng.uniform(size=n) < 0.1] = 0.0  # zero-weight records contribute nothing
+    params = L.init_params(11)
+    params[-40:] = rng.normal(size=40).astype(np.float32) * 0.5
+    rec = np.concatenate([pos, nrm, d, w[:, None]], 1).astype(np.float32)
+    loss, g = ctx.mlp_grad(params, rec, bbox)
+    feats = L.encode(pos, nrm, bbox)
+    ref_loss, ref_g = L.loss_and_grads(params, feats, rec[:, 6:9].astype(np.float64), rec[:, 9].astype(np.float64))
+    assert abs(loss - ref_loss) <= 1e-2 * abs(ref_loss), (loss, ref_loss)
+    cos = float(g @ ref_g / (np.linalg.norm(g) * np.linalg.norm(ref_g)))
+    rel = float(np.linalg.norm(g - ref_g) / np.linalg.norm(ref_g))
+    print(f"n={n}: loss {loss:.6f} vs {ref_loss:.6f}, grad cos {cos:.6f}, rel {rel:.3e}")
+    assert cos > 0.999, cos
+    assert rel < 5e-2, rel
