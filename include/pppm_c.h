@@ -102,6 +102,10 @@ typedef struct {
 
 /* pppm_params.flags */
 #define PPPM_FLAG_COUNT_TRAVERSAL 0x1 /* count BVH nodes visited / triangles tested */
+#define PPPM_FLAG_LEARNED 0x2 /* canonical mode: learned photon proposal (MLP + vMF mixture, MIS with the
+                                 BSDF at a floor of 0.3, retrained every 4 passes); no reference counterpart */
+#define PPPM_FLAG_LEARNED_FROZEN 0x4 /* with PPPM_FLAG_LEARNED: the same pipeline without training (directions
+                                        from the BSDF lobe alone): the method without the network */
 
 /* Per-pass statistics written by pppm_render_pass. */
 typedef struct {
@@ -128,6 +132,9 @@ typedef struct {
     int64_t sss_photons;     /* subsurface photons stored */
     double ms_subsurface;    /* subsurface stage before the photon pass (ms, includes host sampling) */
     double ms_subsurface_host; /* of which host Poisson sampling + octree build (ms) */
+    double ms_train;         /* learned proposal: training after this pass (ms) */
+    double train_loss;       /* learned proposal: loss of the last training step */
+    int64_t train_records;   /* learned proposal: records available to the last training */
 } pppm_pass_stats;
 
 /* ------------------------------------------------------------- lifetime */
@@ -255,6 +262,16 @@ int pppm_subsurface_photon_irradiance(pppm_ctx* ctx, const float* photons, int64
 #define PPPM_MLP_PARAMS 16104
 int pppm_mlp_forward(pppm_ctx* ctx, const float* params, const float* pos, const float* nrm, int64_t n,
                      const double* bbox, float* out);
+
+/* Settings of the learned proposal for the next pppm_render_begin with
+ * PPPM_FLAG_LEARNED (no counterpart in the reference). retrain_every: passes
+ * between trainings (4); steps: Adam steps per training (16); batch: records
+ * per step (65536); lr: Adam learning rate (1e-3); floor_bsdf: probability of
+ * the BSDF lobe in the one-sample MIS mixture (0.3); max_log_kappa: upper
+ * clamp of the lobes' log concentration (7); guide_bounces: 1 to guide
+ * Lambertian bounces as well as emission (1). Values <= 0 keep the default. */
+int pppm_learned_config(pppm_ctx* ctx, int32_t retrain_every, int32_t steps, int64_t batch, float lr,
+                        float floor_bsdf, float max_log_kappa, int32_t guide_bounces);
 
 /* Loss and gradient of the proposal network on n training records (10
  * floats each: pos xyz, normal xyz, unit direction xyz, weight w >= 0): the

@@ -114,6 +114,36 @@ struct SssState {
     cudaEvent_t done = nullptr;  // irradiance of the points computed
 };
 
+// Learned photon proposal of a canonical render (PPPM_FLAG_LEARNED).
+struct GuideState {
+    bool enabled = false;
+    bool trained = false;
+    int retrainEvery = 4;       // passes between trainings
+    int stepsPerTrain = 16;     // Adam steps per training
+    int64_t batch = 65536;      // records per step
+    float lr = 1e-3f;
+    float floorBsdf = 0.3f;     // one-sample MIS: BSDF lobe probability
+    float maxLogKappa = 7.0f;   // clamp of the lobes' log concentration
+    int guideBounces = 1;       // guide Lambertian bounces (1) or emission only (0)
+    float floorLum = 0.01f;     // luminance floor of the relative-error importance
+    int adamStep = 0;
+    DBuf params, adamM, adamV, grad, blob, misc;  // misc: loss, error flag, 1 / sum w
+    DBuf raw;                   // network outputs per queue slot (40 floats)
+    DBuf inPos, inNrm;          // network inputs per queue slot
+    DBuf rec;                   // training records
+    int64_t recCap = 0;
+    DBuf counters;              // record count
+    DBuf imp[2];                // importance grids (this pass, previous pass)
+    int cur = 0;
+    bool impValid = false;
+    int G = 64;
+    float gox = 0, goy = 0, goz = 0, ginv = 1;
+    double box[6] = {0, 0, 0, 1, 1, 1};  // network input box
+    double msTrain = 0.0;
+    float lastLoss = 0.0f;
+    int64_t lastRecords = 0;
+};
+
 struct RenderState {
     bool active = false;
     pppm_camera cam{};
@@ -139,6 +169,7 @@ struct RenderState {
     int64_t storedLast = 0;
     int64_t phantomsLast = 0;
     SssState sss;
+    GuideState guide;
 };
 
 }  // namespace pppm

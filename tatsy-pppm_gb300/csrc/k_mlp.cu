@@ -28,8 +28,10 @@ constexpr int kSmemBias = 1024;               // 240 floats, padded
 constexpr int kSmemA = kMlpRows * kMlpIn * 2;  // 20480
 constexpr int kSmemTotal = kSmemW + kSmemBias + kSmemA + 64 + 1024;  // + barrier/slot + alignment slack
 
-__global__ void __launch_bounds__(128) kMlpForward(MlpInputs in, const uint8_t* __restrict__ blob, int64_t n,
-                                                   float* __restrict__ out, int* __restrict__ err) {
+__global__ void __launch_bounds__(128) kMlpForward(MlpInputs in, const uint8_t* __restrict__ blob, int64_t cap,
+                                                   const unsigned long long* count, float* __restrict__ out,
+                                                   int* __restrict__ err) {
+    const int64_t n = count ? min((int64_t)*count, cap) : cap;
     extern __shared__ uint8_t smemRaw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~(uintptr_t)1023);
     uint8_t* sW = smem;
@@ -130,7 +132,7 @@ __global__ void __launch_bounds__(128) kMlpForward(MlpInputs in, const uint8_t* 
 }  // namespace
 
 cudaError_t launchMlpForward(const MlpInputs& in, const uint8_t* blob, int64_t n, float* out, int* err,
-                             cudaStream_t st) {
+                             cudaStream_t st, const unsigned long long* count) {
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kMlpForward, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTotal);
@@ -140,7 +142,7 @@ cudaError_t launchMlpForward(const MlpInputs& in, const uint8_t* blob, int64_t n
     if (n <= 0) return cudaSuccess;
     const int64_t tiles = (n + kMlpRows - 1) / kMlpRows;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, 152 * 3);
-    kMlpForward<<<grid, 128, kSmemTotal, st>>>(in, blob, n, out, err);
+    kMlpForward<<<grid, 128, kSmemTotal, st>>>(in, blob, n, count, out, err);
     return cudaGetLastError();
 }
 

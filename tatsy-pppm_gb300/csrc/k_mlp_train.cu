@@ -51,7 +51,7 @@ __device__ __forceinline__ void storeHalf(uint8_t* base, int off, float v) {
 }
 
 // d(-s log q)/d(raw outputs) for one record; returns -s log q.
-__device__ float vmfLossGrad(const float* raw, float dx, float dy, float dz, float s, float* g) {
+__device__ float vmfLossGrad(const float* raw, float dx, float dy, float dz, float s, float* g, float maxLk) {
     float logt[kMlpLobes], lw[kMlpLobes], dlog_dlk[kMlpLobes], kap[kMlpLobes], inl[kMlpLobes], cosv[kMlpLobes];
     float mu[kMlpLobes][3], mlen[kMlpLobes];
     float lmax = -1e30f;
@@ -68,8 +68,8 @@ __device__ float vmfLossGrad(const float* raw, float dx, float dy, float dz, flo
         mu[k][1] = my / mlen[k];
         mu[k][2] = mz / mlen[k];
         const float lkr = raw[5 * k + 4];
-        inl[k] = (lkr >= -4.0f && lkr <= 7.0f) ? 1.0f : 0.0f;
-        const float lk = fminf(fmaxf(lkr, -4.0f), 7.0f);
+        inl[k] = (lkr >= -4.0f && lkr <= maxLk) ? 1.0f : 0.0f;
+        const float lk = fminf(fmaxf(lkr, -4.0f), maxLk);
         const float kk = __expf(lk);
         kap[k] = kk;
         cosv[k] = mu[k][0] * dx + mu[k][1] * dy + mu[k][2] * dz;
@@ -100,7 +100,7 @@ __device__ float vmfLossGrad(const float* raw, float dx, float dy, float dz, flo
 __global__ void __launch_bounds__(128, 1) kMlpTrain(const MlpRecord* __restrict__ rec, int64_t n, const float* invSumW,
                                                     MlpInputs box, const uint8_t* __restrict__ blob,
                                                     float* __restrict__ grad, float* __restrict__ loss,
-                                                    int* __restrict__ err) {
+                                                    int* __restrict__ err, float maxLk) {
     extern __shared__ uint8_t smemRaw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = smem + kOffA;
@@ -220,7 +220,8 @@ __global__ void __launch_bounds__(128, 1) kMlpTrain(const MlpRecord* __restrict_
 #pragma unroll
         for (int j = kMlpOut; j < kMlpHidden; j++) g[j] = 0.0f;
         if (row < n && w > 0.0f) {
-            lossSum += vmfLossGrad(v, dx, dy, dz, w * s0, g);
+            // weights clipped at 256x the batch mean keep FP16 gradients finite
+            lossSum += vmfLossGrad(v, dx, dy, dz, fminf(w * s0, 256.0f), g, maxLk);
         } else {
 #pragma unroll
             for (int j = 0; j < kMlpOut; j++) g[j] = 0.0f;
@@ -361,7 +362,7 @@ __global__ void kMlpAdam(float* __restrict__ p, const float* __restrict__ g, flo
                          float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float gi = g[i];
+    const float gi = isfinite(g[i]) ? g[i] : 0.0f;
     const float mi = b1 * m[i] + (1.0f - b1) * gi;
     const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
     m[i] = mi;
@@ -377,7 +378,8 @@ cudaError_t launchMlpPack(const float* params, uint8_t* blob, cudaStream_t st) {
 }
 
 cudaError_t launchMlpTrain(const MlpRecord* rec, int64_t n, const float* invSumW, const MlpInputs& box,
-                           const uint8_t* blob, float* grad, float* loss, int* err, cudaStream_t st) {
+                           const uint8_t* blob, float* grad, float* loss, int* err, cudaStream_t st,
+                           float maxLogKappa) {
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kMlpTrain, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem);
@@ -387,7 +389,7 @@ cudaError_t launchMlpTrain(const MlpRecord* rec, int64_t n, const float* invSumW
     if (n <= 0) return cudaSuccess;
     const int64_t tiles = (n + kMlpRows - 1) / kMlpRows;
     kMlpTrain<<<(unsigned)std::min<int64_t>(tiles, 152), 128, kTrainSmem, st>>>(rec, n, invSumW, box, blob, grad, loss,
-                                                                               err);
+                                                                               err, maxLogKappa);
     return cudaGetLastError();
 }
 

@@ -77,14 +77,6 @@ unsigned blocksFor(int64_t n, int bs, int cap = 152 * 16) {
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, cap));
 }
 
-__device__ __forceinline__ uint32_t mix32(uint32_t x) {
-    x ^= x >> 16;
-    x *= 0x7feb352du;
-    x ^= x >> 15;
-    x *= 0x846ca68bu;
-    x ^= x >> 16;
-    return x;
-}
 
 // Canonical mode: an independent XorShift state per (seed, pass, path).
 __device__ __forceinline__ void seedCanonical(uint32_t seed, int pass, uint64_t id, XorShift& x) {
@@ -146,6 +138,7 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
          g += (int64_t)gridDim.x * blockDim.x) {
         Tape tape;
         tape.pos = 0;
+        tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
         if (tp.mode == PPPM_MODE_COMPAT) {
             const uint4 s = *reinterpret_cast<const uint4*>(photonStates + 4 * g);
             tape.x.s[0] = s.x; tape.x.s[1] = s.y; tape.x.s[2] = s.z; tape.x.s[3] = s.w;
@@ -165,6 +158,12 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
         p.id = (int)g;
         p.bounce = 0;
         p.pad[0] = p.pad[1] = 0;
+        if (tp.guided) {
+            // the direction is drawn by kGuideResolve around the emission normal -d
+            p.dx = -d.x; p.dy = -d.y; p.dz = -d.z;
+            p.pad[0] = -1;
+            p.pad[1] = kPathNeedsDir;
+        }
         queue[g] = p;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -224,11 +223,25 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
                                            order, sTop, &best, &visits, &tests);
         if (alive) {
             traced = 1;
+            if (tp.guided && p.pad[0] >= 0) {
+                // training record of the draw that led here: weight cos I(y) / p
+                float V = 0.0f;
+                if (slot >= 0 && tp.guide.imp) {
+                    double y[3];
+                    hitPosition(p.ox, p.oy, p.oz, p.dx, p.dy, p.dz, best, y);
+                    const int v = impVoxel(tp.guide, (float)y[0], (float)y[1], (float)y[2]);
+                    if (v >= 0) V = __ldg(&tp.guide.imp[v]);
+                }
+                MlpRecord& r = tp.guide.rec[p.pad[0]];
+                r.w = r.pad0 * V;
+                p.pad[0] = -1;
+            }
             if (slot < 0) {
                 alive = false;
             } else {
                 Tape tape;
                 tape.pos = 0;
+                tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
                 tape.x.s[0] = p.rng[0]; tape.x.s[1] = p.rng[1]; tape.x.s[2] = p.rng[2]; tape.x.s[3] = p.rng[3];
                 const uint32_t r0 = tape.popu(), r1 = tape.popu(), r2 = tape.popu();
                 const float4 a = sc.tris[3 * slot], b = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
@@ -261,7 +274,12 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
                                      __uint_as_float(packNormal(on)));
                     db = make_float4(flux.x, flux.y, flux.z, __int_as_float(p.id));
                     if ((unsigned long long)r0 < m.rrCeil) {  // rands[0] < probability
-                        bsdfSample(m, din, on, r1, r2, &nd);
+                        if (tp.guided && tp.guide.guideBounces) {
+                            nd = on;  // kGuideResolve draws the direction around the normal
+                            p.pad[1] |= kPathNeedsDir;
+                        } else {
+                            bsdfSample(m, din, on, r1, r2, &nd);
+                        }
                         flux = flux * refl * m.invRr;
                     } else {
                         alive = false;
@@ -333,6 +351,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
         bool alive = pix < np;
         Tape tape;
         tape.pos = 0;
+        tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
         tape.x.s[0] = tape.x.s[1] = tape.x.s[2] = tape.x.s[3] = 1u;
         f3 d = {0.f, 0.f, 1.f};
         double o[3] = {cam.ex, cam.ey, cam.ez};

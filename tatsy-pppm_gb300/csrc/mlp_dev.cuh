@@ -67,11 +67,78 @@ __device__ __forceinline__ void mlpFeatures(const MlpInputs& in, int64_t row, fl
     mlpEncode((p[0] - in.ox) * in.sx, (p[1] - in.oy) * in.sy, (p[2] - in.oz) * in.sz, n[0], n[1], n[2], f);
 }
 
+// ---------------------------------------------------------------- vMF mixture
+// The network's 40 outputs as a mixture of 8 von Mises-Fisher lobes:
+// weights = softmax(logits), means = normalised 3-vectors, kappa =
+// exp(clamp(log kappa, -4, 7)).
+struct VmfMix {
+    float w[kMlpLobes];
+    float mu[kMlpLobes][3];
+    float kappa[kMlpLobes];
+    float norm[kMlpLobes];  // kappa / (2 pi (1 - e^{-2 kappa}))
+};
+
+__device__ inline void vmfMixFromRaw(const float* raw, VmfMix* m, float maxLogKappa = 7.0f) {
+    float lmax = -1e30f;
+#pragma unroll
+    for (int k = 0; k < kMlpLobes; k++) lmax = fmaxf(lmax, raw[5 * k]);
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kMlpLobes; k++) {
+        m->w[k] = __expf(raw[5 * k] - lmax);
+        s += m->w[k];
+    }
+    const float inv = 1.0f / s;
+#pragma unroll
+    for (int k = 0; k < kMlpLobes; k++) {
+        m->w[k] *= inv;
+        const float x = raw[5 * k + 1], y = raw[5 * k + 2], z = raw[5 * k + 3];
+        const float l = fmaxf(sqrtf(x * x + y * y + z * z), 1e-12f);
+        m->mu[k][0] = x / l;
+        m->mu[k][1] = y / l;
+        m->mu[k][2] = z / l;
+        const float kk = __expf(fminf(fmaxf(raw[5 * k + 4], -4.0f), maxLogKappa));
+        m->kappa[k] = kk;
+        m->norm[k] = kk / (6.283185307179586f * -expm1f(-2.0f * kk));
+    }
+}
+
+__device__ inline float vmfMixPdf(const VmfMix& m, f3 d) {
+    float p = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kMlpLobes; k++) {
+        const float c = m.mu[k][0] * d.x + m.mu[k][1] * d.y + m.mu[k][2] * d.z;
+        p += m.w[k] * m.norm[k] * __expf(m.kappa[k] * (c - 1.0f));
+    }
+    return p;
+}
+
+// Lobe by u0, then the vMF sample of the lobe (cosine to the mean from
+// 1 + log(u1 + (1 - u1) e^{-2 kappa}) / kappa, azimuth 2 pi u2).
+__device__ inline f3 vmfMixSample(const VmfMix& m, float u0, float u1, float u2) {
+    int k = 0;
+    float acc = m.w[0];
+    while (k < kMlpLobes - 1 && u0 >= acc) acc += m.w[++k];
+    const float kk = m.kappa[k];
+    const float e = __expf(-2.0f * kk);
+    const float cw = fminf(fmaxf(1.0f + __logf(u1 + (1.0f - u1) * e) / kk, -1.0f), 1.0f);
+    const float sw = sqrtf(fmaxf(0.0f, 1.0f - cw * cw));
+    float sp, cp;
+    sincospif(2.0f * u2, &sp, &cp);
+    const f3 w = {m.mu[k][0], m.mu[k][1], m.mu[k][2]};
+    f3 u = fabsf(w.x) > 0.1f ? cross(mk(0.f, 1.f, 0.f), w) : cross(mk(1.f, 0.f, 0.f), w);
+    u = normalized(u);
+    const f3 v = cross(w, u);
+    return normalized(u * (sw * cp) + v * (sw * sp) + w * cw);
+}
+
 cudaError_t launchMlpPack(const float* params, uint8_t* blob, cudaStream_t st);
+// n: rows (or capacity when count != nullptr: rows = min(*count, n))
 cudaError_t launchMlpForward(const MlpInputs& in, const uint8_t* blob, int64_t n, float* out, int* err,
-                             cudaStream_t st);
+                             cudaStream_t st, const unsigned long long* count = nullptr);
 cudaError_t launchMlpTrain(const MlpRecord* rec, int64_t n, const float* invSumW, const MlpInputs& box,
-                           const uint8_t* blob, float* grad, float* loss, int* err, cudaStream_t st);
+                           const uint8_t* blob, float* grad, float* loss, int* err, cudaStream_t st,
+                           float maxLogKappa = 7.0f);
 cudaError_t launchMlpAdam(float* params, const float* grad, float* m, float* v, int step, float lr, cudaStream_t st);
 
 }  // namespace pppm

@@ -117,12 +117,34 @@ __host__ __device__ inline double u32ToReal(uint32_t x) { return (double)x * 2.3
 __device__ __forceinline__ float u32ToFloat(uint32_t x) { return __uint2float_rn(x) * 2.3283064365386963e-10f; }
 
 // A 200-number tape consumed in order (RandomSequence, random_sequence.h).
+// Murmur3's 32-bit finaliser: a nonlinear bijection of 32-bit words.
+__host__ __device__ inline uint32_t mix32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// scramble = 1 (canonical mode) passes every output through mix32.
+// xorshift128 is linear: output k+4 is a fixed XOR combination of outputs k
+// and k+3, so draws taken four apart on one path are tied together (the
+// azimuth of a photon's first direction is a function of its env-CDF draw
+// and polar draw, which folds all photons of one small bright env cell onto
+// one curve of directions). Compat mode keeps the raw outputs, as the
+// reference does.
 struct Tape {
     XorShift x;
     int pos;
-    __device__ inline double popd() { pos++; return u32ToReal(x.next()); }
-    __device__ inline float popf() { pos++; return u32ToFloat(x.next()); }
-    __device__ inline uint32_t popu() { pos++; return x.next(); }
+    uint32_t scramble = 0;
+    __device__ inline uint32_t next() {
+        const uint32_t v = x.next();
+        return scramble ? mix32(v) : v;
+    }
+    __device__ inline double popd() { pos++; return u32ToReal(next()); }
+    __device__ inline float popf() { pos++; return u32ToFloat(next()); }
+    __device__ inline uint32_t popu() { pos++; return next(); }
 };
 
 // A tape given explicitly (stage tests feed the reference's own numbers).

@@ -187,6 +187,10 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
         const int e = sssBegin(c);
         if (e) return e;
     }
+    {
+        const int e = guideBegin(c, paths);
+        if (e) return e;
+    }
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
     rs.passesDone = 0;
     rs.storedLast = 0;
@@ -225,6 +229,8 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     tp.countTraversal = (par.flags & PPPM_FLAG_COUNT_TRAVERSAL) ? 1 : 0;
     tp.sssPass = 0;
     tp.hasSss = rs.sss.enabled ? 1 : 0;
+    tp.guided = rs.guide.enabled ? 1 : 0;
+    tp.guide = guideView(c, 3 * paths);
     int64_t launches = 0;
 
     CameraDev cd;
@@ -271,6 +277,11 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters) + 8 * (size_t)N, c->stream));
     PPPM_CUDA(c, cudaMemsetAsync(rs.gatherWork.p, 0, 16, c->stream));
         PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
+        if (tp.guided) {
+            const int e = guideStep(c, tp, rs.pathA.as<PathState>(), &ctr->queue[0], paths, 0);
+            if (e) return e;
+            launches += rs.guide.trained ? 3 : 1;
+        }
         PPPM_CUDA(c, cudaEventRecord(c->ev[5], c->stream));
         launches += 1 + par.max_bounce_photon;
         for (int b = 0; b < par.max_bounce_photon; b++) {
@@ -278,6 +289,11 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
             PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
             PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, rs.photons.as<float4>(), rs.depositCap, ctr,
                                             c->stream));
+            if (tp.guided && b + 1 < par.max_bounce_photon) {
+                const int e = guideStep(c, tp, out, &ctr->queue[(b + 1) % 3], paths, b + 1);
+                if (e) return e;
+                launches += rs.guide.trained ? 3 : 1;
+            }
         }
         PPPM_CUDA(c, cudaEventRecord(c->ev[6], c->stream));
         if (attempt == 0 && rs.sss.enabled) {
@@ -337,6 +353,11 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         PPPM_CUDA(c, launchSubsurfaceGather(sssView(c), sv.mats, rs.sss.queue.as<float4>(), &ctr->sssQueries,
                                             rs.sss.queueCap, rs.accum.as<float>(),
                                             tp.countTraversal ? &ctr->sssVisits : nullptr, c->stream));
+        launches += 1;
+    }
+    if (tp.guided) {
+        const int e = guideImportance(c, rs.queries.as<float4>(), &ctr->queries, pixels, t);
+        if (e) return e;
         launches += 1;
     }
     PPPM_CUDA(c, cudaEventRecord(c->ev[3], c->stream));
@@ -409,6 +430,15 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     rs.storedLast = stored;
     rs.phantomsLast = phantoms;
     rs.passesDone = t;
+    if (rs.guide.enabled) {
+        const int e = guideEndPass(c, t);
+        if (e) return e;
+        if (stats) {
+            stats->ms_train = rs.guide.msTrain;
+            stats->train_loss = rs.guide.lastLoss;
+            stats->train_records = rs.guide.lastRecords;
+        }
+    }
     return PPPM_OK;
 }
 

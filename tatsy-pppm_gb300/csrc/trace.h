@@ -3,6 +3,7 @@
 
 #include "dipole.cuh"
 #include "kernels.h"
+#include "mlp_dev.cuh"
 
 namespace pppm {
 
@@ -42,6 +43,29 @@ struct CameraDev {
     int w, h;
 };
 
+// Learned proposal inside the photon pass (canonical mode): training
+// records and the importance grid that weights them.
+struct GuideView {
+    MlpRecord* rec;                // record pool
+    unsigned long long* recCount;  // records written (may exceed recCap)
+    int64_t recCap;
+    uint32_t recEvery;             // one record per recEvery guided decisions
+    const float* imp;              // importance grid (G^3, previous pass) or nullptr
+    int G;
+    float ox, oy, oz, inv;         // grid origin and 1 / voxel edge
+    float maxLogKappa;             // clamp of the lobes' log concentration
+    int guideBounces;              // 0: emission only
+};
+
+__device__ __forceinline__ int impVoxel(const GuideView& g, float x, float y, float z) {
+    const int ix = (int)floorf((x - g.ox) * g.inv), iy = (int)floorf((y - g.oy) * g.inv),
+              iz = (int)floorf((z - g.oz) * g.inv);
+    if (ix < 0 || iy < 0 || iz < 0 || ix >= g.G || iy >= g.G || iz >= g.G) return -1;
+    return (iz * g.G + iy) * g.G + ix;
+}
+
+constexpr int kPathNeedsDir = 1;  // PathState.pad[1]: direction still to be drawn (normal in d)
+
 struct TraceParams {
     int mode;
     int numStreams;
@@ -55,6 +79,8 @@ struct TraceParams {
     int countTraversal;
     int sssPass;  // 1: the subsurface photon pass (buildPhotonMap semantics)
     int hasSss;   // 1: the scene has BSSRDF materials
+    int guided;   // 1: emission and Lambertian bounces leave their direction to kGuideResolve
+    GuideView guide;
 };
 
 // Jump-ahead matrices: J[k] advances a XorShift state by stride * 2^k draws
@@ -90,6 +116,25 @@ int sssBegin(pppm_ctx* c);
 int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv, const EnvDev& ev, int64_t* launches);
 int sssFinish(pppm_ctx* c);
 OctView sssView(const pppm_ctx* c);
+
+// Learned proposal (k_guide.cu): MLP inputs of the queue's pending paths,
+// direction draw from the BSDF / vMF mixture, importance grid, record sums.
+cudaError_t launchGuidePack(const PathState* q, const unsigned long long* count, int64_t cap, float* pos, float* nrm,
+                            cudaStream_t st);
+cudaError_t launchGuideResolve(const TraceParams& tp, PathState* q, const unsigned long long* count, int64_t cap,
+                               const float* raw, float floorBsdf, int bounce, cudaStream_t st);
+cudaError_t launchImportanceSplat(const GuideView& g, const float4* queries, const unsigned long long* count,
+                                  int64_t cap, const float* accum, float invPasses, float floorLum, float* grid,
+                                  cudaStream_t st);
+cudaError_t launchRecordInvSum(const MlpRecord* rec, int64_t n, float* sum, cudaStream_t st);
+
+// Learned proposal in a canonical render (guide.cu).
+int guideBegin(pppm_ctx* c, int64_t maxPaths);
+GuideView guideView(pppm_ctx* c, int64_t decisionsPerPass);
+int guideStep(pppm_ctx* c, const TraceParams& tp, PathState* q, const unsigned long long* count, int64_t cap,
+              int bounce);
+int guideImportance(pppm_ctx* c, const float4* queries, const unsigned long long* count, int64_t cap, int t);
+int guideEndPass(pppm_ctx* c, int t);
 
 cudaError_t launchStreamCounts(const float4* deposits, const unsigned long long* count, int64_t cap, int64_t tpt,
                                int numStreams, unsigned long long* perStream, cudaStream_t st);

@@ -19,6 +19,8 @@ OK = 0
 E_ARG, E_CUDA, E_STATE, E_CAPACITY, E_UNDEFINED, E_TIMEOUT = -1, -2, -3, -4, -5, -6
 MODE_COMPAT, MODE_CANONICAL = 0, 1
 FLAG_COUNT_TRAVERSAL = 0x1
+FLAG_LEARNED = 0x2
+FLAG_LEARNED_FROZEN = 0x4
 NOALLOC_MAX_PHOTONS = 1 << 17  # PPPM_NOALLOC_MAX_PHOTONS
 MLP_PARAMS = 16104  # PPPM_MLP_PARAMS
 
@@ -53,7 +55,8 @@ class PassStats(ctypes.Structure):
                 ("tri_tests", ctypes.c_int64), ("photon_node_visits", ctypes.c_int64),
                 ("photon_tri_tests", ctypes.c_int64), ("gather_pairs", ctypes.c_int64),
                 ("gather_inside", ctypes.c_int64), ("sss_points", ctypes.c_int64), ("sss_photons", ctypes.c_int64),
-                ("ms_subsurface", ctypes.c_double), ("ms_subsurface_host", ctypes.c_double)]
+                ("ms_subsurface", ctypes.c_double), ("ms_subsurface_host", ctypes.c_double),
+                ("ms_train", ctypes.c_double), ("train_loss", ctypes.c_double), ("train_records", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -85,6 +88,8 @@ SIGNATURES = {
     "pppm_subsurface_photon_irradiance": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int64,
                                            ctypes.c_double, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_mlp_forward": ([_VP, _VP, _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
+    "pppm_learned_config": ([_VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
+                             ctypes.c_float, ctypes.c_int32], ctypes.c_int),
     "pppm_mlp_grad": ([_VP, _VP, _VP, ctypes.c_int64, _VP, _VP, _VP], ctypes.c_int),
     "pppm_knn_noalloc": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
                           ctypes.c_int32, _VP], ctypes.c_int),
@@ -277,6 +282,12 @@ class Context:
         self._check(self.lib.pppm_mlp_forward(self.h, prm.ctypes.data, p.ctypes.data, n.ctypes.data, p.shape[0],
                                               bb.ctypes.data, out.ctypes.data))
         return out
+
+    def learned_config(self, retrain_every=0, steps=0, batch=0, lr=0.0, floor_bsdf=0.0, max_log_kappa=0.0,
+                       guide_bounces=-1):
+        """pppm_learned_config: settings of the learned proposal (0 / -1 keep the default)."""
+        self._check(self.lib.pppm_learned_config(self.h, int(retrain_every), int(steps), int(batch), float(lr),
+                                                 float(floor_bsdf), float(max_log_kappa), int(guide_bounces)))
 
     def mlp_grad(self, params, records10, bbox):
         """pppm_mlp_grad: (loss, gradient) of the proposal's training loss."""
