@@ -47,6 +47,11 @@ WORKLOADS = {
     "config2": dict(photons=4_000_000, depth=12, width=1920, height=1080, triangles=873_622,
                     desc="ppm-apa pass, 1920x1080, displaced icosphere 873,620 tris + ground, 2048x1024 sky env, "
                          "4M photons/pass, depth 12"),
+    "config4": dict(photons=0, depth=8, width=0, height=0, triangles=0,
+                    desc="64 independent ppm-apa renders (canonical), each its own scene: displaced icosphere or "
+                         "torus of log-uniform 5k-500k tris + ground, own sky, image sides log-uniform 128-1024, "
+                         "photons log-uniform 100k-2M, alpha in {0.6, 0.7, 0.8}, 16 passes, depth 8; up to 8 jobs "
+                         "in flight, autotuned launch shapes"),
     "config3": dict(photons=2_000_000, depth=12, width=1280, height=720, triangles=200_002,
                     desc="ppm-apa pass with dipole subsurface scattering, 1280x720, displaced torus 200,000 tris "
                          "(refractive + BSSRDF) + ground, 1024x512 sky env, 2M photons/pass, depth 12, Poisson "
@@ -66,6 +71,7 @@ def parse():
     ap.add_argument("--cell-factor", type=float, default=1.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-study", action="store_true", help="skip the equal-time learned-vs-plain relMSE study")
     args = ap.parse_args()
     global PHOTONS, DEPTH
     PHOTONS = WORKLOADS[args.workload]["photons"]
@@ -177,6 +183,39 @@ def cpu_baseline(scene, sample_scale=16, threads=None):
     return {"value": photons / sec / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"1 pass of {photons} photons at {w}x{h} on the same scene (1/{sample_scale} of the photons "
                       f"and pixels), reference semantics, {threads} OpenMP threads; scene setup untimed"}
+
+
+def equal_time_study(ctx, scene, common, ref_passes=4096, budget_passes=64):
+    """relMSE of plain and learned-proposal renders at equal wall time against
+    a ref_passes plain render (relMSE = mean over pixels and channels of
+    (x - r)^2 / (r^2 + 0.01)). The budget is the wall time of budget_passes
+    plain passes; each method renders whole passes until it is spent."""
+    import pppm_gb300 as P
+
+    def render(flags, seed, passes=None, budget=None):
+        ctx.render_begin(scene.camera, P.Context.make_params(**dict(common, seed=seed, flags=flags)))
+        t0 = time.perf_counter()
+        t = 0
+        while True:
+            t += 1
+            ctx.render_pass(t)
+            el = time.perf_counter() - t0
+            if (passes is not None and t >= passes) or (budget is not None and el >= budget):
+                break
+        return ctx.render_read() / t, t, el
+
+    ref, _, ref_s = render(0, 1000, passes=ref_passes)
+    rel = lambda x: float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))  # noqa: E731
+    plain, n_plain, budget = render(0, 7, passes=budget_passes)
+    learned, n_learned, el = render(P.FLAG_LEARNED, 7, budget=budget)
+    out = {"reference_passes": ref_passes, "reference_s": ref_s, "budget_s": budget,
+           "plain": {"passes": n_plain, "relmse": rel(plain)},
+           "learned": {"passes": n_learned, "seconds": el, "relmse": rel(learned)},
+           "relmse_learned_over_plain": rel(learned) / rel(plain),
+           "relmse": "mean((x - r)^2 / (r^2 + 0.01)) over pixels and channels",
+           "learned_settings": "retrain every 4 passes, 16 Adam steps x 65536 records, lr 1e-3, MIS floor 0.3, "
+                               "max log kappa 7"}
+    return out
 
 
 def run_reference(args):
@@ -321,6 +360,8 @@ def run_gb300(args):
                              "sss_points": int(stats[-1]["sss_points"]), "sss_photons": int(stats[-1]["sss_photons"])}}
         if world == 1 and not args.no_cpu_baseline and args.workload == "config2":
             line["cpu_baseline"] = cpu_baseline(scene)
+        if world == 1 and not args.no_study and args.workload == "config2" and args.mode == "canonical":
+            line["equal_time_relmse"] = equal_time_study(ctx, scene, common)
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
@@ -328,8 +369,49 @@ def run_gb300(args):
     return 0
 
 
+def run_batch(args):
+    """Batched uneven jobs: aggregate Mrays/s over the whole batch and per-job
+    pass latency p50/p99 (wall time of each pppm_render_pass)."""
+    import pppm_gb300 as P
+    import scenes as S
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    jobs = S.config4_jobs(seed=4 + args.warmup)
+    b = P.Batch(local)
+    ids = []
+    for sc, alpha in jobs:
+        par = P.Context.make_params(mode=P.MODE_CANONICAL, photons=sc.photons, max_bounce_photon=8,
+                                    max_bounce_eye=8, alpha=alpha, radius_scale=1 / 64, seed=len(ids) + 1)
+        ids.append(b.submit(sc, par, 16))
+    with ClockSampler(local) as clk:
+        b.run(autotune=True, max_concurrent=8)
+    stats = [b.result(i, image=False)[1] for i in ids]
+    wall = stats[0]["batch_wall_ms"] / 1e3
+    rays = sum(s["rays"] for s in stats)
+    shapes = {}
+    for s in stats:
+        k = f'cell {s["cell_factor"]:.2f} bounce {s["bounce_blocks_per_sm"]} eye {s["eye_blocks_per_sm"]}'
+        shapes[k] = shapes.get(k, 0) + 1
+    line = {"metric": "aggregate Mrays/s over 64 batched uneven jobs (config 4)", "value": rays / wall / 1e6,
+            "unit": "Mrays/s", "n_gpus": 1, "steps": 16, "warmup": 0, "ms_per_step": wall * 1e3 / 16,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 triangle test)",
+            "data": "synthetic (seeded)", "config": workload_config("canonical", 1.0, "config4"),
+            "batch": {"jobs": len(ids), "wall_s": wall, "rays": rays,
+                      "pass_ms_p50_median_over_jobs": statistics.median(s["ms_pass_p50"] for s in stats),
+                      "pass_ms_p99_max_over_jobs": max(s["ms_pass_p99"] for s in stats),
+                      "autotuned_shapes": shapes},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    b.close()
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "config4" and args.impl == "gb300":
+        return run_batch(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

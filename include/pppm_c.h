@@ -308,6 +308,13 @@ int pppm_render_begin(pppm_ctx* ctx, const pppm_camera* cam, const pppm_params* 
  * tracePhotons, photon map build, traceRays + gather, radius update. */
 int pppm_render_pass(pppm_ctx* ctx, int32_t t, pppm_pass_stats* stats);
 
+/* Launch-shape knobs of an active render, applied from the next pass on
+ * (values <= 0 keep the current one): hash-grid cell factor (>= 1), photon
+ * bounce and eye kernel blocks per SM. None changes results beyond the order
+ * of floating-point accumulation; the batch autotuner sets them. No
+ * counterpart in the reference. */
+int pppm_render_tune(pppm_ctx* ctx, float cell_factor, int32_t bounce_blocks_per_sm, int32_t eye_blocks_per_sm);
+
 /* The linear accumulation buffer after the last pass (not divided by the
  * pass count, not flipped): w*h*3 floats, row y = camera pixel row y. */
 int pppm_render_read(pppm_ctx* ctx, float* accum);
@@ -319,6 +326,48 @@ int pppm_render(pppm_ctx* ctx, const pppm_camera* cam, const pppm_params* params
 /* Photon records of the last pass: n x 8 floats (pos xyz, flux xyz, packed
  * normal, stream id as float bits of an int). Returns the count in *n. */
 int pppm_render_photons(pppm_ctx* ctx, float* out, int64_t cap, int64_t* n);
+
+/* ------------------------------------------------------------- batch */
+/* Many uneven render jobs (each with its own scene, env map, camera and
+ * parameters) run together on one GPU. No counterpart in the reference. */
+typedef struct pppm_batch pppm_batch;
+
+typedef struct {
+    const float* tri_xyz;     /* 9 * ntri floats (host) */
+    int64_t ntri;
+    const int32_t* mat_id;    /* ntri */
+    const pppm_material* mats;
+    int32_t nmat;
+    const float* env_rgb;     /* env_w * env_h * 3 floats (host) */
+    int32_t env_w, env_h;
+    pppm_camera camera;
+    pppm_params params;
+    int32_t passes;
+} pppm_job;
+
+typedef struct {
+    int32_t passes;
+    int32_t bounce_blocks_per_sm; /* launch shape chosen by the autotuner */
+    int32_t eye_blocks_per_sm;
+    float cell_factor;
+    int64_t rays;                 /* photon + eye ray segments traced */
+    double ms_total;              /* wall time of the job's passes */
+    double ms_pass_p50, ms_pass_p99;
+    double batch_wall_ms;         /* wall time of the whole pppm_batch_run */
+} pppm_job_stats;
+
+int pppm_batch_create(int device, pppm_batch** out);
+int pppm_batch_destroy(pppm_batch* batch);
+const char* pppm_batch_last_error(const pppm_batch* batch);
+/* Copies nothing it does not need: the scene and env map are uploaded and
+ * the BVH built here. */
+int pppm_batch_submit(pppm_batch* batch, const pppm_job* job, int32_t* job_id);
+/* Runs every job's passes: up to max_concurrent jobs at once (one host
+ * worker and one stream each, longest first). autotune = 1 times the first
+ * passes of each job under different launch shapes and keeps the fastest. */
+int pppm_batch_run(pppm_batch* batch, int32_t autotune, int32_t max_concurrent);
+/* A job's accumulation buffer (as pppm_render_read) and statistics. */
+int pppm_batch_result(pppm_batch* batch, int32_t job_id, float* accum, pppm_job_stats* stats);
 
 #ifdef __cplusplus
 }

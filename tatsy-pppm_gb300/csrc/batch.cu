@@ -1,0 +1,196 @@
+// Batched uneven render jobs: each job owns a context (scene, BVH, env map,
+// render state, stream); worker threads drive up to max_concurrent jobs at a
+// time, so their kernels overlap on the GPU, longest jobs first. With
+// autotune on, a job's first passes each run a different launch shape (hash
+// cell factor, photon-bounce and eye blocks per SM; results do not depend on
+// them) and the remaining passes use the fastest. Per-pass latencies are
+// recorded per job. No counterpart in the reference (its render() handles
+// one scene at a time).
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "context.h"
+
+struct pppm_batch {
+    int device = 0;
+    struct Job {
+        pppm_ctx* ctx = nullptr;
+        pppm_camera cam{};
+        pppm_params par{};
+        int passes = 0;
+        double work = 0.0;  // photons x passes + pixels x passes: scheduling order
+        std::vector<double> passMs;
+        int64_t rays = 0;
+        float cell = 1.0f;
+        int bounceBlocks = 16, eyeBlocks = 16;
+        int status = PPPM_OK;
+        std::string err;
+    };
+    std::vector<Job> jobs;
+    double wallMs = 0.0;
+    std::string err;
+};
+
+namespace {
+
+int jobFail(pppm_batch::Job& j, int code) {
+    j.status = code;
+    j.err = pppm_last_error(j.ctx);
+    return code;
+}
+
+// Launch shapes tried over the first passes: (cell factor, bounce, eye).
+struct Shape {
+    float cell;
+    int bounce, eye;
+};
+const Shape kShapes[] = {{1.0f, 16, 16}, {1.0f, 8, 8}, {1.0f, 32, 32}, {1.25f, 16, 16}, {1.5f, 16, 16}};
+
+int runJob(pppm_batch::Job& j, bool autotune) {
+    pppm_ctx* c = j.ctx;
+    int r = pppm_render_begin(c, &j.cam, &j.par);
+    if (r) return jobFail(j, r);
+    const bool canonical = j.par.mode == PPPM_MODE_CANONICAL;
+    const int nShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
+    // pass 1 pays the allocations (default shape); passes 2 .. 1 + trials
+    // try one shape each; compat renders tune only the launch shapes (their
+    // cell size follows k)
+    const int trials = autotune ? std::min(std::max(j.passes - 2, 0), canonical ? nShapes : 3) : 0;
+    double best = 1e300;
+    Shape bestShape = kShapes[0];
+    for (int t = 1; t <= j.passes; t++) {
+        const int trial = t - 2;  // index of the shape this pass tries
+        if (trial >= 0 && trial < trials) {
+            const Shape& s = kShapes[trial];
+            pppm_render_tune(c, canonical ? s.cell : 0.0f, s.bounce, s.eye);
+        } else if (trials > 0 && trial == trials) {
+            pppm_render_tune(c, canonical ? bestShape.cell : 0.0f, bestShape.bounce, bestShape.eye);
+        }
+        pppm_pass_stats st;
+        const auto t0 = std::chrono::steady_clock::now();
+        r = pppm_render_pass(c, t, &st);
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (r) return jobFail(j, r);
+        j.passMs.push_back(ms);
+        j.rays += st.photon_rays + st.eye_rays;
+        if (trial >= 0 && trial < trials) {
+            // device time of the stages the shapes affect
+            const double dev = st.ms_photon + st.ms_grid + st.ms_eye + st.ms_gather;
+            if (dev < best) {
+                best = dev;
+                bestShape = kShapes[trial];
+            }
+        }
+    }
+    j.cell = c->rs.par.cell_factor;
+    j.bounceBlocks = c->rs.bouncePerSm;
+    j.eyeBlocks = c->rs.eyePerSm;
+    return PPPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pppm_batch_create(int device, pppm_batch** out) {
+    if (!out) return PPPM_E_ARG;
+    *out = new (std::nothrow) pppm_batch();
+    if (!*out) return PPPM_E_CAPACITY;
+    (*out)->device = device;
+    return PPPM_OK;
+}
+
+int pppm_batch_destroy(pppm_batch* b) {
+    if (!b) return PPPM_E_ARG;
+    for (auto& j : b->jobs)
+        if (j.ctx) pppm_destroy(j.ctx);
+    delete b;
+    return PPPM_OK;
+}
+
+const char* pppm_batch_last_error(const pppm_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int pppm_batch_submit(pppm_batch* b, const pppm_job* job, int32_t* job_id) {
+    if (!b || !job || job->passes < 1) return PPPM_E_ARG;
+    pppm_batch::Job j;
+    int r = pppm_create(b->device, &j.ctx);
+    if (r) {
+        b->err = "batch_submit: cannot create a context";
+        return r;
+    }
+    if ((r = pppm_scene_set(j.ctx, job->tri_xyz, job->ntri, job->mat_id, job->mats, job->nmat)) ||
+        (r = pppm_env_set(j.ctx, job->env_rgb, job->env_w, job->env_h))) {
+        b->err = std::string("batch_submit: ") + pppm_last_error(j.ctx);
+        pppm_destroy(j.ctx);
+        return r;
+    }
+    j.cam = job->camera;
+    j.par = job->params;
+    j.passes = job->passes;
+    j.work = (double)job->passes * ((double)job->params.photons + (double)job->camera.width * job->camera.height);
+    if (job_id) *job_id = (int32_t)b->jobs.size();
+    b->jobs.push_back(std::move(j));
+    return PPPM_OK;
+}
+
+int pppm_batch_run(pppm_batch* b, int32_t autotune, int32_t max_concurrent) {
+    if (!b || max_concurrent < 1) return PPPM_E_ARG;
+    std::vector<int> order(b->jobs.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return b->jobs[x].work > b->jobs[y].work; });
+    std::atomic<size_t> next(0);
+    const auto t0 = std::chrono::steady_clock::now();
+    auto worker = [&]() {
+        for (;;) {
+            const size_t k = next.fetch_add(1);
+            if (k >= order.size()) return;
+            pppm_batch::Job& j = b->jobs[order[k]];
+            j.passMs.clear();
+            j.rays = 0;
+            j.status = runJob(j, autotune != 0);
+        }
+    };
+    const int nw = std::min<int>(max_concurrent, (int)order.size());
+    std::vector<std::thread> pool;
+    for (int w = 0; w < nw; w++) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    b->wallMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    for (auto& j : b->jobs)
+        if (j.status) {
+            b->err = "batch_run: " + j.err;
+            return j.status;
+        }
+    return PPPM_OK;
+}
+
+int pppm_batch_result(pppm_batch* b, int32_t id, float* accum, pppm_job_stats* stats) {
+    if (!b || id < 0 || id >= (int32_t)b->jobs.size()) return PPPM_E_ARG;
+    pppm_batch::Job& j = b->jobs[id];
+    if (accum) {
+        const int r = pppm_render_read(j.ctx, accum);
+        if (r) return r;
+    }
+    if (stats) {
+        std::vector<double> s = j.passMs;
+        std::sort(s.begin(), s.end());
+        auto q = [&](double f) { return s.empty() ? 0.0 : s[std::min(s.size() - 1, (size_t)(f * (s.size() - 1) + 0.5))]; };
+        stats->passes = (int32_t)j.passMs.size();
+        stats->rays = j.rays;
+        stats->ms_total = 0.0;
+        for (double v : j.passMs) stats->ms_total += v;
+        stats->ms_pass_p50 = q(0.5);
+        stats->ms_pass_p99 = q(0.99);
+        stats->cell_factor = j.cell;
+        stats->bounce_blocks_per_sm = j.bounceBlocks;
+        stats->eye_blocks_per_sm = j.eyeBlocks;
+        stats->batch_wall_ms = b->wallMs;
+    }
+    return PPPM_OK;
+}
+
+}  // extern "C"

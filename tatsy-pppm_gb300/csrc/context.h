@@ -170,6 +170,9 @@ struct RenderState {
     int64_t phantomsLast = 0;
     SssState sss;
     GuideState guide;
+    // launch shapes the autotuner may change between passes
+    int bouncePerSm = 16;
+    int eyePerSm = 16;
 };
 
 }  // namespace pppm

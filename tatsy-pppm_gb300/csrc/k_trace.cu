@@ -554,10 +554,10 @@ cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int b
                                PathState* out, int64_t maxPaths, float4* deposits, int64_t depositCap,
                                PassCounters* ctr, cudaStream_t st) {
     if (tp.sssPass)
-        kPhotonBounce<true><<<blocksFor(maxPaths, 128, 152 * 16), 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths,
+        kPhotonBounce<true><<<blocksFor(maxPaths, 128, 152 * tp.bouncePerSm), 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths,
                                                                             deposits, depositCap, ctr);
     else
-        kPhotonBounce<false><<<blocksFor(maxPaths, 128, 152 * 16), 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths,
+        kPhotonBounce<false><<<blocksFor(maxPaths, 128, 152 * tp.bouncePerSm), 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths,
                                                                              deposits, depositCap, ctr);
     return cudaGetLastError();
 }
@@ -565,7 +565,7 @@ cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int b
 cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
                            const OctView& oct, const uint32_t* pixelStates, float* accum, float4* queries,
                            float4* sssQ, int64_t sssCap, PassCounters* ctr, cudaStream_t st) {
-    const unsigned blocks = blocksFor((int64_t)cam.w * cam.h, 128, 152 * 16);
+    const unsigned blocks = blocksFor((int64_t)cam.w * cam.h, 128, 152 * tp.eyePerSm);
     if (oct.numNodes > 0 || tp.hasSss)
         kEyeTrace<true><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap, ctr);
     else

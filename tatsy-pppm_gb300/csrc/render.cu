@@ -153,6 +153,8 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     rs.cam = *cam;
     rs.par = *par;
     if (!(rs.par.cell_factor >= 1.0f)) rs.par.cell_factor = 1.0f;
+    rs.bouncePerSm = 16;
+    rs.eyePerSm = 16;
     const double dx = c->bbmax[0] - c->bbmin[0], dy = c->bbmax[1] - c->bbmin[1], dz = c->bbmax[2] - c->bbmin[2];
     rs.bboxDiag = std::sqrt(dx * dx + dy * dy + dz * dz);
     rs.radius = rs.bboxDiag * par->radius_scale;  // ppm_probabilistic.cc:51-55
@@ -229,6 +231,8 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     tp.countTraversal = (par.flags & PPPM_FLAG_COUNT_TRAVERSAL) ? 1 : 0;
     tp.sssPass = 0;
     tp.hasSss = rs.sss.enabled ? 1 : 0;
+    tp.bouncePerSm = rs.bouncePerSm;
+    tp.eyePerSm = rs.eyePerSm;
     tp.guided = rs.guide.enabled ? 1 : 0;
     tp.guide = guideView(c, 3 * paths);
     int64_t launches = 0;
@@ -439,6 +443,18 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
             stats->train_records = rs.guide.lastRecords;
         }
     }
+    return PPPM_OK;
+}
+
+int pppm_render_tune(pppm_ctx* c, float cell_factor, int32_t bounce_blocks_per_sm, int32_t eye_blocks_per_sm) {
+    if (!c) return PPPM_E_ARG;
+    if (!c->rs.active) return fail(c, PPPM_E_STATE, "render_tune: no render");
+    if (cell_factor > 0.0f) {
+        if (cell_factor < 1.0f) return fail(c, PPPM_E_ARG, "render_tune: cell_factor must be >= 1");
+        c->rs.par.cell_factor = cell_factor;
+    }
+    if (bounce_blocks_per_sm > 0) c->rs.bouncePerSm = std::min(bounce_blocks_per_sm, 64);
+    if (eye_blocks_per_sm > 0) c->rs.eyePerSm = std::min(eye_blocks_per_sm, 64);
     return PPPM_OK;
 }
 

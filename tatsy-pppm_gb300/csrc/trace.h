@@ -79,6 +79,8 @@ struct TraceParams {
     int countTraversal;
     int sssPass;  // 1: the subsurface photon pass (buildPhotonMap semantics)
     int hasSss;   // 1: the scene has BSSRDF materials
+    int bouncePerSm = 16;  // photon bounce kernel: blocks per SM (tunable)
+    int eyePerSm = 16;     // eye kernel: blocks per SM (tunable)
     int guided;   // 1: emission and Lambertian bounces leave their direction to kGuideResolve
     GuideView guide;
 };

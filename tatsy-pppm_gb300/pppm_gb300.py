@@ -64,6 +64,23 @@ class PassStats(ctypes.Structure):
 
 _VP = ctypes.c_void_p
 
+
+class Job(ctypes.Structure):
+    _fields_ = [("tri_xyz", ctypes.c_void_p), ("ntri", ctypes.c_int64), ("mat_id", ctypes.c_void_p),
+                ("mats", ctypes.c_void_p), ("nmat", ctypes.c_int32), ("env_rgb", ctypes.c_void_p),
+                ("env_w", ctypes.c_int32), ("env_h", ctypes.c_int32), ("camera", Camera), ("params", Params),
+                ("passes", ctypes.c_int32)]
+
+
+class JobStats(ctypes.Structure):
+    _fields_ = [("passes", ctypes.c_int32), ("bounce_blocks_per_sm", ctypes.c_int32),
+                ("eye_blocks_per_sm", ctypes.c_int32), ("cell_factor", ctypes.c_float), ("rays", ctypes.c_int64),
+                ("ms_total", ctypes.c_double), ("ms_pass_p50", ctypes.c_double), ("ms_pass_p99", ctypes.c_double),
+                ("batch_wall_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
 SIGNATURES = {
     "pppm_create": ([ctypes.c_int, ctypes.POINTER(_VP)], ctypes.c_int),
     "pppm_destroy": ([_VP], ctypes.c_int),
@@ -100,6 +117,13 @@ SIGNATURES = {
     "pppm_render_read": ([_VP, _VP], ctypes.c_int),
     "pppm_render": ([_VP, _VP, _VP, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_render_photons": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_render_tune": ([_VP, ctypes.c_float, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+    "pppm_batch_create": ([ctypes.c_int, ctypes.POINTER(_VP)], ctypes.c_int),
+    "pppm_batch_destroy": ([_VP], ctypes.c_int),
+    "pppm_batch_last_error": ([_VP], ctypes.c_char_p),
+    "pppm_batch_submit": ([_VP, _VP, _VP], ctypes.c_int),
+    "pppm_batch_run": ([_VP, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+    "pppm_batch_result": ([_VP, ctypes.c_int32, _VP, _VP], ctypes.c_int),
 }
 
 
@@ -378,6 +402,64 @@ class Context:
         n = ctypes.c_int64()
         self._check(self.lib.pppm_render_photons(self.h, out.ctypes.data, cap, ctypes.byref(n)))
         return out[: n.value]
+
+
+class Batch:
+    """pppm_batch: many uneven render jobs on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        r = self.lib.pppm_batch_create(device, ctypes.byref(h))
+        if r != OK:
+            raise PppmError(r, "batch_create failed")
+        self.h = h
+        self._keep = []
+        self._cams = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pppm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, r):
+        if r != OK:
+            raise PppmError(r, self.lib.pppm_batch_last_error(self.h).decode())
+
+    def submit(self, scene, params, passes):
+        """Adds one job (a scenes.Scene with its env map and camera)."""
+        tris = np.ascontiguousarray(scene.tris, np.float32)
+        mid = np.ascontiguousarray(scene.mat_id, np.int32)
+        mats = np.ascontiguousarray(scene.mats)
+        env = np.ascontiguousarray(scene.env, np.float32)
+        j = Job()
+        j.tri_xyz, j.ntri, j.mat_id = tris.ctypes.data, tris.shape[0], mid.ctypes.data
+        j.mats, j.nmat = mats.ctypes.data, len(mats)
+        j.env_rgb, j.env_w, j.env_h = env.ctypes.data, env.shape[1], env.shape[0]
+        j.camera = Context.make_camera(scene.camera)
+        j.params = params
+        j.passes = passes
+        jid = ctypes.c_int32()
+        self._check(self.lib.pppm_batch_submit(self.h, ctypes.byref(j), ctypes.byref(jid)))
+        self._cams.append(j.camera)
+        return jid.value
+
+    def run(self, autotune=True, max_concurrent=8):
+        self._check(self.lib.pppm_batch_run(self.h, 1 if autotune else 0, int(max_concurrent)))
+
+    def result(self, job_id, image=True):
+        cam = self._cams[job_id]
+        out = np.zeros((cam.height, cam.width, 3), np.float32) if image else None
+        st = JobStats()
+        self._check(self.lib.pppm_batch_result(self.h, int(job_id), out.ctypes.data if image else None,
+                                               ctypes.byref(st)))
+        return out, st.as_dict()
 
 
 def knn_noalloc(photon_pos, queries, num_target_photons, target_radius, idx, cnt, stream=None):

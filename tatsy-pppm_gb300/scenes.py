@@ -367,6 +367,38 @@ def small_sss_scene(seed=5, width=64, height=48, photons=20_000, nu=48, nv=24):
                      max_depth=64)
 
 
+def config4_jobs(seed=4, n=64, min_side=128, max_side=1024, min_tris=5_000, max_tris=500_000,
+                 min_photons=100_000, max_photons=2_000_000, passes=16):
+    """Batched uneven jobs: n independent scenes (seeded displaced geodesic
+    spheres or tori of log-uniform 5k-500k triangles over a ground quad, each
+    under its own sky), image sides log-uniform in 128-1024 (16:9),
+    photons log-uniform in 100k-2M, alpha in {0.6, 0.7, 0.8}, 16 passes.
+    Returns [(scene, alpha)]."""
+    rng = np.random.default_rng(seed)
+    lu = lambda lo, hi: float(np.exp(rng.uniform(np.log(lo), np.log(hi))))  # noqa: E731
+    jobs = []
+    for k in range(n):
+        tris = lu(min_tris, max_tris)
+        if rng.uniform() < 0.5:
+            freq = max(2, int(round(math.sqrt(tris / 20.0))))
+            obj = displace_sphere(geodesic_sphere(freq), 8.0, 0.05, seed * 1000 + k, center=(0.0, 0.0, 0.0))
+        else:
+            nv = max(8, int(round(math.sqrt(tris / 2.0 / 2.5))))
+            nu = max(8, int(round(tris / 2.0 / nv)))
+            obj = torus(8.0, 3.0, nu, nv, 0.05, seed * 1000 + k)
+        gnd = ground(-9.0, 25.0)
+        mats = [material(LAMBERTIAN, (0.7, 0.7, 0.7)), material(LAMBERTIAN, rng.uniform(0.2, 0.8, 3))]
+        side = lu(min_side, max_side)
+        w = int(round(side)) // 16 * 16
+        h = max(16, int(round(w * 9 / 16)))
+        env = sky_env(256, 128, seed * 1000 + k, sun_peak=2.0e3, sun_deg=3.0)
+        cam = look_camera((-22.0, 9.0, -18.0), (0.0, -1.0, 0.0), 0.9, max(w, 16), h)
+        sc = _assemble(f"job{k}", [(gnd, 0), (obj, 1)], mats, env, cam,
+                       photons=int(round(lu(min_photons, max_photons))), passes=passes, max_depth=8)
+        jobs.append((sc, float(rng.choice([0.6, 0.7, 0.8]))))
+    return jobs
+
+
 # --------------------------------------------------------------------- files
 def write_ply(path, tris):
     """Binary little-endian PLY in the layout Trimesh::loadPly reads
