@@ -51,6 +51,9 @@ extern "C" {
 /* Render modes. */
 #define PPPM_MODE_COMPAT 0    /* the reference's semantics, quirks included */
 #define PPPM_MODE_CANONICAL 1 /* textbook Knaus-Zwicker PPM-APA */
+#define PPPM_MODE_CLASSIC 2   /* ProgressivePhotonMapping (classic PPM, progressive_photon_mapping.cc):
+                                 per-pixel render points with their own radius and photon count,
+                                 permuted Halton sampling, the reference's semantics */
 
 typedef struct pppm_ctx pppm_ctx;
 
@@ -281,6 +284,11 @@ int pppm_learned_config(pppm_ctx* ctx, int32_t retrain_every, int32_t steps, int
  * layout as params); loss: one float. No counterpart in the reference. */
 int pppm_mlp_grad(pppm_ctx* ctx, const float* params, const float* records, int64_t n, const double* bbox,
                   float* grad, float* loss);
+
+/* Halton(200, true, seed)::request (halton.cc:88-152) values of requests
+ * 0 .. count-1 (n <= 200 numbers each) into out (count x n doubles), the
+ * sampler of classic PPM, evaluated on the GPU in the reference's order. */
+int pppm_halton(pppm_ctx* ctx, uint32_t seed, int32_t count, int32_t n, double* out);
 
 /* Allocation-free variant of pppm_knn (same arguments and results) for
  * callers that cannot let a library allocate GPU memory: programs that own

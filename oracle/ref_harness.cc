@@ -419,6 +419,51 @@ int rh_render_passes(void* s, const PassJob* job, double* accum, double* radii, 
     return 0;
 }
 
+// ProgressivePhotonMapping (classic PPM, progressive_photon_mapping.cc:31-345)
+// without its PNG side effects: render points, Halton samplers, then per
+// pass traceRays (+ constructHashGrid) and tracePhotons, as render() does.
+// image: per pixel (emission + flux / (pi r2)) * coeff, NOT divided by the
+// pass count (row y = camera row y).
+int rh_classic_passes(void* s, const PassJob* job, double* image) {
+    const Scene& sc = static_cast<HarnessScene*>(s)->scene;
+    PerspectiveCamera cam(Vector3D(job->eye[0], job->eye[1], job->eye[2]), Vector3D(job->dir[0], job->dir[1], job->dir[2]),
+                          Vector3D(job->up[0], job->up[1], job->up[2]), job->fov, job->w, job->h, 1.0);
+    ProgressivePhotonMapping ppm;
+    const int np = job->w * job->h;
+    std::vector<ProgressivePhotonMapping::RenderPoint> rpoints(np);
+    for (int y = 0; y < job->h; y++)
+        for (int x = 0; x < job->w; x++) {
+            rpoints[y * job->w + x].pixelX = x;
+            rpoints[y * job->w + x].pixelY = y;
+            rpoints[y * job->w + x].n = 0;
+        }
+    Halton* hals = new Halton[OMP_NUM_CORE];
+    for (int i = 0; i < OMP_NUM_CORE; i++) hals[i] = Halton(200, true, i);
+    std::streambuf* old = std::cout.rdbuf(nullptr);
+    for (int t = 0; t < job->npasses; t++) {
+        ppm.traceRays(sc, cam, hals, &rpoints);
+        ppm.tracePhotons(sc, hals, job->photons);
+    }
+    std::cout.rdbuf(old);
+    for (int i = 0; i < np; i++) {
+        const ProgressivePhotonMapping::RenderPoint& rp = rpoints[i];
+        put3(image + 3 * i, (rp.emission + rp.flux / (PI * rp.r2)) * rp.coeff);
+    }
+    delete[] hals;
+    return 0;
+}
+
+// Halton::request (halton.cc:123-133): n numbers of `count` consecutive
+// requests of the sampler Halton(200, true, seed).
+void rh_halton(unsigned int seed, int count, int n, double* out) {
+    Halton h(200, true, seed);
+    for (int k = 0; k < count; k++) {
+        RandomSequence rs;
+        h.request(n, &rs);
+        for (int i = 0; i < n; i++) out[(size_t)k * n + i] = rs.pop();
+    }
+}
+
 // ---------------------------------------------------------------- dipole
 void rh_dipole_rd(const Mat* m, const double* d2, int n, double* out) {
     BSDF b = makeBsdf(*m);

@@ -79,6 +79,8 @@ def lib():
         _lib.rh_dipole_irradiance.argtypes = [ctypes.c_void_p, _D, ctypes.c_int, ctypes.c_double, _D, ctypes.c_int, _D]
         _lib.rh_poisson_disk.argtypes = [_F, ctypes.c_int, ctypes.c_double, _D, _D, ctypes.c_int]
         _lib.rh_poisson_disk.restype = ctypes.c_int
+        _lib.rh_classic_passes.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _D]
+        _lib.rh_halton.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.c_int, _D]
         _lib.rh_irradiance_pm.argtypes = [_D, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_double, _D]
     return _lib
@@ -168,6 +170,22 @@ class RefScene:
                         rays.shape[0], _p(out, _D))
         return out
 
+    def classic_passes(self, camera, photons, npasses):
+        """Passes of ProgressivePhotonMapping (classic PPM): the image
+        (emission + flux / (pi r2)) * coeff per pixel, not divided by the
+        pass count."""
+        job = _PassJob()
+        job.eye[:] = camera.eye
+        job.dir[:] = camera.dir
+        job.up[:] = camera.up
+        job.fov = camera.fov
+        job.w, job.h = camera.width, camera.height
+        job.photons = photons
+        job.npasses = npasses
+        img = np.zeros((camera.height, camera.width, 3))
+        lib().rh_classic_passes(self.h, ctypes.byref(job), _p(img, _D))
+        return img
+
     def render_passes(self, camera, photons, npasses, gather_photons=128, gather_radius=16.0, photon_cap=0,
                       sss_time=0):
         """Passes 1..npasses of ProgressivePhotonMappingProb::render. With a
@@ -196,6 +214,12 @@ class RefScene:
             out["photons"] = ph[: min(cnt[0], photon_cap)]
             out["photon_count"] = int(cnt[0])
         return out
+
+
+def halton(seed, count, n=200):
+    out = np.zeros((count, n))
+    lib().rh_halton(int(seed), int(count), int(n), _p(out, _D))
+    return out
 
 
 class _PassJob(ctypes.Structure):

@@ -144,6 +144,20 @@ struct GuideState {
     int64_t lastRecords = 0;
 };
 
+// Classic PPM (ProgressivePhotonMapping): render points, Halton tables,
+// render-point hash grid and photon-update events.
+struct ClassicState {
+    DBuf pos, nrm, flux, weight, emission, r2, n, coeff;  // per render point (pixel), SoA, double where the reference is
+    DBuf haltonPerm, haltonPrime, haltonOffset;          // permutation tables per stream, first 200 primes
+    int haltonSum = 0;                                   // sum of the first 200 primes
+    DBuf gridCount, gridCursor, gridTmp, gridEntries;     // bucket -> render points
+    int64_t gridEntriesCap = 0;
+    DBuf ev, evCount, evSorted, evCursor, evTmp, evRp;   // photon-update events
+    int64_t evCap = 0;
+    DBuf bbox, misc;
+    double bbmin[3] = {0, 0, 0}, scale = 1.0, irad = 0.0;
+};
+
 struct RenderState {
     bool active = false;
     pppm_camera cam{};
@@ -170,6 +184,7 @@ struct RenderState {
     int64_t phantomsLast = 0;
     SssState sss;
     GuideState guide;
+    ClassicState classic;
     // launch shapes the autotuner may change between passes
     int bouncePerSm = 16;
     int eyePerSm = 16;

@@ -6,9 +6,6 @@
 
 // Minimum resident blocks per SM for the traversal kernels (register cap
 // 65536 / (128 * n)); overridable at build time.
-#ifndef PPPM_TRACE_MINBLOCKS
-#define PPPM_TRACE_MINBLOCKS 6
-#endif
 
 namespace pppm {
 
@@ -173,17 +170,6 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
     }
 }
 
-__device__ __forceinline__ unsigned long long warpAppend(bool take, unsigned long long* counter) {
-    const unsigned mask = __ballot_sync(0xffffffffu, take);
-    const int lane = threadIdx.x & 31;
-    unsigned long long base = 0;
-    if (mask) {
-        const int leader = __ffs(mask) - 1;
-        if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
-        base = __shfl_sync(0xffffffffu, base, leader);
-    }
-    return base + (unsigned long long)__popc(mask & ((1u << lane) - 1u));
-}
 
 // One bounce of every live photon path (ppm_probabilistic.cc:150-193):
 // closest hit, three draws, deposit + Russian roulette on Lambertian
@@ -315,13 +301,6 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
     }
 }
 
-__device__ __forceinline__ void cameraRay(const CameraDev& c, float px, float py, f3* d) {
-    // PerspectiveCamera::getRay (perspective_camera.cc:42-46)
-    const float a = c.halfTan * c.aspect * (2.0f * px / (float)c.w - 1.0f);
-    const float b = c.halfTan * (2.0f * py / (float)c.h - 1.0f);
-    const f3 dir = {c.dx + a * c.ux + b * c.vx, c.dy + a * c.uy + b * c.vy, c.dz + a * c.uz + b * c.vz};
-    *d = normalized(dir);
-}
 
 // Eye paths of ProgressivePhotonMappingProb::radiance (ppm_probabilistic.cc:
 // 236-344) without BSSRDF: tail recursion through specular and refractive

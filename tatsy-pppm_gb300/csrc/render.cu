@@ -142,8 +142,10 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     // The default Scene env map has no importance tables (scene.cc:11-12):
     // photon emission would read an empty CDF.
     if (!c->hasEnv) return fail(c, PPPM_E_STATE, "render_begin: no env map (the only light of the reference)");
-    if (par->mode != PPPM_MODE_COMPAT && par->mode != PPPM_MODE_CANONICAL)
+    if (par->mode != PPPM_MODE_COMPAT && par->mode != PPPM_MODE_CANONICAL && par->mode != PPPM_MODE_CLASSIC)
         return fail(c, PPPM_E_ARG, "render_begin: unknown mode");
+    if (par->mode == PPPM_MODE_CLASSIC && (par->flags & PPPM_FLAG_LEARNED))
+        return fail(c, PPPM_E_ARG, "render_begin: the learned proposal needs canonical mode");
     if (par->num_streams < 1 || par->num_streams > 4096 || par->photons < 1 || cam->width < 1 || cam->height < 1 ||
         par->max_bounce_photon < 0 || par->max_bounce_eye < 0 || !(par->alpha > 0.0) || !(par->radius_scale > 0.0))
         return fail(c, PPPM_E_ARG, "render_begin: bad parameters");
@@ -159,8 +161,9 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     rs.bboxDiag = std::sqrt(dx * dx + dy * dy + dz * dz);
     rs.radius = rs.bboxDiag * par->radius_scale;  // ppm_probabilistic.cc:51-55
     const int N = par->num_streams;
-    rs.taskPerThread = par->mode == PPPM_MODE_COMPAT ? (par->photons + N - 1) / N : par->photons;
-    const int64_t paths = par->mode == PPPM_MODE_COMPAT ? rs.taskPerThread * N : par->photons;
+    const bool perStream = par->mode != PPPM_MODE_CANONICAL;  // compat and classic: N streams of ceil(P/N)
+    rs.taskPerThread = perStream ? (par->photons + N - 1) / N : par->photons;
+    const int64_t paths = perStream ? rs.taskPerThread * N : par->photons;
     const int64_t pixels = (int64_t)cam->width * cam->height;
     rs.streams.assign(N, XorShift());
     for (int i = 0; i < N; i++) rs.streams[i].seed((uint32_t)i);  // Random::generateSampler(i)
@@ -185,11 +188,18 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
         const int e = envFluxScale(c, (double)par->photons);
         if (e) return e;
     }
-    {
+    if (par->mode == PPPM_MODE_CLASSIC) {
+        // classic PPM has no subsurface stage for these materials (its test is
+        // type == BSSRDF, progressive_photon_mapping.cc:42) and no proposal
+        rs.sss.enabled = false;
+        rs.guide.enabled = false;
+        const int e = classicBegin(c, pixels);
+        if (e) return e;
+    } else {
         const int e = sssBegin(c);
         if (e) return e;
     }
-    {
+    if (par->mode != PPPM_MODE_CLASSIC) {
         const int e = guideBegin(c, paths);
         if (e) return e;
     }
@@ -213,7 +223,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     const int W = rs.cam.width, H = rs.cam.height;
     const int64_t pixels = (int64_t)W * H;
     const int64_t T = rs.taskPerThread;
-    const int64_t paths = compat ? T * N : par.photons;
+    const int64_t paths = par.mode != PPPM_MODE_CANONICAL ? T * N : par.photons;
     const int k = (int)rs.radius;
     if (compat && k < 1) return fail(c, PPPM_E_UNDEFINED, "render_pass: k = (int)radius < 1 pops an empty queue in the reference");
     if (compat && k > kMaxKnn) return fail(c, PPPM_E_CAPACITY, "render_pass: k = (int)radius above 64");
@@ -256,6 +266,12 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     }
     const SceneView sv = sceneView(c);
     const EnvDev ev = envView(c);
+    if (par.mode == PPPM_MODE_CLASSIC) {
+        const int e = classicPass(c, t, tp, sv, ev, cd, stats);
+        if (e) return e;
+        rs.passesDone = t;
+        return PPPM_OK;
+    }
     PassCounters* ctr = rs.photonCount.as<PassCounters>();
     unsigned long long* perStream = reinterpret_cast<unsigned long long*>(ctr + 1);
     uint32_t* photonStates = compat ? rs.tapeStates.as<uint32_t>() : nullptr;
@@ -461,6 +477,10 @@ int pppm_render_tune(pppm_ctx* c, float cell_factor, int32_t bounce_blocks_per_s
 int pppm_render_read(pppm_ctx* c, float* accum) {
     if (!c || !accum) return fail(c, PPPM_E_ARG, "render_read: bad arguments");
     if (!c->rs.active) return fail(c, PPPM_E_STATE, "render_read: no render");
+    if (c->rs.par.mode == PPPM_MODE_CLASSIC) {
+        const int e = classicRead(c, nullptr);
+        if (e) return e;
+    }
     const size_t bytes = (size_t)c->rs.cam.width * c->rs.cam.height * 12;
     PPPM_CUDA(c, cudaMemcpyAsync(accum, c->rs.accum.p, bytes, isDevicePtr(accum) ? cudaMemcpyDeviceToDevice
                                                                                   : cudaMemcpyDeviceToHost, c->stream));

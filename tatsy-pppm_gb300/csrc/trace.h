@@ -5,6 +5,11 @@
 #include "kernels.h"
 #include "mlp_dev.cuh"
 
+// blocks per SM promised to ptxas for the traversal kernels
+#ifndef PPPM_TRACE_MINBLOCKS
+#define PPPM_TRACE_MINBLOCKS 6
+#endif
+
 namespace pppm {
 
 // One photon path in the wavefront queue (80 bytes).
@@ -66,6 +71,19 @@ __device__ __forceinline__ int impVoxel(const GuideView& g, float x, float y, fl
 
 constexpr int kPathNeedsDir = 1;  // PathState.pad[1]: direction still to be drawn (normal in d)
 
+// Compaction: each taking lane gets a slot; one atomic per warp.
+__device__ __forceinline__ unsigned long long warpAppend(bool take, unsigned long long* counter) {
+    const unsigned mask = __ballot_sync(0xffffffffu, take);
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (mask) {
+        const int leader = __ffs(mask) - 1;
+        if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    return base + (unsigned long long)__popc(mask & ((1u << lane) - 1u));
+}
+
 struct TraceParams {
     int mode;
     int numStreams;
@@ -84,6 +102,14 @@ struct TraceParams {
     int guided;   // 1: emission and Lambertian bounces leave their direction to kGuideResolve
     GuideView guide;
 };
+
+// PerspectiveCamera::getRay (perspective_camera.cc:42-46) in FP32.
+__device__ __forceinline__ void cameraRay(const CameraDev& c, float px, float py, f3* d) {
+    const float a = c.halfTan * c.aspect * (2.0f * px / (float)c.w - 1.0f);
+    const float b = c.halfTan * (2.0f * py / (float)c.h - 1.0f);
+    const f3 dir = {c.dx + a * c.ux + b * c.vx, c.dy + a * c.uy + b * c.vy, c.dz + a * c.uz + b * c.vz};
+    *d = normalized(dir);
+}
 
 // Jump-ahead matrices: J[k] advances a XorShift state by stride * 2^k draws
 // (stride 200: one tape per photon or pixel). Column j of a matrix is the
@@ -137,6 +163,12 @@ int guideStep(pppm_ctx* c, const TraceParams& tp, PathState* q, const unsigned l
               int bounce);
 int guideImportance(pppm_ctx* c, const float4* queries, const unsigned long long* count, int64_t cap, int t);
 int guideEndPass(pppm_ctx* c, int t);
+
+// Classic PPM (k_classic.cu).
+int classicBegin(pppm_ctx* c, int64_t pixels);
+int classicPass(pppm_ctx* c, int t, const TraceParams& tp, const SceneView& sv, const EnvDev& ev, const CameraDev& cd,
+                pppm_pass_stats* stats);
+int classicRead(pppm_ctx* c, float* out);
 
 cudaError_t launchStreamCounts(const float4* deposits, const unsigned long long* count, int64_t cap, int64_t tpt,
                                int numStreams, unsigned long long* perStream, cudaStream_t st);

@@ -17,7 +17,7 @@ LIB_PATH = HERE / "libpppm_gb300.so"
 
 OK = 0
 E_ARG, E_CUDA, E_STATE, E_CAPACITY, E_UNDEFINED, E_TIMEOUT = -1, -2, -3, -4, -5, -6
-MODE_COMPAT, MODE_CANONICAL = 0, 1
+MODE_COMPAT, MODE_CANONICAL, MODE_CLASSIC = 0, 1, 2
 FLAG_COUNT_TRAVERSAL = 0x1
 FLAG_LEARNED = 0x2
 FLAG_LEARNED_FROZEN = 0x4
@@ -104,6 +104,7 @@ SIGNATURES = {
                           ctypes.c_int),
     "pppm_subsurface_photon_irradiance": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int64,
                                            ctypes.c_double, ctypes.c_int32, _VP], ctypes.c_int),
+    "pppm_halton": ([_VP, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_mlp_forward": ([_VP, _VP, _VP, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
     "pppm_learned_config": ([_VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
                              ctypes.c_float, ctypes.c_int32], ctypes.c_int),
@@ -294,6 +295,11 @@ class Context:
                                                pts.ctypes.data, nrm.ctypes.data, cap, ctypes.byref(n)))
         assert n.value <= cap
         return pts[: n.value], nrm[: n.value], st
+
+    def halton(self, seed, count, n=200):
+        out = np.zeros((count, n))
+        self._check(self.lib.pppm_halton(self.h, int(seed), int(count), int(n), out.ctypes.data))
+        return out
 
     def mlp_forward(self, params, pos, nrm, bbox):
         """pppm_mlp_forward: the proposal network's 40 raw outputs per row."""

@@ -16,7 +16,7 @@ import os
 import pathlib
 import sys
 
-os.environ["OMP_NUM_THREADS"] = "8"
+os.environ.setdefault("OMP_NUM_THREADS", "8")
 
 import numpy as np  # noqa: E402
 
@@ -345,10 +345,28 @@ def gen_sss_render():
          nphotons=np.array(sc.photons), threads=np.array(rh.num_threads()), sss_time=np.array(1234567))
 
 
+def gen_classic():
+    """Classic PPM (ProgressivePhotonMapping) with one OpenMP thread: with
+    more threads its render-point updates run under a lock in an order that
+    changes from run to run. Halton tables of the samplers seeded 0..7."""
+    sc = S.small_test_scene(seed=3, subdiv=3, width=64, height=48, photons=20000)
+    sc.env = quantize_env(sc.env)
+    R = rh.RefScene(sc)
+    img = R.classic_passes(sc.camera, sc.photons, 2)
+    a = scene_arrays(sc)
+    cam = sc.camera
+    hal = np.stack([rh.halton(s, 64, 200) for s in range(8)])
+    save("classic", **a, image=img, eye=np.array(cam.eye), dir=np.array(cam.dir), up=np.array(cam.up),
+         fov=np.array(cam.fov), wh=np.array([cam.width, cam.height]), nphotons=np.array(sc.photons),
+         threads=np.array(rh.num_threads()), halton=hal)
+
+
 GENERATORS.update({"knn": gen_knn, "gather": gen_gather, "render": gen_render, "dipole": gen_dipole,
                    "sss_irradiance": gen_sss_irradiance})
 # generators that need a fresh process (process-wide reference RNG state)
-FRESH = {"poisson": gen_poisson, "render_sss": gen_sss_render}
+FRESH = {"poisson": gen_poisson, "render_sss": gen_sss_render, "classic": gen_classic}
+# fresh processes that must run with a given OpenMP thread count
+FRESH_THREADS = {"classic": "1"}
 
 
 if __name__ == "__main__":
@@ -361,6 +379,9 @@ if __name__ == "__main__":
     names = sys.argv[1:] or list(GENERATORS) + list(FRESH)
     for n in names:
         if n in FRESH:
-            subprocess.run([sys.executable, __file__, "--fresh", n], check=True)
+            env = dict(os.environ)
+            if n in FRESH_THREADS:
+                env["OMP_NUM_THREADS"] = FRESH_THREADS[n]
+            subprocess.run([sys.executable, __file__, "--fresh", n], check=True, env=env)
         else:
             GENERATORS[n]()
