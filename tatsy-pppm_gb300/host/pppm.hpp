@@ -21,6 +21,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <ctime>
 #include <cstdio>
 #include <fstream>
 #include <iterator>
@@ -360,6 +361,9 @@ public:
         p.radius_scale = mode == PPPM_MODE_COMPAT ? 0.1 : 1.0 / 64.0;
         p.cell_factor = 1.0f;
         p.seed = 1;
+        // the subsurface photon streams of the reference are seeded with
+        // time(NULL) + thread (subsurface_integrator.cc:248)
+        p.sss_time = (uint32_t)std::time(nullptr);
         pppm::check(pppm_render_begin(ctx, &camera.c, &p), ctx, "render");
         for (int t = 1; t <= params.spp(); t++) pppm::check(pppm_render_pass(ctx, t, nullptr), ctx, "render");
         w_ = camera.c.width;
@@ -370,6 +374,48 @@ public:
     }
     // Linear radiance per pixel (row y = camera row y, not flipped), divided
     // by the pass count like the reference's per-pass image (:97-100).
+    std::vector<float> result() const {
+        std::vector<float> r(result_);
+        for (auto& v : r) v /= (float)(passes_ > 0 ? passes_ : 1);
+        return r;
+    }
+    int width() const { return w_; }
+    int height() const { return h_; }
+};
+
+class ProgressivePhotonMapping {  // progressive_photon_mapping.h:26-110 (classic PPM)
+    std::vector<float> result_;
+    int w_ = 0, h_ = 0, passes_ = 0;
+
+public:
+    // numStreams is the reference's OMP_NUM_CORE: its Halton sampler count
+    // (with more than one, the reference's update order varies per run).
+    int numStreams = 8;
+
+    // ProgressivePhotonMapping::render (progressive_photon_mapping.cc:31-119)
+    // minus the PNG per pass: result() returns the last pass's image.
+    void render(const Scene& /*scene*/, const Camera& camera, const RenderParameters& params) {
+        pppm_ctx* ctx = pppm::context();
+        pppm_params p{};
+        p.mode = PPPM_MODE_CLASSIC;
+        p.num_streams = numStreams;
+        p.photons = params.photons();
+        p.gather_photons = params.gatherPhotons();
+        p.gather_radius = params.gatherRadius();
+        p.max_bounce_photon = 64;
+        p.max_bounce_eye = 64;
+        p.alpha = 0.7;  // ProgressivePhotonMapping::ALPHA
+        p.radius_scale = 1.0;
+        p.cell_factor = 1.0f;
+        pppm::check(pppm_render_begin(ctx, &camera.c, &p), ctx, "render");
+        for (int t = 1; t <= params.spp(); t++) pppm::check(pppm_render_pass(ctx, t, nullptr), ctx, "render");
+        w_ = camera.c.width;
+        h_ = camera.c.height;
+        passes_ = params.spp();
+        result_.assign((size_t)w_ * h_ * 3, 0.0f);
+        pppm::check(pppm_render_read(ctx, result_.data()), ctx, "render");
+    }
+    // (emission + flux / (pi r^2)) * coeff / passes per pixel (:98-103), not flipped.
     std::vector<float> result() const {
         std::vector<float> r(result_);
         for (auto& v : r) v /= (float)(passes_ > 0 ? passes_ : 1);
