@@ -51,12 +51,19 @@ __device__ inline double haltonValue(const HaltonDev& h, int stream, unsigned lo
     const uint16_t* p = h.perm + (size_t)stream * h.sum + h.offset[dim];
     const double invBase = __drcp_rn((double)base);
     double val = 0.0, invBi = invBase;
-    while (n > 0) {
+    while (n > 0xFFFFFFFFull) {  // 64-bit digits only while the index needs them
         const unsigned long long q = n / (unsigned)base;
         const int d = p[n - q * base];
         val = __dadd_rn(val, __dmul_rn((double)d, invBi));
         invBi = __dmul_rn(invBi, invBase);
         n = q;
+    }
+    for (uint32_t m = (uint32_t)n; m > 0;) {
+        const uint32_t q = m / (uint32_t)base;
+        const int d = p[m - q * (uint32_t)base];
+        val = __dadd_rn(val, __dmul_rn((double)d, invBi));
+        invBi = __dmul_rn(invBi, invBase);
+        m = q;
     }
     return val;
 }
