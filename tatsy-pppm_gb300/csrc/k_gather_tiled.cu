@@ -14,7 +14,11 @@ namespace pppm {
 
 namespace {
 
-constexpr int kTileQ = 128;
+constexpr int kTileQ = 128;  // threads per block
+#ifndef PPPM_GATHER_QPT
+#define PPPM_GATHER_QPT 2
+#endif
+constexpr int kQ = PPPM_GATHER_QPT;  // queries per thread
 constexpr int kStage = 1024;
 
 unsigned blocksFor(int64_t n, int bs, int cap = 152 * 32) {
@@ -49,7 +53,9 @@ __global__ void kQueryScatter(QueryView qv, const uint32_t* __restrict__ keys, u
     }
 }
 
-template <bool kAccum>
+// Each thread owns kQ consecutive sorted queries (usually of the same cell),
+// so every staged photon is read from shared memory once for kQ tests.
+template <bool kAccum, bool kCount>
 __global__ void __launch_bounds__(kTileQ) kGatherTiled(GridDev g, const float4* __restrict__ sq,
                                                        const uint32_t* __restrict__ qcount, int64_t qcap, float r,
                                                        float* __restrict__ out, unsigned long long* __restrict__ work) {
@@ -62,38 +68,56 @@ __global__ void __launch_bounds__(kTileQ) kGatherTiled(GridDev g, const float4* 
     __shared__ int sNk, sLeader, sCx, sCy, sCz;
 
     const int64_t n = qcount ? min((int64_t)*qcount, qcap) : qcap;
-    const int64_t base = (int64_t)blockIdx.x * kTileQ;
+    const int64_t base = (int64_t)blockIdx.x * (kTileQ * kQ);
     if (base >= n) return;  // uniform for the whole block
-    const int64_t i = base + threadIdx.x;
-    const bool valid = i < n;
-    float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0;
-    int cx = -1, cy = -1, cz = -1;
-    if (valid) {
-        q0 = sq[3 * i];
-        q1 = sq[3 * i + 1];
-        q2 = sq[3 * i + 2];
-        cx = cellCoord(q0.x, g.ox, g.invCell, g.nx);
-        cy = cellCoord(q0.y, g.oy, g.invCell, g.ny);
-        cz = cellCoord(q0.z, g.oz, g.invCell, g.nz);
+    float4 q0[kQ], q1[kQ], q2[kQ];
+    int cx[kQ], cy[kQ], cz[kQ];
+    bool valid[kQ], pending[kQ];
+    float sx[kQ], sy[kQ], sz[kQ];
+#pragma unroll
+    for (int j = 0; j < kQ; j++) {
+        const int64_t i = base + (int64_t)kQ * threadIdx.x + j;
+        valid[j] = i < n;
+        q0[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        q1[j] = q0[j];
+        q2[j] = q0[j];
+        cx[j] = cy[j] = cz[j] = -1;
+        if (valid[j]) {
+            q0[j] = sq[3 * i];
+            q1[j] = sq[3 * i + 1];
+            q2[j] = sq[3 * i + 2];
+            cx[j] = cellCoord(q0[j].x, g.ox, g.invCell, g.nx);
+            cy[j] = cellCoord(q0[j].y, g.oy, g.invCell, g.ny);
+            cz[j] = cellCoord(q0[j].z, g.oz, g.invCell, g.nz);
+        }
+        pending[j] = valid[j];
+        sx[j] = sy[j] = sz[j] = 0.f;
     }
     const float r2 = r * r;
-    bool pending = valid;
-    float sx = 0.f, sy = 0.f, sz = 0.f;
     unsigned long long pairs = 0, inside = 0;
     for (;;) {
-        if (threadIdx.x == 0) sLeader = kTileQ;
+        if (threadIdx.x == 0) sLeader = kTileQ * kQ;
         __syncthreads();
-        if (pending) atomicMin(&sLeader, (int)threadIdx.x);
+#pragma unroll
+        for (int j = 0; j < kQ; j++)
+            if (pending[j]) atomicMin(&sLeader, kQ * (int)threadIdx.x + j);
         __syncthreads();
         const int leader = sLeader;
-        if (leader == kTileQ) break;
-        if ((int)threadIdx.x == leader) {
-            sCx = cx;
-            sCy = cy;
-            sCz = cz;
+        if (leader == kTileQ * kQ) break;
+        if ((int)threadIdx.x == leader / kQ) {
+            const int j = leader % kQ;
+            sCx = cx[j];
+            sCy = cy[j];
+            sCz = cz[j];
         }
         __syncthreads();
-        const bool active = pending && cx == sCx && cy == sCy && cz == sCz;
+        bool active[kQ];
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < kQ; j++) {
+            active[j] = pending[j] && cx[j] == sCx && cy[j] == sCy && cz[j] == sCz;
+            any |= active[j];
+        }
         if (threadIdx.x == 0) {
             // the 3x3x3 neighbourhood of the leader's cell, buckets deduplicated
             int nk = 0;
@@ -127,41 +151,59 @@ __global__ void __launch_bounds__(kTileQ) kGatherTiled(GridDev g, const float4* 
                 const uint32_t v = cb + t;
                 int b = 0;
                 while (b + 1 < nk && sOff[b + 1] <= v) b++;
-                const int64_t j = (int64_t)sBeg[b] + (v - sOff[b]);
-                const float4 a = __ldg(&g.rec[2 * j]);
-                const float4 f = __ldg(&g.rec[2 * j + 1]);
+                const int64_t jj = (int64_t)sBeg[b] + (v - sOff[b]);
+                const float4 a = __ldg(&g.rec[2 * jj]);
+                const float4 f = __ldg(&g.rec[2 * jj + 1]);
                 const f3 nn = unpackNormal(__float_as_uint(a.w));
                 sA[t] = make_float4(a.x, a.y, a.z, nn.x);
                 sB[t] = make_float4(f.x, f.y, f.z, nn.y);
                 sC[t] = nn.z;
             }
             __syncthreads();
-            if (active) {
-                pairs += cnt;
-#pragma unroll 4
+            if (any) {
+                if (kCount) {
+#pragma unroll
+                    for (int j = 0; j < kQ; j++) pairs += active[j] ? cnt : 0;
+                }
+#pragma unroll 2
                 for (uint32_t t = 0; t < cnt; t++) {
                     const float4 a = sA[t];
-                    const float dx = a.x - q0.x, dy = a.y - q0.y, dz = a.z - q0.z;
-                    const float d2 = dx * dx + dy * dy + dz * dz;
-                    if (d2 < r2) {
+                    bool in[kQ];
+                    bool anyIn = false;
+#pragma unroll
+                    for (int j = 0; j < kQ; j++) {
+                        const float dx = a.x - q0[j].x, dy = a.y - q0[j].y, dz = a.z - q0[j].z;
+                        in[j] = active[j] && dx * dx + dy * dy + dz * dz < r2;
+                        anyIn |= in[j];
+                    }
+                    if (anyIn) {
                         const float4 b = sB[t];
-                        inside++;
-                        if (a.w * q1.x + b.w * q1.y + sC[t] * q1.z > 0.0f) {
-                            sx += b.x;
-                            sy += b.y;
-                            sz += b.z;
+                        const float c = sC[t];
+#pragma unroll
+                        for (int j = 0; j < kQ; j++) {
+                            if (!in[j]) continue;
+                            if (kCount) inside++;
+                            if (a.w * q1[j].x + b.w * q1[j].y + c * q1[j].z > 0.0f) {
+                                sx[j] += b.x;
+                                sy[j] += b.y;
+                                sz[j] += b.z;
+                            }
                         }
                     }
                 }
             }
             __syncthreads();
         }
-        if (active) pending = false;
+#pragma unroll
+        for (int j = 0; j < kQ; j++)
+            if (active[j]) pending[j] = false;
     }
-    if (valid) {
-        const float norm = 1.0f / (kPiF * kPiF * r2);
-        const float lx = q2.x * sx * norm, ly = q2.y * sy * norm, lz = q2.z * sz * norm;
-        const int64_t px = __float_as_int(q0.w);
+    const float norm = 1.0f / (kPiF * kPiF * r2);
+#pragma unroll
+    for (int j = 0; j < kQ; j++) {
+        if (!valid[j]) continue;
+        const float lx = q2[j].x * sx[j] * norm, ly = q2[j].y * sy[j] * norm, lz = q2[j].z * sz[j] * norm;
+        const int64_t px = __float_as_int(q0[j].w);
         if (kAccum) {
             out[3 * px] += lx;
             out[3 * px + 1] += ly;
@@ -172,7 +214,7 @@ __global__ void __launch_bounds__(kTileQ) kGatherTiled(GridDev g, const float4* 
             out[3 * px + 2] = lz;
         }
     }
-    if (work) {
+    if (kCount) {
         const unsigned long long wp = __reduce_add_sync(0xffffffffu, (unsigned)pairs);
         const unsigned long long wi = __reduce_add_sync(0xffffffffu, (unsigned)inside);
         if ((threadIdx.x & 31) == 0) {
@@ -209,11 +251,12 @@ cudaError_t launchGatherTiled(const GridDev& g, QueryView qv, QuerySortBufs& qs,
     // the sorted count equals the query count; the tiled kernel reads it
     // from the end of the scanned histogram
     const uint32_t* total = qs.hist.as<uint32_t>() + qs.size;
-    const unsigned blocks = (unsigned)std::max<int64_t>(1, (qv.n + kTileQ - 1) / kTileQ);
-    if (accumulate)
-        kGatherTiled<true><<<blocks, kTileQ, 0, st>>>(g, qs.sorted.as<float4>(), total, qv.n, radius, out, work);
-    else
-        kGatherTiled<false><<<blocks, kTileQ, 0, st>>>(g, qs.sorted.as<float4>(), total, qv.n, radius, out, work);
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, (qv.n + kTileQ * kQ - 1) / (kTileQ * kQ));
+    const float4* sq = qs.sorted.as<float4>();
+    if (accumulate && work) kGatherTiled<true, true><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, out, work);
+    else if (accumulate) kGatherTiled<true, false><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, out, work);
+    else if (work) kGatherTiled<false, true><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, out, work);
+    else kGatherTiled<false, false><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, out, work);
     return cudaGetLastError();
 }
 
