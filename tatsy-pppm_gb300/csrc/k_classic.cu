@@ -349,11 +349,12 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kClassicBounce(Trac
                                                                             int64_t evCap, PassCounters* ctr) {
     __shared__ int order[128];
     __shared__ QNode sTop[kTopNodes];
-    loadOrderTable(order);
-    loadTopNodes(sTop, sc.nodes, sc.numNodes);
     const int qi = bounce % 3, qo = (bounce + 1) % 3, qz = (bounce + 2) % 3;
     const int64_t n = min((int64_t)ctr->queue[qi], maxPaths);
     if (blockIdx.x == 0 && threadIdx.x == 0) ctr->queue[qz] = 0;
+    if ((int64_t)blockIdx.x * blockDim.x >= n) return;  // past the live paths
+    loadOrderTable(order);
+    loadTopNodes(sTop, sc.nodes, sc.numNodes);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
         const int64_t i = base + threadIdx.x;

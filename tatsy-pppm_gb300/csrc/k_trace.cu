@@ -179,17 +179,24 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
 // (subsurface_integrator.cc:240-327) instead: records only on BSSRDF
 // surfaces, Russian roulette there on the mean flux, and every BSDF sampled
 // with the geometric normal and draws 1, 2.
-template <bool kSss>
+// kTail: the remaining bounces of the queue in one launch. The few paths
+// left after the first bounces are long chains (inside refractive and
+// mirrored geometry) that leave most of a per-bounce launch idle; here each
+// warp carries its paths to the end (no queue output, `out` unused).
+template <bool kSss, bool kTail>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(TraceParams tp, SceneView sc, int bounce, const PathState* __restrict__ in,
                                                      PathState* __restrict__ out, int64_t maxPaths,
                                                      float4* __restrict__ dep, int64_t depCap, PassCounters* ctr) {
     __shared__ int order[128];
     __shared__ QNode sTop[kTopNodes];
-    loadOrderTable(order);
-    loadTopNodes(sTop, sc.nodes, sc.numNodes);
     const int qi = bounce % 3, qo = (bounce + 1) % 3, qz = (bounce + 2) % 3;
     const int64_t n = min((int64_t)ctr->queue[qi], maxPaths);
     if (blockIdx.x == 0 && threadIdx.x == 0) ctr->queue[qz] = 0;
+    // the grid is sized for the first bounce; blocks past the live paths of
+    // later bounces leave before staging anything (uniform per block)
+    if ((int64_t)blockIdx.x * blockDim.x >= n) return;
+    loadOrderTable(order);
+    loadTopNodes(sTop, sc.nodes, sc.numNodes);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
         const int64_t i = base + threadIdx.x;
@@ -204,11 +211,12 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
             alive = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
         }
         int traced = 0, visits = 0, tests = 0;
+        do {
         double best;
         const int slot = traverseExactWarp(sc.nodes, sc.tris, sc.rootCode, alive, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz,
                                            order, sTop, &best, &visits, &tests);
         if (alive) {
-            traced = 1;
+            traced++;
             if (tp.guided && p.pad[0] >= 0) {
                 // training record of the draw that led here: weight cos I(y) / p
                 float V = 0.0f;
@@ -279,6 +287,8 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
                 p.fx = flux.x; p.fy = flux.y; p.fz = flux.z;
                 p.rng[0] = tape.x.s[0]; p.rng[1] = tape.x.s[1]; p.rng[2] = tape.x.s[2]; p.rng[3] = tape.x.s[3];
                 p.bounce += 1;
+                if (kTail && alive)
+                    alive = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
             }
         }
         const unsigned long long di = warpAppend(store, &ctr->deposits);
@@ -286,8 +296,12 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
             dep[2 * di] = da;
             dep[2 * di + 1] = db;
         }
-        const unsigned long long oi = warpAppend(alive, &ctr->queue[qo]);
-        if (alive) out[oi] = p;
+        store = false;
+        } while (kTail && __any_sync(0xffffffffu, alive));
+        if (!kTail) {
+            const unsigned long long oi = warpAppend(alive, &ctr->queue[qo]);
+            if (alive) out[oi] = p;
+        }
         const unsigned nt = __reduce_add_sync(0xffffffffu, (unsigned)traced);
         if ((threadIdx.x & 31) == 0 && nt) atomicAdd(&ctr->photonRays, (unsigned long long)nt);
         if (tp.countTraversal) {
@@ -532,12 +546,24 @@ cudaError_t launchPhotonEmit(const TraceParams& tp, const EnvDev& env, const uin
 cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
                                PathState* out, int64_t maxPaths, float4* deposits, int64_t depositCap,
                                PassCounters* ctr, cudaStream_t st) {
+    const unsigned blocks = blocksFor(maxPaths, 128, 152 * tp.bouncePerSm);
     if (tp.sssPass)
-        kPhotonBounce<true><<<blocksFor(maxPaths, 128, 152 * tp.bouncePerSm), 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths,
-                                                                            deposits, depositCap, ctr);
+        kPhotonBounce<true, false><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths, deposits, depositCap, ctr);
     else
-        kPhotonBounce<false><<<blocksFor(maxPaths, 128, 152 * tp.bouncePerSm), 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths,
-                                                                             deposits, depositCap, ctr);
+        kPhotonBounce<false, false><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths, deposits, depositCap, ctr);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPhotonTail(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
+                             int64_t maxPaths, float4* deposits, int64_t depositCap, PassCounters* ctr,
+                             cudaStream_t st) {
+    const unsigned blocks = blocksFor(maxPaths, 128, 152 * tp.bouncePerSm);
+    if (tp.sssPass)
+        kPhotonBounce<true, true><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, nullptr, maxPaths, deposits, depositCap,
+                                                           ctr);
+    else
+        kPhotonBounce<false, true><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, nullptr, maxPaths, deposits, depositCap,
+                                                            ctr);
     return cudaGetLastError();
 }
 

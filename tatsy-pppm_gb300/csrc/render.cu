@@ -303,8 +303,11 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
             launches += rs.guide.trained ? 3 : 1;
         }
         PPPM_CUDA(c, cudaEventRecord(c->ev[5], c->stream));
-        launches += 1 + par.max_bounce_photon;
-        for (int b = 0; b < par.max_bounce_photon; b++) {
+        // per-bounce launches while the queue is wide, then one tail launch
+        // (the learned proposal needs every bounce as a queue step)
+        const int waves = tp.guided ? par.max_bounce_photon : std::min(par.max_bounce_photon, kWaveBounces);
+        launches += 1 + waves + (waves < par.max_bounce_photon ? 1 : 0);
+        for (int b = 0; b < waves; b++) {
             PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
             PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
             PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, rs.photons.as<float4>(), rs.depositCap, ctr,
@@ -314,6 +317,11 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
                 if (e) return e;
                 launches += rs.guide.trained ? 3 : 1;
             }
+        }
+        if (waves < par.max_bounce_photon) {
+            PathState* in = (waves & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
+            PPPM_CUDA(c, launchPhotonTail(tp, sv, waves, in, paths, rs.photons.as<float4>(), rs.depositCap, ctr,
+                                          c->stream));
         }
         PPPM_CUDA(c, cudaEventRecord(c->ev[6], c->stream));
         if (attempt == 0 && rs.sss.enabled) {

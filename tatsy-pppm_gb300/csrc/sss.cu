@@ -46,6 +46,22 @@ void packPointQueries(const std::vector<float>& p, const std::vector<float>& n, 
     }
 }
 
+// The subsurface photon bounces: a few wavefront launches, then the tail.
+int tracePhotonsTo(pppm_ctx* c, const TraceParams& tp, const SceneView& sv, int64_t paths, float4* dep, int64_t cap,
+                   PassCounters* ctr, int64_t* launches) {
+    RenderState& rs = c->rs;
+    const int waves = std::min(kSssBounceLimit, kWaveBounces);
+    for (int b = 0; b < waves; b++) {
+        PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
+        PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
+        PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, dep, cap, ctr, c->stream));
+    }
+    PathState* in = (waves & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
+    PPPM_CUDA(c, launchPhotonTail(tp, sv, waves, in, paths, dep, cap, ctr, c->stream));
+    *launches += 2 + waves;
+    return PPPM_OK;
+}
+
 double sssCell(const pppm_ctx* c, int k, int64_t stored) {
     const double area = c->bssrdfArea > 0.0 ? c->bssrdfArea : 1.0;
     const double f = c->rs.par.cell_factor >= 1.0f ? c->rs.par.cell_factor : 1.0;
@@ -101,6 +117,8 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
     TraceParams tp = base;
     tp.sssPass = 1;
     tp.maxBouncePhoton = kSssBounceLimit;
+    // the subsurface photon set keeps the reference's own sampling
+    tp.guided = 0;
     // canonical mode: an independent counter-based key for this photon set
     tp.seed = base.seed ^ 0x5bd1e995u;
     uint32_t* photonStates = compat ? rs.tapeStates.as<uint32_t>() : nullptr;
@@ -125,12 +143,10 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
     // the subsurface photon pass
     PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
     PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
-    for (int b = 0; b < kSssBounceLimit; b++) {
-        PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
-        PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
-        PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, s.photons.as<float4>(), s.cap, ctr, c->stream));
+    {
+        const int e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches);
+        if (e) return e;
     }
-    *launches += 1 + kSssBounceLimit;
 
     // points on the GPU after the photon pass
     int64_t m = 0;
@@ -155,12 +171,10 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
         PPPM_CUDA(c, s.photons.ensure((size_t)s.cap * 32));
         PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
         PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
-        for (int b = 0; b < kSssBounceLimit; b++) {
-            PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
-            PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
-            PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, s.photons.as<float4>(), s.cap, ctr, c->stream));
+        {
+            const int e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches);
+            if (e) return e;
         }
-        *launches += 1 + kSssBounceLimit;
         PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
         PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
         if ((int64_t)hc.deposits > s.cap) return fail(c, PPPM_E_CAPACITY, "render_pass: subsurface photon overflow");

@@ -125,6 +125,17 @@ cudaError_t launchPhotonEmit(const TraceParams& tp, const EnvDev& env, const uin
 cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
                                PathState* out, int64_t maxPaths, float4* deposits, int64_t depositCap,
                                PassCounters* ctr, cudaStream_t st);
+// The bounces from `bounce` on of the queue left after the wavefront
+// launches, in one launch (kPhotonBounce<.., true>).
+cudaError_t launchPhotonTail(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
+                             int64_t maxPaths, float4* deposits, int64_t depositCap, PassCounters* ctr,
+                             cudaStream_t st);
+// Bounces traced as one launch each before the tail kernel takes the rest.
+#ifndef PPPM_WAVE_BOUNCES
+#define PPPM_WAVE_BOUNCES 2
+#endif
+constexpr int kWaveBounces = PPPM_WAVE_BOUNCES;
+
 cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
                            const OctView& oct, const uint32_t* pixelStates, float* accum, float4* queries,
                            float4* sssQ, int64_t sssCap, PassCounters* ctr, cudaStream_t st);

@@ -90,9 +90,9 @@ def render(photons=1_000_000, width=960, height=540, passes=3):
                                 max_bounce_eye=12, radius_scale=1 / 64, seed=1)
     ctx.render_begin(sc.camera, par)
     out = [ctx.render_pass(t + 1).as_dict() for t in range(passes)]
-    keys = ("ms_photon", "ms_bounce", "ms_grid", "ms_eye", "ms_gather")
+    keys = ("ms_photon", "ms_bounce", "ms_grid", "ms_eye", "ms_gather", "photon_rays", "eye_rays", "photons_stored")
     print(json.dumps({"case": "render", "photons": photons, "w": width, "h": height,
-                      **{k: out[-1][k] for k in keys}}))
+                      **{k: out[k2][k] for k2 in (-1,) for k in keys}, "photon_rays_per_pass": [o["photon_rays"] for o in out]}))
 
 
 def subsurface(passes=3):
