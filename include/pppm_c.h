@@ -225,6 +225,14 @@ int pppm_gather(pppm_ctx* ctx, int32_t mode, const float* photons, int64_t n, in
  * (vector3d.cc:11-16). d2: n floats, rgb: n x 3. */
 int pppm_dipole_rd(pppm_ctx* ctx, const pppm_material* mat, const float* d2, int64_t n, float* rgb);
 
+/* Device self-check of the dipole's fast_exp (vector3d.cc:11-16): the
+ * render evaluates it in 64-bit integer arithmetic for |y| <= 700 (FP64 runs
+ * at a small fraction of the FP32 rate on this GPU) and in double outside.
+ * Over the float bit patterns [begin, end) (end <= 2^32) counts the
+ * arguments the integer form covers and, of those, the ones whose result
+ * differs in any bit from the double form. */
+int pppm_fast_exp_check(pppm_ctx* ctx, uint64_t begin, uint64_t end, uint64_t* covered, uint64_t* differ);
+
 /* Replaces SubsurfaceIntegrator::irradiance (subsurface_integrator.cc:234-238)
  * over an octree built like Octree::construct (subsurface_integrator.cc:67-145)
  * from n irradiance points of 10 floats (pos xyz, normal xyz, area,

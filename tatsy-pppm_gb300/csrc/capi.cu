@@ -115,13 +115,19 @@ int pppm_create(int device, pppm_ctx** out) {
     pppm_ctx* c = new (std::nothrow) pppm_ctx();
     if (!c) return PPPM_E_CAPACITY;
     c->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // the main stream (photon pass, grid, gather: the critical path of a
+    // pass) outranks the side stream's eye trace when both have blocks
+    // waiting for an SM
+    int leastPrio = 0, greatestPrio = 0;
+    if (cudaSetDevice(device) != cudaSuccess || cudaDeviceGetStreamPriorityRange(&leastPrio, &greatestPrio) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, greatestPrio) != cudaSuccess) {
         cudaGetLastError();
         delete c;
         return PPPM_E_CUDA;
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
     cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
+    cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, leastPrio);
     cudaEventCreateWithFlags(&c->rs.sss.done, cudaEventDisableTiming);
     {
         XorShift x;
@@ -140,6 +146,10 @@ int pppm_destroy(pppm_ctx* c) {
         if (e) cudaEventDestroy(e);
     if (c->rs.sss.done) cudaEventDestroy(c->rs.sss.done);
     if (c->aux) cudaStreamDestroy(c->aux);
+    if (c->side) {
+        cudaStreamSynchronize(c->side);
+        cudaStreamDestroy(c->side);
+    }
     cudaStreamDestroy(c->stream);
     delete c;
     return PPPM_OK;

@@ -214,6 +214,7 @@ struct pppm_ctx {
     // lives as long as the process there and as long as the context here
     uint32_t poissonRng[4] = {0, 0, 0, 0};
     cudaStream_t aux = nullptr;        // readbacks that overlap the main stream
+    cudaStream_t side = nullptr;       // eye paths traced beside the photon pass
     // env
     bool hasEnv = false;
     int envW = 0, envH = 0;
@@ -230,7 +231,9 @@ struct pppm_ctx {
     pppm::GridBufs stageGrid;
     pppm::QuerySortBufs stageQsort;
     pppm::PoissonGpu stagePoisson;
-    cudaEvent_t ev[8] = {};
+    // stage timing: 0-7 main stream; 8 fork of the side stream, 9-10 its
+    // eye trace
+    cudaEvent_t ev[11] = {};
 };
 
 namespace pppm {

@@ -30,10 +30,103 @@ struct OctView {
     float maxError;  // 0.05 in the render (ppm_probabilistic.cc:84)
 };
 
-// fast_exp(y) of the reference for a float argument.
-__device__ __forceinline__ float fastExpRef(float y) {
+// fast_exp(y) of the reference for a float argument, formed in double:
+// (float) of the double whose high word is (int)(1512775 y + 1072632447).
+__device__ __forceinline__ float fastExpRefD(float y) {
     const int hi = __double2int_rz(__fma_rn(1512775.0, (double)y, 1072632447.0));
     return (float)__hiloint2double(hi, 0);
+}
+
+// The same function in 64-bit integer arithmetic, for |y| <= 700 (every
+// argument of the dipole: y = -sigma_tr d <= 0); other arguments return
+// false. With y = M 2^-k (M the 24-bit significand), S = 1512775 y +
+// 1072632447 is n + f exactly; its double rounding moves it up to n + 1
+// only when the distance to n + 1 is at most half a unit in the last place
+// of S, 2^(L - 53) with L = floor(log2 n), ties going to n + 1 (its
+// significand is even). The double (hi, 0) is then narrowed to float by
+// hand: its 20 significand bits fit, exponents below the float range give
+// denormals rounded to nearest even.
+__host__ __device__ inline bool fastExpRefInt(float y, float* out) {
+    uint32_t b;
+#ifdef __CUDA_ARCH__
+    b = __float_as_uint(y);
+#else
+    __builtin_memcpy(&b, &y, 4);
+#endif
+    const uint32_t ex = (b >> 23) & 0xffu, man = b & 0x7fffffu;
+    const bool neg = (b >> 31) != 0;
+    // |y| <= 700: exponent field at most 136 (700 < 2^10)
+    if (ex > 136 || (ex == 136 && man > 0x2f0000u)) return false;  // 0x2f0000: 700 = 1.3671875 * 2^9
+    constexpr int64_t kC = 1072632447;
+    int64_t hi;
+    if (ex == 0 && man == 0) {
+        hi = kC;
+    } else {
+        const uint64_t M = ex ? (uint64_t)(man | 0x800000u) : (uint64_t)man;
+        const int k = ex ? 150 - (int)ex : 149;  // y = M 2^-k, k >= 14
+        const uint64_t P = 1512775ull * M;        // < 2^45
+        const uint64_t q = k >= 64 ? 0 : P >> k;
+        const uint64_t r = k >= 64 ? P : P & ((1ull << k) - 1);
+        if (r == 0) {
+            hi = neg ? kC - (int64_t)q : kC + (int64_t)q;
+        } else {
+            // S in (n, n + 1): n = C + q (y > 0) or C - q - 1 (y < 0), n >= 2^23
+            const int64_t n = neg ? kC - (int64_t)q - 1 : kC + (int64_t)q;
+#ifdef __CUDA_ARCH__
+            const int L = 63 - __clzll(n);
+#else
+            const int L = 63 - __builtin_clzll((unsigned long long)n);
+#endif
+            const int t = k + L - 53;
+            bool up;
+            if (t < 0) {
+                up = false;  // the distance to n + 1 is at least 2^-k > 2^t
+            } else if (neg) {
+                // distance r 2^-k <= 2^(t - k)
+                up = t >= 45 || r <= (1ull << t);
+            } else {
+                // distance (2^k - r) 2^-k; k >= 64 leaves it above 2^(k-1) > 2^t
+                up = k < 64 && ((1ull << k) - r) <= (1ull << t);
+            }
+            hi = n + (up ? 1 : 0);
+        }
+    }
+    // hi in (0, 2^31): a positive finite double with exponent field Ed
+    const uint32_t h = (uint32_t)hi;
+    const int Ed = (int)(h >> 20);
+    const uint32_t m20 = h & 0xfffffu;
+    const int Ef = Ed - 896;  // float exponent field (1023 - 127)
+    uint32_t fb;
+    if (Ef >= 255) {
+        fb = 0x7f800000u;  // above the float range: +inf
+    } else if (Ef >= 1) {
+        fb = ((uint32_t)Ef << 23) | (m20 << 3);
+    } else {
+        // denormal: (2^20 + m20) 2^(Ed - 894) units of 2^-149
+        const uint64_t v = (1ull << 20) | m20;
+        const int sh = 894 - Ed;
+        if (sh <= 0) {
+            fb = (uint32_t)(v << -sh);
+        } else if (sh > 22) {
+            fb = 0;  // below half the smallest denormal (v < 2^21)
+        } else {
+            uint64_t mq = v >> sh;
+            const uint64_t rem = v & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+            if (rem > half || (rem == half && (mq & 1))) mq++;
+            fb = (uint32_t)mq;
+        }
+    }
+#ifdef __CUDA_ARCH__
+    *out = __uint_as_float(fb);
+#else
+    __builtin_memcpy(out, &fb, 4);
+#endif
+    return true;
+}
+
+__device__ __forceinline__ float fastExpRef(float y) {
+    float v;
+    return fastExpRefInt(y, &v) ? v : fastExpRefD(y);
 }
 
 __device__ __forceinline__ f3 dipoleRd(const DipoleDev& m, float d2) {

@@ -32,6 +32,29 @@ __global__ void kDipoleIrradiance(OctView o, DipoleDev m, const float* __restric
     out[3 * i + 2] = s.z;
 }
 
+// Both forms of fast_exp over the float bit patterns [begin, end): count
+// of arguments the integer form covers and of covered arguments whose
+// results differ in any bit.
+__global__ void kFastExpCheck(uint64_t begin, uint64_t end, unsigned long long* counts) {
+    unsigned long long covered = 0, differ = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t b = begin + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < end; b += stride) {
+        const float y = __uint_as_float((uint32_t)b);
+        float v;
+        if (!fastExpRefInt(y, &v)) continue;
+        covered++;
+        if (__float_as_uint(v) != __float_as_uint(fastExpRefD(y))) differ++;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        covered += __shfl_xor_sync(0xffffffffu, covered, o);
+        differ += __shfl_xor_sync(0xffffffffu, differ, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&counts[0], covered);
+        atomicAdd(&counts[1], differ);
+    }
+}
+
 }  // namespace
 
 }  // namespace pppm
@@ -89,6 +112,23 @@ int pppm_dipole_irradiance(pppm_ctx* c, const pppm_material* mat, const float* i
     PPPM_CUDA(c, cudaGetLastError());
     if ((r = finishOut(c, rgb, dout, (size_t)m * 12))) return r;
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PPPM_OK;
+}
+
+int pppm_fast_exp_check(pppm_ctx* c, uint64_t begin, uint64_t end, uint64_t* covered, uint64_t* differ) {
+    if (!c || !covered || !differ || begin > end || end > (1ull << 32))
+        return fail(c, PPPM_E_ARG, "fast_exp_check: bad arguments");
+    cudaSetDevice(c->device);
+    PPPM_CUDA(c, c->stageCount.ensure(16));
+    unsigned long long* d = c->stageCount.as<unsigned long long>();
+    PPPM_CUDA(c, cudaMemsetAsync(d, 0, 16, c->stream));
+    if (end > begin) kFastExpCheck<<<152 * 8, 256, 0, c->stream>>>(begin, end, d);
+    PPPM_CUDA(c, cudaGetLastError());
+    unsigned long long h[2];
+    PPPM_CUDA(c, cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, c->stream));
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    *covered = h[0];
+    *differ = h[1];
     return PPPM_OK;
 }
 

@@ -293,9 +293,41 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         launches += 1;
     }
     PassCounters hc;
-    for (int attempt = 0;; attempt++) {
-        PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters) + 8 * (size_t)N, c->stream));
+    PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters) + 8 * (size_t)N, c->stream));
     PPPM_CUDA(c, cudaMemsetAsync(rs.gatherWork.p, 0, 16, c->stream));
+    // Eye paths do not depend on the photons: without subsurface scattering
+    // (whose eye pass reads this pass's octree) they are traced on the side
+    // stream while the photon pass runs, filling the SMs its long late
+    // chains leave idle.
+    const bool sideEye = !rs.sss.enabled;
+    // every exit of this function leaves the main stream behind the side
+    // stream's work, so later syncs, reallocations and passes wait for it
+    struct SideJoin {
+        pppm_ctx* c;
+        bool on = false;
+        ~SideJoin() {
+            if (on) cudaStreamWaitEvent(c->stream, c->ev[10], 0);
+        }
+    } sideJoin{c};
+    if (sideEye) {
+        PPPM_CUDA(c, cudaEventRecord(c->ev[8], c->stream));
+        PPPM_CUDA(c, cudaStreamWaitEvent(c->side, c->ev[8], 0));
+        PPPM_CUDA(c, cudaEventRecord(c->ev[9], c->side));
+        PPPM_CUDA(c, launchEyeTrace(tp, sv, ev, cd, sssView(c), pixelStates, rs.accum.as<float>(),
+                                    rs.queries.as<float4>(), rs.sss.queue.as<float4>(), rs.sss.queueCap, ctr, c->side));
+        PPPM_CUDA(c, cudaEventRecord(c->ev[10], c->side));
+        sideJoin.on = true;
+    }
+    for (int attempt = 0;; attempt++) {
+        if (attempt > 0) {
+            // the photon half of the counters (the eye half may be in flight)
+            PPPM_CUDA(c, cudaMemsetAsync(ctr->queue, 0, sizeof(ctr->queue) + sizeof(ctr->deposits), c->stream));
+            PPPM_CUDA(c, cudaMemsetAsync(&ctr->photonRays, 0, 8, c->stream));
+            PPPM_CUDA(c, cudaMemsetAsync(&ctr->undefinedEmit, 0, 8, c->stream));
+            PPPM_CUDA(c, cudaMemsetAsync(&ctr->nodeVisits[0], 0, 8, c->stream));
+            PPPM_CUDA(c, cudaMemsetAsync(&ctr->triTests[0], 0, 8, c->stream));
+            PPPM_CUDA(c, cudaMemsetAsync(perStream, 0, 8 * (size_t)N, c->stream));
+        }
         PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
         if (tp.guided) {
             const int e = guideStep(c, tp, rs.pathA.as<PathState>(), &ctr->queue[0], paths, 0);
@@ -375,8 +407,11 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     PPPM_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
 
     // eye paths and gather
-    PPPM_CUDA(c, launchEyeTrace(tp, sv, ev, cd, sssView(c), pixelStates, rs.accum.as<float>(),
-                                rs.queries.as<float4>(), rs.sss.queue.as<float4>(), rs.sss.queueCap, ctr, c->stream));
+    if (sideEye)
+        PPPM_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev[10], 0));
+    else
+        PPPM_CUDA(c, launchEyeTrace(tp, sv, ev, cd, sssView(c), pixelStates, rs.accum.as<float>(),
+                                    rs.queries.as<float4>(), rs.sss.queue.as<float4>(), rs.sss.queueCap, ctr, c->stream));
     if (rs.sss.enabled) {
         PPPM_CUDA(c, launchSubsurfaceGather(sssView(c), sv.mats, rs.sss.queue.as<float4>(), &ctr->sssQueries,
                                             rs.sss.queueCap, rs.accum.as<float>(),
@@ -421,7 +456,8 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         stats->sss_photons = rs.sss.enabled ? rs.sss.stored : 0;
         cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
         stats->ms_grid = ms;
-        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+        // with the side stream: the eye trace itself (it overlaps ms_photon)
+        cudaEventElapsedTime(&ms, sideEye ? c->ev[9] : c->ev[2], sideEye ? c->ev[10] : c->ev[3]);
         stats->ms_eye = ms;
         cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]);
         stats->ms_gather = ms;

@@ -98,6 +98,7 @@ SIGNATURES = {
     "pppm_knn": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
                   ctypes.c_int32], ctypes.c_int),
     "pppm_dipole_rd": ([_VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_fast_exp_check": ([_VP, ctypes.c_uint64, ctypes.c_uint64, _VP, _VP], ctypes.c_int),
     "pppm_dipole_irradiance": ([_VP, _VP, _VP, ctypes.c_int64, ctypes.c_double, _VP, ctypes.c_int64, _VP],
                                ctypes.c_int),
     "pppm_poisson_disk": ([_VP, _VP, ctypes.c_int64, ctypes.c_double, _VP, _VP, _VP, ctypes.c_int64, _VP],
@@ -346,6 +347,12 @@ class Context:
         out = np.zeros((d2.size, 3), np.float32)
         self._check(self.lib.pppm_dipole_rd(self.h, m.ctypes.data, d2.ctypes.data, d2.size, out.ctypes.data))
         return out
+
+    def fast_exp_check(self, begin=0, end=1 << 32):
+        cov, dif = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self.lib.pppm_fast_exp_check(self.h, ctypes.c_uint64(begin), ctypes.c_uint64(end),
+                                                 ctypes.byref(cov), ctypes.byref(dif)))
+        return cov.value, dif.value
 
     def dipole_irradiance(self, mat, ipts10, max_error, queries):
         ip = np.ascontiguousarray(ipts10, np.float32).reshape(-1, 10)

@@ -43,3 +43,14 @@ def test_dipole_irradiance(ctx, golden, k, e):
     # where a threshold decision flipped, the result is still the same sum to
     # within the approximation the threshold controls
     assert np.all(np.abs(out - ref) <= 0.05 * np.abs(ref) + 1e-6 * scale)
+
+
+def test_fast_exp_integer_form_exhaustive(ctx):
+    # every float argument: the integer form used by the render agrees bit
+    # for bit with the double form wherever it applies (|y| <= 700)
+    covered, differ = ctx.fast_exp_check(0, 1 << 32)
+    assert differ == 0
+    # 0 and the floats of (0, 700] in both signs
+    n_pos = int(np.array([700.0], np.float32).view(np.uint32)[0])
+    assert covered == 2 * (n_pos + 1)
+
