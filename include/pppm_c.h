@@ -134,7 +134,7 @@ typedef struct {
     int64_t sss_points;      /* subsurface irradiance points (Poisson-disc samples) of this pass */
     int64_t sss_photons;     /* subsurface photons stored */
     double ms_subsurface;    /* subsurface stage before the photon pass (ms, includes host sampling) */
-    double ms_subsurface_host; /* of which host Poisson sampling + octree build (ms) */
+    double ms_subsurface_host; /* host time of the octree build loop (level syncs; overlaps the photon pass) (ms) */
     double ms_train;         /* learned proposal: training after this pass (ms) */
     double train_loss;       /* learned proposal: loss of the last training step */
     int64_t train_records;   /* learned proposal: records available to the last training */

@@ -126,9 +126,12 @@ int pppm_create(int device, pppm_ctx** out) {
         return PPPM_E_CUDA;
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
-    cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
+    // the octree build's short level kernels on the aux stream interleave
+    // with the photon pass instead of waiting behind it
+    cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, greatestPrio);
     cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, leastPrio);
     cudaEventCreateWithFlags(&c->rs.sss.done, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->rs.sss.octDone, cudaEventDisableTiming);
     {
         XorShift x;
         x.seed(0u);
@@ -145,6 +148,7 @@ int pppm_destroy(pppm_ctx* c) {
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->rs.sss.done) cudaEventDestroy(c->rs.sss.done);
+    if (c->rs.sss.octDone) cudaEventDestroy(c->rs.sss.octDone);
     if (c->aux) cudaStreamDestroy(c->aux);
     if (c->side) {
         cudaStreamSynchronize(c->side);

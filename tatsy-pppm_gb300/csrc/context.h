@@ -91,6 +91,26 @@ struct PoissonGpu {
 };
 
 // Subsurface stage of a render (SubsurfaceIntegrator, rebuilt every pass).
+// Scratch and output of the GPU octree build (k_octree.cu).
+struct OctreeBufs {
+    DBuf idx, active, big, chunks, chunkCnt, box, nodes, acc, ctr;
+    DBuf out;  // OctNodeDev per node, preorder
+    HostPinned hostCtr;
+    int64_t nodeCap = 0;
+};
+
+// Irradiance points of an octree build (device): position and irradiance
+// (3 floats each, `stride` floats apart) and area (per point or constant).
+struct OctreePoints {
+    const float* pos;
+    int posStride;
+    const float* irad;
+    int iradStride;
+    const float* area;  // null: areaConst for every point
+    int areaStride;
+    double areaConst;
+};
+
 struct SssState {
     bool enabled = false;
     double areaRadius = 0.0;  // sqrt(BSSRDF area / all triangles) (ppm_probabilistic.cc:35-46)
@@ -103,15 +123,15 @@ struct SssState {
     DBuf points;              // 3 x float4 per irradiance point (gather query layout)
     DBuf ptsD, nrmD;          // float3 per point
     DBuf irad;                // float3 per point
-    DBuf octree;              // OctNodeDev per node
+    OctreeBufs oct;           // octree of the points (GPU build)
     int octNodes = 0;
     DBuf queue;               // eye-pass subsurface queries: 2 float4 each
     int64_t queueCap = 0;
-    HostPinned hostBuf;       // points, normals and irradiance read back for the octree
     int64_t numPoints = 0;
     int64_t stored = 0;
-    double msHost = 0.0;      // host time of Poisson sampling and octree build
-    cudaEvent_t done = nullptr;  // irradiance of the points computed
+    double msHost = 0.0;      // host time of the octree build loop
+    cudaEvent_t done = nullptr;     // irradiance of the points computed
+    cudaEvent_t octDone = nullptr;  // octree written
 };
 
 // Learned photon proposal of a canonical render (PPPM_FLAG_LEARNED).
@@ -231,6 +251,7 @@ struct pppm_ctx {
     pppm::GridBufs stageGrid;
     pppm::QuerySortBufs stageQsort;
     pppm::PoissonGpu stagePoisson;
+    pppm::OctreeBufs stageOct;
     // stage timing: 0-7 main stream; 8 fork of the side stream, 9-10 its
     // eye trace
     cudaEvent_t ev[11] = {};
@@ -242,6 +263,12 @@ inline int fail(pppm_ctx* c, int code, const std::string& msg) {
     if (c) c->err = msg;
     return code;
 }
+
+// Octree of n irradiance points on stream st (k_octree.cu): the tree of the
+// reference's Octree::construct in preorder, in b.out; *numNodes its size.
+// Synchronises st a few times (level counts).
+int octreeBuild(pppm_ctx* c, OctreeBufs& b, const OctreePoints& pts, int64_t n, cudaStream_t st, int* numNodes,
+                int64_t* launches);
 
 inline int cudaFail(pppm_ctx* c, cudaError_t e, const char* where) {
     return fail(c, PPPM_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));

@@ -278,147 +278,3 @@ int decodeHdr(const uint8_t* bytes, int64_t n, float* rgb, int64_t capFloats, in
 }
 
 }  // namespace pppm
-
-namespace pppm {
-namespace {
-
-struct OctBuilder {
-    const double* P;
-    std::vector<HostOctNode> nodes;
-    struct Acc {
-        double pos[3], normal[3], area, irad[3];
-    };
-    std::vector<Acc> acc;  // double node values, parallel to `nodes`
-    bool degenerate = false;
-
-    std::vector<int64_t> idx, tmp;  // point indices, partitioned in place per node
-
-    // Node over idx[lo, hi); returns its index or -1 for an empty set. The
-    // child sets are those of the reference (membership only matters: the
-    // boxes are min/max and a leaf holds one point).
-    int rec(int64_t lo, int64_t hi, const double* bmin, const double* bmax, int depth) {
-        if (lo == hi) return -1;
-        const int self = (int)nodes.size();
-        nodes.push_back(HostOctNode());
-        acc.push_back(Acc());
-        for (int d = 0; d < 3; d++) {
-            nodes[self].bmin[d] = (float)bmin[d];
-            nodes[self].bmax[d] = (float)bmax[d];
-        }
-        if (hi - lo == 1) {
-            const double* p = P + 10 * idx[lo];
-            Acc& a = acc[self];
-            for (int d = 0; d < 3; d++) {
-                a.pos[d] = p[d];
-                a.normal[d] = p[3 + d];
-                a.irad[d] = p[7 + d];
-            }
-            a.area = p[6];
-            nodes[self].leaf = 1;
-            nodes[self].skip = (int)nodes.size();
-            return self;
-        }
-        if (depth > 4096 || (bmin[0] == bmax[0] && bmin[1] == bmax[1] && bmin[2] == bmax[2])) {
-            degenerate = true;  // identical points: the reference never terminates
-            nodes[self].leaf = 1;
-            nodes[self].skip = (int)nodes.size();
-            return self;
-        }
-        const double mid[3] = {(bmin[0] + bmax[0]) * 0.5, (bmin[1] + bmax[1]) * 0.5, (bmin[2] + bmax[2]) * 0.5};
-        // 8-way partition into child ranges, each with its tight box
-        int64_t cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        double cmn[8][3], cmx[8][3];
-        for (int c = 0; c < 8; c++)
-            for (int d = 0; d < 3; d++) { cmn[c][d] = 1e20; cmx[c][d] = -1e20; }  // BBox() then merge
-        for (int64_t k = lo; k < hi; k++) {
-            const double* v = P + 10 * idx[k];
-            const int id = (v[0] < mid[0] ? 0 : 4) + (v[1] < mid[1] ? 0 : 2) + (v[2] < mid[2] ? 0 : 1);
-            cnt[id]++;
-            for (int d = 0; d < 3; d++) {
-                cmn[id][d] = std::min(cmn[id][d], v[d]);
-                cmx[id][d] = std::max(cmx[id][d], v[d]);
-            }
-        }
-        int64_t start[9];
-        start[0] = lo;
-        for (int c = 0; c < 8; c++) start[c + 1] = start[c] + cnt[c];
-        int64_t cur[8];
-        for (int c = 0; c < 8; c++) cur[c] = start[c];
-        for (int64_t k = lo; k < hi; k++) {
-            const double* v = P + 10 * idx[k];
-            const int id = (v[0] < mid[0] ? 0 : 4) + (v[1] < mid[1] ? 0 : 2) + (v[2] < mid[2] ? 0 : 1);
-            tmp[cur[id]++] = idx[k];
-        }
-        std::copy(tmp.begin() + lo, tmp.begin() + hi, idx.begin() + lo);
-        int ch[8];
-        for (int c = 0; c < 8; c++) ch[c] = rec(start[c], start[c + 1], cmn[c], cmx[c], depth + 1);
-        // accumulation of the children (subsurface_integrator.cc:123-144)
-        Acc a;
-        std::memset(&a, 0, sizeof(a));
-        double weight = 0.0;
-        int count = 0;
-        for (int c = 0; c < 8; c++) {
-            if (ch[c] < 0) continue;
-            const Acc& k = acc[ch[c]];
-            const double w = k.irad[0] * 0.2126 + k.irad[1] * 0.7152 + k.irad[2] * 0.0722;
-            for (int d = 0; d < 3; d++) {
-                a.pos[d] = a.pos[d] + k.pos[d] * w;
-                a.normal[d] = a.normal[d] + k.normal[d] * w;
-                a.irad[d] = a.irad[d] + k.irad[d];
-            }
-            a.area += k.area;
-            weight += w;
-            count += 1;
-        }
-        if (weight > 0.0) {
-            const double inv = 1.0 / weight;
-            for (int d = 0; d < 3; d++) {
-                a.pos[d] *= inv;
-                a.normal[d] *= inv;
-            }
-        }
-        if (count != 0) {
-            const double inv = 1.0 / count;
-            for (int d = 0; d < 3; d++) a.irad[d] *= inv;
-        }
-        acc[self] = a;
-        nodes[self].leaf = 0;
-        nodes[self].skip = (int)nodes.size();
-        return self;
-    }
-};
-
-}  // namespace
-
-bool buildOctree(const double* pts10, int64_t n, std::vector<HostOctNode>* out, std::string* err) {
-    OctBuilder b;
-    b.P = pts10;
-    b.idx.resize((size_t)n);
-    b.tmp.resize((size_t)n);
-    b.nodes.reserve((size_t)(2 * n + 1));
-    b.acc.reserve((size_t)(2 * n + 1));
-    double mn[3] = {1e20, 1e20, 1e20}, mx[3] = {-1e20, -1e20, -1e20};
-    for (int64_t i = 0; i < n; i++) {
-        b.idx[i] = i;
-        for (int d = 0; d < 3; d++) {
-            mn[d] = std::min(mn[d], pts10[10 * i + d]);
-            mx[d] = std::max(mx[d], pts10[10 * i + d]);
-        }
-    }
-    b.rec(0, n, mn, mx, 0);
-    if (b.degenerate) {
-        *err = "octree: repeated irradiance points (the reference recursion does not terminate)";
-        return false;
-    }
-    for (size_t k = 0; k < b.nodes.size(); k++) {
-        for (int d = 0; d < 3; d++) {
-            b.nodes[k].pos[d] = (float)b.acc[k].pos[d];
-            b.nodes[k].irad[d] = (float)b.acc[k].irad[d];
-        }
-        b.nodes[k].area = (float)b.acc[k].area;
-    }
-    out->swap(b.nodes);
-    return true;
-}
-
-}  // namespace pppm

@@ -34,26 +34,3 @@ void envImportance(const float* rgb, int w, int h, std::vector<double>* pdf, std
 int decodeHdr(const uint8_t* bytes, int64_t n, float* rgb, int64_t capFloats, int* w, int* h);
 
 }  // namespace pppm
-
-namespace pppm {
-
-// One octree node in preorder (children follow their parent; `skip` is the
-// index after the node's subtree), the layout the GPU walks without a stack.
-struct HostOctNode {
-    float pos[3], area;
-    float irad[3];
-    int skip;
-    float bmin[3];
-    int leaf;
-    float bmax[3];
-    int pad;
-};
-
-// SubsurfaceIntegrator::Octree::construct / constructRec
-// (subsurface_integrator.cc:67-145) over irradiance points given as 10
-// doubles each (pos, normal, area, irad). Returns false when points repeat
-// exactly (the reference then recurses without end).
-bool buildOctree(const double* pts10, int64_t n, std::vector<HostOctNode>* out, std::string* err);
-
-
-}  // namespace pppm

@@ -1,15 +1,12 @@
 // Stage entry points of the dipole BSSRDF: Rd tables and the hierarchical
-// irradiance over injected irradiance points (octree built on the host).
+// irradiance over injected irradiance points (octree built by k_octree.cu).
 #include <cmath>
 #include <cstring>
 
 #include "context.h"
 #include "dipole.cuh"
-#include "host_build.h"
 
 namespace pppm {
-
-static_assert(sizeof(OctNodeDev) == sizeof(HostOctNode), "octree node layout");
 
 namespace {
 
@@ -85,28 +82,20 @@ int pppm_dipole_irradiance(pppm_ctx* c, const pppm_material* mat, const float* i
         return fail(c, PPPM_E_ARG, "dipole_irradiance: bad arguments");
     if (m == 0) return PPPM_OK;
     cudaSetDevice(c->device);
-    // irradiance points to host doubles for the octree build
-    std::vector<float> hp((size_t)n * 10);
-    if (n > 0) {
-        if (isDevicePtr(ipts)) {
-            PPPM_CUDA(c, cudaMemcpy(hp.data(), ipts, hp.size() * 4, cudaMemcpyDeviceToHost));
-        } else {
-            std::memcpy(hp.data(), ipts, hp.size() * 4);
-        }
-    }
-    std::vector<double> pd(hp.begin(), hp.end());
-    std::vector<HostOctNode> nodes;
-    std::string err;
-    if (n > 0 && !buildOctree(pd.data(), n, &nodes, &err)) return fail(c, PPPM_E_UNDEFINED, "dipole_irradiance: " + err);
-    PPPM_CUDA(c, c->stageRec.ensure(std::max<size_t>(nodes.size(), 1) * sizeof(OctNodeDev)));
-    if (!nodes.empty())
-        PPPM_CUDA(c, cudaMemcpy(c->stageRec.p, nodes.data(), nodes.size() * sizeof(OctNodeDev), cudaMemcpyHostToDevice));
+    const void* dp = nullptr;
+    int r;
+    if (n > 0 && (r = stageIn(c, ipts, (size_t)n * 40, 2, &dp))) return r;
+    const float* P = static_cast<const float*>(dp);
+    // IrradiancePoint rows: pos xyz, normal xyz, area, irradiance rgb
+    const OctreePoints op{P, 10, P ? P + 7 : nullptr, 10, P ? P + 6 : nullptr, 10, 0.0};
+    int numNodes = 0;
+    int64_t launches = 0;
+    if ((r = octreeBuild(c, c->stageOct, op, n, c->stream, &numNodes, &launches))) return r;
     const void* dq;
     void* dout;
-    int r;
     if ((r = stageIn(c, queries, (size_t)m * 12, 0, &dq))) return r;
     if ((r = stageOut(c, rgb, (size_t)m * 12, 1, &dout))) return r;
-    const OctView ov{c->stageRec.as<OctNodeDev>(), (int)nodes.size(), (float)maxError};
+    const OctView ov{numNodes > 0 ? c->stageOct.out.as<OctNodeDev>() : nullptr, numNodes, (float)maxError};
     kDipoleIrradiance<<<(unsigned)((m + 127) / 128), 128, 0, c->stream>>>(ov, dipoleFrom(*mat), (const float*)dq, m,
                                                                           (float*)dout);
     PPPM_CUDA(c, cudaGetLastError());

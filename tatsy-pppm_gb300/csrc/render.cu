@@ -357,8 +357,8 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         }
         PPPM_CUDA(c, cudaEventRecord(c->ev[6], c->stream));
         if (attempt == 0 && rs.sss.enabled) {
-            // octree on the host while the GPU traces this pass's photons
-            const int e = sssFinish(c);
+            // octree build beside this pass's photons
+            const int e = sssFinish(c, &launches);
             if (e) return e;
         }
         PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));

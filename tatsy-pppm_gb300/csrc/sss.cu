@@ -10,15 +10,14 @@
 //   3. irradiance at the points: irradianceWithPM (subsurface_integrator.cc:
 //      329-365), the compat kNN gather with k = (int)gatherRadius,
 //      epsilon = #photons and the normal filter gatherPhotons^2 * 0.01;
-//   4. octree over the points (host, constructRec's splits) while the GPU
-//      traces the pass's main photons; uploaded before the eye pass.
+//   4. octree over the points (k_octree.cu, constructRec's tree) on the aux
+//      stream while the pass's main photons are traced.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 
 #include "context.h"
-#include "host_build.h"
 #include "trace.h"
 
 namespace pppm {
@@ -204,47 +203,25 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
     return PPPM_OK;
 }
 
-int sssFinish(pppm_ctx* c) {
+int sssFinish(pppm_ctx* c, int64_t* launches) {
     SssState& s = c->rs.sss;
-    const int64_t m = s.numPoints;
     const auto t0 = std::chrono::steady_clock::now();
-    std::vector<HostOctNode> nodes;
-    if (m > 0) {
-        PPPM_CUDA(c, s.hostBuf.ensure((size_t)m * 36));
-        float* hp = s.hostBuf.as<float>();
-        PPPM_CUDA(c, cudaStreamWaitEvent(c->aux, s.done, 0));
-        PPPM_CUDA(c, cudaMemcpyAsync(hp, s.ptsD.p, (size_t)m * 12, cudaMemcpyDeviceToHost, c->aux));
-        PPPM_CUDA(c, cudaMemcpyAsync(hp + 3 * m, s.nrmD.p, (size_t)m * 12, cudaMemcpyDeviceToHost, c->aux));
-        PPPM_CUDA(c, cudaMemcpyAsync(hp + 6 * m, s.irad.p, (size_t)m * 12, cudaMemcpyDeviceToHost, c->aux));
-        PPPM_CUDA(c, cudaStreamSynchronize(c->aux));
-        // IrradiancePoint {pos, normal, dA, irad} (subsurface_integrator.cc:224-230)
-        std::vector<double> ip((size_t)m * 10);
-        for (int64_t i = 0; i < m; i++) {
-            double* q = &ip[(size_t)i * 10];
-            for (int d = 0; d < 3; d++) {
-                q[d] = hp[3 * i + d];
-                q[3 + d] = hp[3 * m + 3 * i + d];
-                q[7 + d] = hp[6 * m + 3 * i + d];
-            }
-            q[6] = s.dA;
-        }
-        std::string err;
-        if (!buildOctree(ip.data(), m, &nodes, &err)) return fail(c, PPPM_E_UNDEFINED, "render_pass: " + err);
-    }
-    s.octNodes = (int)nodes.size();
-    if (!nodes.empty()) {
-        PPPM_CUDA(c, s.octree.ensure(nodes.size() * sizeof(OctNodeDev)));
-        PPPM_CUDA(c, cudaMemcpyAsync(s.octree.p, nodes.data(), nodes.size() * sizeof(OctNodeDev), cudaMemcpyHostToDevice,
-                                     c->stream));
-        // the pageable source is consumed before the call returns
-    }
+    // on the aux stream, beside the photon pass; the main stream waits for it
+    PPPM_CUDA(c, cudaStreamWaitEvent(c->aux, s.done, 0));
+    const OctreePoints op{s.ptsD.as<float>(), 3, s.irad.as<float>(), 3, nullptr, 0, s.dA};
+    int nodes = 0;
+    const int e = octreeBuild(c, s.oct, op, s.numPoints, c->aux, &nodes, launches);
+    if (e) return e;
+    s.octNodes = nodes;
+    PPPM_CUDA(c, cudaEventRecord(s.octDone, c->aux));
+    PPPM_CUDA(c, cudaStreamWaitEvent(c->stream, s.octDone, 0));
     s.msHost += msSince(t0);
     return PPPM_OK;
 }
 
 OctView sssView(const pppm_ctx* c) {
     const SssState& s = c->rs.sss;
-    return {s.octNodes > 0 ? s.octree.as<OctNodeDev>() : nullptr, s.octNodes, 0.05f};
+    return {s.octNodes > 0 ? s.oct.out.as<OctNodeDev>() : nullptr, s.octNodes, 0.05f};
 }
 
 }  // namespace pppm

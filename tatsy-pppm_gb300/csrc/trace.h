@@ -150,10 +150,10 @@ int poissonRun(pppm_ctx* c, PoissonGpu& g, uint32_t rng[4], float4* queries, flo
                int64_t* count);
 
 // Subsurface stage of a render (sss.cu): per-render setup, the per-pass
-// photon map + points + irradiance (enqueued), and the octree upload.
+// photon map + points + irradiance (enqueued), and the octree build.
 int sssBegin(pppm_ctx* c);
 int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv, const EnvDev& ev, int64_t* launches);
-int sssFinish(pppm_ctx* c);
+int sssFinish(pppm_ctx* c, int64_t* launches);
 OctView sssView(const pppm_ctx* c);
 
 // Learned proposal (k_guide.cu): MLP inputs of the queue's pending paths,
