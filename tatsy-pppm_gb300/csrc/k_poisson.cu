@@ -142,15 +142,29 @@ __global__ void kBboxPartial(const double* __restrict__ pos, int64_t n, double* 
         for (int d = 0; d < 6; d++) part[6 * blockIdx.x + d] = s[d][0];
 }
 
+// one block of 256 threads over the partial boxes
 __global__ void kBboxFinal(const double* __restrict__ part, int nb, double* __restrict__ out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double r[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
-    for (int b = 0; b < nb; b++)
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
         for (int d = 0; d < 3; d++) {
             r[d] = fmin(r[d], part[6 * b + d]);
             r[3 + d] = fmax(r[3 + d], part[6 * b + 3 + d]);
         }
-    for (int d = 0; d < 6; d++) out[d] = r[d];
+    for (int o = 16; o > 0; o >>= 1)
+        for (int d = 0; d < 3; d++) {
+            r[d] = fmin(r[d], __shfl_xor_sync(0xffffffffu, r[d], o));
+            r[3 + d] = fmax(r[3 + d], __shfl_xor_sync(0xffffffffu, r[3 + d], o));
+        }
+    __shared__ double s[8][6];
+    if ((threadIdx.x & 31) == 0)
+        for (int d = 0; d < 6; d++) s[threadIdx.x >> 5][d] = r[d];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int d = threadIdx.x;
+        double v = s[0][d];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) v = d < 3 ? fmin(v, s[w][d]) : fmax(v, s[w][d]);
+        out[d] = v;
+    }
 }
 
 // HashGrid<int> on the candidates (hash_grid_detail.h): the bucket a
@@ -385,7 +399,7 @@ int poissonRun(pppm_ctx* c, PoissonGpu& g, uint32_t rng[4], float4* queries, flo
     const int nb = 152 * 4;
     double* bbox = g.bbox.as<double>();
     kBboxPartial<<<nb, 256, 0, st>>>(g.pos.as<double>(), n, bbox + 6);
-    kBboxFinal<<<1, 32, 0, st>>>(bbox + 6, nb, bbox);
+    kBboxFinal<<<1, 256, 0, st>>>(bbox + 6, nb, bbox);
     double hb[6];
     PPPM_CUDA(c, cudaMemcpyAsync(hb, bbox, 48, cudaMemcpyDeviceToHost, st));
     PPPM_CUDA(c, cudaStreamSynchronize(st));

@@ -4,7 +4,7 @@
   python tatsy-pppm_gb300/profile_cases.py mlp_forward [rows]
   python tatsy-pppm_gb300/profile_cases.py mlp_train [records]
   python tatsy-pppm_gb300/profile_cases.py render [photons] [width] [height]
-  python tatsy-pppm_gb300/profile_cases.py subsurface
+  python tatsy-pppm_gb300/profile_cases.py subsurface [passes] [full]
   python tatsy-pppm_gb300/profile_cases.py classic
 
 Each case builds its inputs from seeded synthetic data, runs the kernels a
@@ -95,8 +95,10 @@ def render(photons=1_000_000, width=960, height=540, passes=3):
                       **{k: out[k2][k] for k2 in (-1,) for k in keys}, "photon_rays_per_pass": [o["photon_rays"] for o in out]}))
 
 
-def subsurface(passes=3):
-    sc = S.config3(width=640, height=360, photons=1_000_000, nu=250, nv=100)
+def subsurface(passes=3, full=0):
+    """full=1: the subsurface workload's own sizes (1280x720, 2M photons,
+    200k-triangle torus); else a quarter-size case."""
+    sc = S.config3() if full else S.config3(width=640, height=360, photons=1_000_000, nu=250, nv=100)
     ctx = P.Context(0)
     ctx.set_scene(sc)
     par = P.Context.make_params(mode=P.MODE_CANONICAL, photons=sc.photons, max_bounce_photon=12,
