@@ -105,10 +105,12 @@ typedef struct {
 
 /* pppm_params.flags */
 #define PPPM_FLAG_COUNT_TRAVERSAL 0x1 /* count BVH nodes visited / triangles tested */
-#define PPPM_FLAG_LEARNED 0x2 /* canonical mode: learned photon proposal (MLP + vMF mixture, MIS with the
-                                 BSDF at a floor of 0.3, retrained every 4 passes); no reference counterpart */
-#define PPPM_FLAG_LEARNED_FROZEN 0x4 /* with PPPM_FLAG_LEARNED: the same pipeline without training (directions
-                                        from the BSDF lobe alone): the method without the network */
+#define PPPM_FLAG_LEARNED 0x2 /* canonical mode: learned photon proposal (MLP + vMF mixture, one-sample MIS
+                                 with the reference's environment sampling, and optionally with the BSDF at
+                                 Lambertian bounces, at a floor of 0.3; retrained every 4 passes); no
+                                 reference counterpart */
+#define PPPM_FLAG_LEARNED_FROZEN 0x4 /* with PPPM_FLAG_LEARNED: the same pipeline without training (the
+                                        reference's sampling alone): the method without the network */
 
 /* Per-pass statistics written by pppm_render_pass. */
 typedef struct {
@@ -278,9 +280,12 @@ int pppm_mlp_forward(pppm_ctx* ctx, const float* params, const float* pos, const
  * PPPM_FLAG_LEARNED (no counterpart in the reference). retrain_every: passes
  * between trainings (4); steps: Adam steps per training (16); batch: records
  * per step (65536); lr: Adam learning rate (1e-3); floor_bsdf: probability of
- * the BSDF lobe in the one-sample MIS mixture (0.3); max_log_kappa: upper
+ * the reference's own sampling (environment cell draw, BSDF lobe) in the
+ * one-sample MIS mixtures (0.3); max_log_kappa: upper
  * clamp of the lobes' log concentration (7); guide_bounces: 1 to guide
- * Lambertian bounces as well as emission (1). Values <= 0 keep the default. */
+ * Lambertian bounces as well as the environment direction of emission, 0 for
+ * emission only (0). Values < 0 (guide_bounces) or <= 0 (the others) keep the
+ * current setting. */
 int pppm_learned_config(pppm_ctx* ctx, int32_t retrain_every, int32_t steps, int64_t batch, float lr,
                         float floor_bsdf, float max_log_kappa, int32_t guide_bounces);
 

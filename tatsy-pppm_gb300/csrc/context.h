@@ -142,14 +142,15 @@ struct GuideState {
     int stepsPerTrain = 16;     // Adam steps per training
     int64_t batch = 65536;      // records per step
     float lr = 1e-3f;
-    float floorBsdf = 0.3f;     // one-sample MIS: BSDF lobe probability
+    float floorBsdf = 0.3f;     // one-sample MIS: probability of the reference's sampling
     float maxLogKappa = 7.0f;   // clamp of the lobes' log concentration
-    int guideBounces = 1;       // guide Lambertian bounces (1) or emission only (0)
+    int guideBounces = 0;       // guide Lambertian bounces too (1) or the emission direction only (0)
     float floorLum = 0.01f;     // luminance floor of the relative-error importance
     int adamStep = 0;
     DBuf params, adamM, adamV, grad, blob, misc;  // misc: loss, error flag, 1 / sum w
     DBuf raw;                   // network outputs per queue slot (40 floats)
     DBuf inPos, inNrm;          // network inputs per queue slot
+    DBuf emitIn, emitRaw;       // the emission input row (position, zero normal) and its 40 outputs
     DBuf rec;                   // training records
     int64_t recCap = 0;
     DBuf counters;              // record count

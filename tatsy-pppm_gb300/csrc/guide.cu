@@ -1,7 +1,7 @@
 // Host side of the learned photon proposal in a canonical render: state set
-// up at render_begin, the per-bounce network step, the importance grid after
-// the eye pass, and the retraining schedule (every 4 passes: 16 Adam steps of
-// 65,536 records at lr 1e-3).
+// up at render_begin, the emission mixture of each pass, the per-bounce
+// network step, the importance grid after the eye pass, and the retraining
+// schedule (every 4 passes: 16 Adam steps of 65,536 records at lr 1e-3).
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -67,6 +67,13 @@ int guideBegin(pppm_ctx* c, int64_t maxPaths) {
         g.box[d] = std::min(c->bbmin[d], -50.0);
         g.box[3 + d] = std::max(c->bbmax[d], 50.0);
     }
+    // the emission distribution's input: the box centre with a zero normal
+    // (surface rows carry unit normals)
+    const float ein[6] = {(float)(0.5 * (g.box[0] + g.box[3])), (float)(0.5 * (g.box[1] + g.box[4])),
+                          (float)(0.5 * (g.box[2] + g.box[5])), 0.0f, 0.0f, 0.0f};
+    PPPM_CUDA(c, g.emitIn.ensure(sizeof(ein)));
+    PPPM_CUDA(c, g.emitRaw.ensure((size_t)kMlpOut * 4));
+    PPPM_CUDA(c, cudaMemcpy(g.emitIn.p, ein, sizeof(ein), cudaMemcpyHostToDevice));
     return PPPM_OK;
 }
 
@@ -89,7 +96,25 @@ GuideView guideView(pppm_ctx* c, int64_t decisionsPerPass) {
     v.inv = g.ginv;
     v.maxLogKappa = g.maxLogKappa;
     v.guideBounces = g.guideBounces;
+    v.emitRaw = g.trained ? g.emitRaw.as<float>() : nullptr;
+    v.emitFloor = g.floorBsdf;
+    // Envmap::samplePhoton's flux factor area / (pdf numPhotons) without the pdf
+    const double area = ((double)((unsigned)c->envW * (unsigned)c->envH)) / (4.0 * 3.14159265358979323846 * 64 * 64);
+    v.emitK = (float)(area / (double)c->rs.par.photons);
+    v.epx = (float)(0.5 * (g.box[0] + g.box[3]));
+    v.epy = (float)(0.5 * (g.box[1] + g.box[4]));
+    v.epz = (float)(0.5 * (g.box[2] + g.box[5]));
     return v;
+}
+
+// The network's environment-direction mixture for this pass: one row, the
+// emission input.
+int guideEmission(pppm_ctx* c) {
+    GuideState& g = c->rs.guide;
+    const float* in = g.emitIn.as<float>();
+    PPPM_CUDA(c, launchMlpForward(mlpInputs(g.box, in, in + 3), g.blob.as<uint8_t>(), 1, g.emitRaw.as<float>(),
+                                  reinterpret_cast<int*>(g.misc.as<float>() + 1), c->stream));
+    return PPPM_OK;
 }
 
 // Directions of the pending paths of queue q (count on the device).

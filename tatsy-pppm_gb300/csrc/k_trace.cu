@@ -129,8 +129,54 @@ __global__ void kTapeStates(TraceParams tp, const uint32_t* __restrict__ streamS
     }
 }
 
+// Learned emission (canonical mode): one-sample MIS of the environment
+// direction between the reference's cell draw (probability c) and the
+// network's vMF mixture m. The density of the mixture in cell units is
+//     p = c pdf[cell(d)] + (1 - c) q_m(d) 4 pi / 4096
+// (cells are equal in solid angle and uniform inside), and the flux
+// L(d) emitK / p is the reference's L(d) area / (pdf numPhotons) with p in
+// place of pdf, so the photon set keeps the plain estimator's expectation.
+// The cosine draw of the first direction is the reference's.
+template <class TapeT>
+__device__ bool emitPhotonMis(const EnvDev& e, TapeT& tp, const VmfMix& m, float c, float emitK, f3* emitDir, f3* dir,
+                              f3* flux) {
+    const float us = tp.popf();
+    f3 d;
+    int index;
+    if (us < c) {
+        d = envCellDraw(e, tp, &index);
+        if (index >= 4096) return false;
+    } else {
+        const float u0 = tp.popf(), u1 = tp.popf(), u2 = tp.popf();
+        d = vmfMixSample(m, u0, u1, u2);
+        index = envCellOf(d);
+    }
+    const float pMix = c * (float)__ldg(&e.pdf[index]) + (1.0f - c) * vmfMixPdf(m, d) * (4.0f * kPiF / 4096.0f);
+    const float s = (pMix > 0.0f && isfinite(pMix)) ? emitK / pMix : 0.0f;
+    *flux = envLookup(e, d) * s;
+    *emitDir = d;
+    const float a0 = tp.popf();
+    const float a1 = tp.popf();
+    *dir = onHemisphere(-d, a1, a0);
+    return true;
+}
+
+__device__ inline bool vmfMixFinite(const VmfMix& m) {
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kMlpLobes; k++) s += m.w[k] + m.mu[k][0] + m.mu[k][1] + m.mu[k][2] + m.kappa[k] + m.norm[k];
+    return isfinite(s);
+}
+
 __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restrict__ photonStates,
                             PathState* __restrict__ queue, PassCounters* ctr) {
+    const GuideView& gv = tp.guide;
+    VmfMix mix;
+    bool learned = tp.guided && gv.emitRaw != nullptr;
+    if (learned) {
+        vmfMixFromRaw(gv.emitRaw, &mix, gv.maxLogKappa);
+        learned = vmfMixFinite(mix);  // a non-finite network output: the reference's sampling alone
+    }
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < tp.numPaths;
          g += (int64_t)gridDim.x * blockDim.x) {
         Tape tape;
@@ -143,7 +189,8 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
             seedCanonical(tp.seed, tp.pass, (uint64_t)g, tape.x);
         }
         f3 d, dir, flux;
-        const bool ok = emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux, tp.sssPass != 0);
+        const bool ok = learned ? emitPhotonMis(env, tape, mix, gv.emitFloor, gv.emitK, &d, &dir, &flux)
+                                : emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux, tp.sssPass != 0);
         if (!ok) atomicAdd(&ctr->undefinedEmit, 1ull);
         PathState p;
         p.ox = 50.0 * (double)d.x;  // R * dir with R = 50 (envmap.cc:63,85)
@@ -154,12 +201,24 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
         p.rng[0] = tape.x.s[0]; p.rng[1] = tape.x.s[1]; p.rng[2] = tape.x.s[2]; p.rng[3] = tape.x.s[3];
         p.id = (int)g;
         p.bounce = 0;
-        p.pad[0] = p.pad[1] = 0;
-        if (tp.guided) {
-            // the direction is drawn by kGuideResolve around the emission normal -d
-            p.dx = -d.x; p.dy = -d.y; p.dz = -d.z;
-            p.pad[0] = -1;
-            p.pad[1] = kPathNeedsDir;
+        p.pad[0] = -1;  // no pending bounce record
+        p.pad[1] = 0;
+        if (tp.guided && gv.rec && ok &&
+            mix32((uint32_t)g * 0x85EBCA77u + (uint32_t)tp.pass * 0xC2B2AE3Du + 0x27D4EB2Fu) % gv.recEvery == 0) {
+            // emission record: the network's emission input and the direction;
+            // its weight collects the importance of the path's deposits
+            const unsigned long long r = atomicAdd(gv.recCount, 1ull);
+            if ((int64_t)r < gv.recCap) {
+                MlpRecord rec;
+                rec.px = gv.epx; rec.py = gv.epy; rec.pz = gv.epz;
+                rec.w = 0.0f;
+                rec.nx = rec.ny = rec.nz = 0.0f;
+                rec.pad0 = 0.0f;
+                rec.dx = d.x; rec.dy = d.y; rec.dz = d.z;
+                rec.pad1 = 0.0f;
+                gv.rec[r] = rec;
+                p.pad[1] = (int)((r + 1) << kPathEmitRecShift);
+            }
         }
         queue[g] = p;
     }
@@ -267,6 +326,14 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
                     da = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
                                      __uint_as_float(packNormal(on)));
                     db = make_float4(flux.x, flux.y, flux.z, __int_as_float(p.id));
+                    const int er = p.pad[1] >> kPathEmitRecShift;
+                    if (tp.guided && er > 0 && tp.guide.imp) {
+                        // emission record: importance-weighted flux of this deposit
+                        const int v = impVoxel(tp.guide, da.x, da.y, da.z);
+                        if (v >= 0)
+                            tp.guide.rec[er - 1].w +=
+                                (0.2126f * flux.x + 0.7152f * flux.y + 0.0722f * flux.z) * __ldg(&tp.guide.imp[v]);
+                    }
                     if ((unsigned long long)r0 < m.rrCeil) {  // rands[0] < probability
                         if (tp.guided && tp.guide.guideBounces) {
                             nd = on;  // kGuideResolve draws the direction around the normal

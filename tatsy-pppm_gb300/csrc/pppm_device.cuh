@@ -667,6 +667,38 @@ __device__ inline f3 envLookup(const EnvDev& e, f3 d) {
     return {p[0], p[1], p[2]};
 }
 
+// The cell draw of Envmap::samplePhoton (envmap.cc:62-79): the first cell
+// whose CDF reaches the draw, then a uniform point of the cell in (u, v),
+// i.e. uniform in solid angle (y is linear in v). *index = 4096 past the CDF.
+template <class TapeT>
+__device__ inline f3 envCellDraw(const EnvDev& e, TapeT& tp, int* index) {
+    const unsigned long long r = tp.popu();
+    int lo = 0, hi = 4096;  // first index with cdf[i] >= r * 2^-32
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&e.ucdf[mid]) < r) lo = mid + 1; else hi = mid;
+    }
+    *index = lo;
+    const int ix = lo % 64, iy = lo / 64;
+    const float u = ((float)ix + tp.popf()) * (1.0f / 64.0f);
+    const float v = ((float)iy + tp.popf()) * (1.0f / 64.0f);
+    const float phi = u * kPiF * 2.0f;
+    const float y = (1.0f - v) * 2.0f - 1.0f;
+    const float sxz = sqrtf(fmaxf(0.0f, 1.0f - y * y));
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    return {sxz * cp, y, sxz * sp};
+}
+
+// The importance cell of a direction (the inverse of envCellDraw's map).
+__device__ inline int envCellOf(f3 d) {
+    float phi = atan2f(d.z, d.x);
+    if (phi < 0.0f) phi += 2.0f * kPiF;
+    const int ix = min(max((int)(phi * (64.0f / (2.0f * kPiF))), 0), 63);
+    const int iy = min(max((int)((1.0f - d.y) * 0.5f * 64.0f), 0), 63);
+    return iy * 64 + ix;
+}
+
 // Envmap::samplePhoton (envmap.cc:62-86) followed by the cosine hemisphere
 // draw of tracePhotons (ppm_probabilistic.cc:137-144). The CDF inversion is
 // std::lower_bound over the double CDF, done in double. Returns false when
@@ -676,22 +708,8 @@ __device__ inline f3 envLookup(const EnvDev& e, f3 d) {
 template <class TapeT>
 __device__ inline bool emitPhoton(const EnvDev& e, TapeT& tp, double numPhotons, f3* emitDir, f3* dir, f3* flux,
                                   bool inOrder = false) {
-    const unsigned long long r = tp.popu();
-    int lo = 0, hi = 4096;  // first index with cdf[i] >= r * 2^-32
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (__ldg(&e.ucdf[mid]) < r) lo = mid + 1; else hi = mid;
-    }
-    const int index = lo;
-    const int ix = index % 64, iy = index / 64;
-    const float u = ((float)ix + tp.popf()) * (1.0f / 64.0f);
-    const float v = ((float)iy + tp.popf()) * (1.0f / 64.0f);
-    const float phi = u * kPiF * 2.0f;
-    const float y = (1.0f - v) * 2.0f - 1.0f;
-    const float sxz = sqrtf(fmaxf(0.0f, 1.0f - y * y));
-    float sp, cp;
-    sincosf(phi, &sp, &cp);
-    const f3 d = {sxz * cp, y, sxz * sp};
+    int index;
+    const f3 d = envCellDraw(e, tp, &index);
     *flux = envLookup(e, d) * __ldg(&e.fluxScale[min(index, 4095)]);
     *emitDir = d;
     // onHemisphere(normalLight, &nextDir, rseq.pop(), rseq.pop()) in

@@ -328,23 +328,25 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
             PPPM_CUDA(c, cudaMemsetAsync(&ctr->triTests[0], 0, 8, c->stream));
             PPPM_CUDA(c, cudaMemsetAsync(perStream, 0, 8 * (size_t)N, c->stream));
         }
-        PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
-        if (tp.guided) {
-            const int e = guideStep(c, tp, rs.pathA.as<PathState>(), &ctr->queue[0], paths, 0);
+        if (tp.guided && rs.guide.trained) {
+            // the network's emission mixture for this pass
+            const int e = guideEmission(c);
             if (e) return e;
-            launches += rs.guide.trained ? 3 : 1;
+            launches += 2;
         }
+        PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
         PPPM_CUDA(c, cudaEventRecord(c->ev[5], c->stream));
         // per-bounce launches while the queue is wide, then one tail launch
-        // (the learned proposal needs every bounce as a queue step)
-        const int waves = tp.guided ? par.max_bounce_photon : std::min(par.max_bounce_photon, kWaveBounces);
+        // (guided bounces need every bounce as a queue step)
+        const bool guideBounces = tp.guided && rs.guide.guideBounces;
+        const int waves = guideBounces ? par.max_bounce_photon : std::min(par.max_bounce_photon, kWaveBounces);
         launches += 1 + waves + (waves < par.max_bounce_photon ? 1 : 0);
         for (int b = 0; b < waves; b++) {
             PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
             PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
             PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, rs.photons.as<float4>(), rs.depositCap, ctr,
                                             c->stream));
-            if (tp.guided && b + 1 < par.max_bounce_photon) {
+            if (guideBounces && b + 1 < par.max_bounce_photon) {
                 const int e = guideStep(c, tp, out, &ctr->queue[(b + 1) % 3], paths, b + 1);
                 if (e) return e;
                 launches += rs.guide.trained ? 3 : 1;

@@ -59,7 +59,13 @@ struct GuideView {
     int G;
     float ox, oy, oz, inv;         // grid origin and 1 / voxel edge
     float maxLogKappa;             // clamp of the lobes' log concentration
-    int guideBounces;              // 0: emission only
+    int guideBounces;              // 1: Lambertian bounces are guided too
+    // emission: the network's direction mixture at one fixed input (emission
+    // position epx..epz, zero normal) proposes the environment direction
+    const float* emitRaw;          // its 40 outputs, or nullptr before the first training
+    float emitFloor;               // MIS probability of the reference's environment sampling
+    float emitK;                   // area / numPhotons of Envmap::samplePhoton (flux = L emitK / p_cell)
+    float epx, epy, epz;
 };
 
 __device__ __forceinline__ int impVoxel(const GuideView& g, float x, float y, float z) {
@@ -70,6 +76,9 @@ __device__ __forceinline__ int impVoxel(const GuideView& g, float x, float y, fl
 }
 
 constexpr int kPathNeedsDir = 1;  // PathState.pad[1]: direction still to be drawn (normal in d)
+// PathState.pad[1] >> kPathEmitRecShift: 1 + index of the path's emission
+// record (0: none); its weight collects the path's importance-weighted deposits
+constexpr int kPathEmitRecShift = 8;
 
 // Compaction: each taking lane gets a slot; one atomic per warp.
 __device__ __forceinline__ unsigned long long warpAppend(bool take, unsigned long long* counter) {
@@ -99,7 +108,7 @@ struct TraceParams {
     int hasSss;   // 1: the scene has BSSRDF materials
     int bouncePerSm = 16;  // photon bounce kernel: blocks per SM (tunable)
     int eyePerSm = 16;     // eye kernel: blocks per SM (tunable)
-    int guided;   // 1: emission and Lambertian bounces leave their direction to kGuideResolve
+    int guided;   // 1: learned proposal (emission direction; Lambertian bounces through kGuideResolve)
     GuideView guide;
 };
 
@@ -173,6 +182,7 @@ GuideView guideView(pppm_ctx* c, int64_t decisionsPerPass);
 int guideStep(pppm_ctx* c, const TraceParams& tp, PathState* q, const unsigned long long* count, int64_t cap,
               int bounce);
 int guideImportance(pppm_ctx* c, const float4* queries, const unsigned long long* count, int64_t cap, int t);
+int guideEmission(pppm_ctx* c);
 int guideEndPass(pppm_ctx* c, int t);
 
 // Classic PPM (k_classic.cu).

@@ -1,11 +1,13 @@
 """The learned photon proposal inside a canonical render.
 
-The proposal must not change the estimator's expectation: with training
-switched off (PPPM_FLAG_LEARNED_FROZEN) every direction still goes through
-the MIS resolve kernel, drawn from the BSDF lobe alone, and the image must
-agree with the plain render; with training on, the image stays unbiased and
-the trained network sends more of the emitted photons into the part of the
-scene the camera sees (what it is trained for).
+The proposal must not change the estimator's expectation. Without training
+(PPPM_FLAG_LEARNED_FROZEN) the network is never used: the render is the
+plain render, draw for draw. With training on, the network proposes the
+environment direction of every photon (one-sample MIS with the reference's
+own cell sampling at a floor of 0.3) and, optionally, the directions of
+Lambertian bounces. The image must stay unbiased against a plain reference,
+and the trained proposal must lower the error of the plain method at equal
+passes: what the network gains over the method without it.
 """
 import numpy as np
 import pytest
@@ -27,9 +29,16 @@ def setup():
     c.close()
 
 
-def _render(c, sc, flags, passes, seed, photons=300_000):
-    c.learned_config(retrain_every=4, steps=16, batch=65536, lr=1e-3, floor_bsdf=0.3, max_log_kappa=4.0,
-                     guide_bounces=1)
+@pytest.fixture(scope="module")
+def reference(setup):
+    sc, c = setup
+    img, _ = _render(c, sc, 0, 1024, 99)
+    return img
+
+
+def _render(c, sc, flags, passes, seed, photons=300_000, guide_bounces=0):
+    c.learned_config(retrain_every=4, steps=16, batch=65536, lr=1e-3, floor_bsdf=0.3, max_log_kappa=7.0,
+                     guide_bounces=guide_bounces)
     par = P.Context.make_params(mode=P.MODE_CANONICAL, photons=photons, max_bounce_photon=12, max_bounce_eye=12,
                                 radius_scale=1 / 64, seed=seed, flags=flags)
     c.render_begin(sc.camera, par)
@@ -37,42 +46,56 @@ def _render(c, sc, flags, passes, seed, photons=300_000):
     return c.render_read() / passes, stats
 
 
-def _in_view(sc, pts):
-    cam = sc.camera
-    eye = np.array(cam.eye)
-    f = np.array(cam.dir) / np.linalg.norm(cam.dir)
-    u = np.cross(f, np.array(cam.up))
-    u /= np.linalg.norm(u)
-    v = np.cross(u, f)
-    d = pts - eye
-    z = d @ f
-    h = np.tan(cam.fov * 0.5)
-    x, y = (d @ u) / np.maximum(z, 1e-6), (d @ v) / np.maximum(z, 1e-6)
-    return (z > 0) & (np.abs(x) < h * cam.width / cam.height) & (np.abs(y) < h)
+def _relmse(x, r):
+    return float(np.mean((x - r) ** 2 / (r ** 2 + 1e-2)))
 
 
-def test_frozen_proposal_matches_plain(setup):
+def test_frozen_proposal_is_the_plain_render(setup):
     sc, c = setup
-    ref, _ = _render(c, sc, 0, 128, 99)
-    plain = np.mean([(_render(c, sc, 0, 24, s)[0] @ LUM).mean() for s in (1, 2)])
-    frozen = np.mean([(_render(c, sc, P.FLAG_LEARNED | P.FLAG_LEARNED_FROZEN, 24, s)[0] @ LUM).mean() for s in (1, 2)])
-    r = (ref @ LUM).mean()
-    print(f"mean luminance: reference {r:.4f}, plain {plain:.4f}, frozen proposal {frozen:.4f}")
-    assert abs(plain / r - 1) < 0.06
+    plain, _ = _render(c, sc, 0, 12, 5)
+    frozen, _ = _render(c, sc, P.FLAG_LEARNED | P.FLAG_LEARNED_FROZEN, 12, 5)
+    # the same photons and paths; the order of the float sums in the gather
+    # follows the atomics of the photon deposits, so the last bits may differ
+    np.testing.assert_allclose(frozen, plain, rtol=1e-5, atol=1e-7)
+
+
+def test_frozen_bounce_resolve_matches_plain(setup, reference):
+    # every Lambertian bounce drawn by the MIS resolve kernel from the BSDF
+    # lobe alone: other draws, the same expectation
+    sc, c = setup
+    r = (reference @ LUM).mean()
+    frozen = np.mean([(_render(c, sc, P.FLAG_LEARNED | P.FLAG_LEARNED_FROZEN, 24, s, guide_bounces=1)[0]
+                       @ LUM).mean() for s in (1, 2)])
+    print(f"mean luminance: reference {r:.4f}, frozen bounce resolve {frozen:.4f}")
     assert abs(frozen / r - 1) < 0.06
 
 
-def test_trained_proposal_is_unbiased_and_sends_photons_into_view(setup):
+def test_trained_proposal_gains_over_plain(setup, reference):
     sc, c = setup
-    ref, _ = _render(c, sc, 0, 128, 99)
-    img, st = _render(c, sc, P.FLAG_LEARNED, 24, 3)
+    passes = 32
+    plain = [_render(c, sc, 0, passes, s)[0] for s in (3, 4)]
+    learned, stats = [], []
+    for s in (3, 4):
+        img, st = _render(c, sc, P.FLAG_LEARNED, passes, s)
+        learned.append(img)
+        stats += st
+    assert all(np.isfinite(x).all() for x in learned)
+    assert any(s.ms_train > 0 for s in stats), "the network was never trained"
+    e_plain = np.mean([_relmse(x, reference) for x in plain])
+    e_learned = np.mean([_relmse(x, reference) for x in learned])
+    r = (reference @ LUM).mean()
+    ratio = np.mean([(x @ LUM).mean() for x in learned]) / r
+    print(f"relMSE at {passes} passes: plain {e_plain:.4f}, learned {e_learned:.4f} "
+          f"({e_plain / e_learned:.1f}x lower); learned mean luminance / reference {ratio:.4f}")
+    assert abs(ratio - 1) < 0.05
+    assert e_learned < 0.5 * e_plain
+
+
+def test_trained_bounce_guiding_stays_unbiased(setup, reference):
+    sc, c = setup
+    img, st = _render(c, sc, P.FLAG_LEARNED, 24, 6, guide_bounces=1)
     assert np.isfinite(img).all()
-    assert any(s.ms_train > 0 for s in st), "the network was never trained"
-    ratio = (img @ LUM).mean() / (ref @ LUM).mean()
-    view_learned = _in_view(sc, c.render_photons(4_000_000)[:, :3].astype(np.float64)).sum()
-    _render(c, sc, P.FLAG_LEARNED | P.FLAG_LEARNED_FROZEN, 24, 3)
-    view_frozen = _in_view(sc, c.render_photons(4_000_000)[:, :3].astype(np.float64)).sum()
-    print(f"mean luminance ratio {ratio:.4f}; photons in view per pass: trained {view_learned}, without training "
-          f"{view_frozen} ({view_learned / view_frozen:.2f}x)")
-    assert abs(ratio - 1) < 0.08
-    assert view_learned > 1.5 * view_frozen
+    assert any(s.ms_train > 0 for s in st)
+    ratio = (img @ LUM).mean() / (reference @ LUM).mean()
+    print(f"bounce guiding: mean luminance / reference {ratio:.4f}")
+    assert abs(ratio - 1) < 0.06
