@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-study", action="store_true", help="skip the equal-time learned-vs-plain relMSE study")
+    ap.add_argument("--no-graph", action="store_true", help="config4: run every pass through pppm_render_pass")
+    ap.add_argument("--graph-lanes", type=int, default=0, help="config4: jobs at once inside the graph")
     args = ap.parse_args()
     global PHOTONS, DEPTH
     PHOTONS = WORKLOADS[args.workload]["photons"]
@@ -400,6 +402,7 @@ def run_batch(args):
         return 0
     jobs = S.config4_jobs(seed=4 + args.warmup)
     b = P.Batch(local)
+    b.config(use_graph=not args.no_graph, graph_lanes=args.graph_lanes)
     ids = []
     for sc, alpha in jobs:
         par = P.Context.make_params(mode=P.MODE_CANONICAL, photons=sc.photons, max_bounce_photon=8,
@@ -421,6 +424,10 @@ def run_batch(args):
             "batch": {"jobs": len(ids), "wall_s": wall, "rays": rays,
                       "pass_ms_p50_median_over_jobs": statistics.median(s["ms_pass_p50"] for s in stats),
                       "pass_ms_p99_max_over_jobs": max(s["ms_pass_p99"] for s in stats),
+                      "graph_passes": sum(s["graph_passes"] for s in stats),
+                      "graph_s": stats[0]["batch_graph_ms"] / 1e3,
+                      "graph_capture_s": stats[0]["batch_graph_capture_ms"] / 1e3,
+                      "graph_instantiate_s": stats[0]["batch_graph_instantiate_ms"] / 1e3,
                       "autotuned_shapes": shapes},
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)

@@ -329,6 +329,20 @@ int pppm_render_begin(pppm_ctx* ctx, const pppm_camera* cam, const pppm_params* 
  * tracePhotons, photon map build, traceRays + gather, radius update. */
 int pppm_render_pass(pppm_ctx* ctx, int32_t t, pppm_pass_stats* stats);
 
+/* The next `count` passes of a canonical render as one CUDA graph launch (no
+ * counterpart in the reference, whose render() loops over passes on the
+ * host). Only for canonical renders without subsurface scattering, learned
+ * proposal or traversal counting (else PPPM_E_STATE). The photon buffer, the
+ * grid table and the sort buffers are sized before the capture for 1.5x the
+ * most photons one earlier pass stored (a render with no pass done runs pass
+ * 1 normally first); a captured pass that stores more returns
+ * PPPM_E_CAPACITY after the launch, with the render left invalid. Results
+ * equal those of pppm_render_pass up to the order of float sums. stats:
+ * count entries (or NULL); for captured passes ms_photon (emission and
+ * bounces, the eye paths beside them), ms_bounce and ms_gather (grid build
+ * and gather) are device times, ms_grid and ms_eye 0. */
+int pppm_render_graph(pppm_ctx* ctx, int32_t count, pppm_pass_stats* stats);
+
 /* Launch-shape knobs of an active render, applied from the next pass on
  * (values <= 0 keep the current one): hash-grid cell factor (>= 1), photon
  * bounce and eye kernel blocks per SM. None changes results beyond the order
@@ -375,6 +389,10 @@ typedef struct {
     double ms_total;              /* wall time of the job's passes */
     double ms_pass_p50, ms_pass_p99;
     double batch_wall_ms;         /* wall time of the whole pppm_batch_run */
+    int32_t graph_passes;         /* passes of this job run inside the batch graph */
+    double batch_graph_ms;        /* capture, instantiation and run of the batch graph */
+    double batch_graph_capture_ms;     /* of which recording the passes */
+    double batch_graph_instantiate_ms; /* of which cudaGraphInstantiate */
 } pppm_job_stats;
 
 int pppm_batch_create(int device, pppm_batch** out);
@@ -383,9 +401,16 @@ const char* pppm_batch_last_error(const pppm_batch* batch);
 /* Copies nothing it does not need: the scene and env map are uploaded and
  * the BVH built here. */
 int pppm_batch_submit(pppm_batch* batch, const pppm_job* job, int32_t* job_id);
+/* use_graph = 1 (the default): pppm_batch_run records the passes that
+ * follow the tuning passes of every canonical job without subsurface
+ * scattering or learned proposal into one CUDA graph (one branch per job,
+ * the branches chained into graph_lanes lanes; 0 = 2 x max_concurrent) and
+ * launches it once; 0 runs every pass through pppm_render_pass. */
+int pppm_batch_config(pppm_batch* batch, int32_t use_graph, int32_t graph_lanes);
 /* Runs every job's passes: up to max_concurrent jobs at once (one host
- * worker and one stream each, longest first). autotune = 1 times the first
- * passes of each job under different launch shapes and keeps the fastest. */
+ * worker and one stream each, longest first), then the batch graph (see
+ * pppm_batch_config). autotune = 1 times the first passes of each job under
+ * different launch shapes and keeps the fastest. */
 int pppm_batch_run(pppm_batch* batch, int32_t autotune, int32_t max_concurrent);
 /* A job's accumulation buffer (as pppm_render_read) and statistics. */
 int pppm_batch_result(pppm_batch* batch, int32_t job_id, float* accum, pppm_job_stats* stats);

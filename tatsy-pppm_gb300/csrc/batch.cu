@@ -3,9 +3,11 @@
 // time, so their kernels overlap on the GPU, longest jobs first. With
 // autotune on, a job's first passes each run a different launch shape (hash
 // cell factor, photon-bounce and eye blocks per SM; results do not depend on
-// them) and the remaining passes use the fastest. Per-pass latencies are
-// recorded per job. No counterpart in the reference (its render() handles
-// one scene at a time).
+// them) and the remaining passes use the fastest. Then the remaining passes
+// of every job that can be captured (canonical, no subsurface stage, no
+// learned proposal) are recorded into one CUDA graph, one branch per job,
+// and launched once. Per-pass latencies are recorded per job. No
+// counterpart in the reference (its render() handles one scene at a time).
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -15,6 +17,8 @@
 #include <vector>
 
 #include "context.h"
+
+using namespace pppm;
 
 struct pppm_batch {
     int device = 0;
@@ -28,11 +32,17 @@ struct pppm_batch {
         int64_t rays = 0;
         float cell = 1.0f;
         int bounceBlocks = 16, eyeBlocks = 16;
+        bool graph = false;  // remaining passes go into the batch graph
+        int graphPasses = 0;
         int status = PPPM_OK;
         std::string err;
     };
     std::vector<Job> jobs;
     double wallMs = 0.0;
+    double graphMs = 0.0;  // capture, instantiation and run of the graph
+    double graphCaptureMs = 0.0, graphInstantiateMs = 0.0;
+    bool useGraph = true;
+    int graphLanes = 0;  // jobs at once inside the graph (0: 2 x max_concurrent)
     std::string err;
 };
 
@@ -51,7 +61,7 @@ struct Shape {
 };
 const Shape kShapes[] = {{1.0f, 16, 16}, {1.0f, 8, 8}, {1.0f, 32, 32}, {1.25f, 16, 16}, {1.5f, 16, 16}};
 
-int runJob(pppm_batch::Job& j, bool autotune) {
+int runJob(pppm_batch::Job& j, bool autotune, bool useGraph) {
     pppm_ctx* c = j.ctx;
     int r = pppm_render_begin(c, &j.cam, &j.par);
     if (r) return jobFail(j, r);
@@ -61,9 +71,13 @@ int runJob(pppm_batch::Job& j, bool autotune) {
     // try one shape each; compat renders tune only the launch shapes (their
     // cell size follows k)
     const int trials = autotune ? std::min(std::max(j.passes - 2, 0), canonical ? nShapes : 3) : 0;
+    // passes run here; with the graph, the rest are captured after the tuning
+    j.graph = useGraph && graphEligible(c) && j.passes > 1 + trials;
+    const int eager = j.graph ? 1 + trials : j.passes;
+    j.graphPasses = j.passes - eager;
     double best = 1e300;
     Shape bestShape = kShapes[0];
-    for (int t = 1; t <= j.passes; t++) {
+    for (int t = 1; t <= eager; t++) {
         const int trial = t - 2;  // index of the shape this pass tries
         if (trial >= 0 && trial < trials) {
             const Shape& s = kShapes[trial];
@@ -87,9 +101,108 @@ int runJob(pppm_batch::Job& j, bool autotune) {
             }
         }
     }
+    if (j.graph && trials > 0)
+        pppm_render_tune(c, canonical ? bestShape.cell : 0.0f, bestShape.bounce, bestShape.eye);
     j.cell = c->rs.par.cell_factor;
     j.bounceBlocks = c->rs.bouncePerSm;
     j.eyeBlocks = c->rs.eyePerSm;
+    return PPPM_OK;
+}
+
+// The remaining passes of the graph jobs: one capture on `origin`, one
+// launch. Each job is a branch (its context stream and side stream); the
+// branches form `lanes` chains. Jobs go, longest first, to the chain with the
+// least work so far (the work of a job: its remaining passes times the median
+// of its tuned passes), so at most `lanes` jobs run at once and the chains
+// end close together.
+int runGraph(pppm_batch* b, std::vector<pppm_batch::Job*>& gj, int lanes) {
+    cudaSetDevice(b->device);
+    for (auto* j : gj) {
+        const int r = graphPrepare(j->ctx, j->graphPasses);
+        if (r) return jobFail(*j, r);
+        if (cudaStreamSynchronize(j->ctx->stream) != cudaSuccess) return jobFail(*j, PPPM_E_CUDA);
+    }
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join(gj.size(), nullptr);
+    auto cleanup = [&]() {
+        for (auto e : join)
+            if (e) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        if (origin) cudaStreamDestroy(origin);
+    };
+    auto failAll = [&](const std::string& msg) {
+        for (auto* j : gj) {
+            j->status = PPPM_E_CUDA;
+            j->err = msg;
+        }
+        cleanup();
+        return PPPM_E_CUDA;
+    };
+    if (cudaStreamCreateWithFlags(&origin, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess)
+        return failAll("batch graph: cannot create its stream");
+    for (auto& e : join)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return failAll("batch graph: cannot create its events");
+    const auto t0 = std::chrono::steady_clock::now();
+    if (cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal) != cudaSuccess ||
+        cudaEventRecord(fork, origin) != cudaSuccess)
+        return failAll("batch graph: cannot begin the capture");
+    lanes = std::max(1, std::min<int>(lanes, (int)gj.size()));
+    std::vector<double> est(gj.size());
+    for (size_t k = 0; k < gj.size(); k++) {
+        std::vector<double> s(gj[k]->passMs.begin() + std::min<size_t>(1, gj[k]->passMs.size()), gj[k]->passMs.end());
+        std::sort(s.begin(), s.end());
+        est[k] = (s.empty() ? 1.0 : s[s.size() / 2]) * gj[k]->graphPasses;
+    }
+    std::vector<size_t> order(gj.size());
+    for (size_t k = 0; k < order.size(); k++) order[k] = k;
+    std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return est[x] > est[y]; });
+    std::vector<double> laneWork(lanes, 0.0);
+    std::vector<int> laneLast(lanes, -1);  // last job of each chain
+    for (size_t k : order) {
+        const int l = (int)(std::min_element(laneWork.begin(), laneWork.end()) - laneWork.begin());
+        pppm_ctx* c = gj[k]->ctx;
+        // after the fork, or after the previous job of its chain
+        cudaStreamWaitEvent(c->stream, laneLast[l] >= 0 ? join[laneLast[l]] : fork, 0);
+        laneWork[l] += est[k];
+        laneLast[l] = (int)k;
+        const int first = c->rs.passesDone + 1;
+        for (int i = 0; i < gj[k]->graphPasses; i++) {
+            const int r = graphEnqueuePass(c, first + i, i, false);
+            if (r) {
+                graphAbort(origin);
+                return failAll(std::string("batch graph: ") + pppm_last_error(c));
+            }
+        }
+        cudaEventRecord(join[k], c->stream);
+    }
+    for (int l = 0; l < lanes; l++)
+        if (laneLast[l] >= 0) cudaStreamWaitEvent(origin, join[laneLast[l]], 0);
+    cudaGraph_t g = nullptr;
+    if (cudaStreamEndCapture(origin, &g) != cudaSuccess || !g) {
+        cudaGetLastError();
+        return failAll("batch graph: the capture failed");
+    }
+    b->graphCaptureMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    const int r = graphRun(gj[0]->ctx, g, origin, &b->graphInstantiateMs);
+    b->graphMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (r) return failAll(std::string("batch graph: ") + pppm_last_error(gj[0]->ctx));
+    for (auto* j : gj) {
+        for (int i = 0; i < j->graphPasses; i++) {
+            pppm_pass_stats st;
+            double ms = 0.0;
+            const int e = graphFinishPass(j->ctx, i, &st, &ms);
+            if (e) {
+                jobFail(*j, e);
+                break;
+            }
+            j->passMs.push_back(ms);
+            j->rays += st.photon_rays + st.eye_rays;
+        }
+    }
+    cleanup();
     return PPPM_OK;
 }
 
@@ -114,6 +227,13 @@ int pppm_batch_destroy(pppm_batch* b) {
 }
 
 const char* pppm_batch_last_error(const pppm_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int pppm_batch_config(pppm_batch* b, int32_t use_graph, int32_t graph_lanes) {
+    if (!b || graph_lanes < 0) return PPPM_E_ARG;
+    b->useGraph = use_graph != 0;
+    b->graphLanes = graph_lanes;
+    return PPPM_OK;
+}
 
 int pppm_batch_submit(pppm_batch* b, const pppm_job* job, int32_t* job_id) {
     if (!b || !job || job->passes < 1) return PPPM_E_ARG;
@@ -152,13 +272,20 @@ int pppm_batch_run(pppm_batch* b, int32_t autotune, int32_t max_concurrent) {
             pppm_batch::Job& j = b->jobs[order[k]];
             j.passMs.clear();
             j.rays = 0;
-            j.status = runJob(j, autotune != 0);
+            j.status = runJob(j, autotune != 0, b->useGraph);
         }
     };
     const int nw = std::min<int>(max_concurrent, (int)order.size());
     std::vector<std::thread> pool;
     for (int w = 0; w < nw; w++) pool.emplace_back(worker);
     for (auto& t : pool) t.join();
+    b->graphMs = 0.0;
+    std::vector<pppm_batch::Job*> gj;
+    for (auto& j : b->jobs)
+        if (j.status == PPPM_OK && j.graph && j.graphPasses > 0) gj.push_back(&j);
+    // inside the graph no host thread bounds the jobs in flight: twice as
+    // many as the eager phase measured best on the batched workload
+    if (!gj.empty()) runGraph(b, gj, b->graphLanes > 0 ? b->graphLanes : 2 * max_concurrent);
     b->wallMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     for (auto& j : b->jobs)
         if (j.status) {
@@ -189,6 +316,10 @@ int pppm_batch_result(pppm_batch* b, int32_t id, float* accum, pppm_job_stats* s
         stats->bounce_blocks_per_sm = j.bounceBlocks;
         stats->eye_blocks_per_sm = j.eyeBlocks;
         stats->batch_wall_ms = b->wallMs;
+        stats->graph_passes = j.graph ? j.graphPasses : 0;
+        stats->batch_graph_ms = b->graphMs;
+        stats->batch_graph_capture_ms = b->graphCaptureMs;
+        stats->batch_graph_instantiate_ms = b->graphInstantiateMs;
     }
     return PPPM_OK;
 }

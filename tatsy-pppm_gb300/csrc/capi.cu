@@ -147,6 +147,7 @@ int pppm_destroy(pppm_ctx* c) {
     cudaStreamSynchronize(c->stream);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : c->graphEvents) cudaEventDestroy(e);
     if (c->rs.sss.done) cudaEventDestroy(c->rs.sss.done);
     if (c->rs.sss.octDone) cudaEventDestroy(c->rs.sss.octDone);
     if (c->aux) cudaStreamDestroy(c->aux);

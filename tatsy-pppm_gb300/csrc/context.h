@@ -202,6 +202,10 @@ struct RenderState {
     DBuf gatherWork;  // 2 counters: photon pairs tested, pairs within the radius
     int64_t depositCap = 0;
     int64_t storedLast = 0;
+    int64_t storedMax = 0;     // most photons stored by one pass of this render
+    HostPinned graphSlots;      // counters of captured passes (graph.cu)
+    std::vector<double> graphRadius;  // radius of each captured pass
+    bool graphSideEye = false;        // the captured passes traced eye paths on the side stream
     int64_t phantomsLast = 0;
     SssState sss;
     GuideState guide;
@@ -256,6 +260,7 @@ struct pppm_ctx {
     // stage timing: 0-7 main stream; 8 fork of the side stream, 9-10 its
     // eye trace
     cudaEvent_t ev[11] = {};
+    std::vector<cudaEvent_t> graphEvents;  // stage timing of captured passes
 };
 
 namespace pppm {
@@ -270,6 +275,20 @@ inline int fail(pppm_ctx* c, int code, const std::string& msg) {
 // Synchronises st a few times (level counts).
 int octreeBuild(pppm_ctx* c, OctreeBufs& b, const OctreePoints& pts, int64_t n, cudaStream_t st, int* numNodes,
                 int64_t* launches);
+
+// Captured canonical passes (graph.cu). graphEligible: canonical, no
+// subsurface stage, no learned proposal, no traversal counting.
+// graphPrepare fixes the capacities of `count` passes; graphEnqueuePass
+// records pass t (counter slot `slot`) into the context stream under capture
+// (sideEye: eye paths on the side stream beside the photon pass); graphFinishPass reads a slot after the graph ran (msPass: the
+// pass's device time); graphAbort ends a failed capture; graphRun
+// instantiates, launches and waits.
+bool graphEligible(const pppm_ctx* c);
+int graphPrepare(pppm_ctx* c, int count);
+int graphEnqueuePass(pppm_ctx* c, int t, int slot, bool sideEye);
+int graphFinishPass(pppm_ctx* c, int slot, pppm_pass_stats* st, double* msPass);
+void graphAbort(cudaStream_t st);
+int graphRun(pppm_ctx* c, cudaGraph_t g, cudaStream_t st, double* instantiateMs = nullptr);
 
 inline int cudaFail(pppm_ctx* c, cudaError_t e, const char* where) {
     return fail(c, PPPM_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));

@@ -52,6 +52,52 @@ double knnCell(const double* mn, const double* mx, int64_t n, int k) {
 
 using namespace pppm;
 
+namespace pppm {
+
+// Kernel parameters and camera of pass t (everything a pass needs from the
+// host besides its buffers).
+void passSetup(pppm_ctx* c, int t, int64_t paths, TraceParams* tp, CameraDev* cd) {
+    RenderState& rs = c->rs;
+    const pppm_params& par = rs.par;
+    const int N = par.num_streams;
+    const int W = rs.cam.width, H = rs.cam.height;
+    const int64_t T = rs.taskPerThread;
+    tp->mode = par.mode;
+    tp->numStreams = N;
+    tp->taskPerThread = T;
+    tp->numPaths = paths;
+    tp->numPhotons = (double)par.photons;
+    tp->maxBouncePhoton = par.max_bounce_photon;
+    tp->maxBounceEye = par.max_bounce_eye;
+    tp->seed = par.seed;
+    tp->pass = t;
+    tp->countTraversal = (par.flags & PPPM_FLAG_COUNT_TRAVERSAL) ? 1 : 0;
+    tp->sssPass = 0;
+    tp->hasSss = rs.sss.enabled ? 1 : 0;
+    tp->bouncePerSm = rs.bouncePerSm;
+    tp->eyePerSm = rs.eyePerSm;
+    tp->guided = rs.guide.enabled ? 1 : 0;
+    tp->guide = guideView(c, 3 * paths);
+    {
+        const double ex = rs.cam.eye[0], ey = rs.cam.eye[1], ez = rs.cam.eye[2];
+        const double dx = rs.cam.dir[0], dy = rs.cam.dir[1], dz = rs.cam.dir[2];
+        const double ux = rs.cam.up[0], uy = rs.cam.up[1], uz = rs.cam.up[2];
+        // ICamera: unitU = cross(direction, up), unitV = cross(unitU, direction) (camera_interface.h:40-41)
+        const double Ux = dy * uz - dz * uy, Uy = dz * ux - dx * uz, Uz = dx * uy - dy * ux;
+        const double Vx = Uy * dz - Uz * dy, Vy = Uz * dx - Ux * dz, Vz = Ux * dy - Uy * dx;
+        cd->ex = ex; cd->ey = ey; cd->ez = ez;
+        cd->dx = (float)dx; cd->dy = (float)dy; cd->dz = (float)dz;
+        cd->ux = (float)Ux; cd->uy = (float)Uy; cd->uz = (float)Uz;
+        cd->vx = (float)Vx; cd->vy = (float)Vy; cd->vz = (float)Vz;
+        cd->halfTan = (float)std::tan((double)rs.cam.fov * 0.5);
+        cd->aspect = (float)((double)W / (double)H);
+        cd->w = W;
+        cd->h = H;
+    }
+}
+
+}  // namespace pppm
+
 extern "C" {
 
 int pppm_knn(pppm_ctx* c, const float* photonPos, int64_t n, const float* queries, int64_t m, int32_t numTarget,
@@ -206,6 +252,7 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
     rs.passesDone = 0;
     rs.storedLast = 0;
+    rs.storedMax = 0;
     rs.phantomsLast = 0;
     rs.active = true;
     return PPPM_OK;
@@ -229,41 +276,9 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     if (compat && k > kMaxKnn) return fail(c, PPPM_E_CAPACITY, "render_pass: k = (int)radius above 64");
 
     TraceParams tp;
-    tp.mode = par.mode;
-    tp.numStreams = N;
-    tp.taskPerThread = T;
-    tp.numPaths = paths;
-    tp.numPhotons = (double)par.photons;
-    tp.maxBouncePhoton = par.max_bounce_photon;
-    tp.maxBounceEye = par.max_bounce_eye;
-    tp.seed = par.seed;
-    tp.pass = t;
-    tp.countTraversal = (par.flags & PPPM_FLAG_COUNT_TRAVERSAL) ? 1 : 0;
-    tp.sssPass = 0;
-    tp.hasSss = rs.sss.enabled ? 1 : 0;
-    tp.bouncePerSm = rs.bouncePerSm;
-    tp.eyePerSm = rs.eyePerSm;
-    tp.guided = rs.guide.enabled ? 1 : 0;
-    tp.guide = guideView(c, 3 * paths);
-    int64_t launches = 0;
-
     CameraDev cd;
-    {
-        const double ex = rs.cam.eye[0], ey = rs.cam.eye[1], ez = rs.cam.eye[2];
-        const double dx = rs.cam.dir[0], dy = rs.cam.dir[1], dz = rs.cam.dir[2];
-        const double ux = rs.cam.up[0], uy = rs.cam.up[1], uz = rs.cam.up[2];
-        // ICamera: unitU = cross(direction, up), unitV = cross(unitU, direction) (camera_interface.h:40-41)
-        const double Ux = dy * uz - dz * uy, Uy = dz * ux - dx * uz, Uz = dx * uy - dy * ux;
-        const double Vx = Uy * dz - Uz * dy, Vy = Uz * dx - Ux * dz, Vz = Ux * dy - Uy * dx;
-        cd.ex = ex; cd.ey = ey; cd.ez = ez;
-        cd.dx = (float)dx; cd.dy = (float)dy; cd.dz = (float)dz;
-        cd.ux = (float)Ux; cd.uy = (float)Uy; cd.uz = (float)Uz;
-        cd.vx = (float)Vx; cd.vy = (float)Vy; cd.vz = (float)Vz;
-        cd.halfTan = (float)std::tan((double)rs.cam.fov * 0.5);
-        cd.aspect = (float)((double)W / (double)H);
-        cd.w = W;
-        cd.h = H;
-    }
+    passSetup(c, t, paths, &tp, &cd);
+    int64_t launches = 0;
     const SceneView sv = sceneView(c);
     const EnvDev ev = envView(c);
     if (par.mode == PPPM_MODE_CLASSIC) {
@@ -494,6 +509,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         }
     }
     rs.storedLast = stored;
+    rs.storedMax = std::max(rs.storedMax, stored);
     rs.phantomsLast = phantoms;
     rs.passesDone = t;
     if (rs.guide.enabled) {

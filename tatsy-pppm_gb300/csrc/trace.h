@@ -177,6 +177,9 @@ cudaError_t launchImportanceSplat(const GuideView& g, const float4* queries, con
 cudaError_t launchRecordInvSum(const MlpRecord* rec, int64_t n, float* sum, cudaStream_t st);
 
 // Learned proposal in a canonical render (guide.cu).
+// Kernel parameters and camera of pass t of the current render (render.cu).
+void passSetup(pppm_ctx* c, int t, int64_t paths, TraceParams* tp, CameraDev* cd);
+
 int guideBegin(pppm_ctx* c, int64_t maxPaths);
 GuideView guideView(pppm_ctx* c, int64_t decisionsPerPass);
 int guideStep(pppm_ctx* c, const TraceParams& tp, PathState* q, const unsigned long long* count, int64_t cap,

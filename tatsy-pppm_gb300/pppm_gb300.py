@@ -76,7 +76,9 @@ class JobStats(ctypes.Structure):
     _fields_ = [("passes", ctypes.c_int32), ("bounce_blocks_per_sm", ctypes.c_int32),
                 ("eye_blocks_per_sm", ctypes.c_int32), ("cell_factor", ctypes.c_float), ("rays", ctypes.c_int64),
                 ("ms_total", ctypes.c_double), ("ms_pass_p50", ctypes.c_double), ("ms_pass_p99", ctypes.c_double),
-                ("batch_wall_ms", ctypes.c_double)]
+                ("batch_wall_ms", ctypes.c_double), ("graph_passes", ctypes.c_int32),
+                ("batch_graph_ms", ctypes.c_double), ("batch_graph_capture_ms", ctypes.c_double),
+                ("batch_graph_instantiate_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -98,6 +100,7 @@ SIGNATURES = {
     "pppm_knn": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
                   ctypes.c_int32], ctypes.c_int),
     "pppm_dipole_rd": ([_VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_render_graph": ([_VP, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_fast_exp_check": ([_VP, ctypes.c_uint64, ctypes.c_uint64, _VP, _VP], ctypes.c_int),
     "pppm_dipole_irradiance": ([_VP, _VP, _VP, ctypes.c_int64, ctypes.c_double, _VP, ctypes.c_int64, _VP],
                                ctypes.c_int),
@@ -125,6 +128,7 @@ SIGNATURES = {
     "pppm_batch_last_error": ([_VP], ctypes.c_char_p),
     "pppm_batch_submit": ([_VP, _VP, _VP], ctypes.c_int),
     "pppm_batch_run": ([_VP, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+    "pppm_batch_config": ([_VP, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
     "pppm_batch_result": ([_VP, ctypes.c_int32, _VP, _VP], ctypes.c_int),
 }
 
@@ -404,6 +408,12 @@ class Context:
         self._check(self.lib.pppm_render_pass(self.h, int(t), ctypes.byref(st)))
         return st
 
+    def render_graph(self, count):
+        """pppm_render_graph: the next `count` canonical passes as one CUDA graph launch."""
+        st = (PassStats * int(count))()
+        self._check(self.lib.pppm_render_graph(self.h, int(count), st))
+        return list(st)
+
     def render_read(self, out=None):
         if out is None:
             out = np.zeros((self._cam.height, self._cam.width, 3), np.float32)
@@ -462,6 +472,10 @@ class Batch:
         self._check(self.lib.pppm_batch_submit(self.h, ctypes.byref(j), ctypes.byref(jid)))
         self._cams.append(j.camera)
         return jid.value
+
+    def config(self, use_graph=True, graph_lanes=0):
+        """pppm_batch_config: capture the passes after tuning into one CUDA graph."""
+        self._check(self.lib.pppm_batch_config(self.h, 1 if use_graph else 0, int(graph_lanes)))
 
     def run(self, autotune=True, max_concurrent=8):
         self._check(self.lib.pppm_batch_run(self.h, 1 if autotune else 0, int(max_concurrent)))
