@@ -354,6 +354,34 @@ int pppm_render_tune(pppm_ctx* ctx, float cell_factor, int32_t bounce_blocks_per
  * pass count, not flipped): w*h*3 floats, row y = camera pixel row y. */
 int pppm_render_read(pppm_ctx* ctx, float* accum);
 
+/* The image the reference writes after a pass (ppm_probabilistic.cc:96-106):
+ * accumulation / t with rows flipped (result(x, H - 1 - y) = buffer(x, y) / t),
+ * Image::gamma(2.2, true) (image.cc:202-212), then Image::toByte
+ * (image.cc:530-533). tonemap = 1 applies Image::tonemap first (image.cc:
+ * 498-524: Reinhard, a = 0.18, log-average and maximum luminance of the
+ * image). The arithmetic is the reference's, in double, on the FP32
+ * accumulator. rgb8: w*h*3 bytes, host or device. */
+int pppm_render_image(pppm_ctx* ctx, int32_t tonemap, uint8_t* rgb8);
+
+/* PNG file (8-bit RGB, no interlace) of w*h*3 bytes (host), in place of
+ * stbi_write_png in Image::savePng (image.cc:484-495). The zlib stream holds
+ * stored deflate blocks, one per row, so the file is larger than stb's but
+ * decodes to the same pixels. out = NULL: *size only; else out must hold
+ * *size bytes (PPPM_E_CAPACITY). Host only: needs no context and no GPU. */
+int pppm_png_encode(const uint8_t* rgb8, int32_t w, int32_t h, uint8_t* out, int64_t cap, int64_t* size);
+
+/* Checkpoint of the current render (no counterpart in the reference): the
+ * camera, parameters, pass count, radius, tuned launch shapes, accumulation
+ * buffer, per-stream XorShift states, the Poisson sampler's XorShift state,
+ * classic PPM's render points and the learned proposal's network, Adam
+ * moments, importance grids and pending records. out = NULL: *size only.
+ * The learned proposal's settings (pppm_learned_config) are not part of it. */
+int pppm_render_save(pppm_ctx* ctx, uint8_t* out, int64_t cap, int64_t* size);
+/* Resumes a render from a checkpoint into a context that holds the same
+ * scene and environment map (else PPPM_E_STATE): the next pppm_render_pass
+ * continues with the saved pass count + 1. */
+int pppm_render_load(pppm_ctx* ctx, const uint8_t* in, int64_t size);
+
 /* ProgressivePhotonMappingProb::render (ppm_probabilistic.cc:24-121) minus
  * the PNG side effects: begin + `passes` passes + read. */
 int pppm_render(pppm_ctx* ctx, const pppm_camera* cam, const pppm_params* params, int32_t passes, float* accum);

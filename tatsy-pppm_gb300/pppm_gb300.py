@@ -101,6 +101,10 @@ SIGNATURES = {
                   ctypes.c_int32], ctypes.c_int),
     "pppm_dipole_rd": ([_VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_render_graph": ([_VP, ctypes.c_int32, _VP], ctypes.c_int),
+    "pppm_render_image": ([_VP, ctypes.c_int32, _VP], ctypes.c_int),
+    "pppm_png_encode": ([_VP, ctypes.c_int32, ctypes.c_int32, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_render_save": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_render_load": ([_VP, _VP, ctypes.c_int64], ctypes.c_int),
     "pppm_fast_exp_check": ([_VP, ctypes.c_uint64, ctypes.c_uint64, _VP, _VP], ctypes.c_int),
     "pppm_dipole_irradiance": ([_VP, _VP, _VP, ctypes.c_int64, ctypes.c_double, _VP, ctypes.c_int64, _VP],
                                ctypes.c_int),
@@ -408,6 +412,27 @@ class Context:
         self._check(self.lib.pppm_render_pass(self.h, int(t), ctypes.byref(st)))
         return st
 
+    def render_image(self, tonemap=False):
+        """pppm_render_image: the reference's output bytes of the current pass (H x W x 3 uint8)."""
+        out = np.zeros((self._cam.height, self._cam.width, 3), np.uint8)
+        self._check(self.lib.pppm_render_image(self.h, 1 if tonemap else 0, out.ctypes.data))
+        return out
+
+    def render_save(self):
+        """pppm_render_save: the checkpoint as bytes."""
+        n = ctypes.c_int64()
+        self._check(self.lib.pppm_render_save(self.h, None, 0, ctypes.byref(n)))
+        buf = np.zeros(n.value, np.uint8)
+        self._check(self.lib.pppm_render_save(self.h, buf.ctypes.data, n.value, ctypes.byref(n)))
+        return buf.tobytes()
+
+    def render_load(self, blob):
+        """pppm_render_load: resume a render from render_save's bytes."""
+        b = np.frombuffer(blob, np.uint8)
+        self._check(self.lib.pppm_render_load(self.h, b.ctypes.data, b.size))
+        # the checkpoint header: magic (8 bytes), version, header size, camera
+        self._cam = Camera.from_buffer_copy(bytes(blob[16:16 + ctypes.sizeof(Camera)]))
+
     def render_graph(self, count):
         """pppm_render_graph: the next `count` canonical passes as one CUDA graph launch."""
         st = (PassStats * int(count))()
@@ -487,6 +512,22 @@ class Batch:
         self._check(self.lib.pppm_batch_result(self.h, int(job_id), out.ctypes.data if image else None,
                                                ctypes.byref(st)))
         return out, st.as_dict()
+
+
+def png_encode(rgb8):
+    """pppm_png_encode: PNG file bytes of an H x W x 3 uint8 image (host only)."""
+    lib = load()
+    img = np.ascontiguousarray(rgb8, np.uint8)
+    h, w = img.shape[:2]
+    n = ctypes.c_int64()
+    r = lib.pppm_png_encode(img.ctypes.data, w, h, None, 0, ctypes.byref(n))
+    if r != OK:
+        raise PppmError(r, "png_encode: bad arguments")
+    out = np.zeros(n.value, np.uint8)
+    r = lib.pppm_png_encode(img.ctypes.data, w, h, out.ctypes.data, n.value, ctypes.byref(n))
+    if r != OK:
+        raise PppmError(r, "png_encode failed")
+    return out.tobytes()
 
 
 def knn_noalloc(photon_pos, queries, num_target_photons, target_radius, idx, cnt, stream=None):
