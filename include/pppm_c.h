@@ -54,6 +54,10 @@ extern "C" {
 #define PPPM_MODE_CLASSIC 2   /* ProgressivePhotonMapping (classic PPM, progressive_photon_mapping.cc):
                                  per-pixel render points with their own radius and photon count,
                                  permuted Halton sampling, the reference's semantics */
+#define PPPM_MODE_PATH_TRACING 3 /* PathTracing (path_tracing.cc:23-198), the reference's other integrator:
+                                   one path per pixel per pass from the reference's row tapes (num_streams
+                                   XorShift streams), env light at misses, max_bounce_eye = bounceLimit
+                                   (64 in the reference); photons drive only the subsurface stage */
 
 typedef struct pppm_ctx pppm_ctx;
 

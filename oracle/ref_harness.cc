@@ -419,6 +419,68 @@ int rh_render_passes(void* s, const PassJob* job, double* accum, double* radii, 
     return 0;
 }
 
+// PathTracing::render (path_tracing.cc:23-127) with the pseudo-random
+// sampler and without its PNG side effects: npasses samples per pixel, rows
+// y to stream y % N, a 200-number tape per pixel (path_tracing.cc:82-90),
+// bounceLimit 64. With a BSSRDF in the scene, sample t's subsurface photon
+// streams see time(NULL) = sssTime + t - 1. accum: w*h*3 doubles with row
+// y = camera row y (the reference's buffer holds pixel (x, y) at
+// (x, H - 1 - y)).
+int rh_path_trace(void* s, const PassJob* job, double* accum) {
+    const Scene& sc = static_cast<HarnessScene*>(s)->scene;
+    PerspectiveCamera cam(Vector3D(job->eye[0], job->eye[1], job->eye[2]), Vector3D(job->dir[0], job->dir[1], job->dir[2]),
+                          Vector3D(job->up[0], job->up[1], job->up[2]), job->fov, job->w, job->h, 1.0);
+    RenderParameters params(job->photons, job->npasses, job->gatherPhotons, job->gatherRadius);
+    PathTracing pt;
+    bool enableBssrdf = false;
+    double avgArea = 0.0;
+    for (int i = 0; i < sc.numTriangles(); i++) {
+        if (sc.getBsdf(i).type() & BSDF_TYPE_BSSRDF) {
+            enableBssrdf = true;
+            avgArea += sc.getTriangle(i).area();
+        }
+    }
+    avgArea /= sc.numTriangles();
+    double areaRadius = 0.0;
+    if (enableBssrdf) {
+        areaRadius = sqrt(avgArea) * 1.0;
+        pt._integrator = new SubsurfaceIntegrator();
+    }
+    RandomSampler* rs = new RandomSampler[OMP_NUM_CORE];
+    for (int i = 0; i < OMP_NUM_CORE; i++) rs[i] = Random::generateSampler(i);
+    const int w = job->w, h = job->h;
+    const int taskPerThread = (h + OMP_NUM_CORE - 1) / OMP_NUM_CORE;
+    std::vector<std::vector<int> > tasks(OMP_NUM_CORE);
+    for (int y = 0; y < h; y++) tasks[y % OMP_NUM_CORE].push_back(y);
+    Image buffer(w, h);
+    buffer.fill(Vector3D(0.0, 0.0, 0.0));
+    std::streambuf* old = std::cout.rdbuf(nullptr);
+    for (int i = 0; i < job->npasses; i++) {
+        if (enableBssrdf) {
+            gFakeTime = (time_t)(job->sssTime + (unsigned int)i);
+            pt._integrator->initialize(sc, params, areaRadius, 0.05);
+        }
+        for (int t = 0; t < taskPerThread; t++) {
+#pragma omp parallel for
+            for (int threadID = 0; threadID < OMP_NUM_CORE; threadID++) {
+                RandomSequence rseq;
+                if (t < (int)tasks[threadID].size()) {
+                    const int y = tasks[threadID][t];
+                    for (int x = 0; x < w; x++) {
+                        rs[threadID].request(200, &rseq);
+                        buffer.pixel(x, h - y - 1) += pt.executePathTracing(sc, cam, params, x, y, rseq);
+                    }
+                }
+            }
+        }
+    }
+    std::cout.rdbuf(old);
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) put3(accum + 3 * (y * w + x), buffer(x, h - 1 - y));
+    delete[] rs;
+    return 0;
+}
+
 // ProgressivePhotonMapping (classic PPM, progressive_photon_mapping.cc:31-345)
 // without its PNG side effects: render points, Halton samplers, then per
 // pass traceRays (+ constructHashGrid) and tracePhotons, as render() does.

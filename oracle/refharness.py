@@ -80,6 +80,7 @@ def lib():
         _lib.rh_poisson_disk.argtypes = [_F, ctypes.c_int, ctypes.c_double, _D, _D, ctypes.c_int]
         _lib.rh_poisson_disk.restype = ctypes.c_int
         _lib.rh_classic_passes.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _D]
+        _lib.rh_path_trace.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _D]
         _lib.rh_halton.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.c_int, _D]
         _lib.rh_irradiance_pm.argtypes = [_D, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_double, _D]
@@ -185,6 +186,25 @@ class RefScene:
         img = np.zeros((camera.height, camera.width, 3))
         lib().rh_classic_passes(self.h, ctypes.byref(job), _p(img, _D))
         return img
+
+    def path_trace(self, camera, photons, npasses, sss_time=0):
+        """npasses samples per pixel of PathTracing::render (pseudo-random
+        sampler): the linear buffer, row y = camera row y, not divided by the
+        sample count."""
+        job = _PassJob()
+        job.eye[:] = camera.eye
+        job.dir[:] = camera.dir
+        job.up[:] = camera.up
+        job.fov = camera.fov
+        job.w, job.h = camera.width, camera.height
+        job.photons = photons
+        job.gatherPhotons = 128
+        job.gatherRadius = 16.0
+        job.npasses = npasses
+        job.sssTime = int(sss_time)
+        accum = np.zeros((camera.height, camera.width, 3))
+        lib().rh_path_trace(self.h, ctypes.byref(job), _p(accum, _D))
+        return accum
 
     def render_passes(self, camera, photons, npasses, gather_photons=128, gather_radius=16.0, photon_cap=0,
                       sss_time=0):

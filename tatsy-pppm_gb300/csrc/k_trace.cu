@@ -390,7 +390,10 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
 // the accumulation buffer; queries are compacted with one atomic per warp.
 // kSss: the scene has BSSRDF materials (the subsurface branches of radiance
 // are compiled in only then).
-template <bool kSss>
+// kPT: PathTracing::radiance (path_tracing.cc:137-198) instead: a Lambertian
+// hit continues with the BSDF sample (pdf 1) like every other surface; the
+// rest of the recursion is the same.
+template <bool kSss, bool kPT>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TraceParams tp, SceneView sc, EnvDev env, CameraDev cam,
                                                  OctView oct, const uint32_t* __restrict__ pixelStates,
                                                  float* __restrict__ accum, float4* __restrict__ queries,
@@ -418,7 +421,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
         f3 w = {1.f, 1.f, 1.f}, L = {0.f, 0.f, 0.f};
         if (alive) {
             const int x = (int)(pix % cam.w), y = (int)(pix / cam.w);
-            if (tp.mode == PPPM_MODE_COMPAT) {
+            if (tp.mode == PPPM_MODE_COMPAT || tp.mode == PPPM_MODE_PATH_TRACING) {
                 const uint4 s = *reinterpret_cast<const uint4*>(pixelStates + 4 * pix);
                 tape.x.s[0] = s.x; tape.x.s[1] = s.y; tape.x.s[2] = s.z; tape.x.s[3] = s.w;
             } else {
@@ -510,7 +513,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
                 }
                 if (m.type & PPPM_BSDF_REFRACTION) continue;
             }
-            if (m.type & PPPM_BSDF_LAMBERTIAN) {
+            if (!kPT && (m.type & PPPM_BSDF_LAMBERTIAN)) {
                 const f3 on = dot(nrm, d) < 0.0f ? nrm : -nrm;
                 const f3 wq = w * refl * (1.0f / roul);
                 q0 = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
@@ -530,7 +533,8 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
         }
         // a compat tape holds 200 numbers (ppm_probabilistic.cc:222); the
         // reference aborts when a path pops more
-        if (tp.mode == PPPM_MODE_COMPAT && tape.pos > 200) atomicAdd(&ctr->undefinedEye, 1ull);
+        if ((tp.mode == PPPM_MODE_COMPAT || tp.mode == PPPM_MODE_PATH_TRACING) && tape.pos > 200)
+            atomicAdd(&ctr->undefinedEye, 1ull);
         if (onImage) {
             accum[3 * pix] += L.x;
             accum[3 * pix + 1] += L.y;
@@ -636,12 +640,20 @@ cudaError_t launchPhotonTail(const TraceParams& tp, const SceneView& sc, int bou
 
 cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
                            const OctView& oct, const uint32_t* pixelStates, float* accum, float4* queries,
-                           float4* sssQ, int64_t sssCap, PassCounters* ctr, cudaStream_t st) {
+                           float4* sssQ, int64_t sssCap, PassCounters* ctr, cudaStream_t st, bool pathTrace) {
     const unsigned blocks = blocksFor((int64_t)cam.w * cam.h, 128, 152 * tp.eyePerSm);
-    if (oct.numNodes > 0 || tp.hasSss)
-        kEyeTrace<true><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap, ctr);
+    const bool sss = oct.numNodes > 0 || tp.hasSss;
+    if (pathTrace && sss)
+        kEyeTrace<true, true><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap, ctr);
+    else if (pathTrace)
+        kEyeTrace<false, true><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap,
+                                                       ctr);
+    else if (sss)
+        kEyeTrace<true, false><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap,
+                                                       ctr);
     else
-        kEyeTrace<false><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap, ctr);
+        kEyeTrace<false, false><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap,
+                                                        ctr);
     return cudaGetLastError();
 }
 

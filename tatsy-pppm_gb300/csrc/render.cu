@@ -96,6 +96,75 @@ void passSetup(pppm_ctx* c, int t, int64_t paths, TraceParams* tp, CameraDev* cd
     }
 }
 
+// Sample t of PathTracing::render (path_tracing.cc:74-97): the subsurface
+// stage as in PPM (path_tracing.cc:30-46, 75-77), then one path per pixel.
+// Rows go to stream y % N and every pixel of a row draws a 200-number tape
+// from its stream (path_tracing.cc:82-90), so the tapes of sample t start
+// where sample t - 1's ended. The accumulation keeps row y = camera row y
+// (the reference stores pixel (x, y) at buffer(x, H - 1 - y)).
+int ptPass(pppm_ctx* c, int t, const TraceParams& tp, const SceneView& sv, const EnvDev& ev, const CameraDev& cd,
+           pppm_pass_stats* stats) {
+    RenderState& rs = c->rs;
+    const pppm_params& par = rs.par;
+    const int N = par.num_streams;
+    const int W = rs.cam.width, H = rs.cam.height;
+    PassCounters* ctr = rs.photonCount.as<PassCounters>();
+    int64_t launches = 0;
+    PPPM_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
+    if (rs.sss.enabled) {
+        int e = sssPrepare(c, t, tp, sv, ev, &launches);
+        if (!e) e = sssFinish(c, &launches);
+        if (e) return e;
+    }
+    PPPM_CUDA(c, cudaEventRecord(c->ev[7], c->stream));
+    // pixel tapes only (no photon tapes in this integrator)
+    std::vector<uint32_t> ss((size_t)N * 4);
+    for (int s = 0; s < N; s++) std::memcpy(&ss[4 * s], rs.streams[s].s, 16);
+    PPPM_CUDA(c, cudaMemcpyAsync(rs.streamStatesD.p, ss.data(), ss.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    TraceParams tt = tp;
+    tt.taskPerThread = 0;
+    uint32_t* pixelStates = rs.tapeStates.as<uint32_t>() + 4 * tp.numPaths;
+    PPPM_CUDA(c, launchTapeStates(tt, rs.streamStatesD.as<uint32_t>(), rs.jumpMats.as<uint32_t>(), W, H,
+                                  rs.tapeStates.as<uint32_t>(), pixelStates, c->stream));
+    PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
+    PPPM_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
+    PPPM_CUDA(c, launchEyeTrace(tp, sv, ev, cd, sssView(c), pixelStates, rs.accum.as<float>(), rs.queries.as<float4>(),
+                                rs.sss.queue.as<float4>(), rs.sss.queueCap, ctr, c->stream, true));
+    launches += 2;
+    if (rs.sss.enabled) {
+        PPPM_CUDA(c, launchSubsurfaceGather(sssView(c), sv.mats, rs.sss.queue.as<float4>(), &ctr->sssQueries,
+                                            rs.sss.queueCap, rs.accum.as<float>(),
+                                            tp.countTraversal ? &ctr->sssVisits : nullptr, c->stream));
+        launches += 1;
+    }
+    PPPM_CUDA(c, cudaEventRecord(c->ev[3], c->stream));
+    PassCounters hc;
+    PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->eye_rays = (int64_t)hc.eyeRays;
+        float ms;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[7]);
+        stats->ms_subsurface = rs.sss.enabled ? ms : 0.0;
+        stats->ms_subsurface_host = rs.sss.enabled ? rs.sss.msHost : 0.0;
+        stats->sss_points = rs.sss.enabled ? rs.sss.numPoints : 0;
+        stats->sss_photons = rs.sss.enabled ? rs.sss.stored : 0;
+        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+        stats->ms_eye = ms;
+        stats->kernel_launches = launches;
+        stats->node_visits = (int64_t)hc.nodeVisits[1];
+        stats->tri_tests = (int64_t)hc.triTests[1];
+    }
+    if (hc.undefinedEye)
+        return fail(c, PPPM_E_UNDEFINED, "render_pass: a path drew more than its 200 random numbers (the reference aborts)");
+    for (int s = 0; s < N; s++) {
+        const int64_t rows = s < H ? (H - 1 - s) / N + 1 : 0;
+        xorshiftJumpHost(c->jumpTables, (uint64_t)(rows * W), &rs.streams[s]);
+    }
+    return PPPM_OK;
+}
+
 }  // namespace pppm
 
 extern "C" {
@@ -188,9 +257,10 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     // The default Scene env map has no importance tables (scene.cc:11-12):
     // photon emission would read an empty CDF.
     if (!c->hasEnv) return fail(c, PPPM_E_STATE, "render_begin: no env map (the only light of the reference)");
-    if (par->mode != PPPM_MODE_COMPAT && par->mode != PPPM_MODE_CANONICAL && par->mode != PPPM_MODE_CLASSIC)
+    if (par->mode != PPPM_MODE_COMPAT && par->mode != PPPM_MODE_CANONICAL && par->mode != PPPM_MODE_CLASSIC &&
+        par->mode != PPPM_MODE_PATH_TRACING)
         return fail(c, PPPM_E_ARG, "render_begin: unknown mode");
-    if (par->mode == PPPM_MODE_CLASSIC && (par->flags & PPPM_FLAG_LEARNED))
+    if ((par->mode == PPPM_MODE_CLASSIC || par->mode == PPPM_MODE_PATH_TRACING) && (par->flags & PPPM_FLAG_LEARNED))
         return fail(c, PPPM_E_ARG, "render_begin: the learned proposal needs canonical mode");
     if (par->num_streams < 1 || par->num_streams > 4096 || par->photons < 1 || cam->width < 1 || cam->height < 1 ||
         par->max_bounce_photon < 0 || par->max_bounce_eye < 0 || !(par->alpha > 0.0) || !(par->radius_scale > 0.0))
@@ -213,7 +283,7 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     const int64_t pixels = (int64_t)cam->width * cam->height;
     rs.streams.assign(N, XorShift());
     for (int i = 0; i < N; i++) rs.streams[i].seed((uint32_t)i);  // Random::generateSampler(i)
-    if (par->mode == PPPM_MODE_COMPAT) {
+    if (par->mode == PPPM_MODE_COMPAT || par->mode == PPPM_MODE_PATH_TRACING) {
         if (c->jumpTables.empty()) xorshiftJumpTables(&c->jumpTables);
         PPPM_CUDA(c, rs.jumpMats.ensure(c->jumpTables.size() * 4));
         PPPM_CUDA(c, cudaMemcpy(rs.jumpMats.p, c->jumpTables.data(), c->jumpTables.size() * 4, cudaMemcpyHostToDevice));
@@ -283,6 +353,12 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     const EnvDev ev = envView(c);
     if (par.mode == PPPM_MODE_CLASSIC) {
         const int e = classicPass(c, t, tp, sv, ev, cd, stats);
+        if (e) return e;
+        rs.passesDone = t;
+        return PPPM_OK;
+    }
+    if (par.mode == PPPM_MODE_PATH_TRACING) {
+        const int e = ptPass(c, t, tp, sv, ev, cd, stats);
         if (e) return e;
         rs.passesDone = t;
         return PPPM_OK;

@@ -109,11 +109,13 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
     SssState& s = c->rs.sss;
     RenderState& rs = c->rs;
     const pppm_params& par = rs.par;
-    const bool compat = par.mode == PPPM_MODE_COMPAT;
+    // the path tracer's subsurface stage is the reference's, as in compat mode
+    const bool compat = par.mode == PPPM_MODE_COMPAT || par.mode == PPPM_MODE_PATH_TRACING;
     const int N = par.num_streams;
     const int64_t paths = base.numPaths;
 
     TraceParams tp = base;
+    if (compat) tp.mode = PPPM_MODE_COMPAT;
     tp.sssPass = 1;
     tp.maxBouncePhoton = kSssBounceLimit;
     // the subsurface photon set keeps the reference's own sampling

@@ -147,7 +147,8 @@ constexpr int kWaveBounces = PPPM_WAVE_BOUNCES;
 
 cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const EnvDev& env, const CameraDev& cam,
                            const OctView& oct, const uint32_t* pixelStates, float* accum, float4* queries,
-                           float4* sssQ, int64_t sssCap, PassCounters* ctr, cudaStream_t st);
+                           float4* sssQ, int64_t sssCap, PassCounters* ctr, cudaStream_t st,
+                           bool pathTrace = false);
 cudaError_t launchSubsurfaceGather(const OctView& oct, const DevMaterial* mats, const float4* q,
                                    const unsigned long long* count, int64_t cap, float* accum,
                                    unsigned long long* visits, cudaStream_t st);

@@ -17,7 +17,7 @@ LIB_PATH = HERE / "libpppm_gb300.so"
 
 OK = 0
 E_ARG, E_CUDA, E_STATE, E_CAPACITY, E_UNDEFINED, E_TIMEOUT = -1, -2, -3, -4, -5, -6
-MODE_COMPAT, MODE_CANONICAL, MODE_CLASSIC = 0, 1, 2
+MODE_COMPAT, MODE_CANONICAL, MODE_CLASSIC, MODE_PATH_TRACING = 0, 1, 2, 3
 FLAG_COUNT_TRAVERSAL = 0x1
 FLAG_LEARNED = 0x2
 FLAG_LEARNED_FROZEN = 0x4

@@ -361,10 +361,40 @@ def gen_classic():
          threads=np.array(rh.num_threads()), halton=hal)
 
 
+def gen_path_trace():
+    """Two samples per pixel of PathTracing::render (pseudo-random sampler,
+    N = 8 streams) on the small mixed-material scene."""
+    sc = S.small_test_scene(seed=3, subdiv=3, width=64, height=48, photons=20000)
+    sc.env = quantize_env(sc.env)
+    R = rh.RefScene(sc)
+    acc = R.path_trace(sc.camera, sc.photons, 2)
+    a = scene_arrays(sc)
+    cam = sc.camera
+    save("path_trace", **a, accum=acc, eye=np.array(cam.eye), dir=np.array(cam.dir), up=np.array(cam.up),
+         fov=np.array(cam.fov), wh=np.array([cam.width, cam.height]), nphotons=np.array(sc.photons),
+         threads=np.array(rh.num_threads()))
+
+
+def gen_path_trace_sss():
+    """Two samples per pixel of PathTracing::render with subsurface
+    scattering, in a fresh process (process-wide Poisson RNG), time(NULL)
+    fixed at 1234567 + t - 1 for sample t's subsurface photons."""
+    sc = S.small_sss_scene()
+    sc.env = quantize_env(sc.env)
+    R = rh.RefScene(sc)
+    acc = R.path_trace(sc.camera, sc.photons, 2, sss_time=1234567)
+    a = scene_arrays(sc)
+    cam = sc.camera
+    save("path_trace_sss", **a, accum=acc, eye=np.array(cam.eye), dir=np.array(cam.dir), up=np.array(cam.up),
+         fov=np.array(cam.fov), wh=np.array([cam.width, cam.height]), nphotons=np.array(sc.photons),
+         threads=np.array(rh.num_threads()), sss_time=np.array(1234567))
+
+
 GENERATORS.update({"knn": gen_knn, "gather": gen_gather, "render": gen_render, "dipole": gen_dipole,
-                   "sss_irradiance": gen_sss_irradiance})
+                   "sss_irradiance": gen_sss_irradiance, "path_trace": gen_path_trace})
 # generators that need a fresh process (process-wide reference RNG state)
-FRESH = {"poisson": gen_poisson, "render_sss": gen_sss_render, "classic": gen_classic}
+FRESH = {"poisson": gen_poisson, "render_sss": gen_sss_render, "classic": gen_classic,
+         "path_trace_sss": gen_path_trace_sss}
 # fresh processes that must run with a given OpenMP thread count
 FRESH_THREADS = {"classic": "1"}
 
