@@ -197,12 +197,18 @@ __device__ __forceinline__ bool registersInto(const int* __restrict__ b, uint32_
     return false;
 }
 
-// Earlier candidates that block candidate c. kFill = false counts them,
-// kFill = true writes them at cnt[c] (exclusive offsets).
-template <bool kFill>
+// Earlier candidates that block candidate c. kMode 0 counts them into
+// cnt[c]; 1 writes them at cnt[c] (exclusive offsets); 2 (one pass) writes
+// the first kConflictSlots of them at list[c * kConflictSlots], their count
+// into cnt[c] and the largest count into *maxCount.
+constexpr int kConflictSlots = 16;
+
+template <int kMode>
 __global__ void kConflicts(GridDev g, const double* __restrict__ pos, const uint32_t* __restrict__ own,
                            const int* __restrict__ box, const int* __restrict__ rank, int64_t n, uint32_t hsize,
-                           double dd, float reach, uint32_t* __restrict__ cnt, int* __restrict__ list) {
+                           double dd, float reach, uint32_t* __restrict__ cnt, int* __restrict__ list,
+                           unsigned* __restrict__ maxCount) {
+    constexpr bool kFill = kMode == 1;
     for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
         const double cx = pos[3 * c], cy = pos[3 * c + 1], cz = pos[3 * c + 2];
         const float fx = (float)cx, fy = (float)cy, fz = (float)cz;
@@ -211,7 +217,7 @@ __global__ void kConflicts(GridDev g, const double* __restrict__ pos, const uint
         const int gx = cellCoord(fx, g.ox, g.invCell, g.nx), gy = cellCoord(fy, g.oy, g.invCell, g.ny),
                   gz = cellCoord(fz, g.oz, g.invCell, g.nz);
         uint32_t k = 0;
-        const uint32_t base = kFill ? cnt[c] : 0u;
+        const uint32_t base = kFill ? cnt[c] : (kMode == 2 ? (uint32_t)c * kConflictSlots : 0u);
         for (int dz = -1; dz <= 1; dz++) {
             const int zz = gz + dz;
             if (zz < 0 || zz >= g.nz) continue;
@@ -239,24 +245,29 @@ __global__ void kConflicts(GridDev g, const double* __restrict__ pos, const uint
                         const double q2 = dadd(dadd(dmul(qx, qx), dmul(qy, qy)), dmul(qz, qz));
                         if (!(q2 <= dd)) continue;
                         if (!registersInto(box + 6 * (size_t)p, hc, hsize)) continue;
-                        if (kFill) list[base + k] = p;
+                        if (kFill || (kMode == 2 && k < kConflictSlots)) list[base + k] = p;
                         k++;
                     }
                 }
             }
         }
         if (!kFill) cnt[c] = k;
+        if (kMode == 2 && k > kConflictSlots) atomicMax(maxCount, k);
     }
 }
 
-// One round: state 0 undecided, 1 accepted, 2 rejected.
-__global__ void kDecide(const uint32_t* __restrict__ offs, const int* __restrict__ list, int64_t n,
+// One round: state 0 undecided, 1 accepted, 2 rejected. kSlots: the lists
+// of kConflicts<2> (conf = counts), else CSR (conf = offsets).
+template <bool kSlots>
+__global__ void kDecide(const uint32_t* __restrict__ conf, const int* __restrict__ list, int64_t n,
                         uint8_t* __restrict__ state, unsigned long long* __restrict__ undecided) {
     unsigned left = 0;
     for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
         if (state[c] != 0) continue;
         bool open = false, blocked = false;
-        for (uint32_t j = offs[c]; j < offs[c + 1]; j++) {
+        const uint32_t j0 = kSlots ? (uint32_t)c * kConflictSlots : conf[c];
+        const uint32_t j1 = kSlots ? j0 + conf[c] : conf[c + 1];
+        for (uint32_t j = j0; j < j1; j++) {
             const uint8_t s = ((volatile uint8_t*)state)[list[j]];
             if (s == 1) { blocked = true; break; }
             if (s == 0) open = true;
@@ -420,30 +431,51 @@ int poissonRun(pppm_ctx* c, PoissonGpu& g, uint32_t rng[4], float4* queries, flo
     PPPM_CUDA(c, gridBuild(g.grid, gv, g.rec.as<float4>(), cntD, n, st));
     gv = gridView(g.grid, mn, mx);
     uint32_t* conf = g.conf.as<uint32_t>();
-    kConflicts<false><<<gridFor(n, 128), 128, 0, st>>>(gv, g.pos.as<double>(), g.own.as<uint32_t>(), g.box.as<int>(),
-                                                       g.rank.as<int>(), n, (uint32_t)n, d * d, reach, conf, nullptr);
-    PPPM_CUDA(c, exclusiveScan(conf, n, g.cursor.as<uint32_t>(), g.tmp.as<uint32_t>(), st));
-    uint32_t links = 0;
-    PPPM_CUDA(c, cudaMemcpyAsync(&links, conf + n, 4, cudaMemcpyDeviceToHost, st));
+    // one pass into fixed slots; a candidate with more conflicts than slots
+    // sends the whole set through the counted CSR form (its counts are in conf)
+    PPPM_CUDA(c, g.list.ensure((size_t)std::max<int64_t>(n, 1) * kConflictSlots * 4));
+    unsigned* maxCount = reinterpret_cast<unsigned*>(g.misc.as<char>() + 16);
+    PPPM_CUDA(c, cudaMemsetAsync(maxCount, 0, 4, st));
+    kConflicts<2><<<gridFor(n, 128), 128, 0, st>>>(gv, g.pos.as<double>(), g.own.as<uint32_t>(), g.box.as<int>(),
+                                                   g.rank.as<int>(), n, (uint32_t)n, d * d, reach, conf,
+                                                   g.list.as<int>(), maxCount);
+    unsigned over = 0;
+    PPPM_CUDA(c, cudaMemcpyAsync(&over, maxCount, 4, cudaMemcpyDeviceToHost, st));
     PPPM_CUDA(c, cudaStreamSynchronize(st));
-    PPPM_CUDA(c, g.list.ensure((size_t)std::max<uint32_t>(links, 1) * 4));
-    kConflicts<true><<<gridFor(n, 128), 128, 0, st>>>(gv, g.pos.as<double>(), g.own.as<uint32_t>(), g.box.as<int>(),
-                                                      g.rank.as<int>(), n, (uint32_t)n, d * d, reach, conf,
-                                                      g.list.as<int>());
+    const bool slots = over == 0;
+    if (!slots) {
+        PPPM_CUDA(c, exclusiveScan(conf, n, g.cursor.as<uint32_t>(), g.tmp.as<uint32_t>(), st));
+        uint32_t links = 0;
+        PPPM_CUDA(c, cudaMemcpyAsync(&links, conf + n, 4, cudaMemcpyDeviceToHost, st));
+        PPPM_CUDA(c, cudaStreamSynchronize(st));
+        PPPM_CUDA(c, g.list.ensure((size_t)std::max<uint32_t>(links, 1) * 4));
+        kConflicts<1><<<gridFor(n, 128), 128, 0, st>>>(gv, g.pos.as<double>(), g.own.as<uint32_t>(), g.box.as<int>(),
+                                                       g.rank.as<int>(), n, (uint32_t)n, d * d, reach, conf,
+                                                       g.list.as<int>(), nullptr);
+    }
     PPPM_CUDA(c, cudaMemsetAsync(g.state.p, 0, (size_t)n, st));
     unsigned long long* und = reinterpret_cast<unsigned long long*>(g.misc.as<char>() + 8);
-    // each round decides at least the earliest undecided candidate
+    // each round decides at least the earliest undecided candidate; rounds
+    // go in groups of kRoundsPerSync between reads of the undecided count
+    // (rounds after the last decision change nothing)
+    constexpr int kRoundsPerSync = 4;
     int64_t rounds = 0;
-    for (;; rounds++) {
+    for (;;) {
         if (rounds > n + 1) return fail(c, PPPM_E_CUDA, "poisson: decision rounds did not converge");
-        PPPM_CUDA(c, cudaMemsetAsync(und, 0, 8, st));
-        kDecide<<<gridFor(n, 256), 256, 0, st>>>(conf, g.list.as<int>(), n, g.state.as<uint8_t>(), und);
+        for (int r = 0; r < kRoundsPerSync; r++) {
+            if (r == kRoundsPerSync - 1) PPPM_CUDA(c, cudaMemsetAsync(und, 0, 8, st));
+            if (slots)
+                kDecide<true><<<gridFor(n, 256), 256, 0, st>>>(conf, g.list.as<int>(), n, g.state.as<uint8_t>(), und);
+            else
+                kDecide<false><<<gridFor(n, 256), 256, 0, st>>>(conf, g.list.as<int>(), n, g.state.as<uint8_t>(), und);
+        }
+        rounds += kRoundsPerSync;
         unsigned long long left = 0;
         PPPM_CUDA(c, cudaMemcpyAsync(&left, und, 8, cudaMemcpyDeviceToHost, st));
         PPPM_CUDA(c, cudaStreamSynchronize(st));
         if (left == 0) break;
     }
-    g.rounds = rounds + 1;
+    g.rounds = rounds;
     uint32_t* flag = g.flag.as<uint32_t>();
     kPopFlags<<<gridFor(n, 256), 256, 0, st>>>(g.state.as<uint8_t>(), g.rank.as<int>(), n, g.byPop.as<int>(), flag);
     PPPM_CUDA(c, exclusiveScan(flag, n, g.cursor.as<uint32_t>(), g.tmp.as<uint32_t>(), st));
