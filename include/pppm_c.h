@@ -349,7 +349,8 @@ int pppm_render_graph(pppm_ctx* ctx, int32_t count, pppm_pass_stats* stats);
 
 /* Launch-shape knobs of an active render, applied from the next pass on
  * (values <= 0 keep the current one): hash-grid cell factor (>= 1), photon
- * bounce and eye kernel blocks per SM. None changes results beyond the order
+ * bounce and eye kernel blocks per SM (grid caps; default 64, at most 64).
+ * None changes results beyond the order
  * of floating-point accumulation; the batch autotuner sets them. No
  * counterpart in the reference. */
 int pppm_render_tune(pppm_ctx* ctx, float cell_factor, int32_t bounce_blocks_per_sm, int32_t eye_blocks_per_sm);

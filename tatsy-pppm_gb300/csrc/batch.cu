@@ -59,7 +59,7 @@ struct Shape {
     float cell;
     int bounce, eye;
 };
-const Shape kShapes[] = {{1.0f, 16, 16}, {1.0f, 8, 8}, {1.0f, 32, 32}, {1.25f, 16, 16}, {1.5f, 16, 16}};
+const Shape kShapes[] = {{1.0f, 64, 64}, {1.0f, 16, 16}, {1.0f, 32, 32}, {1.25f, 64, 64}, {1.5f, 64, 64}};
 
 int runJob(pppm_batch::Job& j, bool autotune, bool useGraph) {
     pppm_ctx* c = j.ctx;

@@ -271,8 +271,11 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     rs.cam = *cam;
     rs.par = *par;
     if (!(rs.par.cell_factor >= 1.0f)) rs.par.cell_factor = 1.0f;
-    rs.bouncePerSm = 16;
-    rs.eyePerSm = 16;
+    // grid caps of the trace kernels (blocks of 128 per SM): more blocks
+    // than can be resident balance the long paths better; 64 measured
+    // fastest on the 1080p workload (16: +4% pass time)
+    rs.bouncePerSm = 64;
+    rs.eyePerSm = 64;
     const double dx = c->bbmax[0] - c->bbmin[0], dy = c->bbmax[1] - c->bbmin[1], dz = c->bbmax[2] - c->bbmin[2];
     rs.bboxDiag = std::sqrt(dx * dx + dy * dy + dz * dz);
     rs.radius = rs.bboxDiag * par->radius_scale;  // ppm_probabilistic.cc:51-55
