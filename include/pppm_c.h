@@ -347,6 +347,17 @@ int pppm_render_pass(pppm_ctx* ctx, int32_t t, pppm_pass_stats* stats);
  * and gather) are device times, ms_grid and ms_eye 0. */
 int pppm_render_graph(pppm_ctx* ctx, int32_t count, pppm_pass_stats* stats);
 
+/* Advances an active render by `count` passes without rendering them: the
+ * pass count, the radius schedule and (compat, path tracing) the streams'
+ * tapes move on as if the passes had run, and nothing is accumulated (no
+ * counterpart in the reference). For sharding the passes of one image over
+ * processes or GPUs: a process that renders passes t = r + 1, r + 1 + n, ...
+ * (skipping the others) accumulates exactly those passes, and the sum of
+ * the n accumulators is the render of all passes up to the order of float
+ * sums. Not for classic PPM, the subsurface stage or the learned proposal
+ * (their passes depend on earlier ones): PPPM_E_STATE. */
+int pppm_render_skip(pppm_ctx* ctx, int32_t count);
+
 /* Launch-shape knobs of an active render, applied from the next pass on
  * (values <= 0 keep the current one): hash-grid cell factor (>= 1), photon
  * bounce and eye kernel blocks per SM (grid caps; default 64, at most 64).

@@ -603,6 +603,34 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     return PPPM_OK;
 }
 
+int pppm_render_skip(pppm_ctx* c, int32_t count) {
+    if (!c || count < 0) return fail(c, PPPM_E_ARG, "render_skip: bad arguments");
+    RenderState& rs = c->rs;
+    if (!rs.active) return fail(c, PPPM_E_STATE, "render_skip: call render_begin first");
+    const pppm_params& par = rs.par;
+    if ((par.mode != PPPM_MODE_CANONICAL && par.mode != PPPM_MODE_COMPAT && par.mode != PPPM_MODE_PATH_TRACING) ||
+        rs.sss.enabled || rs.guide.enabled)
+        return fail(c, PPPM_E_STATE,
+                    "render_skip: passes depend on earlier ones here (classic PPM, subsurface stage, learned proposal)");
+    const int N = par.num_streams;
+    const int W = rs.cam.width, H = rs.cam.height;
+    const int64_t T = par.mode == PPPM_MODE_PATH_TRACING ? 0 : rs.taskPerThread;
+    for (int i = 0; i < count; i++) {
+        const int t = rs.passesDone + 1;
+        // what pass t would leave behind: its radius update and, with the
+        // reference's streams, the tapes it would have drawn
+        if (par.mode == PPPM_MODE_COMPAT) rs.radius = (t + 1.0) / (t + par.alpha) * rs.radius;
+        else if (par.mode == PPPM_MODE_CANONICAL) rs.radius = rs.radius * std::sqrt((t + par.alpha) / (t + 1.0));
+        if (par.mode != PPPM_MODE_CANONICAL)
+            for (int s = 0; s < N; s++) {
+                const int64_t rows = s < H ? (H - 1 - s) / N + 1 : 0;
+                xorshiftJumpHost(c->jumpTables, (uint64_t)(T + rows * W), &rs.streams[s]);
+            }
+        rs.passesDone = t;
+    }
+    return PPPM_OK;
+}
+
 int pppm_render_tune(pppm_ctx* c, float cell_factor, int32_t bounce_blocks_per_sm, int32_t eye_blocks_per_sm) {
     if (!c) return PPPM_E_ARG;
     if (!c->rs.active) return fail(c, PPPM_E_STATE, "render_tune: no render");

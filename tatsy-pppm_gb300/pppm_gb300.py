@@ -101,6 +101,7 @@ SIGNATURES = {
                   ctypes.c_int32], ctypes.c_int),
     "pppm_dipole_rd": ([_VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_render_graph": ([_VP, ctypes.c_int32, _VP], ctypes.c_int),
+    "pppm_render_skip": ([_VP, ctypes.c_int32], ctypes.c_int),
     "pppm_render_image": ([_VP, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_png_encode": ([_VP, ctypes.c_int32, ctypes.c_int32, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_render_save": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
@@ -433,6 +434,10 @@ class Context:
         # the checkpoint header: magic (8 bytes), version, header size, camera
         self._cam = Camera.from_buffer_copy(bytes(blob[16:16 + ctypes.sizeof(Camera)]))
 
+    def render_skip(self, count):
+        """pppm_render_skip: advance the render by `count` passes without rendering them."""
+        self._check(self.lib.pppm_render_skip(self.h, int(count)))
+
     def render_graph(self, count):
         """pppm_render_graph: the next `count` canonical passes as one CUDA graph launch."""
         st = (PassStats * int(count))()
@@ -512,6 +517,42 @@ class Batch:
         self._check(self.lib.pppm_batch_result(self.h, int(job_id), out.ctypes.data if image else None,
                                                ctypes.byref(st)))
         return out, st.as_dict()
+
+
+def shard_passes(total, rank, world):
+    """Passes 1..total of one image dealt round robin over `world` ranks:
+    rank r renders r + 1, r + 1 + world, ..."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad rank / world")
+    return list(range(rank + 1, total + 1, world))
+
+
+def render_shard(ctx, camera, params, total, rank, world):
+    """Renders this rank's passes of a `total`-pass image (pppm_render_skip
+    over the others) and returns its accumulation buffer (not divided)."""
+    ctx.render_begin(camera, params)
+    done = 0
+    for t in shard_passes(total, rank, world):
+        if t - 1 > done:
+            ctx.render_skip(t - 1 - done)
+        ctx.render_pass(t)
+        done = t
+    return ctx.render_read()
+
+
+def merge_shards(accum, total, group=None):
+    """The image of all `total` passes from each rank's accumulation buffer:
+    one sum over the ranks (torch.distributed, when initialised), divided by
+    the pass count. accum: numpy array (host)."""
+    import torch
+
+    t = torch.from_numpy(np.ascontiguousarray(accum, np.float32))
+    if torch.distributed.is_available() and torch.distributed.is_initialized():
+        nccl = torch.distributed.get_backend(group) == "nccl"
+        x = t.cuda() if nccl else t
+        torch.distributed.all_reduce(x, op=torch.distributed.ReduceOp.SUM, group=group)
+        t = x.cpu() if nccl else x
+    return t.numpy() / float(total)
 
 
 def png_encode(rgb8):
