@@ -3,7 +3,8 @@
 // given on the command line because the reference's contest assets are not
 // all available:
 //
-//   appmain_gpu <width> <height> <spp> <mesh.ply> <env.hdr> <out.ppm> [photons] [compat|canonical]
+//   appmain_gpu <width> <height> <spp> <mesh.ply> <env.hdr> <out.ppm> [photons] [compat|canonical|pt]
+//               [result directory: per-pass PNG files as the reference writes them]
 //
 // The mesh gets a Lambertian material on a checker floor of mirror and
 // Phong tiles like appmain.cc:97-112. The result is written after the last
@@ -18,7 +19,8 @@
 
 int main(int argc, char** argv) {
     if (argc < 7) {
-        std::fprintf(stderr, "usage: %s width height spp mesh.ply env.hdr out.ppm [photons] [compat|canonical]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s width height spp mesh.ply env.hdr out.ppm [photons] [compat|canonical|pt] [dir]\n",
+                     argv[0]);
         return 2;
     }
     const int width = std::atoi(argv[1]);
@@ -48,10 +50,20 @@ int main(int argc, char** argv) {
         const Vector3D eye(-25.0, 5.0, -18.0);
         Camera camera(eye, -eye.normalized(), Vector3D(0.0, 1.0, 0.0), 0.9, width, height, 1.0);
         RenderParameters params(photons, spp, 128, 16.0);
-        ProgressivePhotonMappingProb ppm;
-        ppm.mode = mode == "canonical" ? PPPM_MODE_CANONICAL : PPPM_MODE_COMPAT;
-        ppm.render(scene, camera, params);
-        const std::vector<float> img = ppm.result();
+        const std::string dir = argc >= 10 ? argv[9] : "";
+        std::vector<float> img;
+        if (mode == "pt") {
+            PathTracing pt;
+            pt.resultDirectory = dir;
+            pt.render(scene, camera, params);
+            img = pt.result();
+        } else {
+            ProgressivePhotonMappingProb ppm;
+            ppm.mode = mode == "canonical" ? PPPM_MODE_CANONICAL : PPPM_MODE_COMPAT;
+            ppm.resultDirectory = dir;
+            ppm.render(scene, camera, params);
+            img = ppm.result();
+        }
         FILE* f = std::fopen(argv[6], "wb");
         if (!f) throw pppm::Error(PPPM_E_ARG, std::string("cannot write ") + argv[6]);
         std::fprintf(f, "P6\n%d %d\n255\n", width, height);

@@ -11,7 +11,7 @@
 //   scene.setAccelerator();
 //   Camera camera(eye, dir, up, 45.0, w, h, 1.0);
 //   RenderParameters params(2000000, spp, 128, 16.0);
-//   ProgressivePhotonMappingProb ppm;
+//   ProgressivePhotonMappingProb ppm;     // or ProgressivePhotonMapping, PathTracing
 //   ppm.render(scene, camera, params);
 //
 // Where the reference aborts (Assertion, common.h:24-35) the mirror throws
@@ -52,6 +52,28 @@ inline pppm_ctx* context() {
         ctx.reset(c);
     }
     return ctx.get();
+}
+
+// The current pass's image as the reference saves it (flip, gamma 1/2.2,
+// toByte; ppm_probabilistic.cc:96-106) written to a PNG file.
+inline void savePassPng(pppm_ctx* c, int w, int h, const std::string& filename) {
+    std::vector<uint8_t> rgb((size_t)w * h * 3);
+    check(pppm_render_image(c, 0, rgb.data()), c, "savePng");
+    int64_t n = 0;
+    check(pppm_png_encode(rgb.data(), w, h, nullptr, 0, &n), nullptr, "savePng");
+    std::vector<uint8_t> png((size_t)n);
+    check(pppm_png_encode(rgb.data(), w, h, png.data(), n, &n), nullptr, "savePng");
+    FILE* f = std::fopen(filename.c_str(), "wb");
+    if (!f) throw Error(PPPM_E_ARG, "cannot write " + filename);
+    const size_t wrote = std::fwrite(png.data(), 1, png.size(), f);
+    std::fclose(f);
+    if (wrote != png.size()) throw Error(PPPM_E_ARG, "short write to " + filename);
+}
+
+inline std::string passFile(const std::string& dir, const char* pattern, int t) {
+    char name[64];
+    std::snprintf(name, sizeof(name), pattern, t);
+    return dir + name;
 }
 
 }  // namespace pppm
@@ -343,6 +365,9 @@ public:
     // numStreams is the reference's OMP_NUM_CORE (its RNG stream count).
     int mode = PPPM_MODE_COMPAT;
     int numStreams = 8;
+    // Non-empty: after every pass the image is written to
+    // resultDirectory + "%03d.png", as the reference does with RESULT_DIRECTORY.
+    std::string resultDirectory;
 
     // ProgressivePhotonMappingProb::render (ppm_probabilistic.cc:24-121): the
     // reference writes a PNG per pass; here the linear buffer stays on the
@@ -365,7 +390,11 @@ public:
         // time(NULL) + thread (subsurface_integrator.cc:248)
         p.sss_time = (uint32_t)std::time(nullptr);
         pppm::check(pppm_render_begin(ctx, &camera.c, &p), ctx, "render");
-        for (int t = 1; t <= params.spp(); t++) pppm::check(pppm_render_pass(ctx, t, nullptr), ctx, "render");
+        for (int t = 1; t <= params.spp(); t++) {
+            pppm::check(pppm_render_pass(ctx, t, nullptr), ctx, "render");
+            if (!resultDirectory.empty())
+                pppm::savePassPng(ctx, camera.c.width, camera.c.height, pppm::passFile(resultDirectory, "%03d.png", t));
+        }
         w_ = camera.c.width;
         h_ = camera.c.height;
         passes_ = params.spp();
@@ -391,9 +420,12 @@ public:
     // numStreams is the reference's OMP_NUM_CORE: its Halton sampler count
     // (with more than one, the reference's update order varies per run).
     int numStreams = 8;
+    // Non-empty: after every pass the image is written to resultDirectory +
+    // "progressive_photonmap_%03d.png" (progressive_photon_mapping.cc:103).
+    std::string resultDirectory;
 
-    // ProgressivePhotonMapping::render (progressive_photon_mapping.cc:31-119)
-    // minus the PNG per pass: result() returns the last pass's image.
+    // ProgressivePhotonMapping::render (progressive_photon_mapping.cc:31-119):
+    // result() returns the last pass's image.
     void render(const Scene& /*scene*/, const Camera& camera, const RenderParameters& params) {
         pppm_ctx* ctx = pppm::context();
         pppm_params p{};
@@ -408,7 +440,12 @@ public:
         p.radius_scale = 1.0;
         p.cell_factor = 1.0f;
         pppm::check(pppm_render_begin(ctx, &camera.c, &p), ctx, "render");
-        for (int t = 1; t <= params.spp(); t++) pppm::check(pppm_render_pass(ctx, t, nullptr), ctx, "render");
+        for (int t = 1; t <= params.spp(); t++) {
+            pppm::check(pppm_render_pass(ctx, t, nullptr), ctx, "render");
+            if (!resultDirectory.empty())
+                pppm::savePassPng(ctx, camera.c.width, camera.c.height,
+                                  pppm::passFile(resultDirectory, "progressive_photonmap_%03d.png", t));
+        }
         w_ = camera.c.width;
         h_ = camera.c.height;
         passes_ = params.spp();
@@ -416,6 +453,64 @@ public:
         pppm::check(pppm_render_read(ctx, result_.data()), ctx, "render");
     }
     // (emission + flux / (pi r^2)) * coeff / passes per pixel (:98-103), not flipped.
+    std::vector<float> result() const {
+        std::vector<float> r(result_);
+        for (auto& v : r) v /= (float)(passes_ > 0 ? passes_ : 1);
+        return r;
+    }
+    int width() const { return w_; }
+    int height() const { return h_; }
+};
+
+enum RandomSamplerType {  // random_sampler.h
+    RANDOM_SAMPLER_PSEUDO_RANDOM = 0,
+    RANDOM_SAMPLER_QUASI_MONTE_CARLO = 1
+};
+
+class PathTracing {  // path_tracing.h:20-37
+    std::vector<float> result_;
+    int w_ = 0, h_ = 0, passes_ = 0;
+
+public:
+    // numStreams is the reference's OMP_NUM_CORE (its RNG stream count).
+    int numStreams = 8;
+    // Non-empty: after every sample the image is written to
+    // resultDirectory + "%03d.png" (path_tracing.cc:107-110).
+    std::string resultDirectory;
+
+    // PathTracing::render (path_tracing.cc:23-127) with the pseudo-random
+    // sampler (the quasi-Monte Carlo one is not provided: PPPM_E_ARG);
+    // bounceLimit 64 as executePathTracing's default.
+    void render(const Scene& /*scene*/, const Camera& camera, const RenderParameters& params,
+                RandomSamplerType randomSamplerType = RANDOM_SAMPLER_PSEUDO_RANDOM) {
+        if (randomSamplerType != RANDOM_SAMPLER_PSEUDO_RANDOM)
+            throw pppm::Error(PPPM_E_ARG, "PathTracing: only the pseudo-random sampler");
+        pppm_ctx* ctx = pppm::context();
+        pppm_params p{};
+        p.mode = PPPM_MODE_PATH_TRACING;
+        p.num_streams = numStreams;
+        p.photons = params.photons();
+        p.gather_photons = params.gatherPhotons();
+        p.gather_radius = params.gatherRadius();
+        p.max_bounce_photon = 64;
+        p.max_bounce_eye = 64;
+        p.alpha = 0.7;
+        p.radius_scale = 0.1;
+        p.cell_factor = 1.0f;
+        p.sss_time = (uint32_t)std::time(nullptr);
+        pppm::check(pppm_render_begin(ctx, &camera.c, &p), ctx, "render");
+        for (int t = 1; t <= params.spp(); t++) {
+            pppm::check(pppm_render_pass(ctx, t, nullptr), ctx, "render");
+            if (!resultDirectory.empty())
+                pppm::savePassPng(ctx, camera.c.width, camera.c.height, pppm::passFile(resultDirectory, "%03d.png", t));
+        }
+        w_ = camera.c.width;
+        h_ = camera.c.height;
+        passes_ = params.spp();
+        result_.assign((size_t)w_ * h_ * 3, 0.0f);
+        pppm::check(pppm_render_read(ctx, result_.data()), ctx, "render");
+    }
+    // Linear radiance per pixel (row y = camera row y, not flipped) / samples.
     std::vector<float> result() const {
         std::vector<float> r(result_);
         for (auto& v : r) v /= (float)(passes_ > 0 ? passes_ : 1);

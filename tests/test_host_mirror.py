@@ -77,3 +77,44 @@ def test_appmain_gpu_matches_python_api(tmp_path, golden):
     ref = np.clip(np.power(acc, 1 / 2.2), 0, 1)
     ref = (255.0 * ref).astype(np.uint8)[::-1]
     assert np.mean(np.abs(img.astype(int) - ref.astype(int)) <= 1) > 0.999
+
+
+def _decode_png(data):
+    import struct
+    import zlib
+
+    pos, idat, w, h = 8, b"", 0, 0
+    while pos < len(data):
+        (n,) = struct.unpack(">I", data[pos:pos + 4])
+        typ, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
+        if typ == b"IHDR":
+            w, h = struct.unpack(">II", body[:8])
+        elif typ == b"IDAT":
+            idat += body
+        pos += 12 + n
+    rows = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, 1 + 3 * w)
+    assert (rows[:, 0] == 0).all()
+    return rows[:, 1:].reshape(h, w, 3)
+
+
+@pytest.mark.gpu
+def test_appmain_gpu_path_tracing_writes_pass_pngs(tmp_path, golden):
+    """PathTracing through the mirror with a result directory: one PNG per
+    sample (the reference's %03d.png), holding the same image as the demo's
+    own output after the last sample."""
+    demo = ROOT / "tatsy-pppm_gb300" / "appmain_gpu"
+    assert demo.exists(), "build() makes the demo binary"
+    mesh = S.displace_sphere(S.geodesic_sphere(8), 6.0, 0.05, 2, center=(0.0, -4.0, 0.0)).reshape(-1, 9)
+    S.write_ply(tmp_path / "mesh.ply", mesh)
+    S.write_hdr(tmp_path / "env.hdr", golden("env")["decoded"].astype(np.float32))
+    out = tmp_path / "out"
+    out.mkdir()
+    w, h, spp = 80, 48, 3
+    r = subprocess.run([str(demo), str(w), str(h), str(spp), str(tmp_path / "mesh.ply"), str(tmp_path / "env.hdr"),
+                        str(tmp_path / "out.ppm"), "20000", "pt", str(out) + "/"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert sorted(p.name for p in out.iterdir()) == ["001.png", "002.png", "003.png"]
+    png = _decode_png((out / "003.png").read_bytes())
+    ppm = np.frombuffer((tmp_path / "out.ppm").read_bytes().split(b"255\n", 1)[1], np.uint8).reshape(h, w, 3)
+    assert np.mean(np.abs(png.astype(int) - ppm.astype(int)) <= 1) > 0.999
