@@ -395,7 +395,10 @@ __device__ __forceinline__ int traverseExact(const QNode* __restrict__ nodes, co
 // lane performs the reference's operations in the reference's order: the
 // same box tests against the same (float)best, the same strict updates.
 // All 32 lanes of the warp must call it (inactive lanes pass active=false).
-constexpr int kExactBatch = 8;
+#ifndef PPPM_EXACT_BATCH
+#define PPPM_EXACT_BATCH 8
+#endif
+constexpr int kExactBatch = PPPM_EXACT_BATCH;
 
 __device__ __forceinline__ int traverseExactWarp(const QNode* __restrict__ nodes, const float4* __restrict__ tris,
                                                  int rootCode, bool active, double odx, double ody, double odz,
