@@ -94,14 +94,17 @@ int graphEnqueuePass(pppm_ctx* c, int t, int slot, bool sideEye) {
     // photons: two wavefront bounces, then the tail
     PPPM_CUDA(c, launchPhotonEmit(tp, ev, nullptr, rs.pathA.as<PathState>(), ctr, c->stream));
     if (sideEye) PPPM_CUDA(c, cudaEventRecordWithFlags(e[1], c->stream, cudaEventRecordExternal));
-    const int waves = std::min(par.max_bounce_photon, kWaveBounces);
+    const int waves = kPersistentPhotons ? 0 : std::min(par.max_bounce_photon, kWaveBounces);
+    if (kPersistentPhotons && par.max_bounce_photon > 0)
+        PPPM_CUDA(c, launchPhotonPersistent(tp, sv, rs.pathA.as<PathState>(), paths, rs.photons.as<float4>(),
+                                            rs.depositCap, ctr, c->stream));
     for (int b = 0; b < waves; b++) {
         PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
         PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
         PPPM_CUDA(c, launchPhotonBounce(tp, sv, b, in, out, paths, rs.photons.as<float4>(), rs.depositCap, ctr,
                                         c->stream));
     }
-    if (waves < par.max_bounce_photon) {
+    if (!kPersistentPhotons && waves < par.max_bounce_photon) {
         PathState* in = (waves & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
         PPPM_CUDA(c, launchPhotonTail(tp, sv, waves, in, paths, rs.photons.as<float4>(), rs.depositCap, ctr, c->stream));
     }

@@ -230,6 +230,161 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
 }
 
 
+// The hit of a photon path at triangle slot `slot`, distance `best`
+// (ppm_probabilistic.cc:150-193; subsurface pass: subsurface_integrator.cc:
+// 262-320): three draws from the path's tape, the deposit (store, da, db) on
+// Lambertian (subsurface pass: BSSRDF) surfaces, Russian roulette, and the
+// next ray in p. alive turns false when the path ends here.
+template <bool kSss>
+__device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView& sc, PathState& p, int slot, double best,
+                                          bool& alive, bool& store, float4& da, float4& db) {
+    Tape tape;
+    tape.pos = 0;
+    tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
+    tape.x.s[0] = p.rng[0]; tape.x.s[1] = p.rng[1]; tape.x.s[2] = p.rng[2]; tape.x.s[3] = p.rng[3];
+    const uint32_t r0 = tape.popu(), r1 = tape.popu(), r2 = tape.popu();
+    const float4 a = sc.tris[3 * slot], b = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
+    const int tid = __float_as_int(a.w);
+    const DevMaterial& m = sc.mats[sc.matId[tid]];
+    double hp[3];
+    hitPosition(p.ox, p.oy, p.oz, p.dx, p.dy, p.dz, best, hp);
+    const f3 nrm = triNormalF(a, b, c);
+    const f3 din = {p.dx, p.dy, p.dz};
+    const f3 on = dot(nrm, din) < 0.0f ? nrm : -nrm;
+    f3 flux = {p.fx, p.fy, p.fz};
+    const f3 refl = {m.refl[0], m.refl[1], m.refl[2]};
+    f3 nd;
+    if (kSss) {
+        if (kSss && (m.type & PPPM_BSDF_BSSRDF)) {
+            store = true;
+            da = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
+                             __uint_as_float(packNormal(on)));
+            db = make_float4(flux.x, flux.y, flux.z, __int_as_float(p.id));
+            const float prob = (flux.x + flux.y + flux.z) / 3.0f;
+            if (!(u32ToFloat(r0) < prob)) alive = false;  // rands[0] >= probability: break
+        }
+        if (alive) {
+            const float pdf = bsdfSample(m, din, nrm, r1, r2, &nd);
+            flux = flux * refl * (1.0f / pdf);
+        }
+    } else if (m.type & PPPM_BSDF_LAMBERTIAN) {
+        store = true;
+        da = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
+                         __uint_as_float(packNormal(on)));
+        db = make_float4(flux.x, flux.y, flux.z, __int_as_float(p.id));
+        const int er = p.pad[1] >> kPathEmitRecShift;
+        if (tp.guided && er > 0 && tp.guide.imp) {
+            // emission record: importance-weighted flux of this deposit
+            const int v = impVoxel(tp.guide, da.x, da.y, da.z);
+            if (v >= 0)
+                tp.guide.rec[er - 1].w +=
+                    (0.2126f * flux.x + 0.7152f * flux.y + 0.0722f * flux.z) * __ldg(&tp.guide.imp[v]);
+        }
+        if ((unsigned long long)r0 < m.rrCeil) {  // rands[0] < probability
+            if (tp.guided && tp.guide.guideBounces) {
+                nd = on;  // kGuideResolve draws the direction around the normal
+                p.pad[1] |= kPathNeedsDir;
+            } else {
+                bsdfSample(m, din, on, r1, r2, &nd);
+            }
+            flux = flux * refl * m.invRr;
+        } else {
+            alive = false;
+        }
+    } else {
+        const float pdf = bsdfSample(m, din, on, r0, r1, &nd);
+        flux = flux * refl * (1.0f / pdf);
+    }
+    p.ox = hp[0]; p.oy = hp[1]; p.oz = hp[2];
+    p.dx = nd.x; p.dy = nd.y; p.dz = nd.z;
+    p.fx = flux.x; p.fy = flux.y; p.fz = flux.z;
+    p.rng[0] = tape.x.s[0]; p.rng[1] = tape.x.s[1]; p.rng[2] = tape.x.s[2]; p.rng[3] = tape.x.s[3];
+    p.bounce += 1;
+}
+
+// Every bounce of every emitted photon path in one launch. Warps stay
+// resident and keep their lanes busy: the warp advances its lanes'
+// traversals together until at least kRefill of them have found their hit
+// (or all have), shades those (photonHit: deposit, roulette, next ray), and
+// lanes whose path ended take the next path of the emitted queue (one
+// atomic per warp). A path's own random numbers and traversal are those of
+// the per-bounce kernels; only the order in which paths are processed and
+// deposits appended changes.
+constexpr int kRefill = 8;
+
+template <bool kSss>
+__global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(TraceParams tp, SceneView sc,
+                                                                               const PathState* __restrict__ in,
+                                                                               int64_t maxPaths, float4* __restrict__ dep,
+                                                                               int64_t depCap, PassCounters* ctr) {
+    __shared__ int order[128];
+    __shared__ QNode sTop[kTopNodes];
+    const int64_t n = min((int64_t)ctr->queue[0], maxPaths);
+    loadOrderTable(order);
+    loadTopNodes(sTop, sc.nodes, sc.numNodes);
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    PathState p;
+    WarpTrav s;
+    s.sp = 0;
+    s.ncand = 0;
+    bool has = false;
+    int traced = 0, visits = 0, tests = 0;
+    for (;;) {
+        // lanes without a path take the next ones of the queue
+        const unsigned empty = __ballot_sync(0xffffffffu, !has);
+        if (empty) {
+            const int leader = __ffs(empty) - 1;
+            unsigned long long b = 0;
+            if (lane == leader) b = atomicAdd(&ctr->fetched, (unsigned long long)__popc(empty));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (!has) {
+                const int64_t i = (int64_t)(b + __popc(empty & lt));
+                if (i < n) {
+                    p = in[i];
+                    has = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
+                    if (has) s.begin(sc.rootCode, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz);
+                }
+            }
+            // a path that was dead on arrival leaves its lane empty: refill
+            // again while the queue lasts
+            if (__any_sync(0xffffffffu, !has) && b + __popc(empty) < (unsigned long long)n) continue;
+        }
+        if (!__any_sync(0xffffffffu, has)) break;
+        warpTravRun(s, has, kRefill, sc.nodes, sc.tris, order, sTop, &visits, &tests);
+        const bool fin = has && s.done();
+        bool store = false;
+        float4 da, db;
+        if (fin) {
+            traced++;
+            bool alive = true;
+            if (s.hit < 0) {
+                alive = false;
+            } else {
+                photonHit<kSss>(tp, sc, p, s.hit, s.best, alive, store, da, db);
+                if (alive) alive = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
+            }
+            if (alive) s.begin(sc.rootCode, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz);
+            else has = false;
+        }
+        const unsigned long long di = warpAppend(store, &ctr->deposits);
+        if (store && (int64_t)di < depCap) {
+            dep[2 * di] = da;
+            dep[2 * di + 1] = db;
+        }
+    }
+    const unsigned nt = __reduce_add_sync(0xffffffffu, (unsigned)traced);
+    if (lane == 0 && nt) atomicAdd(&ctr->photonRays, (unsigned long long)nt);
+    if (tp.countTraversal) {
+        const unsigned nv = __reduce_add_sync(0xffffffffu, (unsigned)visits);
+        const unsigned nx = __reduce_add_sync(0xffffffffu, (unsigned)tests);
+        if (lane == 0) {
+            atomicAdd(&ctr->nodeVisits[0], (unsigned long long)nv);
+            atomicAdd(&ctr->triTests[0], (unsigned long long)nx);
+        }
+    }
+}
+
 // One bounce of every live photon path (ppm_probabilistic.cc:150-193):
 // closest hit, three draws, deposit + Russian roulette on Lambertian
 // surfaces, BSDF sampling elsewhere. Survivors are compacted into `out`
@@ -292,68 +447,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
             if (slot < 0) {
                 alive = false;
             } else {
-                Tape tape;
-                tape.pos = 0;
-                tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
-                tape.x.s[0] = p.rng[0]; tape.x.s[1] = p.rng[1]; tape.x.s[2] = p.rng[2]; tape.x.s[3] = p.rng[3];
-                const uint32_t r0 = tape.popu(), r1 = tape.popu(), r2 = tape.popu();
-                const float4 a = sc.tris[3 * slot], b = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
-                const int tid = __float_as_int(a.w);
-                const DevMaterial& m = sc.mats[sc.matId[tid]];
-                double hp[3];
-                hitPosition(p.ox, p.oy, p.oz, p.dx, p.dy, p.dz, best, hp);
-                const f3 nrm = triNormalF(a, b, c);
-                const f3 din = {p.dx, p.dy, p.dz};
-                const f3 on = dot(nrm, din) < 0.0f ? nrm : -nrm;
-                f3 flux = {p.fx, p.fy, p.fz};
-                const f3 refl = {m.refl[0], m.refl[1], m.refl[2]};
-                f3 nd;
-                if (kSss) {
-                    if (kSss && (m.type & PPPM_BSDF_BSSRDF)) {
-                        store = true;
-                        da = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
-                                         __uint_as_float(packNormal(on)));
-                        db = make_float4(flux.x, flux.y, flux.z, __int_as_float(p.id));
-                        const float prob = (flux.x + flux.y + flux.z) / 3.0f;
-                        if (!(u32ToFloat(r0) < prob)) alive = false;  // rands[0] >= probability: break
-                    }
-                    if (alive) {
-                        const float pdf = bsdfSample(m, din, nrm, r1, r2, &nd);
-                        flux = flux * refl * (1.0f / pdf);
-                    }
-                } else if (m.type & PPPM_BSDF_LAMBERTIAN) {
-                    store = true;
-                    da = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
-                                     __uint_as_float(packNormal(on)));
-                    db = make_float4(flux.x, flux.y, flux.z, __int_as_float(p.id));
-                    const int er = p.pad[1] >> kPathEmitRecShift;
-                    if (tp.guided && er > 0 && tp.guide.imp) {
-                        // emission record: importance-weighted flux of this deposit
-                        const int v = impVoxel(tp.guide, da.x, da.y, da.z);
-                        if (v >= 0)
-                            tp.guide.rec[er - 1].w +=
-                                (0.2126f * flux.x + 0.7152f * flux.y + 0.0722f * flux.z) * __ldg(&tp.guide.imp[v]);
-                    }
-                    if ((unsigned long long)r0 < m.rrCeil) {  // rands[0] < probability
-                        if (tp.guided && tp.guide.guideBounces) {
-                            nd = on;  // kGuideResolve draws the direction around the normal
-                            p.pad[1] |= kPathNeedsDir;
-                        } else {
-                            bsdfSample(m, din, on, r1, r2, &nd);
-                        }
-                        flux = flux * refl * m.invRr;
-                    } else {
-                        alive = false;
-                    }
-                } else {
-                    const float pdf = bsdfSample(m, din, on, r0, r1, &nd);
-                    flux = flux * refl * (1.0f / pdf);
-                }
-                p.ox = hp[0]; p.oy = hp[1]; p.oz = hp[2];
-                p.dx = nd.x; p.dy = nd.y; p.dz = nd.z;
-                p.fx = flux.x; p.fy = flux.y; p.fz = flux.z;
-                p.rng[0] = tape.x.s[0]; p.rng[1] = tape.x.s[1]; p.rng[2] = tape.x.s[2]; p.rng[3] = tape.x.s[3];
-                p.bounce += 1;
+                photonHit<kSss>(tp, sc, p, slot, best, alive, store, da, db);
                 if (kTail && alive)
                     alive = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
             }
@@ -622,6 +716,17 @@ cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int b
         kPhotonBounce<true, false><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths, deposits, depositCap, ctr);
     else
         kPhotonBounce<false, false><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths, deposits, depositCap, ctr);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPhotonPersistent(const TraceParams& tp, const SceneView& sc, const PathState* in, int64_t maxPaths,
+                                   float4* deposits, int64_t depositCap, PassCounters* ctr, cudaStream_t st) {
+    // resident warps only: every block stays until the queue is drained
+    const unsigned blocks = 152 * PPPM_TRACE_MINBLOCKS;
+    if (tp.sssPass)
+        kPhotonPersistent<true><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr);
+    else
+        kPhotonPersistent<false><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr);
     return cudaGetLastError();
 }
 

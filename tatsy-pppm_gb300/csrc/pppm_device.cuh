@@ -504,6 +504,131 @@ __device__ __forceinline__ int traverseExactWarp(const QNode* __restrict__ nodes
     return hit;
 }
 
+// Resumable form of traverseExactWarp for persistent kernels: one lane's
+// traversal state, advanced by the whole warp (warpTravRun) until enough
+// lanes have finished that the kernel can give them new rays. Each lane
+// still performs the reference's operations in the reference's order (the
+// same box tests against the same (float)best, the same strict updates), so
+// the hits equal traverseExact's.
+struct WarpTrav {
+    int stack[kStackSize];
+    int sp;
+    double best;
+    float bestf;
+    int hit;
+    int cand0, cand1, cand2, ncand;
+    double odx, ody, odz;
+    float dx, dy, dz;
+    float ox, oy, oz, idx, idy, idz;
+    int sgnBits;
+
+    __device__ __forceinline__ void begin(int rootCode, double x, double y, double z, float ux, float uy, float uz) {
+        odx = x; ody = y; odz = z;
+        dx = ux; dy = uy; dz = uz;
+        ox = __double2float_rn(x); oy = __double2float_rn(y); oz = __double2float_rn(z);
+        idx = ux == 0.0f ? 1.0e20f : __frcp_rn(ux);
+        idy = uy == 0.0f ? 1.0e20f : __frcp_rn(uy);
+        idz = uz == 0.0f ? 1.0e20f : __frcp_rn(uz);
+        const int sx = idx > 0.0f ? 0 : 1, sy = idy > 0.0f ? 0 : 1, sz = idz > 0.0f ? 0 : 1;
+        sgnBits = sx | (sy << 1) | (sz << 2);
+        sp = 0;
+        stack[sp++] = rootCode;
+        best = kInfty;
+        bestf = 1.0e20f;
+        hit = -1;
+        ncand = 0;
+    }
+    __device__ __forceinline__ bool done() const { return sp == 0 && ncand == 0; }
+};
+
+// Advances the traversals of the lanes in `live` until every one of them is
+// done or at least minDone of them are (lanes outside `live` only take part
+// in the warp votes). All 32 lanes call it.
+__device__ __forceinline__ void warpTravRun(WarpTrav& s, bool live, int minDone, const QNode* __restrict__ nodes,
+                                            const float4* __restrict__ tris, const int* orderTab, const QNode* sTop,
+                                            int* nodeVisits, int* triTests) {
+    for (;;) {
+        const bool canRun = live && s.sp > 0 && s.ncand == 0;
+        const unsigned runMask = __ballot_sync(0xffffffffu, canRun);
+        const unsigned pendMask = __ballot_sync(0xffffffffu, live && s.ncand > 0);
+        if ((runMask | pendMask) == 0) break;
+        if (__popc(__ballot_sync(0xffffffffu, live && s.done())) >= minDone) break;
+        if (pendMask != 0 && (__popc(pendMask) >= kExactBatch || runMask == 0)) {
+            if (live && s.ncand > 0) {
+                const double ddx = s.dx, ddy = s.dy, ddz = s.dz;
+                for (int c = 0; c < s.ncand; c++) {
+                    const int slot = c == 0 ? s.cand0 : (c == 1 ? s.cand1 : s.cand2);
+                    const float4 a = tris[3 * slot], b = tris[3 * slot + 1], cc = tris[3 * slot + 2];
+                    double t;
+                    if (triHitExact(s.odx, s.ody, s.odz, ddx, ddy, ddz, a, b, cc, &t) && s.best > t) {
+                        s.best = t;
+                        s.bestf = __double2float_rn(t);
+                        s.hit = slot;
+                    }
+                }
+                s.ncand = 0;
+            }
+            continue;
+        }
+        if (!canRun) continue;
+        const int code = s.stack[--s.sp];
+        if (code < 0) {
+            const int lc = ~code;
+            const int first = lc >> 2, cnt = lc & 3;
+            for (int i = 0; i < cnt; i++) {
+                const int slot = first + i;
+                const float4 a = tris[3 * slot], b = tris[3 * slot + 1], c = tris[3 * slot + 2];
+                (*triTests)++;
+                if (!triMayHit(s.ox, s.oy, s.oz, s.dx, s.dy, s.dz, a, b, c, s.bestf)) continue;
+                if (s.ncand == 0) s.cand0 = slot; else if (s.ncand == 1) s.cand1 = slot; else s.cand2 = slot;
+                s.ncand++;
+            }
+            continue;
+        }
+        (*nodeVisits)++;
+        const QNode* nd = (sTop != nullptr && code < kTopNodes) ? sTop + code : nodes + code;
+        const float hd = s.bestf;
+        float tmin[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        float tmax[4] = {hd, hd, hd, hd};
+        const float o3[3] = {s.ox, s.oy, s.oz};
+        const float i3[3] = {s.idx, s.idy, s.idz};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const float4 lo = nd->bmin[d];
+            const float4 hi = nd->bmax[d];
+            const bool neg = (s.sgnBits >> d) & 1;
+            const float4 nearB = neg ? hi : lo;
+            const float4 farB = neg ? lo : hi;
+            const float nb[4] = {nearB.x, nearB.y, nearB.z, nearB.w};
+            const float fb[4] = {farB.x, farB.y, farB.z, farB.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float t0 = __fmul_rn(__fsub_rn(nb[k], o3[d]), i3[d]);
+                const float t1 = __fmul_rn(__fsub_rn(fb[k], o3[d]), i3[d]);
+                tmin[k] = tmin[k] > t0 ? tmin[k] : t0;
+                tmax[k] = tmax[k] < t1 ? tmax[k] : t1;
+            }
+        }
+        int hitMask = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) hitMask |= (tmax[k] >= tmin[k]) ? (1 << k) : 0;
+        if (hitMask != 0) {
+            const int4 ch = nd->child;
+            const int meta = nd->meta.x;
+            const int a0 = meta & 3, a1 = (meta >> 2) & 3, a2 = (meta >> 4) & 3;
+            const int sepMask = (((s.sgnBits >> a0) & 1) << 2) | (((s.sgnBits >> a1) & 1) << 1) | ((s.sgnBits >> a2) & 1);
+            int ord = orderTab[hitMask * 8 + sepMask];
+            const int c4[4] = {ch.x, ch.y, ch.z, ch.w};
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                if (ord & 0x04) break;
+                s.stack[s.sp++] = c4[ord & 0x03];
+                ord >>= 4;
+            }
+        }
+    }
+}
+
 // Hit record of the exact path: position o + t*d and the triangle's
 // normal cross(p1-p0, p2-p0).normalized() computed in double like
 // Triangle::normal (triangle.cc:45-47), rounded to float.

@@ -420,6 +420,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
             PPPM_CUDA(c, cudaMemsetAsync(&ctr->undefinedEmit, 0, 8, c->stream));
             PPPM_CUDA(c, cudaMemsetAsync(&ctr->nodeVisits[0], 0, 8, c->stream));
             PPPM_CUDA(c, cudaMemsetAsync(&ctr->triTests[0], 0, 8, c->stream));
+            PPPM_CUDA(c, cudaMemsetAsync(&ctr->fetched, 0, 8, c->stream));
             PPPM_CUDA(c, cudaMemsetAsync(perStream, 0, 8 * (size_t)N, c->stream));
         }
         if (tp.guided && rs.guide.trained) {
@@ -433,8 +434,13 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         // per-bounce launches while the queue is wide, then one tail launch
         // (guided bounces need every bounce as a queue step)
         const bool guideBounces = tp.guided && rs.guide.guideBounces;
-        const int waves = guideBounces ? par.max_bounce_photon : std::min(par.max_bounce_photon, kWaveBounces);
+        const bool persistent = kPersistentPhotons && !guideBounces;
+        const int waves = persistent ? 0
+                          : guideBounces ? par.max_bounce_photon : std::min(par.max_bounce_photon, kWaveBounces);
         launches += 1 + waves + (waves < par.max_bounce_photon ? 1 : 0);
+        if (persistent && par.max_bounce_photon > 0)
+            PPPM_CUDA(c, launchPhotonPersistent(tp, sv, rs.pathA.as<PathState>(), paths, rs.photons.as<float4>(),
+                                                rs.depositCap, ctr, c->stream));
         for (int b = 0; b < waves; b++) {
             PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
             PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();
@@ -446,7 +452,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
                 launches += rs.guide.trained ? 3 : 1;
             }
         }
-        if (waves < par.max_bounce_photon) {
+        if (!persistent && waves < par.max_bounce_photon) {
             PathState* in = (waves & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
             PPPM_CUDA(c, launchPhotonTail(tp, sv, waves, in, paths, rs.photons.as<float4>(), rs.depositCap, ctr,
                                           c->stream));

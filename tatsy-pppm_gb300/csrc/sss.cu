@@ -49,6 +49,11 @@ void packPointQueries(const std::vector<float>& p, const std::vector<float>& n, 
 int tracePhotonsTo(pppm_ctx* c, const TraceParams& tp, const SceneView& sv, int64_t paths, float4* dep, int64_t cap,
                    PassCounters* ctr, int64_t* launches) {
     RenderState& rs = c->rs;
+    if (kPersistentPhotons) {
+        PPPM_CUDA(c, launchPhotonPersistent(tp, sv, rs.pathA.as<PathState>(), paths, dep, cap, ctr, c->stream));
+        *launches += 1;
+        return PPPM_OK;
+    }
     const int waves = std::min(kSssBounceLimit, kWaveBounces);
     for (int b = 0; b < waves; b++) {
         PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();

@@ -37,6 +37,7 @@ struct PassCounters {
     unsigned long long undefinedEye;  // eye paths past their 200-number tape (compat) or the segment cap
     unsigned long long sssQueries;    // subsurface radiance queries queued by the eye pass
     unsigned long long sssVisits;     // octree nodes visited by them (counting flag)
+    unsigned long long fetched;       // paths taken from the emitted queue by the persistent photon kernel
 };
 
 struct CameraDev {
@@ -134,11 +135,21 @@ cudaError_t launchPhotonEmit(const TraceParams& tp, const EnvDev& env, const uin
 cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
                                PathState* out, int64_t maxPaths, float4* deposits, int64_t depositCap,
                                PassCounters* ctr, cudaStream_t st);
+// Every bounce of the emitted queue (ctr->queue[0] paths in `in`) in one
+// persistent launch with dynamic ray fetching (kPhotonPersistent).
+cudaError_t launchPhotonPersistent(const TraceParams& tp, const SceneView& sc, const PathState* in, int64_t maxPaths,
+                                   float4* deposits, int64_t depositCap, PassCounters* ctr, cudaStream_t st);
 // The bounces from `bounce` on of the queue left after the wavefront
 // launches, in one launch (kPhotonBounce<.., true>).
 cudaError_t launchPhotonTail(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
                              int64_t maxPaths, float4* deposits, int64_t depositCap, PassCounters* ctr,
                              cudaStream_t st);
+// Photon passes without guided bounces run in the persistent kernel (1) or
+// as wavefront launches plus the tail kernel (0).
+#ifndef PPPM_PERSISTENT
+#define PPPM_PERSISTENT 1
+#endif
+constexpr bool kPersistentPhotons = PPPM_PERSISTENT != 0;
 // Bounces traced as one launch each before the tail kernel takes the rest.
 #ifndef PPPM_WAVE_BOUNCES
 #define PPPM_WAVE_BOUNCES 2
