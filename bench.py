@@ -368,7 +368,7 @@ def run_gb300(args):
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic, "kernel": "kPhotonBounce (all bounces)",
+                             "frac": achieved / peak, "traffic": traffic, "kernel": "kPhotonPersistent (all photon bounces)",
                              "peak_kind": peak_kind,
                              "algorithmic_bytes_per_pass": alg},
                 "clocks": clocks,

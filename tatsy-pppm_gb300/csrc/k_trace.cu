@@ -310,7 +310,10 @@ __device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView
 // atomic per warp). A path's own random numbers and traversal are those of
 // the per-bounce kernels; only the order in which paths are processed and
 // deposits appended changes.
-constexpr int kRefill = 8;
+#ifndef PPPM_REFILL
+#define PPPM_REFILL 16
+#endif
+constexpr int kRefill = PPPM_REFILL;
 
 template <bool kSss>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(TraceParams tp, SceneView sc,
