@@ -1,13 +1,13 @@
 // Canonical gather with shared-memory staging of grid cells.
 //
-// Queries are counting-sorted by the cell they fall in, then each block
-// takes 128 consecutive sorted queries. For every distinct cell among them
-// the block stages the photons of the cell's 3x3x3 neighbourhood (cell edge
+// Queries are counting-sorted by the cell they fall in, then each warp
+// takes 64 consecutive sorted queries. For every distinct cell among them
+// the warp stages the photons of the cell's 3x3x3 neighbourhood (cell edge
 // >= radius, so the neighbourhood covers every photon within the radius of
-// any query in the cell) into shared memory in rounds of kStage photons, and
-// each query of that cell tests every staged photon. The photons of a
-// neighbourhood are read from L2/HBM once per block instead of once per
-// query; hundreds of eye hit points typically share a cell.
+// any query in the cell) into its shared-memory tile in rounds of kWStage
+// photons, and each query of that cell tests every staged photon. The
+// photons of a neighbourhood are read from L2/HBM once per warp instead of
+// once per query; hundreds of eye hit points typically share a cell.
 #include "kernels.h"
 
 namespace pppm {
@@ -19,7 +19,18 @@ constexpr int kTileQ = 128;  // threads per block
 #define PPPM_GATHER_QPT 2
 #endif
 constexpr int kQ = PPPM_GATHER_QPT;  // queries per thread
-constexpr int kStage = 1024;
+constexpr int kWarps = kTileQ / 32;
+#ifndef PPPM_GATHER_WSTAGE
+#define PPPM_GATHER_WSTAGE 128
+#endif
+constexpr int kWStage = PPPM_GATHER_WSTAGE;  // photons per warp tile
+#ifndef PPPM_GATHER_SUBBITS
+#define PPPM_GATHER_SUBBITS 1
+#endif
+constexpr int kSubBits = PPPM_GATHER_SUBBITS;  // query sort: sub-cells per axis = 2^kSubBits
+#ifndef PPPM_GATHER_MINBLOCKS
+#define PPPM_GATHER_MINBLOCKS 1
+#endif
 
 unsigned blocksFor(int64_t n, int bs, int cap = 152 * 32) {
     const int64_t want = (n + bs - 1) / bs;
@@ -30,13 +41,31 @@ __device__ __forceinline__ int64_t queryCount(const QueryView& qv) {
     return qv.count ? min((int64_t)*qv.count, qv.n) : qv.n;
 }
 
+// Sort key of a query: its cell's bucket, then the Morton index of its
+// sub-cell (2^kSubBits per axis), so that the 64 queries of a warp lie close
+// together and the photons it stages can be culled against their bounding
+// box.
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    uint32_t r = 0;
+#pragma unroll
+    for (int b = 0; b < kSubBits; b++) r |= ((v >> b) & 1u) << (3 * b);
+    return r;
+}
+
 __global__ void kQueryKeys(QueryView qv, GridDev g, uint32_t qmask, uint32_t* __restrict__ keys,
                            uint32_t* __restrict__ hist) {
     const int64_t n = queryCount(qv);
+    constexpr int kSub = 1 << kSubBits;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float4 q0 = qv.q[3 * i];
-        const uint32_t k = bucketOf(cellCoord(q0.x, g.ox, g.invCell, g.nx), cellCoord(q0.y, g.oy, g.invCell, g.ny),
-                                    cellCoord(q0.z, g.oz, g.invCell, g.nz), qmask);
+        const float fx = (q0.x - g.ox) * g.invCell, fy = (q0.y - g.oy) * g.invCell, fz = (q0.z - g.oz) * g.invCell;
+        const int cx = cellCoord(q0.x, g.ox, g.invCell, g.nx), cy = cellCoord(q0.y, g.oy, g.invCell, g.ny),
+                  cz = cellCoord(q0.z, g.oz, g.invCell, g.nz);
+        const uint32_t sx = (uint32_t)min(max(__float2int_rd((fx - (float)cx) * kSub), 0), kSub - 1);
+        const uint32_t sy = (uint32_t)min(max(__float2int_rd((fy - (float)cy) * kSub), 0), kSub - 1);
+        const uint32_t sz = (uint32_t)min(max(__float2int_rd((fz - (float)cz) * kSub), 0), kSub - 1);
+        const uint32_t k = (bucketOf(cx, cy, cz, qmask >> (3 * kSubBits)) << (3 * kSubBits)) | spread3(sx) |
+                           (spread3(sy) << 1) | (spread3(sz) << 2);
         keys[i] = k;
         atomicAdd(&hist[k], 1u);
     }
@@ -53,30 +82,34 @@ __global__ void kQueryScatter(QueryView qv, const uint32_t* __restrict__ keys, u
     }
 }
 
-// Each thread owns kQ consecutive sorted queries (usually of the same cell),
-// so every staged photon is read from shared memory once for kQ tests.
+// Each warp owns 32 * kQ consecutive sorted queries (kQ per lane, usually of
+// one cell) and stages the photons of its cell's 3x3x3 neighbourhood in its
+// own shared-memory tile, synchronising with __syncwarp only: warps whose
+// queries lie in different cells work on their neighbourhoods side by side
+// instead of waiting for one another at block barriers. Every staged photon
+// is read from shared memory once for kQ tests per lane.
 template <bool kAccum, bool kCount>
-__global__ void __launch_bounds__(kTileQ) kGatherTiled(GridDev g, const float4* __restrict__ sq,
+__global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(GridDev g, const float4* __restrict__ sq,
                                                        const uint32_t* __restrict__ qcount, int64_t qcap, float r,
                                                        float* __restrict__ out, unsigned long long* __restrict__ work) {
-    __shared__ float4 sA[kStage];  // pos.xyz, normal.x
-    __shared__ float4 sB[kStage];  // flux.xyz, normal.y
-    __shared__ float sC[kStage];   // normal.z
-    __shared__ uint32_t sKey[27];
-    __shared__ uint32_t sBeg[27];
-    __shared__ uint32_t sOff[28];
-    __shared__ int sNk, sLeader, sCx, sCy, sCz;
+    __shared__ float4 sA[kWarps][kWStage];  // pos.xyz, normal.x
+    __shared__ float4 sB[kWarps][kWStage];  // flux.xyz, normal.y
+    __shared__ float sC[kWarps][kWStage];   // normal.z
 
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t n = qcount ? min((int64_t)*qcount, qcap) : qcap;
-    const int64_t base = (int64_t)blockIdx.x * (kTileQ * kQ);
-    if (base >= n) return;  // uniform for the whole block
+    const int64_t base = ((int64_t)blockIdx.x * kWarps + warp) * (32 * kQ);
+    if (base >= n) return;  // uniform for the warp; the kernel has no block barrier
+    float4* wA = sA[warp];
+    float4* wB = sB[warp];
+    float* wC = sC[warp];
     float4 q0[kQ], q1[kQ], q2[kQ];
     int cx[kQ], cy[kQ], cz[kQ];
     bool valid[kQ], pending[kQ];
     float sx[kQ], sy[kQ], sz[kQ];
 #pragma unroll
     for (int j = 0; j < kQ; j++) {
-        const int64_t i = base + (int64_t)kQ * threadIdx.x + j;
+        const int64_t i = base + (int64_t)kQ * lane + j;
         valid[j] = i < n;
         q0[j] = make_float4(0.f, 0.f, 0.f, 0.f);
         q1[j] = q0[j];
@@ -96,78 +129,79 @@ __global__ void __launch_bounds__(kTileQ) kGatherTiled(GridDev g, const float4* 
     const float r2 = r * r;
     unsigned long long pairs = 0, inside = 0;
     for (;;) {
-        if (threadIdx.x == 0) sLeader = kTileQ * kQ;
-        __syncthreads();
+        // the leader: the first pending query of the warp
+        bool pend = false;
+        int fx = 0, fy = 0, fz = 0;
 #pragma unroll
-        for (int j = 0; j < kQ; j++)
-            if (pending[j]) atomicMin(&sLeader, kQ * (int)threadIdx.x + j);
-        __syncthreads();
-        const int leader = sLeader;
-        if (leader == kTileQ * kQ) break;
-        if ((int)threadIdx.x == leader / kQ) {
-            const int j = leader % kQ;
-            sCx = cx[j];
-            sCy = cy[j];
-            sCz = cz[j];
-        }
-        __syncthreads();
+        for (int j = kQ - 1; j >= 0; j--)
+            if (pending[j]) {
+                pend = true;
+                fx = cx[j];
+                fy = cy[j];
+                fz = cz[j];
+            }
+        const unsigned pm = __ballot_sync(0xffffffffu, pend);
+        if (pm == 0) break;
+        const int leader = __ffs(pm) - 1;
+        const int lx = __shfl_sync(0xffffffffu, fx, leader);
+        const int ly = __shfl_sync(0xffffffffu, fy, leader);
+        const int lz = __shfl_sync(0xffffffffu, fz, leader);
         bool active[kQ];
         bool any = false;
 #pragma unroll
         for (int j = 0; j < kQ; j++) {
-            active[j] = pending[j] && cx[j] == sCx && cy[j] == sCy && cz[j] == sCz;
+            active[j] = pending[j] && cx[j] == lx && cy[j] == ly && cz[j] == lz;
             any |= active[j];
         }
-        if (threadIdx.x == 0) {
-            // the 3x3x3 neighbourhood of the leader's cell, buckets deduplicated
-            int nk = 0;
-            uint32_t off = 0;
-            for (int dz = -1; dz <= 1; dz++)
-                for (int dy = -1; dy <= 1; dy++)
-                    for (int dx = -1; dx <= 1; dx++) {
-                        const int x = sCx + dx, y = sCy + dy, z = sCz + dz;
-                        if (x < 0 || y < 0 || z < 0 || x >= g.nx || y >= g.ny || z >= g.nz) continue;
-                        const uint32_t k = bucketOf(x, y, z, g.mask);
-                        bool dup = false;
-                        for (int t = 0; t < nk; t++) dup |= sKey[t] == k;
-                        if (dup) continue;
-                        const uint32_t b0 = g.start[k], b1 = g.start[k + 1];
-                        if (b1 == b0) continue;
-                        sKey[nk] = k;
-                        sBeg[nk] = b0;
-                        sOff[nk] = off;
-                        off += b1 - b0;
-                        nk++;
-                    }
-            sOff[nk] = off;
-            sNk = nk;
+        // lane i < 27 holds neighbour cell (i % 3 - 1, i / 3 % 3 - 1, i / 9 - 1)
+        // of the leader's cell; a bucket reached from two cells (hash
+        // collision) is kept at its first lane only
+        uint32_t key = 0xffffffffu, b0 = 0, nc = 0;
+        if (lane < 27) {
+            const int x = lx + lane % 3 - 1, y = ly + (lane / 3) % 3 - 1, z = lz + lane / 9 - 1;
+            if (x >= 0 && y >= 0 && z >= 0 && x < g.nx && y < g.ny && z < g.nz) key = bucketOf(x, y, z, g.mask);
         }
-        __syncthreads();
-        const int nk = sNk;
-        const uint32_t total = sOff[nk];
-        for (uint32_t cb = 0; cb < total; cb += kStage) {
-            const uint32_t cnt = min((uint32_t)kStage, total - cb);
-            for (uint32_t t = threadIdx.x; t < cnt; t += kTileQ) {
-                const uint32_t v = cb + t;
-                int b = 0;
-                while (b + 1 < nk && sOff[b + 1] <= v) b++;
-                const int64_t jj = (int64_t)sBeg[b] + (v - sOff[b]);
-                const float4 a = __ldg(&g.rec[2 * jj]);
-                const float4 f = __ldg(&g.rec[2 * jj + 1]);
-                const f3 nn = unpackNormal(__float_as_uint(a.w));
-                sA[t] = make_float4(a.x, a.y, a.z, nn.x);
-                sB[t] = make_float4(f.x, f.y, f.z, nn.y);
-                sC[t] = nn.z;
+        const unsigned same = __match_any_sync(0xffffffffu, key);
+        if (key != 0xffffffffu && (same & ((1u << lane) - 1u)) == 0) {
+            b0 = g.start[key];
+            nc = g.start[key + 1] - b0;
+        }
+        // bounding box of the warp's active queries; a photon farther than r
+        // from the box is farther than r from each of them (kept with a
+        // margin over the rounding of the distance tests)
+        const float inf = __int_as_float(0x7f800000);
+        float blx = inf, bly = inf, blz = inf, bhx = -inf, bhy = -inf, bhz = -inf;
+#pragma unroll
+        for (int j = 0; j < kQ; j++)
+            if (active[j]) {
+                blx = fminf(blx, q0[j].x);
+                bly = fminf(bly, q0[j].y);
+                blz = fminf(blz, q0[j].z);
+                bhx = fmaxf(bhx, q0[j].x);
+                bhy = fmaxf(bhy, q0[j].y);
+                bhz = fmaxf(bhz, q0[j].z);
             }
-            __syncthreads();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            blx = fminf(blx, __shfl_xor_sync(0xffffffffu, blx, o));
+            bly = fminf(bly, __shfl_xor_sync(0xffffffffu, bly, o));
+            blz = fminf(blz, __shfl_xor_sync(0xffffffffu, blz, o));
+            bhx = fmaxf(bhx, __shfl_xor_sync(0xffffffffu, bhx, o));
+            bhy = fmaxf(bhy, __shfl_xor_sync(0xffffffffu, bhy, o));
+            bhz = fmaxf(bhz, __shfl_xor_sync(0xffffffffu, bhz, o));
+        }
+        const float rc2 = r2 * 1.0001f;
+        // tests every query of the leader's cell against the tile's photons
+        auto testTile = [&](uint32_t fill) {
+            __syncwarp();
             if (any) {
                 if (kCount) {
 #pragma unroll
-                    for (int j = 0; j < kQ; j++) pairs += active[j] ? cnt : 0;
+                    for (int j = 0; j < kQ; j++) pairs += active[j] ? fill : 0;
                 }
 #pragma unroll 2
-                for (uint32_t t = 0; t < cnt; t++) {
-                    const float4 a = sA[t];
+                for (uint32_t t = 0; t < fill; t++) {
+                    const float4 a = wA[t];
                     bool in[kQ];
                     bool anyIn = false;
 #pragma unroll
@@ -177,8 +211,8 @@ __global__ void __launch_bounds__(kTileQ) kGatherTiled(GridDev g, const float4* 
                         anyIn |= in[j];
                     }
                     if (anyIn) {
-                        const float4 b = sB[t];
-                        const float c = sC[t];
+                        const float4 b = wB[t];
+                        const float c = wC[t];
 #pragma unroll
                         for (int j = 0; j < kQ; j++) {
                             if (!in[j]) continue;
@@ -192,8 +226,45 @@ __global__ void __launch_bounds__(kTileQ) kGatherTiled(GridDev g, const float4* 
                     }
                 }
             }
-            __syncthreads();
+            __syncwarp();
+        };
+        // the neighbourhood's photons in bucket order, 32 at a time; those
+        // within reach are packed into the tile in the same order
+        const unsigned lt = (1u << lane) - 1u;
+        unsigned segs = __ballot_sync(0xffffffffu, nc > 0);
+        uint32_t fill = 0;
+        while (segs) {
+            const int sgi = __ffs(segs) - 1;
+            segs &= segs - 1;
+            const uint32_t sb = __shfl_sync(0xffffffffu, b0, sgi), sn = __shfl_sync(0xffffffffu, nc, sgi);
+            for (uint32_t i = 0; i < sn; i += 32) {
+                if (fill > (uint32_t)kWStage - 32) {
+                    testTile(fill);
+                    fill = 0;
+                }
+                const uint32_t t = i + lane;
+                bool keep = false;
+                float4 a;
+                if (t < sn) {
+                    a = __ldg(&g.rec[2 * ((int64_t)sb + t)]);
+                    const float ex = fmaxf(fmaxf(blx - a.x, a.x - bhx), 0.0f);
+                    const float ey = fmaxf(fmaxf(bly - a.y, a.y - bhy), 0.0f);
+                    const float ez = fmaxf(fmaxf(blz - a.z, a.z - bhz), 0.0f);
+                    keep = ex * ex + ey * ey + ez * ez < rc2;
+                }
+                const unsigned km = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    const float4 f = __ldg(&g.rec[2 * ((int64_t)sb + t) + 1]);
+                    const f3 nn = unpackNormal(__float_as_uint(a.w));
+                    const uint32_t k = fill + __popc(km & lt);
+                    wA[k] = make_float4(a.x, a.y, a.z, nn.x);
+                    wB[k] = make_float4(f.x, f.y, f.z, nn.y);
+                    wC[k] = nn.z;
+                }
+                fill += __popc(km);
+            }
         }
+        if (fill) testTile(fill);
 #pragma unroll
         for (int j = 0; j < kQ; j++)
             if (active[j]) pending[j] = false;
@@ -217,7 +288,7 @@ __global__ void __launch_bounds__(kTileQ) kGatherTiled(GridDev g, const float4* 
     if (kCount) {
         const unsigned long long wp = __reduce_add_sync(0xffffffffu, (unsigned)pairs);
         const unsigned long long wi = __reduce_add_sync(0xffffffffu, (unsigned)inside);
-        if ((threadIdx.x & 31) == 0) {
+        if (lane == 0) {
             atomicAdd(&work[0], wp);
             atomicAdd(&work[1], wi);
         }
