@@ -190,6 +190,32 @@ int pppm_emit_photons(pppm_ctx* ctx, const double* tapes, int64_t n, int64_t num
  * to query the size. */
 int pppm_hdr_decode(const uint8_t* bytes, int64_t nbytes, float* rgb, int64_t cap_floats, int32_t* w, int32_t* h);
 
+/* Decodes a PLY file image held in memory as Trimesh::loadPly does
+ * (trimesh.cc:139-217): the first line must be "ply", the format
+ * binary_little_endian, the elements "vertex" and "face" only; the body is 3
+ * little-endian floats per vertex (whatever properties the header declares)
+ * and, per face, one uchar count and 3 int32 indices. Call with verts and
+ * faces NULL to query nverts/nfaces. A header without end_header gives an
+ * empty mesh (PPPM_OK, 0 and 0), as in the reference. Where the reference
+ * aborts or exits (other formats or elements, zero counts, a polygon of more
+ * than 3 vertices) and where it reads past the data or outside the vertex
+ * array (truncated body, index out of range), this returns PPPM_E_ARG.
+ * Blank header lines are skipped. */
+int pppm_ply_decode(const uint8_t* bytes, int64_t nbytes, float* verts, int64_t vcap_floats, int32_t* faces,
+                    int64_t fcap_ints, int64_t* nverts, int64_t* nfaces);
+
+/* Placement of a mesh before Scene::add, on n double vertices (3 per
+ * vertex) with the reference's arithmetic in its order:
+ * Trimesh::translate (trimesh.cc:272-276), Trimesh::scale(sx, sy, sz)
+ * (:278-288), Trimesh::putOnPlane(Plane(distance, normal)) (:290-300),
+ * Trimesh::fitToBBox(BBox(bmin, bmax)) (:302-320). The scene holds FP32
+ * triangles, so transformed vertices are rounded once when the scene is
+ * set. */
+int pppm_mesh_translate(double* v, int64_t n, const double move[3]);
+int pppm_mesh_scale(double* v, int64_t n, double sx, double sy, double sz);
+int pppm_mesh_put_on_plane(double* v, int64_t n, double distance, const double normal[3]);
+int pppm_mesh_fit_bbox(double* v, int64_t n, const double bmin[3], const double bmax[3]);
+
 /* ------------------------------------------------------------- stages */
 /* Replaces QBVHAccel::intersect (qbvh_accel.cc:205-285) through
  * Scene::intersect (scene.cc:40-47): closest hit of n rays. tri: original

@@ -132,6 +132,34 @@ int rh_scene_add_ply(void* s, const char* path, const Mat* m) {
 
 void rh_scene_finalize(void* s) { static_cast<HarnessScene*>(s)->scene.setAccelerator(); }
 
+// Loads a PLY through Trimesh::load (trimesh.cc:125-217) and places it the
+// way the reference's demo driver does (main/appmain.cc:38-40): fitToBBox
+// when fit != 0, scale(scaleAll) when scaleAll != 1, putOnPlane when
+// onPlane != 0, then translate(move). Writes the double vertices and faces;
+// returns the face count (vertex count in *nv), or -1 when a buffer is short.
+int rh_mesh_place(const char* path, int fit, const double* bmin, const double* bmax, double scaleAll, int onPlane,
+                  double planeDist, const double* planeN, const double* move, double* verts, int vcap, int* faces,
+                  int fcap, int* nv) {
+    Trimesh mesh;
+    mesh.load(path);
+    if (fit) mesh.fitToBBox(BBox(bmin[0], bmin[1], bmin[2], bmax[0], bmax[1], bmax[2]));
+    if (scaleAll != 1.0) mesh.scale(scaleAll);
+    if (onPlane) mesh.putOnPlane(Plane(planeDist, Vector3D(planeN[0], planeN[1], planeN[2])));
+    mesh.translate(Vector3D(move[0], move[1], move[2]));
+    *nv = (int)mesh.numVerts();
+    if (mesh.numVerts() > vcap || mesh.numFaces() > fcap) return -1;
+    for (int i = 0; i < (int)mesh.numVerts(); i++) {
+        const Vector3D v = mesh.getVertex(i);
+        verts[3 * i] = v.x();
+        verts[3 * i + 1] = v.y();
+        verts[3 * i + 2] = v.z();
+    }
+    const std::vector<Triplet> ids = mesh.getIndices();
+    for (int i = 0; i < (int)ids.size(); i++)
+        for (int k = 0; k < 3; k++) faces[3 * i + k] = ids[i][k];
+    return (int)mesh.numFaces();
+}
+
 // Writes an RGB float image as Radiance HDR with the reference writer
 // (image.cc:436-482) so the env map goes through its own RGBE round trip.
 void rh_write_hdr(const char* path, const float* rgb, int w, int h) {

@@ -53,6 +53,9 @@ def lib():
             getattr(_lib, name).argtypes = [ctypes.c_void_p]
         _lib.rh_scene_add.argtypes = [ctypes.c_void_p, _F, ctypes.c_int, ctypes.c_void_p]
         _lib.rh_scene_add_ply.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
+        _lib.rh_mesh_place.argtypes = [ctypes.c_char_p, ctypes.c_int, _D, _D, ctypes.c_double, ctypes.c_int,
+                                       ctypes.c_double, _D, _D, _D, ctypes.c_int, _I, ctypes.c_int, _I]
+        _lib.rh_mesh_place.restype = ctypes.c_int
         _lib.rh_scene_set_envmap.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
         _lib.rh_write_hdr.argtypes = [ctypes.c_char_p, _F, ctypes.c_int, ctypes.c_int]
         _lib.rh_load_hdr.argtypes = [ctypes.c_char_p, _D, ctypes.c_int, _I, _I]
@@ -381,3 +384,23 @@ def poisson_disk(tris9, min_dist, cap=1 << 22):
     nrm = np.zeros((cap, 3))
     n = lib().rh_poisson_disk(_p(t, _F), t.shape[0], float(min_dist), _p(pts, _D), _p(nrm, _D), cap)
     return pts[:n], nrm[:n]
+
+
+def mesh_place(path, fit=None, scale_all=1.0, plane=None, move=(0.0, 0.0, 0.0), vcap=1 << 22, fcap=1 << 22):
+    """Trimesh::load + fitToBBox / scale / putOnPlane / translate in the
+    reference. fit: (bmin, bmax) or None; plane: (distance, normal) or None.
+    Returns (double vertices [n, 3], int faces [m, 3])."""
+    L = lib()
+    bmin = np.ascontiguousarray(fit[0] if fit else (0, 0, 0), np.float64)
+    bmax = np.ascontiguousarray(fit[1] if fit else (0, 0, 0), np.float64)
+    pn = np.ascontiguousarray(plane[1] if plane else (0, 1, 0), np.float64)
+    mv = np.ascontiguousarray(move, np.float64)
+    verts = np.zeros((vcap, 3), np.float64)
+    faces = np.zeros((fcap, 3), np.int32)
+    nv = np.zeros(1, np.int32)
+    nf = L.rh_mesh_place(str(path).encode(), 1 if fit else 0, _p(bmin, _D), _p(bmax, _D), float(scale_all),
+                         1 if plane else 0, float(plane[0]) if plane else 0.0, _p(pn, _D), _p(mv, _D),
+                         _p(verts, _D), vcap, _p(faces, _I), fcap, _p(nv, _I))
+    if nf < 0:
+        raise RuntimeError("mesh_place: buffers too small")
+    return verts[: nv[0]].copy(), faces[:nf].copy()

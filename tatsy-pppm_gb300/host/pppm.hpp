@@ -114,51 +114,82 @@ public:
     std::vector<Triangle> triangulate() const { return {*this}; }
 };
 
-class Trimesh {  // trimesh.h:68-166: binary little-endian PLY (float xyz, uchar + 3 int faces)
-    std::vector<Vector3D> verts_;
+class Plane {  // plane.h: distance and normal, as Plane(double, const Vector3D&) takes them
+    double d_ = 0.0;
+    Vector3D n_;
+
+public:
+    Plane() = default;
+    Plane(double distance, const Vector3D& normal) : d_(distance), n_(normal) {}
+    double distance() const { return d_; }
+    const Vector3D& normal() const { return n_; }
+};
+
+class BBox {  // bbox.h: BBox(minX, minY, minZ, maxX, maxY, maxZ)
+    Vector3D lo_, hi_;
+
+public:
+    BBox(double minX, double minY, double minZ, double maxX, double maxY, double maxZ)
+        : lo_(minX, minY, minZ), hi_(maxX, maxY, maxZ) {}
+    BBox(const Vector3D& posMin, const Vector3D& posMax) : lo_(posMin), hi_(posMax) {}
+    const Vector3D& posMin() const { return lo_; }
+    const Vector3D& posMax() const { return hi_; }
+};
+
+class Trimesh {  // trimesh.h:68-166: binary little-endian PLY through pppm_ply_decode
+    std::vector<double> verts_;  // 3 per vertex, double like the reference's Vector3D
     std::vector<int> faces_;
 
 public:
     Trimesh() = default;
     explicit Trimesh(const std::string& filename) { load(filename); }
-    Trimesh(const std::vector<Vector3D>& v, const std::vector<int>& f) : verts_(v), faces_(f) {}
+    Trimesh(const std::vector<Vector3D>& v, const std::vector<int>& f) : faces_(f) {
+        for (const Vector3D& x : v)
+            for (int d = 0; d < 3; d++) verts_.push_back(x[d]);
+    }
     void load(const std::string& filename) {  // trimesh.cc:125-217
         std::ifstream in(filename, std::ios::binary);
         if (!in) throw pppm::Error(PPPM_E_ARG, "Failed to open mesh file: " + filename);
-        std::string line;
-        size_t nv = 0, nf = 0;
-        std::getline(in, line);
-        if (line.rfind("ply", 0) != 0) throw pppm::Error(PPPM_E_ARG, "Invalid format identifier");
-        while (std::getline(in, line)) {
-            if (line.rfind("format", 0) == 0 && line.find("binary_little_endian") == std::string::npos)
-                throw pppm::Error(PPPM_E_ARG, "PLY must be binary little endian format!");
-            if (line.rfind("element vertex", 0) == 0) nv = std::stoull(line.substr(15));
-            if (line.rfind("element face", 0) == 0) nf = std::stoull(line.substr(13));
-            if (line.rfind("end_header", 0) == 0) break;
+        const std::vector<uint8_t> bytes((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+        int64_t nv = 0, nf = 0;
+        int r = pppm_ply_decode(bytes.data(), (int64_t)bytes.size(), nullptr, 0, nullptr, 0, &nv, &nf);
+        if (r) throw pppm::Error(r, "Invalid PLY file: " + filename);
+        std::vector<float> v((size_t)(3 * nv));
+        faces_.assign((size_t)(3 * nf), 0);
+        if (nv > 0) {
+            r = pppm_ply_decode(bytes.data(), (int64_t)bytes.size(), v.data(), 3 * nv, faces_.data(), 3 * nf, &nv,
+                                &nf);
+            if (r) throw pppm::Error(r, "Invalid PLY file: " + filename);
         }
-        if (nv == 0 || nf == 0) throw pppm::Error(PPPM_E_ARG, "numVerts and numFaces must be positive");
-        verts_.resize(nv);
-        for (auto& v : verts_) {
-            float f[3];
-            in.read(reinterpret_cast<char*>(f), 12);
-            v = Vector3D(f[0], f[1], f[2]);
-        }
-        faces_.resize(3 * nf);
-        for (size_t i = 0; i < nf; i++) {
-            unsigned char n;
-            in.read(reinterpret_cast<char*>(&n), 1);
-            if (n != 3) throw pppm::Error(PPPM_E_ARG, "mesh contains non-triangle polygon");
-            in.read(reinterpret_cast<char*>(&faces_[3 * i]), 12);
-        }
-        if (!in) throw pppm::Error(PPPM_E_ARG, "truncated PLY body");
+        verts_.assign(v.begin(), v.end());
     }
-    size_t numVerts() const { return verts_.size(); }
+    // placement before Scene::add, with the reference's arithmetic
+    void translate(const Vector3D& move) {  // trimesh.cc:272-276
+        const double m[3] = {move.x(), move.y(), move.z()};
+        pppm_mesh_translate(verts_.data(), (int64_t)numVerts(), m);
+    }
+    void scale(double sx, double sy, double sz) { pppm_mesh_scale(verts_.data(), (int64_t)numVerts(), sx, sy, sz); }
+    void scale(double s) { scale(s, s, s); }  // trimesh.cc:286-288
+    void putOnPlane(const Plane& plane) {  // trimesh.cc:290-300
+        const double n[3] = {plane.normal().x(), plane.normal().y(), plane.normal().z()};
+        pppm_mesh_put_on_plane(verts_.data(), (int64_t)numVerts(), plane.distance(), n);
+    }
+    void fitToBBox(const BBox& box) {  // trimesh.cc:302-320
+        const double lo[3] = {box.posMin().x(), box.posMin().y(), box.posMin().z()};
+        const double hi[3] = {box.posMax().x(), box.posMax().y(), box.posMax().z()};
+        pppm_mesh_fit_bbox(verts_.data(), (int64_t)numVerts(), lo, hi);
+    }
+    size_t numVerts() const { return verts_.size() / 3; }
     size_t numFaces() const { return faces_.size() / 3; }
+    Vector3D getVertex(int id) const {
+        if (id < 0 || (size_t)id >= numVerts()) throw pppm::Error(PPPM_E_ARG, "Vertex index out of bounds");
+        return Vector3D(verts_[3 * id], verts_[3 * id + 1], verts_[3 * id + 2]);
+    }
     std::vector<Triangle> triangulate() const {
         std::vector<Triangle> out;
         out.reserve(numFaces());
         for (size_t i = 0; i < numFaces(); i++)
-            out.emplace_back(verts_.at(faces_[3 * i]), verts_.at(faces_[3 * i + 1]), verts_.at(faces_[3 * i + 2]));
+            out.emplace_back(getVertex(faces_[3 * i]), getVertex(faces_[3 * i + 1]), getVertex(faces_[3 * i + 2]));
         return out;
     }
 };

@@ -95,6 +95,11 @@ SIGNATURES = {
     "pppm_env_lookup": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_emit_photons": ([_VP, _VP, ctypes.c_int64, ctypes.c_int64, _VP, _VP, _VP, _VP], ctypes.c_int),
     "pppm_hdr_decode": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
+    "pppm_ply_decode": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
+    "pppm_mesh_translate": ([_VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_mesh_scale": ([_VP, ctypes.c_int64, ctypes.c_double, ctypes.c_double, ctypes.c_double], ctypes.c_int),
+    "pppm_mesh_put_on_plane": ([_VP, ctypes.c_int64, ctypes.c_double, _VP], ctypes.c_int),
+    "pppm_mesh_fit_bbox": ([_VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
     "pppm_intersect": ([_VP, _VP, ctypes.c_int64, _VP, _VP, _VP, _VP], ctypes.c_int),
     "pppm_hash_points": ([_VP, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP], ctypes.c_int),
     "pppm_knn": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
@@ -603,3 +608,74 @@ def hdr_decode(data: bytes):
     if r != OK:
         raise PppmError(r, "bad HDR data")
     return out
+
+
+def ply_decode(data: bytes):
+    """pppm_ply_decode (Trimesh::loadPly, trimesh.cc:139-217) on a PLY file
+    image: (vertices float32 [n, 3], faces int32 [m, 3])."""
+    lib = load()
+    buf = np.frombuffer(data, np.uint8)
+    nv, nf = ctypes.c_int64(), ctypes.c_int64()
+    r = lib.pppm_ply_decode(buf.ctypes.data, buf.size, None, 0, None, 0, ctypes.byref(nv), ctypes.byref(nf))
+    if r != OK:
+        raise PppmError(r, "bad PLY header")
+    verts = np.zeros((nv.value, 3), np.float32)
+    faces = np.zeros((nf.value, 3), np.int32)
+    if nv.value:
+        r = lib.pppm_ply_decode(buf.ctypes.data, buf.size, verts.ctypes.data, verts.size, faces.ctypes.data,
+                                faces.size, ctypes.byref(nv), ctypes.byref(nf))
+        if r != OK:
+            raise PppmError(r, "bad PLY data")
+    return verts, faces
+
+
+class Trimesh:
+    """The reference's Trimesh (trimesh.h:68-166) for scene setup: double
+    vertices and int faces, loaded from a binary PLY and placed with the
+    reference's own arithmetic (pppm_mesh_*). triangles() gives the FP32
+    triangle soup that Context.set_scene / scenes.Scene take."""
+
+    def __init__(self, vertices=None, faces=None):
+        self.vertices = np.zeros((0, 3), np.float64) if vertices is None else np.array(vertices, np.float64)
+        self.faces = np.zeros((0, 3), np.int32) if faces is None else np.array(faces, np.int32)
+
+    @classmethod
+    def load(cls, path_or_bytes):
+        data = path_or_bytes if isinstance(path_or_bytes, (bytes, bytearray)) else open(path_or_bytes, "rb").read()
+        v, f = ply_decode(bytes(data))
+        return cls(v.astype(np.float64), f)
+
+    def _call(self, fn, *args):
+        self.vertices = np.ascontiguousarray(self.vertices, np.float64)
+        r = getattr(load(), fn)(self.vertices.ctypes.data, self.vertices.shape[0], *args)
+        if r != OK:
+            raise PppmError(r, fn)
+        return self
+
+    def translate(self, move):
+        m = np.ascontiguousarray(move, np.float64)
+        return self._call("pppm_mesh_translate", m.ctypes.data)
+
+    def scale(self, sx, sy=None, sz=None):
+        sy = sx if sy is None else sy
+        sz = sx if sz is None else sz
+        return self._call("pppm_mesh_scale", float(sx), float(sy), float(sz))
+
+    def put_on_plane(self, distance, normal):
+        n = np.ascontiguousarray(normal, np.float64)
+        return self._call("pppm_mesh_put_on_plane", float(distance), n.ctypes.data)
+
+    def fit_to_bbox(self, bmin, bmax):
+        lo = np.ascontiguousarray(bmin, np.float64)
+        hi = np.ascontiguousarray(bmax, np.float64)
+        return self._call("pppm_mesh_fit_bbox", lo.ctypes.data, hi.ctypes.data)
+
+    def num_verts(self):
+        return self.vertices.shape[0]
+
+    def num_faces(self):
+        return self.faces.shape[0]
+
+    def triangles(self):
+        """Triangle soup, 9 floats per face (Trimesh::getTriangle rounded to FP32)."""
+        return self.vertices[self.faces].reshape(-1, 9).astype(np.float32)

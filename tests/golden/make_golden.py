@@ -390,8 +390,77 @@ def gen_path_trace_sss():
          threads=np.array(rh.num_threads()), sss_time=np.array(1234567))
 
 
+def ply_bytes(verts, faces, counts=None, header_extra=(), vertex_props=("x", "y", "z"), trailer=b""):
+    """Binary little-endian PLY image in the layout Trimesh::loadPly reads."""
+    head = ["ply", "format binary_little_endian 1.0", *header_extra, f"element vertex {len(verts)}"]
+    head += [f"property float {p}" for p in vertex_props]
+    head += [f"element face {len(faces)}", "property list uchar int vertex_indices", "end_header"]
+    rec = np.zeros(len(faces), np.dtype([("n", "u1"), ("i", "<i4", (3,))]))
+    rec["n"] = 3 if counts is None else counts
+    rec["i"] = faces
+    return ("\n".join(head) + "\n").encode() + np.asarray(verts, "<f4").tobytes() + rec.tobytes() + trailer
+
+
+def gen_ply():
+    """Trimesh::loadPly and the placement helpers (fitToBBox, scale,
+    putOnPlane, translate) of the reference on synthetic PLY images, and
+    digests of the reference's own assets placed as its demo driver places
+    them (main/appmain.cc:38-40, 69-80)."""
+    import hashlib
+    import tempfile
+
+    rng = np.random.default_rng(21)
+    v0 = rng.normal(size=(60, 3)) * [3.0, 1.0, 2.0] + [1.0, -2.0, 0.5]
+    v3 = rng.normal(size=(40, 3)).astype(np.float32)
+    v3[:4] = [[1e-30, -0.0, 3e38], [-1e-40, 7.0, -2.5], [0.0, 1e-38, 1.0], [-3e38, 2.0, 5e-45]]
+    cases = [
+        # comments and obj_info lines; the bunny's placement
+        (ply_bytes(v0, rng.integers(0, 60, (100, 3)), header_extra=("comment made by a test", "obj_info x")),
+         ((-5.0, -5.0, -5.0), (5.0, 5.0, 5.0)), 0.8, (10.0, (0.0, 1.0, 0.0)), (5.0, 0.0, -10.0)),
+        # six vertex properties declared, three floats stored (the reader ignores declarations)
+        (ply_bytes(rng.normal(size=(30, 3)), rng.integers(0, 30, (20, 3)),
+                   vertex_props=("x", "y", "z", "nx", "ny", "nz")),
+         ((-1.0, -2.0, -3.0), (4.0, 5.0, 6.0)), 1.0, (2.5, (0.0, 0.0, 1.0)), (0.1, 0.2, 0.3)),
+        # faces with count 2 (three indices read anyway), non-unit plane normal, trailing bytes
+        (ply_bytes(rng.uniform(-7, 9, (25, 3)), rng.integers(0, 25, (15, 3)), counts=rng.integers(2, 4, 15),
+                   trailer=b"\x00garbage"),
+         None, 1.5, (-3.0, (0.0, 2.0, 0.5)), (0.0, 0.0, 0.0)),
+        # decode only, extreme and signed-zero coordinates
+        (ply_bytes(v3, rng.integers(0, 40, (30, 3))), None, 1.0, None, (0.0, 0.0, 0.0)),
+    ]
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        for i, (data, fit, sc, plane, move) in enumerate(cases):
+            path = pathlib.Path(d) / f"m{i}.ply"
+            path.write_bytes(data)
+            rv, rf = rh.mesh_place(path, fit=fit, scale_all=sc, plane=plane, move=move)
+            out[f"ply_{i}"] = np.frombuffer(data, np.uint8)
+            out[f"fit_{i}"] = np.array(fit if fit else [[np.nan] * 3, [np.nan] * 3], np.float64)
+            out[f"scale_{i}"] = np.array(sc)
+            out[f"plane_{i}"] = np.array([plane[0], *plane[1]] if plane else [np.nan] * 4, np.float64)
+            out[f"move_{i}"] = np.array(move, np.float64)
+            out[f"ref_verts_{i}"] = rv
+            out[f"ref_faces_{i}"] = rf
+    out["cases"] = np.array(len(cases))
+    # the reference's assets with the demo driver's placement: digests only
+    demo = {"bunny.ply": (((-5.0, -5.0, -5.0), (5.0, 5.0, 5.0)), 0.8, (10.0, (0.0, 1.0, 0.0)), (5.0, 0.0, -10.0)),
+            "rt3.ply": (((-10.0, -10.0, -10.0), (10.0, 10.0, 10.0)), 1.5, (10.0, (0.0, 1.0, 0.0)), (20.0, 0.0, -5.0))}
+    names, digests = [], []
+    for name, (fit, sc, plane, move) in demo.items():
+        path = pathlib.Path("/root/reference/assets") / name
+        if not path.exists():
+            continue
+        rv, rf = rh.mesh_place(path, fit=fit, scale_all=sc, plane=plane, move=move)
+        h = hashlib.sha256(rv.astype("<f8").tobytes() + rf.astype("<i4").tobytes()).hexdigest()
+        names.append(name)
+        digests.append(f"{len(rv)} {len(rf)} {h}")
+    out["asset_names"] = np.array(names)
+    out["asset_digests"] = np.array(digests)
+    save("ply", **out)
+
+
 GENERATORS.update({"knn": gen_knn, "gather": gen_gather, "render": gen_render, "dipole": gen_dipole,
-                   "sss_irradiance": gen_sss_irradiance, "path_trace": gen_path_trace})
+                   "sss_irradiance": gen_sss_irradiance, "path_trace": gen_path_trace, "ply": gen_ply})
 # generators that need a fresh process (process-wide reference RNG state)
 FRESH = {"poisson": gen_poisson, "render_sss": gen_sss_render, "classic": gen_classic,
          "path_trace_sss": gen_path_trace_sss}
