@@ -29,7 +29,7 @@ constexpr int kWStage = PPPM_GATHER_WSTAGE;  // photons per warp tile
 #endif
 constexpr int kSubBits = PPPM_GATHER_SUBBITS;  // query sort: sub-cells per axis = 2^kSubBits
 #ifndef PPPM_GATHER_MINBLOCKS
-#define PPPM_GATHER_MINBLOCKS 1
+#define PPPM_GATHER_MINBLOCKS 6
 #endif
 
 unsigned blocksFor(int64_t n, int bs, int cap = 152 * 32) {
@@ -103,7 +103,9 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
     float4* wA = sA[warp];
     float4* wB = sB[warp];
     float* wC = sC[warp];
-    float4 q0[kQ], q1[kQ], q2[kQ];
+    // position and normal of each query stay in registers; its weight and
+    // pixel are read again for the final write
+    float3 q0[kQ], q1[kQ];
     int cx[kQ], cy[kQ], cz[kQ];
     bool valid[kQ], pending[kQ];
     float sx[kQ], sy[kQ], sz[kQ];
@@ -111,14 +113,13 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
     for (int j = 0; j < kQ; j++) {
         const int64_t i = base + (int64_t)kQ * lane + j;
         valid[j] = i < n;
-        q0[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        q0[j] = make_float3(0.f, 0.f, 0.f);
         q1[j] = q0[j];
-        q2[j] = q0[j];
         cx[j] = cy[j] = cz[j] = -1;
         if (valid[j]) {
-            q0[j] = sq[3 * i];
-            q1[j] = sq[3 * i + 1];
-            q2[j] = sq[3 * i + 2];
+            const float4 a = sq[3 * i], b = sq[3 * i + 1];
+            q0[j] = make_float3(a.x, a.y, a.z);
+            q1[j] = make_float3(b.x, b.y, b.z);
             cx[j] = cellCoord(q0[j].x, g.ox, g.invCell, g.nx);
             cy[j] = cellCoord(q0[j].y, g.oy, g.invCell, g.ny);
             cz[j] = cellCoord(q0[j].z, g.oz, g.invCell, g.nz);
@@ -273,8 +274,10 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
 #pragma unroll
     for (int j = 0; j < kQ; j++) {
         if (!valid[j]) continue;
-        const float lx = q2[j].x * sx[j] * norm, ly = q2[j].y * sy[j] * norm, lz = q2[j].z * sz[j] * norm;
-        const int64_t px = __float_as_int(q0[j].w);
+        const int64_t i = base + (int64_t)kQ * lane + j;
+        const float4 w = sq[3 * i + 2];
+        const float lx = w.x * sx[j] * norm, ly = w.y * sy[j] * norm, lz = w.z * sz[j] * norm;
+        const int64_t px = __float_as_int(sq[3 * i].w);
         if (kAccum) {
             out[3 * px] += lx;
             out[3 * px + 1] += ly;
