@@ -116,6 +116,11 @@ class ClockSampler:
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi's start (NVML initialisation) can stall the driver:
+            # the timed region begins once the first sample has arrived
+            t0 = time.perf_counter()
+            while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self

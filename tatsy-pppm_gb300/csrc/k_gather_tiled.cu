@@ -29,7 +29,7 @@ constexpr int kWStage = PPPM_GATHER_WSTAGE;  // photons per warp tile
 #endif
 constexpr int kSubBits = PPPM_GATHER_SUBBITS;  // query sort: sub-cells per axis = 2^kSubBits
 #ifndef PPPM_GATHER_MINBLOCKS
-#define PPPM_GATHER_MINBLOCKS 6
+#define PPPM_GATHER_MINBLOCKS 7
 #endif
 
 unsigned blocksFor(int64_t n, int bs, int cap = 152 * 32) {
