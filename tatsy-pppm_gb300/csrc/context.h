@@ -193,6 +193,7 @@ struct RenderState {
     DBuf photons;     // 2 x float4 per stored photon (pos|normal, flux|stream)
     DBuf photonCount; // counters (see render.cu)
     DBuf pathA, pathB;  // wavefront path state
+    DBuf sortKeys, sortHist, sortCursor, sortTmp, sortPerm;  // trace order of the emitted photon paths
     DBuf queries;     // gather queries
     DBuf tapeStates;  // uint4 start state per photon / pixel (compat)
     DBuf jumpMats;    // jump-ahead matrices

@@ -168,8 +168,26 @@ __device__ inline bool vmfMixFinite(const VmfMix& m) {
     return isfinite(s);
 }
 
+// Octahedral cell (2^bits per side, Morton order) of a direction.
+__device__ __forceinline__ uint32_t octCell(const f3& v, int bits) {
+    const float s = 1.0f / (fabsf(v.x) + fabsf(v.y) + fabsf(v.z));
+    float u = v.x * s, w = v.y * s;
+    if (v.z < 0.0f) {
+        const float uu = (1.0f - fabsf(w)) * (u >= 0.0f ? 1.0f : -1.0f);
+        w = (1.0f - fabsf(u)) * (w >= 0.0f ? 1.0f : -1.0f);
+        u = uu;
+    }
+    const int m = (1 << bits) - 1;
+    const uint32_t qu = (uint32_t)min(max(__float2int_rd((u + 1.0f) * 0.5f * (float)(m + 1)), 0), m);
+    const uint32_t qw = (uint32_t)min(max(__float2int_rd((w + 1.0f) * 0.5f * (float)(m + 1)), 0), m);
+    uint32_t r = 0;
+    for (int b = 0; b < bits; b++) r |= (((qu >> b) & 1u) << (2 * b)) | (((qw >> b) & 1u) << (2 * b + 1));
+    return r;
+}
+
 __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restrict__ photonStates,
-                            PathState* __restrict__ queue, PassCounters* ctr) {
+                            PathState* __restrict__ queue, PassCounters* ctr, uint32_t* __restrict__ sortKeys,
+                            uint32_t* __restrict__ sortHist) {
     const GuideView& gv = tp.guide;
     VmfMix mix;
     bool learned = tp.guided && gv.emitRaw != nullptr;
@@ -221,6 +239,11 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
             }
         }
         queue[g] = p;
+        if (sortKeys) {
+            const uint32_t key = (octCell(dir, 6) << 4) | octCell(d, 2);
+            sortKeys[g] = key;
+            atomicAdd(&sortHist[key], 1u);
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ctr->queue[0] = (unsigned long long)tp.numPaths;
@@ -319,7 +342,8 @@ template <bool kSss>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(TraceParams tp, SceneView sc,
                                                                                const PathState* __restrict__ in,
                                                                                int64_t maxPaths, float4* __restrict__ dep,
-                                                                               int64_t depCap, PassCounters* ctr) {
+                                                                               int64_t depCap, PassCounters* ctr,
+                                                                               const uint32_t* __restrict__ perm) {
     __shared__ int order[128];
     __shared__ QNode sTop[kTopNodes];
     const int64_t n = min((int64_t)ctr->queue[0], maxPaths);
@@ -344,7 +368,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(T
             if (!has) {
                 const int64_t i = (int64_t)(b + __popc(empty & lt));
                 if (i < n) {
-                    p = in[i];
+                    p = in[perm ? (int64_t)perm[i] : i];
                     has = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
                     if (has) s.begin(sc.rootCode, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz);
                 }
@@ -706,8 +730,24 @@ cudaError_t launchTapeStates(const TraceParams& tp, const uint32_t* streamStates
 }
 
 cudaError_t launchPhotonEmit(const TraceParams& tp, const EnvDev& env, const uint32_t* photonStates, PathState* queue,
-                             PassCounters* ctr, cudaStream_t st) {
-    kPhotonEmit<<<blocksFor(tp.numPaths, 256), 256, 0, st>>>(tp, env, photonStates, queue, ctr);
+                             PassCounters* ctr, cudaStream_t st, const PhotonSort* sort) {
+    kPhotonEmit<<<blocksFor(tp.numPaths, 256), 256, 0, st>>>(tp, env, photonStates, queue, ctr,
+                                                             sort ? sort->keys : nullptr, sort ? sort->hist : nullptr);
+    return cudaGetLastError();
+}
+
+namespace {
+__global__ void kPathOrder(const uint32_t* __restrict__ keys, uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm,
+                           int64_t n) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+        perm[atomicAdd(&cursor[keys[g]], 1u)] = (uint32_t)g;
+}
+}  // namespace
+
+cudaError_t photonSortPaths(const PhotonSort& sort, int64_t paths, cudaStream_t st) {
+    cudaError_t e = exclusiveScan(sort.hist, kPhotonSortBins, sort.cursor, sort.tmp, st);
+    if (e != cudaSuccess) return e;
+    kPathOrder<<<blocksFor(paths, 256), 256, 0, st>>>(sort.keys, sort.cursor, sort.perm, paths);
     return cudaGetLastError();
 }
 
@@ -723,13 +763,14 @@ cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int b
 }
 
 cudaError_t launchPhotonPersistent(const TraceParams& tp, const SceneView& sc, const PathState* in, int64_t maxPaths,
-                                   float4* deposits, int64_t depositCap, PassCounters* ctr, cudaStream_t st) {
+                                   float4* deposits, int64_t depositCap, PassCounters* ctr, cudaStream_t st,
+                                   const uint32_t* perm) {
     // resident warps only: every block stays until the queue is drained
     const unsigned blocks = 152 * PPPM_TRACE_MINBLOCKS;
     if (tp.sssPass)
-        kPhotonPersistent<true><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr);
+        kPhotonPersistent<true><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr, perm);
     else
-        kPhotonPersistent<false><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr);
+        kPhotonPersistent<false><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr, perm);
     return cudaGetLastError();
 }
 

@@ -296,6 +296,13 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     PPPM_CUDA(c, cudaMemsetAsync(rs.accum.p, 0, (size_t)pixels * 12, c->stream));
     PPPM_CUDA(c, rs.pathA.ensure((size_t)paths * sizeof(PathState)));
     PPPM_CUDA(c, rs.pathB.ensure((size_t)paths * sizeof(PathState)));
+    if (kPhotonSort) {
+        PPPM_CUDA(c, rs.sortKeys.ensure((size_t)paths * 4));
+        PPPM_CUDA(c, rs.sortPerm.ensure((size_t)paths * 4));
+        PPPM_CUDA(c, rs.sortHist.ensure(((size_t)kPhotonSortBins + 1) * 4));
+        PPPM_CUDA(c, rs.sortCursor.ensure(((size_t)kPhotonSortBins + 1) * 4));
+        PPPM_CUDA(c, rs.sortTmp.ensure((size_t)scanTmpWords(kPhotonSortBins) * 4));
+    }
     if (rs.depositCap == 0) rs.depositCap = std::max<int64_t>(2 * paths, 1 << 16);
     PPPM_CUDA(c, rs.photons.ensure((size_t)rs.depositCap * 32));
     PPPM_CUDA(c, rs.queries.ensure((size_t)pixels * 48));
@@ -429,18 +436,27 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
             if (e) return e;
             launches += 2;
         }
-        PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
-        PPPM_CUDA(c, cudaEventRecord(c->ev[5], c->stream));
         // per-bounce launches while the queue is wide, then one tail launch
         // (guided bounces need every bounce as a queue step)
         const bool guideBounces = tp.guided && rs.guide.guideBounces;
         const bool persistent = kPersistentPhotons && !guideBounces;
+        const bool sorted = kPhotonSort && persistent;
+        const PhotonSort sort{rs.sortKeys.as<uint32_t>(), rs.sortHist.as<uint32_t>(), rs.sortCursor.as<uint32_t>(),
+                              rs.sortTmp.as<uint32_t>(), rs.sortPerm.as<uint32_t>()};
+        if (sorted) PPPM_CUDA(c, cudaMemsetAsync(sort.hist, 0, ((size_t)kPhotonSortBins + 1) * 4, c->stream));
+        PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream,
+                                      sorted ? &sort : nullptr));
+        if (sorted) {
+            PPPM_CUDA(c, photonSortPaths(sort, paths, c->stream));
+            launches += 5;
+        }
+        PPPM_CUDA(c, cudaEventRecord(c->ev[5], c->stream));
         const int waves = persistent ? 0
                           : guideBounces ? par.max_bounce_photon : std::min(par.max_bounce_photon, kWaveBounces);
         launches += 1 + waves + (waves < par.max_bounce_photon ? 1 : 0);
         if (persistent && par.max_bounce_photon > 0)
             PPPM_CUDA(c, launchPhotonPersistent(tp, sv, rs.pathA.as<PathState>(), paths, rs.photons.as<float4>(),
-                                                rs.depositCap, ctr, c->stream));
+                                                rs.depositCap, ctr, c->stream, sorted ? sort.perm : nullptr));
         for (int b = 0; b < waves; b++) {
             PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
             PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();

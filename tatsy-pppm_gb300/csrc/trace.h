@@ -130,15 +130,37 @@ void xorshiftJumpHost(const std::vector<uint32_t>& tables, uint64_t tapes, XorSh
 
 cudaError_t launchTapeStates(const TraceParams& tp, const uint32_t* streamStates, const uint32_t* jump, int width,
                              int height, uint32_t* photonStates, uint32_t* pixelStates, cudaStream_t st);
+// Coherent trace order of the emitted photon paths: a 16-bit key per path
+// (the octahedral cell of its first direction, 64x64 in Morton order, then
+// the 4x4 cell of its emission direction) counted while emitting, then a
+// counting sort of the path indices. Neighbouring lanes of the persistent
+// kernel then start from nearby origins in nearby directions. The order in
+// which paths are traced changes no path.
+#ifndef PPPM_PHOTON_SORT
+#define PPPM_PHOTON_SORT 1
+#endif
+constexpr bool kPhotonSort = PPPM_PHOTON_SORT != 0;
+constexpr int kPhotonSortBins = 1 << 16;
+struct PhotonSort {
+    uint32_t* keys;    // one per path
+    uint32_t* hist;    // kPhotonSortBins + 1 counts, zero before emission
+    uint32_t* cursor;  // kPhotonSortBins + 1
+    uint32_t* tmp;     // scanTmpWords(kPhotonSortBins)
+    uint32_t* perm;    // one per path: trace position -> path index
+};
 cudaError_t launchPhotonEmit(const TraceParams& tp, const EnvDev& env, const uint32_t* photonStates, PathState* queue,
-                             PassCounters* ctr, cudaStream_t st);
+                             PassCounters* ctr, cudaStream_t st, const PhotonSort* sort = nullptr);
+// Scan of the key counts and the scatter of path indices into sort.perm.
+cudaError_t photonSortPaths(const PhotonSort& sort, int64_t paths, cudaStream_t st);
 cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
                                PathState* out, int64_t maxPaths, float4* deposits, int64_t depositCap,
                                PassCounters* ctr, cudaStream_t st);
 // Every bounce of the emitted queue (ctr->queue[0] paths in `in`) in one
 // persistent launch with dynamic ray fetching (kPhotonPersistent).
+// perm (optional): the order in which the paths of `in` are taken.
 cudaError_t launchPhotonPersistent(const TraceParams& tp, const SceneView& sc, const PathState* in, int64_t maxPaths,
-                                   float4* deposits, int64_t depositCap, PassCounters* ctr, cudaStream_t st);
+                                   float4* deposits, int64_t depositCap, PassCounters* ctr, cudaStream_t st,
+                                   const uint32_t* perm = nullptr);
 // The bounces from `bounce` on of the queue left after the wavefront
 // launches, in one launch (kPhotonBounce<.., true>).
 cudaError_t launchPhotonTail(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
