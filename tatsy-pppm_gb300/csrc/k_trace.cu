@@ -240,7 +240,8 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
         }
         queue[g] = p;
         if (sortKeys) {
-            const uint32_t key = (octCell(dir, 6) << 4) | octCell(d, 2);
+            const uint32_t kd = octCell(dir, kSortDirBits), ke = octCell(d, kSortEnvBits);
+            const uint32_t key = PPPM_SORT_ENV_HIGH ? (ke << (2 * kSortDirBits)) | kd : (kd << (2 * kSortEnvBits)) | ke;
             sortKeys[g] = key;
             atomicAdd(&sortHist[key], 1u);
         }

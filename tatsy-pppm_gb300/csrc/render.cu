@@ -54,6 +54,24 @@ using namespace pppm;
 
 namespace pppm {
 
+int emitPhotonPaths(pppm_ctx* c, const TraceParams& tp, const EnvDev& ev, const uint32_t* photonStates,
+                    PassCounters* ctr, bool sorted, const uint32_t** perm, int64_t* launches) {
+    RenderState& rs = c->rs;
+    sorted = sorted && kPhotonSort && rs.sortPerm.p != nullptr;
+    const PhotonSort sort{rs.sortKeys.as<uint32_t>(), rs.sortHist.as<uint32_t>(), rs.sortCursor.as<uint32_t>(),
+                          rs.sortTmp.as<uint32_t>(), rs.sortPerm.as<uint32_t>()};
+    if (sorted) PPPM_CUDA(c, cudaMemsetAsync(sort.hist, 0, ((size_t)kPhotonSortBins + 1) * 4, c->stream));
+    PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream,
+                                  sorted ? &sort : nullptr));
+    *launches += 1;
+    if (sorted) {
+        PPPM_CUDA(c, photonSortPaths(sort, tp.numPaths, c->stream));
+        *launches += 4;
+    }
+    *perm = sorted ? sort.perm : nullptr;
+    return PPPM_OK;
+}
+
 // Kernel parameters and camera of pass t (everything a pass needs from the
 // host besides its buffers).
 void passSetup(pppm_ctx* c, int t, int64_t paths, TraceParams* tp, CameraDev* cd) {
@@ -440,15 +458,12 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         // (guided bounces need every bounce as a queue step)
         const bool guideBounces = tp.guided && rs.guide.guideBounces;
         const bool persistent = kPersistentPhotons && !guideBounces;
-        const bool sorted = kPhotonSort && persistent;
-        const PhotonSort sort{rs.sortKeys.as<uint32_t>(), rs.sortHist.as<uint32_t>(), rs.sortCursor.as<uint32_t>(),
-                              rs.sortTmp.as<uint32_t>(), rs.sortPerm.as<uint32_t>()};
-        if (sorted) PPPM_CUDA(c, cudaMemsetAsync(sort.hist, 0, ((size_t)kPhotonSortBins + 1) * 4, c->stream));
-        PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream,
-                                      sorted ? &sort : nullptr));
-        if (sorted) {
-            PPPM_CUDA(c, photonSortPaths(sort, paths, c->stream));
-            launches += 5;
+        const uint32_t* perm = nullptr;
+        {
+            int64_t emitLaunches = 0;
+            const int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, persistent, &perm, &emitLaunches);
+            if (e) return e;
+            launches += emitLaunches - 1;  // the emission launch is counted below
         }
         PPPM_CUDA(c, cudaEventRecord(c->ev[5], c->stream));
         const int waves = persistent ? 0
@@ -456,7 +471,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         launches += 1 + waves + (waves < par.max_bounce_photon ? 1 : 0);
         if (persistent && par.max_bounce_photon > 0)
             PPPM_CUDA(c, launchPhotonPersistent(tp, sv, rs.pathA.as<PathState>(), paths, rs.photons.as<float4>(),
-                                                rs.depositCap, ctr, c->stream, sorted ? sort.perm : nullptr));
+                                                rs.depositCap, ctr, c->stream, perm));
         for (int b = 0; b < waves; b++) {
             PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
             PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();

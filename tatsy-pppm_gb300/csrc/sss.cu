@@ -47,10 +47,10 @@ void packPointQueries(const std::vector<float>& p, const std::vector<float>& n, 
 
 // The subsurface photon bounces: a few wavefront launches, then the tail.
 int tracePhotonsTo(pppm_ctx* c, const TraceParams& tp, const SceneView& sv, int64_t paths, float4* dep, int64_t cap,
-                   PassCounters* ctr, int64_t* launches) {
+                   PassCounters* ctr, int64_t* launches, const uint32_t* perm) {
     RenderState& rs = c->rs;
     if (kPersistentPhotons) {
-        PPPM_CUDA(c, launchPhotonPersistent(tp, sv, rs.pathA.as<PathState>(), paths, dep, cap, ctr, c->stream));
+        PPPM_CUDA(c, launchPhotonPersistent(tp, sv, rs.pathA.as<PathState>(), paths, dep, cap, ctr, c->stream, perm));
         *launches += 1;
         return PPPM_OK;
     }
@@ -148,9 +148,10 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
 
     // the subsurface photon pass
     PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
-    PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
     {
-        const int e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches);
+        const uint32_t* perm = nullptr;
+        int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, kPersistentPhotons, &perm, launches);
+        if (!e) e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches, perm);
         if (e) return e;
     }
 
@@ -176,9 +177,10 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
         s.cap = (int64_t)(hc.deposits * 1.25) + 1024;
         PPPM_CUDA(c, s.photons.ensure((size_t)s.cap * 32));
         PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
-        PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream));
         {
-            const int e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches);
+            const uint32_t* perm = nullptr;
+            int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, kPersistentPhotons, &perm, launches);
+            if (!e) e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches, perm);
             if (e) return e;
         }
         PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));

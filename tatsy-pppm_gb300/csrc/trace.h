@@ -139,8 +139,19 @@ cudaError_t launchTapeStates(const TraceParams& tp, const uint32_t* streamStates
 #ifndef PPPM_PHOTON_SORT
 #define PPPM_PHOTON_SORT 1
 #endif
+#ifndef PPPM_SORT_DIR_BITS
+#define PPPM_SORT_DIR_BITS 7
+#endif
+#ifndef PPPM_SORT_ENV_BITS
+#define PPPM_SORT_ENV_BITS 1
+#endif
+#ifndef PPPM_SORT_ENV_HIGH
+#define PPPM_SORT_ENV_HIGH 0
+#endif
 constexpr bool kPhotonSort = PPPM_PHOTON_SORT != 0;
-constexpr int kPhotonSortBins = 1 << 16;
+constexpr int kSortDirBits = PPPM_SORT_DIR_BITS;  // per octahedral axis
+constexpr int kSortEnvBits = PPPM_SORT_ENV_BITS;
+constexpr int kPhotonSortBins = 1 << (2 * (kSortDirBits + kSortEnvBits));
 struct PhotonSort {
     uint32_t* keys;    // one per path
     uint32_t* hist;    // kPhotonSortBins + 1 counts, zero before emission
@@ -213,6 +224,11 @@ cudaError_t launchRecordInvSum(const MlpRecord* rec, int64_t n, float* sum, cuda
 // Learned proposal in a canonical render (guide.cu).
 // Kernel parameters and camera of pass t of the current render (render.cu).
 void passSetup(pppm_ctx* c, int t, int64_t paths, TraceParams* tp, CameraDev* cd);
+// Emission of the pass's photon paths into rs.pathA; with `sorted`, also the
+// coherent trace order (memset, emission with keys, scan, scatter), whose
+// permutation is returned in *perm (nullptr otherwise). Adds its launches.
+int emitPhotonPaths(pppm_ctx* c, const TraceParams& tp, const EnvDev& ev, const uint32_t* photonStates,
+                    PassCounters* ctr, bool sorted, const uint32_t** perm, int64_t* launches);
 
 int guideBegin(pppm_ctx* c, int64_t maxPaths);
 GuideView guideView(pppm_ctx* c, int64_t decisionsPerPass);
