@@ -515,6 +515,11 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
 // kPT: PathTracing::radiance (path_tracing.cc:137-198) instead: a Lambertian
 // hit continues with the BSDF sample (pdf 1) like every other surface; the
 // rest of the recursion is the same.
+#ifndef PPPM_EYE_TILES
+#define PPPM_EYE_TILES 1
+#endif
+constexpr bool kEyeTiles = PPPM_EYE_TILES != 0;
+
 template <bool kSss, bool kPT>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TraceParams tp, SceneView sc, EnvDev env, CameraDev cam,
                                                  OctView oct, const uint32_t* __restrict__ pixelStates,
@@ -526,8 +531,19 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
     loadTopNodes(sTop, sc.nodes, sc.numNodes);
     const int64_t np = (int64_t)cam.w * cam.h;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < np; base += stride) {
-        const int64_t pix = base + threadIdx.x;
+    // a block takes a 16x8 pixel tile, each warp an 8x4 quarter of it, so
+    // the lanes' secondary rays leave nearby points of nearby pixels
+    const int tilesX = (cam.w + 15) >> 4;
+    const int64_t nt = (int64_t)tilesX * ((cam.h + 7) >> 3) * 128;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < (kEyeTiles ? nt : np); base += stride) {
+        int64_t pix = base + threadIdx.x;
+        if (kEyeTiles) {
+            const int64_t tile = base >> 7;
+            const int wv = threadIdx.x >> 5, ln = threadIdx.x & 31;
+            const int x = (int)(tile % tilesX) * 16 + (wv & 1) * 8 + (ln & 7);
+            const int y = (int)(tile / tilesX) * 8 + (wv >> 1) * 4 + (ln >> 3);
+            pix = (x < cam.w && y < cam.h) ? (int64_t)y * cam.w + x : np;
+        }
         bool query = false;
         float4 q0, q1, q2;
         int traced = 0, visits = 0, tests = 0;
