@@ -93,16 +93,17 @@ int graphEnqueuePass(pppm_ctx* c, int t, int slot, bool sideEye) {
     else PPPM_CUDA(c, cudaEventRecordWithFlags(e[1], c->stream, cudaEventRecordExternal));
     // photons: two wavefront bounces, then the tail
     const uint32_t* perm = nullptr;
+    const PathState* traced = nullptr;
     {
         int64_t emitLaunches = 0;
-        const int r = emitPhotonPaths(c, tp, ev, nullptr, ctr, kPersistentPhotons, &perm, &emitLaunches);
+        const int r = emitPhotonPaths(c, tp, ev, nullptr, ctr, kPersistentPhotons, &traced, &perm, &emitLaunches);
         if (r) return r;
     }
     if (sideEye) PPPM_CUDA(c, cudaEventRecordWithFlags(e[1], c->stream, cudaEventRecordExternal));
     const int waves = kPersistentPhotons ? 0 : std::min(par.max_bounce_photon, kWaveBounces);
     if (kPersistentPhotons && par.max_bounce_photon > 0)
-        PPPM_CUDA(c, launchPhotonPersistent(tp, sv, rs.pathA.as<PathState>(), paths, rs.photons.as<float4>(),
-                                            rs.depositCap, ctr, c->stream, perm));
+        PPPM_CUDA(c, launchPhotonPersistent(tp, sv, traced, paths, rs.photons.as<float4>(), rs.depositCap, ctr,
+                                            c->stream, perm));
     for (int b = 0; b < waves; b++) {
         PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
         PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();

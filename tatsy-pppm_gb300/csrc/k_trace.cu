@@ -759,12 +759,22 @@ __global__ void kPathOrder(const uint32_t* __restrict__ keys, uint32_t* __restri
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
         perm[atomicAdd(&cursor[keys[g]], 1u)] = (uint32_t)g;
 }
+
+__global__ void kPathMove(const uint32_t* __restrict__ keys, uint32_t* __restrict__ cursor,
+                          const PathState* __restrict__ from, PathState* __restrict__ to, int64_t n) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+        to[atomicAdd(&cursor[keys[g]], 1u)] = from[g];
+}
 }  // namespace
 
-cudaError_t photonSortPaths(const PhotonSort& sort, int64_t paths, cudaStream_t st) {
+cudaError_t photonSortPaths(const PhotonSort& sort, int64_t paths, cudaStream_t st, const PathState* from,
+                            PathState* moveTo) {
     cudaError_t e = exclusiveScan(sort.hist, kPhotonSortBins, sort.cursor, sort.tmp, st);
     if (e != cudaSuccess) return e;
-    kPathOrder<<<blocksFor(paths, 256), 256, 0, st>>>(sort.keys, sort.cursor, sort.perm, paths);
+    if (moveTo)
+        kPathMove<<<blocksFor(paths, 256), 256, 0, st>>>(sort.keys, sort.cursor, from, moveTo, paths);
+    else
+        kPathOrder<<<blocksFor(paths, 256), 256, 0, st>>>(sort.keys, sort.cursor, sort.perm, paths);
     return cudaGetLastError();
 }
 

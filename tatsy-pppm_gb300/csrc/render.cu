@@ -55,7 +55,8 @@ using namespace pppm;
 namespace pppm {
 
 int emitPhotonPaths(pppm_ctx* c, const TraceParams& tp, const EnvDev& ev, const uint32_t* photonStates,
-                    PassCounters* ctr, bool sorted, const uint32_t** perm, int64_t* launches) {
+                    PassCounters* ctr, bool sorted, const PathState** paths, const uint32_t** perm,
+                    int64_t* launches) {
     RenderState& rs = c->rs;
     sorted = sorted && kPhotonSort && rs.sortPerm.p != nullptr;
     const PhotonSort sort{rs.sortKeys.as<uint32_t>(), rs.sortHist.as<uint32_t>(), rs.sortCursor.as<uint32_t>(),
@@ -64,11 +65,14 @@ int emitPhotonPaths(pppm_ctx* c, const TraceParams& tp, const EnvDev& ev, const 
     PPPM_CUDA(c, launchPhotonEmit(tp, ev, photonStates, rs.pathA.as<PathState>(), ctr, c->stream,
                                   sorted ? &sort : nullptr));
     *launches += 1;
+    const bool move = sorted && kSortMove;
     if (sorted) {
-        PPPM_CUDA(c, photonSortPaths(sort, tp.numPaths, c->stream));
+        PPPM_CUDA(c, photonSortPaths(sort, tp.numPaths, c->stream, rs.pathA.as<PathState>(),
+                                     move ? rs.pathB.as<PathState>() : nullptr));
         *launches += 4;
     }
-    *perm = sorted ? sort.perm : nullptr;
+    *paths = move ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
+    *perm = sorted && !move ? sort.perm : nullptr;
     return PPPM_OK;
 }
 
@@ -459,9 +463,10 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         const bool guideBounces = tp.guided && rs.guide.guideBounces;
         const bool persistent = kPersistentPhotons && !guideBounces;
         const uint32_t* perm = nullptr;
+        const PathState* traced = nullptr;
         {
             int64_t emitLaunches = 0;
-            const int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, persistent, &perm, &emitLaunches);
+            const int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, persistent, &traced, &perm, &emitLaunches);
             if (e) return e;
             launches += emitLaunches - 1;  // the emission launch is counted below
         }
@@ -470,8 +475,8 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
                           : guideBounces ? par.max_bounce_photon : std::min(par.max_bounce_photon, kWaveBounces);
         launches += 1 + waves + (waves < par.max_bounce_photon ? 1 : 0);
         if (persistent && par.max_bounce_photon > 0)
-            PPPM_CUDA(c, launchPhotonPersistent(tp, sv, rs.pathA.as<PathState>(), paths, rs.photons.as<float4>(),
-                                                rs.depositCap, ctr, c->stream, perm));
+            PPPM_CUDA(c, launchPhotonPersistent(tp, sv, traced, paths, rs.photons.as<float4>(), rs.depositCap, ctr,
+                                                c->stream, perm));
         for (int b = 0; b < waves; b++) {
             PathState* in = (b & 1) ? rs.pathB.as<PathState>() : rs.pathA.as<PathState>();
             PathState* out = (b & 1) ? rs.pathA.as<PathState>() : rs.pathB.as<PathState>();

@@ -47,10 +47,10 @@ void packPointQueries(const std::vector<float>& p, const std::vector<float>& n, 
 
 // The subsurface photon bounces: a few wavefront launches, then the tail.
 int tracePhotonsTo(pppm_ctx* c, const TraceParams& tp, const SceneView& sv, int64_t paths, float4* dep, int64_t cap,
-                   PassCounters* ctr, int64_t* launches, const uint32_t* perm) {
+                   PassCounters* ctr, int64_t* launches, const PathState* traced, const uint32_t* perm) {
     RenderState& rs = c->rs;
     if (kPersistentPhotons) {
-        PPPM_CUDA(c, launchPhotonPersistent(tp, sv, rs.pathA.as<PathState>(), paths, dep, cap, ctr, c->stream, perm));
+        PPPM_CUDA(c, launchPhotonPersistent(tp, sv, traced, paths, dep, cap, ctr, c->stream, perm));
         *launches += 1;
         return PPPM_OK;
     }
@@ -150,8 +150,9 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
     PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
     {
         const uint32_t* perm = nullptr;
-        int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, kPersistentPhotons, &perm, launches);
-        if (!e) e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches, perm);
+        const PathState* traced = nullptr;
+        int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, kPersistentPhotons, &traced, &perm, launches);
+        if (!e) e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches, traced, perm);
         if (e) return e;
     }
 
@@ -179,8 +180,9 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
         PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
         {
             const uint32_t* perm = nullptr;
-            int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, kPersistentPhotons, &perm, launches);
-            if (!e) e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches, perm);
+            const PathState* traced = nullptr;
+            int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, kPersistentPhotons, &traced, &perm, launches);
+            if (!e) e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches, traced, perm);
             if (e) return e;
         }
         PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));

@@ -161,8 +161,14 @@ struct PhotonSort {
 };
 cudaError_t launchPhotonEmit(const TraceParams& tp, const EnvDev& env, const uint32_t* photonStates, PathState* queue,
                              PassCounters* ctr, cudaStream_t st, const PhotonSort* sort = nullptr);
-// Scan of the key counts and the scatter of path indices into sort.perm.
-cudaError_t photonSortPaths(const PhotonSort& sort, int64_t paths, cudaStream_t st);
+// Scan of the key counts and the scatter of path indices into sort.perm,
+// or (moveTo != nullptr) of the path records themselves into moveTo.
+cudaError_t photonSortPaths(const PhotonSort& sort, int64_t paths, cudaStream_t st, const PathState* from = nullptr,
+                            PathState* moveTo = nullptr);
+#ifndef PPPM_SORT_MOVE
+#define PPPM_SORT_MOVE 0
+#endif
+constexpr bool kSortMove = PPPM_SORT_MOVE != 0;
 cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int bounce, const PathState* in,
                                PathState* out, int64_t maxPaths, float4* deposits, int64_t depositCap,
                                PassCounters* ctr, cudaStream_t st);
@@ -225,10 +231,13 @@ cudaError_t launchRecordInvSum(const MlpRecord* rec, int64_t n, float* sum, cuda
 // Kernel parameters and camera of pass t of the current render (render.cu).
 void passSetup(pppm_ctx* c, int t, int64_t paths, TraceParams* tp, CameraDev* cd);
 // Emission of the pass's photon paths into rs.pathA; with `sorted`, also the
-// coherent trace order (memset, emission with keys, scan, scatter), whose
-// permutation is returned in *perm (nullptr otherwise). Adds its launches.
+// coherent trace order (memset, emission with keys, scan, scatter): either
+// the records moved in that order into rs.pathB (*paths points there) or a
+// permutation in *perm. Otherwise *paths = rs.pathA and *perm = nullptr.
+// Adds its launches.
 int emitPhotonPaths(pppm_ctx* c, const TraceParams& tp, const EnvDev& ev, const uint32_t* photonStates,
-                    PassCounters* ctr, bool sorted, const uint32_t** perm, int64_t* launches);
+                    PassCounters* ctr, bool sorted, const PathState** paths, const uint32_t** perm,
+                    int64_t* launches);
 
 int guideBegin(pppm_ctx* c, int64_t maxPaths);
 GuideView guideView(pppm_ctx* c, int64_t decisionsPerPass);
