@@ -131,9 +131,10 @@ void xorshiftJumpHost(const std::vector<uint32_t>& tables, uint64_t tapes, XorSh
 cudaError_t launchTapeStates(const TraceParams& tp, const uint32_t* streamStates, const uint32_t* jump, int width,
                              int height, uint32_t* photonStates, uint32_t* pixelStates, cudaStream_t st);
 // Coherent trace order of the emitted photon paths: a 16-bit key per path
-// (the octahedral cell of its first direction, 64x64 in Morton order, then
-// the 4x4 cell of its emission direction) counted while emitting, then a
-// counting sort of the path indices. Neighbouring lanes of the persistent
+// (the octahedral cell of its first direction, 2^kSortDirBits per side in
+// Morton order, then the 2^kSortEnvBits-per-side cell of its emission
+// direction) counted while emitting, then a counting sort of the path
+// indices. Neighbouring lanes of the persistent
 // kernel then start from nearby origins in nearby directions. The order in
 // which paths are traced changes no path.
 #ifndef PPPM_PHOTON_SORT
