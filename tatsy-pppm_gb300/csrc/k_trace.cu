@@ -335,7 +335,7 @@ __device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView
 // the per-bounce kernels; only the order in which paths are processed and
 // deposits appended changes.
 #ifndef PPPM_REFILL
-#define PPPM_REFILL 16
+#define PPPM_REFILL 24
 #endif
 constexpr int kRefill = PPPM_REFILL;
 

@@ -396,7 +396,7 @@ __device__ __forceinline__ int traverseExact(const QNode* __restrict__ nodes, co
 // same box tests against the same (float)best, the same strict updates.
 // All 32 lanes of the warp must call it (inactive lanes pass active=false).
 #ifndef PPPM_EXACT_BATCH
-#define PPPM_EXACT_BATCH 8
+#define PPPM_EXACT_BATCH 12
 #endif
 constexpr int kExactBatch = PPPM_EXACT_BATCH;
 
