@@ -82,20 +82,25 @@ struct XorShift {
     double real() { return (double)next() * (double)(1.0f / 4294967295u); }
 };
 
+// Murmur3's 32-bit finaliser (a nonlinear bijection of 32-bit words).
+inline uint32_t mix32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+    return x;
+}
+
 struct Tape {
     double v[200];
     int pos = 0;
-    void fill(XorShift& x) {
-        for (int i = 0; i < 200; i++) v[i] = x.real();
+    // scramble (canonical mode): every output through mix32 before it
+    // becomes a real, as the GPU library's canonical tapes do
+    void fill(XorShift& x, bool scramble = false) {
+        for (int i = 0; i < 200; i++)
+            v[i] = scramble ? (double)mix32(x.next()) * (double)(1.0f / 4294967295u) : x.real();
         pos = 0;
     }
     double pop() { return v[pos++]; }
 };
 
-inline uint32_t mix32(uint32_t x) {
-    x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
-    return x;
-}
 // Canonical mode: the same per-path seeding as the GPU library.
 inline XorShift seedCanonical(uint32_t seed, int pass, uint64_t id) {
     XorShift x;
@@ -632,7 +637,7 @@ struct Renderer {
             for (int64_t g = 0; g < T; g++) {
                 Tape tp;
                 XorShift x = seedCanonical(par.seed, t, (uint64_t)g);
-                tp.fill(x);
+                tp.fill(x, true);
                 tracePath(tp, &loc[omp_get_thread_num()], t);
             }
             for (auto& v : loc) ph[0].insert(ph[0].end(), v.begin(), v.end());
@@ -679,7 +684,7 @@ struct Renderer {
             for (int64_t pix = 0; pix < (int64_t)W * H; pix++) {
                 Tape tp;
                 XorShift x = seedCanonical(par.seed, t, (uint64_t)T + (uint64_t)pix);
-                tp.fill(x);
+                tp.fill(x, true);
                 const double px = (pix % W) + tp.pop() - 0.5;
                 const double py = (pix / W) + tp.pop() - 0.5;
                 const V L = radiance(cam.center, cam.ray(px, py), tp);

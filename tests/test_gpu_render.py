@@ -92,3 +92,41 @@ def test_render_errors(ctx, golden):
     with pytest.raises(P.PppmError) as e:
         ctx.render_pass(1)
     assert e.value.code == P.E_UNDEFINED
+
+
+def test_render_canonical_matches_port(ctx, golden):
+    """Canonical mode (the headline's pass) against the C++ port of the same
+    semantics: counter-seeded paths, radius-ball gather, Knaus-Zwicker
+    radius. The paths follow the same random numbers on both sides and
+    differ only where FP32 shading moves a ray across a triangle edge, so,
+    as for the compat render, photon records must match for almost all
+    photons and the image must agree to a small relMSE."""
+    import port
+
+    g = golden("render_small")
+    sc = _scene(g)
+    ctx.set_scene(sc)
+    par = P.Context.make_params(mode=P.MODE_CANONICAL, photons=sc.photons, radius_scale=1 / 16, seed=7)
+    passes = 3
+    ctx.render_begin(sc.camera, par)
+    st = [ctx.render_pass(t) for t in range(1, passes + 1)]
+    img = ctx.render_read()
+    gpu = ctx.render_photons(1 << 20)
+    out = port.PortScene(sc).render(P.Context.make_camera(sc.camera), par, passes, photon_cap=1 << 20)
+    assert [s.radius for s in st] == [s["radius"] for s in out["stats"]]
+    ref_ph = out["photons"]
+    assert abs(len(gpu) - len(ref_ph)) <= 0.02 * len(ref_ph)
+    from scipy.spatial import cKDTree
+
+    tree = cKDTree(ref_ph[:, :3])
+    dist, j = tree.query(gpu[:, :3].astype(np.float64))
+    rflux = ref_ph[j, 3:6]
+    match = (dist < 1e-3) & np.all(np.abs(gpu[:, 3:6] - rflux) <= 1e-4 * np.abs(rflux) + 1e-12, axis=1)
+    ref = out["accum"]
+    rel = np.abs(img - ref) / np.maximum(np.abs(ref), 1e-3)
+    close = np.all(rel < 1e-3, axis=2).mean()
+    relmse = np.mean((img - ref) ** 2) / np.mean(ref ** 2)
+    print(f"photons matched {match.mean():.4f}, pixels within 1e-3: {close:.4f}, relMSE {relmse:.3e}")
+    assert match.mean() > 0.98, match.mean()
+    assert close > 0.9
+    assert relmse < 1e-3
