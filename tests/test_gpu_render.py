@@ -130,3 +130,42 @@ def test_render_canonical_matches_port(ctx, golden):
     assert match.mean() > 0.98, match.mean()
     assert close > 0.9
     assert relmse < 1e-3
+
+
+def test_full_size_canonical_pass_matches_port():
+    """One pass of the headline workload at its full size (1920x1080,
+    873,622 triangles, 4M photons, depth 12, canonical) against the port on
+    the host cores: the same per-path random numbers, so photon records and
+    pixels agree except where FP32 shading moves a ray across an edge."""
+    import port
+
+    sc = S.config2()
+    par = P.Context.make_params(mode=P.MODE_CANONICAL, photons=4_000_000, max_bounce_photon=12, max_bounce_eye=12,
+                                radius_scale=1 / 64, seed=3)
+    c = P.Context(0)
+    try:
+        c.set_scene(sc)
+        c.render_begin(sc.camera, par)
+        st = c.render_pass(1)
+        img = c.render_read()
+        gpu = c.render_photons(1 << 23)
+    finally:
+        c.close()
+    out = port.PortScene(sc).render(P.Context.make_camera(sc.camera), par, 1, photon_cap=1 << 23)
+    ref_ph = out["photons"]
+    assert st.radius == out["stats"][0]["radius"]
+    assert abs(len(gpu) - len(ref_ph)) <= 0.01 * len(ref_ph)
+    from scipy.spatial import cKDTree
+
+    tree = cKDTree(ref_ph[:, :3])
+    dist, j = tree.query(gpu[:, :3].astype(np.float64))
+    rflux = ref_ph[j, 3:6]
+    match = (dist < 1e-3) & np.all(np.abs(gpu[:, 3:6] - rflux) <= 1e-4 * np.abs(rflux) + 1e-12, axis=1)
+    ref = out["accum"]
+    rel = np.abs(img - ref) / np.maximum(np.abs(ref), 1e-3)
+    close = np.all(rel < 1e-3, axis=2).mean()
+    relmse = np.mean((img - ref) ** 2) / np.mean(ref ** 2)
+    print(f"{len(gpu)} photons, matched {match.mean():.5f}; pixels within 1e-3: {close:.5f}, relMSE {relmse:.3e}")
+    assert match.mean() > 0.98, match.mean()
+    assert close > 0.9
+    assert relmse < 1e-3
