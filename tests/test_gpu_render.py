@@ -169,3 +169,43 @@ def test_full_size_canonical_pass_matches_port():
     assert match.mean() > 0.98, match.mean()
     assert close > 0.9
     assert relmse < 1e-3
+
+
+def test_full_size_compat_pass_matches_port():
+    """The same at full size in compat mode (the reference's semantics:
+    16 XorShift streams, kNN gather, phantom slots), against the port that
+    the golden fixtures pin to the reference."""
+    import port
+
+    sc = S.config2()
+    par = P.Context.make_params(mode=P.MODE_COMPAT, photons=4_000_000, num_streams=16, max_bounce_photon=12,
+                                max_bounce_eye=12, radius_scale=0.1)
+    c = P.Context(0)
+    try:
+        c.set_scene(sc)
+        c.render_begin(sc.camera, par)
+        st = c.render_pass(1)
+        img = c.render_read()
+        gpu = c.render_photons(1 << 23)
+    finally:
+        c.close()
+    out = port.PortScene(sc).render(P.Context.make_camera(sc.camera), par, 1, photon_cap=1 << 23)
+    ps = out["stats"][0]
+    assert st.radius == ps["radius"]
+    assert abs(st.photons_stored - ps["stored"]) <= 0.01 * ps["stored"]
+    ref_ph = out["photons"]
+    real = ~np.all(ref_ph[:, :6] == 0, axis=1)
+    from scipy.spatial import cKDTree
+
+    tree = cKDTree(ref_ph[real, :3])
+    dist, j = tree.query(gpu[:, :3].astype(np.float64))
+    rflux = ref_ph[real][j, 3:6]
+    match = (dist < 1e-3) & np.all(np.abs(gpu[:, 3:6] - rflux) <= 1e-4 * np.abs(rflux) + 1e-12, axis=1)
+    ref = out["accum"]
+    rel = np.abs(img - ref) / np.maximum(np.abs(ref), 1e-3)
+    close = np.all(rel < 1e-3, axis=2).mean()
+    relmse = np.mean((img - ref) ** 2) / np.mean(ref ** 2)
+    print(f"{len(gpu)} photons, matched {match.mean():.5f}; pixels within 1e-3: {close:.5f}, relMSE {relmse:.3e}")
+    assert match.mean() > 0.98, match.mean()
+    assert close > 0.9
+    assert relmse < 1e-3
