@@ -231,7 +231,7 @@ struct pppm_ctx {
     double bbmin[3] = {0, 0, 0}, bbmax[3] = {0, 0, 0};
     std::vector<pppm_material> mats;
     bool anyBssrdf = false;
-    pppm::DBuf nodes, tris, matId, devMats;
+    pppm::DBuf nodes, tris, matId, devMats, triE;
     double lambertArea = 0.0;  // summed area of Lambertian triangles
     std::vector<float> hostTri;        // triangle soup (9 floats each), for the Poisson sampler
     std::vector<int64_t> bssrdfTris;   // triangles with a BSSRDF, in scene order
@@ -322,10 +322,11 @@ struct SceneView {
     const DevMaterial* mats;
     int rootCode;
     int numNodes;
+    const double* triE;  // per slot: double p0, e1 = b - a, e2 = c - a (10 doubles), or nullptr
 };
 inline SceneView sceneView(const pppm_ctx* c) {
     return {c->nodes.as<QNode>(), c->tris.as<float4>(), c->matId.as<int>(), c->devMats.as<DevMaterial>(), c->rootCode,
-            c->numNodes};
+            c->numNodes, kTriEdges ? c->triE.as<double>() : nullptr};
 }
 inline EnvDev envView(const pppm_ctx* c) {
     EnvDev e;

@@ -20,7 +20,7 @@ __global__ void __launch_bounds__(128) kIntersect(SceneView sc, const float* __r
     int slot;
     if (kPrefilter) {
         slot = traverseExactWarp(sc.nodes, sc.tris, sc.rootCode, valid, ox, oy, oz, dx, dy, dz, order, sTop, &best,
-                                 nullptr, nullptr);
+                                 nullptr, nullptr, sc.triE);
     } else {
         if (!valid) return;
         slot = traverseExact<false>(sc.nodes, sc.tris, sc.rootCode, ox, oy, oz, dx, dy, dz, order, &best, nullptr,

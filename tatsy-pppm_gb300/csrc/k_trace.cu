@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(T
             if (__any_sync(0xffffffffu, !has) && b + __popc(empty) < (unsigned long long)n) continue;
         }
         if (!__any_sync(0xffffffffu, has)) break;
-        warpTravRun(s, has, kRefill, sc.nodes, sc.tris, order, sTop, &visits, &tests);
+        warpTravRun(s, has, kRefill, sc.nodes, sc.tris, order, sTop, &visits, &tests, sc.triE);
         const bool fin = has && s.done();
         bool store = false;
         float4 da, db;
@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
         do {
         double best;
         const int slot = traverseExactWarp(sc.nodes, sc.tris, sc.rootCode, alive, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz,
-                                           order, sTop, &best, &visits, &tests);
+                                           order, sTop, &best, &visits, &tests, sc.triE);
         if (alive) {
             traced++;
             if (tp.guided && p.pad[0] >= 0) {
@@ -588,7 +588,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
             }
             double best;
             const int slot = traverseExactWarp(sc.nodes, sc.tris, sc.rootCode, doTrace, o[0], o[1], o[2], d.x, d.y,
-                                               d.z, order, sTop, &best, &visits, &tests);
+                                               d.z, order, sTop, &best, &visits, &tests, sc.triE);
             if (!doTrace) continue;
             traced++;
             if (slot < 0) {

@@ -176,11 +176,10 @@ __device__ inline float maxc(f3 v) { return fmaxf(v.x, fmaxf(v.y, v.z)); }
 // Moller-Trumbore in double with the reference's operation order
 // (triangle.cc:53-78); every product and sum is an explicitly rounded IEEE
 // double op so the result is bit-identical to the reference.
-__device__ __forceinline__ bool triHitExact(double ox, double oy, double oz, double dx, double dy, double dz,
-                                            const float4& a, const float4& b, const float4& c, double* tOut) {
-    const double p0x = a.x, p0y = a.y, p0z = a.z;
-    const double e1x = __dsub_rn((double)b.x, p0x), e1y = __dsub_rn((double)b.y, p0y), e1z = __dsub_rn((double)b.z, p0z);
-    const double e2x = __dsub_rn((double)c.x, p0x), e2y = __dsub_rn((double)c.y, p0y), e2z = __dsub_rn((double)c.z, p0z);
+// The test after the edges: p0 = (double)a, e1 = b - a, e2 = c - a.
+__device__ __forceinline__ bool triHitExactEdges(double ox, double oy, double oz, double dx, double dy, double dz,
+                                                 double p0x, double p0y, double p0z, double e1x, double e1y,
+                                                 double e1z, double e2x, double e2y, double e2z, double* tOut) {
     // pVec = cross(d, e2)
     const double px = __dsub_rn(__dmul_rn(dy, e2z), __dmul_rn(dz, e2y));
     const double py = __dsub_rn(__dmul_rn(dz, e2x), __dmul_rn(dx, e2z));
@@ -200,6 +199,29 @@ __device__ __forceinline__ bool triHitExact(double ox, double oy, double oz, dou
     const double t = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(e2x, qx), __dmul_rn(e2y, qy)), __dmul_rn(e2z, qz)), invdet);
     if (t > kEps) { *tOut = t; return true; }
     return false;
+}
+
+__device__ __forceinline__ bool triHitExact(double ox, double oy, double oz, double dx, double dy, double dz,
+                                            const float4& a, const float4& b, const float4& c, double* tOut) {
+    const double p0x = a.x, p0y = a.y, p0z = a.z;
+    const double e1x = __dsub_rn((double)b.x, p0x), e1y = __dsub_rn((double)b.y, p0y), e1z = __dsub_rn((double)b.z, p0z);
+    const double e2x = __dsub_rn((double)c.x, p0x), e2y = __dsub_rn((double)c.y, p0y), e2z = __dsub_rn((double)c.z, p0z);
+    return triHitExactEdges(ox, oy, oz, dx, dy, dz, p0x, p0y, p0z, e1x, e1y, e1z, e2x, e2y, e2z, tOut);
+}
+
+#ifndef PPPM_TRI_EDGES
+#define PPPM_TRI_EDGES 1
+#endif
+constexpr bool kTriEdges = PPPM_TRI_EDGES != 0;
+
+// The same test from the slot's double vertex and edges, computed on the
+// host with the same operations (10 doubles per slot: p0, e1, e2, pad), so
+// that the test converts nothing and subtracts no vertices.
+__device__ __forceinline__ bool triHitExactPre(double ox, double oy, double oz, double dx, double dy, double dz,
+                                               const double* __restrict__ triE, int slot, double* tOut) {
+    const double2* q = reinterpret_cast<const double2*>(triE + 10 * (int64_t)slot);
+    const double2 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), d = __ldg(q + 3), e = __ldg(q + 4);
+    return triHitExactEdges(ox, oy, oz, dx, dy, dz, a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x, tOut);
 }
 
 // Conservative FP32 pre-test for triHitExact. Returns false only when the
@@ -404,7 +426,7 @@ __device__ __forceinline__ int traverseExactWarp(const QNode* __restrict__ nodes
                                                  int rootCode, bool active, double odx, double ody, double odz,
                                                  float dx, float dy, float dz, const int* orderTab,
                                                  const QNode* sTop, double* bestOut, int* nodeVisits,
-                                                 int* triTests) {
+                                                 int* triTests, const double* __restrict__ triE = nullptr) {
     const float ox = __double2float_rn(odx), oy = __double2float_rn(ody), oz = __double2float_rn(odz);
     const float idx = dx == 0.0f ? 1.0e20f : __frcp_rn(dx);
     const float idy = dy == 0.0f ? 1.0e20f : __frcp_rn(dy);
@@ -429,9 +451,15 @@ __device__ __forceinline__ int traverseExactWarp(const QNode* __restrict__ nodes
                 const double ddx = dx, ddy = dy, ddz = dz;
                 for (int c = 0; c < ncand; c++) {
                     const int slot = c == 0 ? cand0 : (c == 1 ? cand1 : cand2);
-                    const float4 a = tris[3 * slot], b = tris[3 * slot + 1], cc = tris[3 * slot + 2];
                     double t;
-                    if (triHitExact(odx, ody, odz, ddx, ddy, ddz, a, b, cc, &t) && best > t) {
+                    bool h;
+                    if (triE) {
+                        h = triHitExactPre(odx, ody, odz, ddx, ddy, ddz, triE, slot, &t);
+                    } else {
+                        const float4 a = tris[3 * slot], b = tris[3 * slot + 1], cc = tris[3 * slot + 2];
+                        h = triHitExact(odx, ody, odz, ddx, ddy, ddz, a, b, cc, &t);
+                    }
+                    if (h && best > t) {
                         best = t;
                         bestf = __double2float_rn(t);
                         hit = slot;
@@ -546,7 +574,7 @@ struct WarpTrav {
 // in the warp votes). All 32 lanes call it.
 __device__ __forceinline__ void warpTravRun(WarpTrav& s, bool live, int minDone, const QNode* __restrict__ nodes,
                                             const float4* __restrict__ tris, const int* orderTab, const QNode* sTop,
-                                            int* nodeVisits, int* triTests) {
+                                            int* nodeVisits, int* triTests, const double* __restrict__ triE = nullptr) {
     for (;;) {
         const bool canRun = live && s.sp > 0 && s.ncand == 0;
         const unsigned runMask = __ballot_sync(0xffffffffu, canRun);
@@ -558,9 +586,15 @@ __device__ __forceinline__ void warpTravRun(WarpTrav& s, bool live, int minDone,
                 const double ddx = s.dx, ddy = s.dy, ddz = s.dz;
                 for (int c = 0; c < s.ncand; c++) {
                     const int slot = c == 0 ? s.cand0 : (c == 1 ? s.cand1 : s.cand2);
-                    const float4 a = tris[3 * slot], b = tris[3 * slot + 1], cc = tris[3 * slot + 2];
                     double t;
-                    if (triHitExact(s.odx, s.ody, s.odz, ddx, ddy, ddz, a, b, cc, &t) && s.best > t) {
+                    bool h;
+                    if (triE) {
+                        h = triHitExactPre(s.odx, s.ody, s.odz, ddx, ddy, ddz, triE, slot, &t);
+                    } else {
+                        const float4 a = tris[3 * slot], b = tris[3 * slot + 1], cc = tris[3 * slot + 2];
+                        h = triHitExact(s.odx, s.ody, s.odz, ddx, ddy, ddz, a, b, cc, &t);
+                    }
+                    if (h && s.best > t) {
                         s.best = t;
                         s.bestf = __double2float_rn(t);
                         s.hit = slot;

@@ -7,7 +7,7 @@
 
 // blocks per SM promised to ptxas for the traversal kernels
 #ifndef PPPM_TRACE_MINBLOCKS
-#define PPPM_TRACE_MINBLOCKS 6
+#define PPPM_TRACE_MINBLOCKS 7
 #endif
 
 namespace pppm {
