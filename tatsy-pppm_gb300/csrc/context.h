@@ -260,7 +260,7 @@ struct pppm_ctx {
     pppm::OctreeBufs stageOct;
     // stage timing: 0-7 main stream; 8 fork of the side stream, 9-10 its
     // eye trace
-    cudaEvent_t ev[11] = {};
+    cudaEvent_t ev[12] = {};
     std::vector<cudaEvent_t> graphEvents;  // stage timing of captured passes
 };
 

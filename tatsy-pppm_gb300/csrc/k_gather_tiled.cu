@@ -312,8 +312,7 @@ cudaError_t querySortLayout(QuerySortBufs& qs, int64_t maxQueries) {
     return qs.sorted.ensure((size_t)std::max<int64_t>(maxQueries, 1) * 48);
 }
 
-cudaError_t launchGatherTiled(const GridDev& g, QueryView qv, QuerySortBufs& qs, float radius, float* out,
-                              bool accumulate, unsigned long long* work, cudaStream_t st) {
+cudaError_t querySort(const GridDev& g, QueryView qv, QuerySortBufs& qs, cudaStream_t st) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(qs.hist.p, 0, ((size_t)qs.size + 1) * 4, st)) != cudaSuccess) return e;
     kQueryKeys<<<blocksFor(qv.n, 256), 256, 0, st>>>(qv, g, qs.size - 1, qs.keys.as<uint32_t>(), qs.hist.as<uint32_t>());
@@ -322,6 +321,18 @@ cudaError_t launchGatherTiled(const GridDev& g, QueryView qv, QuerySortBufs& qs,
         return e;
     kQueryScatter<<<blocksFor(qv.n, 256), 256, 0, st>>>(qv, qs.keys.as<uint32_t>(), qs.cursor.as<uint32_t>(),
                                                         qs.sorted.as<float4>());
+    return cudaGetLastError();
+}
+
+cudaError_t launchGatherTiled(const GridDev& g, QueryView qv, QuerySortBufs& qs, float radius, float* out,
+                              bool accumulate, unsigned long long* work, cudaStream_t st) {
+    const cudaError_t e = querySort(g, qv, qs, st);
+    if (e != cudaSuccess) return e;
+    return launchGatherSorted(g, qv, qs, radius, out, accumulate, work, st);
+}
+
+cudaError_t launchGatherSorted(const GridDev& g, QueryView qv, QuerySortBufs& qs, float radius, float* out,
+                               bool accumulate, unsigned long long* work, cudaStream_t st) {
     // the sorted count equals the query count; the tiled kernel reads it
     // from the end of the scanned histogram
     const uint32_t* total = qs.hist.as<uint32_t>() + qs.size;

@@ -141,19 +141,41 @@ cudaError_t exclusiveScan(uint32_t* data, int64_t n, uint32_t* cursor, uint32_t*
 
 int64_t scanTmpWords(int64_t n) { return (n + kScanChunk - 1) / kScanChunk + 1; }
 
+namespace {
+// cell edge, its inverse and the origin of the grid over the box; the cell
+// count per axis stays below 2^20
+void gridGeom(const double* bbmin, const double* bbmax, double cell, float* cellF, float* inv, float* origin) {
+    double ext = 0.0;
+    for (int d = 0; d < 3; d++) ext = std::max(ext, bbmax[d] - bbmin[d]);
+    if (cell < ext / (double)(1 << 20)) cell = ext / (double)(1 << 20);
+    if (!(cell > 0.0)) cell = 1.0;
+    *cellF = (float)cell;
+    *inv = (float)(1.0 / cell);
+    for (int d = 0; d < 3; d++) origin[d] = (float)(bbmin[d] - 1e-3 * cell);
+}
+
+int cellsAlong(double hi, float origin, float inv) { return std::max(1, (int)std::ceil((hi - origin) * inv) + 1); }
+}  // namespace
+
+GridDev gridGeometry(const double* bbmin, const double* bbmax, double cell) {
+    GridDev d{};
+    float origin[3];
+    gridGeom(bbmin, bbmax, cell, &d.cell, &d.invCell, origin);
+    d.ox = origin[0];
+    d.oy = origin[1];
+    d.oz = origin[2];
+    d.nx = cellsAlong(bbmax[0], origin[0], d.invCell);
+    d.ny = cellsAlong(bbmax[1], origin[1], d.invCell);
+    d.nz = cellsAlong(bbmax[2], origin[2], d.invCell);
+    return d;
+}
+
 cudaError_t gridLayout(GridBufs& g, const double* bbmin, const double* bbmax, double cell, int64_t nPhotons) {
     // bucket table: next power of two >= 2 * photons, within [2^12, 2^26]
     uint32_t size = 1u << 12;
     while ((int64_t)size < 2 * nPhotons && size < (1u << 26)) size <<= 1;
     g.size = size;
-    // keep the cell count per axis below 2^20
-    double ext = 0.0;
-    for (int d = 0; d < 3; d++) ext = std::max(ext, bbmax[d] - bbmin[d]);
-    if (cell < ext / (double)(1 << 20)) cell = ext / (double)(1 << 20);
-    if (!(cell > 0.0)) cell = 1.0;
-    g.cell = (float)cell;
-    g.invCell = (float)(1.0 / cell);
-    for (int d = 0; d < 3; d++) g.origin[d] = (float)(bbmin[d] - 1e-3 * cell);
+    gridGeom(bbmin, bbmax, cell, &g.cell, &g.invCell, g.origin);
     cudaError_t e;
     if ((e = g.counts.ensure(((size_t)size + 1) * 4)) != cudaSuccess) return e;
     if ((e = g.cursor.ensure(((size_t)size + 1) * 4)) != cudaSuccess) return e;
@@ -172,9 +194,9 @@ GridDev gridView(const GridBufs& g, const double* bbmin, const double* bbmax) {
     d.oz = g.origin[2];
     d.cell = g.cell;
     d.invCell = g.invCell;
-    d.nx = std::max(1, (int)std::ceil((bbmax[0] - g.origin[0]) * g.invCell) + 1);
-    d.ny = std::max(1, (int)std::ceil((bbmax[1] - g.origin[1]) * g.invCell) + 1);
-    d.nz = std::max(1, (int)std::ceil((bbmax[2] - g.origin[2]) * g.invCell) + 1);
+    d.nx = cellsAlong(bbmax[0], g.origin[0], g.invCell);
+    d.ny = cellsAlong(bbmax[1], g.origin[1], g.invCell);
+    d.nz = cellsAlong(bbmax[2], g.origin[2], g.invCell);
     return d;
 }
 

@@ -20,6 +20,8 @@ cudaError_t exclusiveScan(uint32_t* data, int64_t n, uint32_t* cursor, uint32_t*
 int64_t scanTmpWords(int64_t n);
 cudaError_t gridLayout(GridBufs& g, const double* bbmin, const double* bbmax, double cell, int64_t nPhotons);
 GridDev gridView(const GridBufs& g, const double* bbmin, const double* bbmax);
+// Origin, cell edge and cells per axis of the grid gridLayout would give.
+GridDev gridGeometry(const double* bbmin, const double* bbmax, double cell);
 cudaError_t gridBuild(GridBufs& g, const GridDev& view, const float4* rec, const uint64_t* dCount, int64_t capacity,
                       cudaStream_t st);
 
@@ -32,6 +34,12 @@ cudaError_t launchGatherCanonical(const GridDev& g, QueryView q, float radius, f
 cudaError_t querySortLayout(QuerySortBufs& qs, int64_t maxQueries);
 cudaError_t launchGatherTiled(const GridDev& g, QueryView q, QuerySortBufs& qs, float radius, float* out,
                               bool accumulate, unsigned long long* work, cudaStream_t st);
+// The two halves of launchGatherTiled: the query sort needs only the grid's
+// geometry (gridGeometry), so it can run as soon as the queries exist; the
+// gather then reads the sorted queries.
+cudaError_t querySort(const GridDev& geometry, QueryView q, QuerySortBufs& qs, cudaStream_t st);
+cudaError_t launchGatherSorted(const GridDev& g, QueryView q, QuerySortBufs& qs, float radius, float* out,
+                               bool accumulate, unsigned long long* work, cudaStream_t st);
 // Compat kNN gather (ppm_probabilistic.cc:300-335; irradianceWithPM,
 // subsurface_integrator.cc:329-365): k nearest within eps, normal filter
 // |n.(q-p)|/|q-p| < rlim, cone filter, output scaled by the query weight.

@@ -429,9 +429,12 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         pppm_ctx* c;
         bool on = false;
         ~SideJoin() {
-            if (on) cudaStreamWaitEvent(c->stream, c->ev[10], 0);
+            if (on) cudaStreamWaitEvent(c->stream, c->ev[11], 0);
         }
     } sideJoin{c};
+    // canonical: the queries are sorted on the side stream right after the
+    // eye paths (the sort needs only the grid's geometry), beside the photons
+    const bool sideSort = sideEye && !compat;
     if (sideEye) {
         PPPM_CUDA(c, cudaEventRecord(c->ev[8], c->stream));
         PPPM_CUDA(c, cudaStreamWaitEvent(c->side, c->ev[8], 0));
@@ -439,6 +442,12 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         PPPM_CUDA(c, launchEyeTrace(tp, sv, ev, cd, sssView(c), pixelStates, rs.accum.as<float>(),
                                     rs.queries.as<float4>(), rs.sss.queue.as<float4>(), rs.sss.queueCap, ctr, c->side));
         PPPM_CUDA(c, cudaEventRecord(c->ev[10], c->side));
+        if (sideSort) {
+            const GridDev geom = gridGeometry(c->bbmin, c->bbmax, par.cell_factor * rs.radius);
+            const QueryView qs{rs.queries.as<float4>(), reinterpret_cast<const uint32_t*>(&ctr->queries), pixels};
+            PPPM_CUDA(c, querySort(geom, qs, rs.qsort, c->side));
+        }
+        PPPM_CUDA(c, cudaEventRecord(c->ev[11], c->side));
         sideJoin.on = true;
     }
     for (int attempt = 0;; attempt++) {
@@ -546,7 +555,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
 
     // eye paths and gather
     if (sideEye)
-        PPPM_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev[10], 0));
+        PPPM_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev[11], 0));
     else
         PPPM_CUDA(c, launchEyeTrace(tp, sv, ev, cd, sssView(c), pixelStates, rs.accum.as<float>(),
                                     rs.queries.as<float4>(), rs.sss.queue.as<float4>(), rs.sss.queueCap, ctr, c->stream));
@@ -566,6 +575,10 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     if (compat)
         PPPM_CUDA(c, launchGatherCompat(gv, qv, k, (float)par.gather_photons, compatDiscLimit(rs.radius), phantoms,
                                         rs.accum.as<float>(), true, c->stream));
+    else if (sideSort)
+        PPPM_CUDA(c, launchGatherSorted(gv, qv, rs.qsort, (float)rs.radius, rs.accum.as<float>(), true,
+                                        tp.countTraversal ? rs.gatherWork.as<unsigned long long>() : nullptr,
+                                        c->stream));
     else
         PPPM_CUDA(c, launchGatherTiled(gv, qv, rs.qsort, (float)rs.radius, rs.accum.as<float>(), true,
                                        tp.countTraversal ? rs.gatherWork.as<unsigned long long>() : nullptr,
