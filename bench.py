@@ -347,8 +347,8 @@ def run_gb300(args):
     d2h = host.numel() * 4 + 2 * 112  # image + two counter readbacks
 
     # roofline of the photon bounce kernels (traversal dominated): the
-    # traversal bytes per ray of the survey's byte model, 32 B ray + 16 B hit
-    # + 128 B per node visited + 48 B per triangle tested
+    # algorithmic bytes of a traversal, 32 B ray + 16 B hit + 128 B per node
+    # visited + 48 B per triangle tested
     ms_bounce = sum(s["ms_bounce"] for s in stats) / len(stats)
     alg = cnt.photon_rays * 48 + cnt.photon_node_visits * 128 + cnt.photon_tri_tests * 48
     peak, peak_kind = measured_peak()
