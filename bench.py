@@ -228,7 +228,7 @@ def equal_time_study(ctx, scene, common, ref_passes=4096, budget_passes=64):
     cp, cl = [], []
     plain, n_plain, budget = render(0, 7, passes=budget_passes, curve=cp)
     e_plain = rel(plain)
-    ctx.learned_config(retrain_every=4, steps=16, batch=65536, lr=1e-3, floor_bsdf=0.3, max_log_kappa=7.0,
+    ctx.learned_config(retrain_every=2, steps=2, batch=65536, lr=4e-3, floor_bsdf=0.3, max_log_kappa=7.0,
                        guide_bounces=0)
     learned, n_learned, el = render(P.FLAG_LEARNED, 7, budget=budget, curve=cl)
     match = next((c for c in cl if c["relmse"] <= e_plain), None)
@@ -240,8 +240,8 @@ def equal_time_study(ctx, scene, common, ref_passes=4096, budget_passes=64):
             "time_ratio_plain_over_learned": budget / match["seconds"] if match else None,
             "relmse": "mean((x - r)^2 / (r^2 + 0.01)) over pixels and channels",
             "learned_settings": "environment direction proposed by the network (8 vMF lobes at the emission input), "
-                                "one-sample MIS with the reference's cell sampling at floor 0.3; retrain every 4 "
-                                "passes, 16 Adam steps x 65536 records, lr 1e-3, max log kappa 7; bounces not "
+                                "one-sample MIS with the reference's cell sampling at floor 0.3; retrain every 2 "
+                                "passes, 2 Adam steps x 65536 records, lr 4e-3, max log kappa 7; bounces not "
                                 "guided"}
 
 

@@ -111,7 +111,7 @@ typedef struct {
 #define PPPM_FLAG_COUNT_TRAVERSAL 0x1 /* count BVH nodes visited / triangles tested */
 #define PPPM_FLAG_LEARNED 0x2 /* canonical mode: learned photon proposal (MLP + vMF mixture, one-sample MIS
                                  with the reference's environment sampling, and optionally with the BSDF at
-                                 Lambertian bounces, at a floor of 0.3; retrained every 4 passes); no
+                                 Lambertian bounces, at a floor of 0.3; retrained every 2 passes); no
                                  reference counterpart */
 #define PPPM_FLAG_LEARNED_FROZEN 0x4 /* with PPPM_FLAG_LEARNED: the same pipeline without training (the
                                         reference's sampling alone): the method without the network */
@@ -308,8 +308,8 @@ int pppm_mlp_forward(pppm_ctx* ctx, const float* params, const float* pos, const
 
 /* Settings of the learned proposal for the next pppm_render_begin with
  * PPPM_FLAG_LEARNED (no counterpart in the reference). retrain_every: passes
- * between trainings (4); steps: Adam steps per training (16); batch: records
- * per step (65536); lr: Adam learning rate (1e-3); floor_bsdf: probability of
+ * between trainings (2); steps: Adam steps per training (2); batch: records
+ * per step (65536); lr: Adam learning rate (4e-3); floor_bsdf: probability of
  * the reference's own sampling (environment cell draw, BSDF lobe) in the
  * one-sample MIS mixtures (0.3); max_log_kappa: upper
  * clamp of the lobes' log concentration (7); guide_bounces: 1 to guide

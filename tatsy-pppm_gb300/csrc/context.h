@@ -138,10 +138,10 @@ struct SssState {
 struct GuideState {
     bool enabled = false;
     bool trained = false;
-    int retrainEvery = 4;       // passes between trainings
-    int stepsPerTrain = 16;     // Adam steps per training
+    int retrainEvery = 2;       // passes between trainings
+    int stepsPerTrain = 2;      // Adam steps per training
     int64_t batch = 65536;      // records per step
-    float lr = 1e-3f;
+    float lr = 4e-3f;
     float floorBsdf = 0.3f;     // one-sample MIS: probability of the reference's sampling
     float maxLogKappa = 7.0f;   // clamp of the lobes' log concentration
     int guideBounces = 0;       // guide Lambertian bounces too (1) or the emission direction only (0)

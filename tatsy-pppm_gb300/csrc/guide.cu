@@ -1,7 +1,7 @@
 // Host side of the learned photon proposal in a canonical render: state set
 // up at render_begin, the emission mixture of each pass, the per-bounce
 // network step, the importance grid after the eye pass, and the retraining
-// schedule (every 4 passes: 16 Adam steps of 65,536 records at lr 1e-3).
+// schedule (every 2 passes: 2 Adam steps of 65,536 records at lr 4e-3).
 #include <chrono>
 #include <cmath>
 #include <cstring>

@@ -37,7 +37,7 @@ def reference(setup):
 
 
 def _render(c, sc, flags, passes, seed, photons=300_000, guide_bounces=0):
-    c.learned_config(retrain_every=4, steps=16, batch=65536, lr=1e-3, floor_bsdf=0.3, max_log_kappa=7.0,
+    c.learned_config(retrain_every=2, steps=2, batch=65536, lr=4e-3, floor_bsdf=0.3, max_log_kappa=7.0,
                      guide_bounces=guide_bounces)
     par = P.Context.make_params(mode=P.MODE_CANONICAL, photons=photons, max_bounce_photon=12, max_bounce_eye=12,
                                 radius_scale=1 / 64, seed=seed, flags=flags)
