@@ -86,6 +86,13 @@ __device__ __forceinline__ void seedCanonical(uint32_t seed, int pass, uint64_t 
 }
 
 constexpr int kRun = 32;  // tapes generated sequentially per thread
+// 1: the trace kernels stage the top BVH levels (85 nodes, 10.9 KB) in
+// shared memory per block. 0: they read them through L1 like the rest of
+// the tree; the shared memory this frees is L1 cache for the BVH (measured
+// faster, 0 is the default).
+#ifndef PPPM_TOP_SMEM
+#define PPPM_TOP_SMEM 0
+#endif
 constexpr int kMaxEyeSegments = 4096;  // eye path segments before a path is cut (subsurface scenes)
 
 // Start state of every photon tape and pixel tape of this pass. Stream s
@@ -346,10 +353,17 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(T
                                                                                int64_t depCap, PassCounters* ctr,
                                                                                const uint32_t* __restrict__ perm) {
     __shared__ int order[128];
-    __shared__ QNode sTop[kTopNodes];
+#if PPPM_TOP_SMEM
+    __shared__ QNode sTopBuf[kTopNodes];
+    QNode* sTop = sTopBuf;
+#else
+    QNode* sTop = nullptr;  // top levels through L1 like the rest of the tree
+#endif
     const int64_t n = min((int64_t)ctr->queue[0], maxPaths);
     loadOrderTable(order);
+#if PPPM_TOP_SMEM
     loadTopNodes(sTop, sc.nodes, sc.numNodes);
+#endif
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     PathState p;
@@ -430,7 +444,12 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
                                                      PathState* __restrict__ out, int64_t maxPaths,
                                                      float4* __restrict__ dep, int64_t depCap, PassCounters* ctr) {
     __shared__ int order[128];
-    __shared__ QNode sTop[kTopNodes];
+#if PPPM_TOP_SMEM
+    __shared__ QNode sTopBuf[kTopNodes];
+    QNode* sTop = sTopBuf;
+#else
+    QNode* sTop = nullptr;  // top levels through L1 like the rest of the tree
+#endif
     const int qi = bounce % 3, qo = (bounce + 1) % 3, qz = (bounce + 2) % 3;
     const int64_t n = min((int64_t)ctr->queue[qi], maxPaths);
     if (blockIdx.x == 0 && threadIdx.x == 0) ctr->queue[qz] = 0;
@@ -438,7 +457,9 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
     // later bounces leave before staging anything (uniform per block)
     if ((int64_t)blockIdx.x * blockDim.x >= n) return;
     loadOrderTable(order);
+#if PPPM_TOP_SMEM
     loadTopNodes(sTop, sc.nodes, sc.numNodes);
+#endif
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
         const int64_t i = base + threadIdx.x;
@@ -526,9 +547,16 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
                                                  float* __restrict__ accum, float4* __restrict__ queries,
                                                  float4* __restrict__ sssQ, int64_t sssCap, PassCounters* ctr) {
     __shared__ int order[128];
-    __shared__ QNode sTop[kTopNodes];
+#if PPPM_TOP_SMEM
+    __shared__ QNode sTopBuf[kTopNodes];
+    QNode* sTop = sTopBuf;
+#else
+    QNode* sTop = nullptr;  // top levels through L1 like the rest of the tree
+#endif
     loadOrderTable(order);
+#if PPPM_TOP_SMEM
     loadTopNodes(sTop, sc.nodes, sc.numNodes);
+#endif
     const int64_t np = (int64_t)cam.w * cam.h;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     // a block takes a 16x8 pixel tile, each warp an 8x4 quarter of it, so
