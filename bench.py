@@ -268,7 +268,8 @@ def run_reference(args):
     value = photons * args.steps / sec / 1e6
     sample = (f"each step: 1 pass of {photons} photons at {w}x{h} (1/{scale} of the photons and pixels of the "
               f"workload), reference semantics (kNN gather, growing radius), {threads} OpenMP threads")
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+    # n_gpus: the launch's N (rank 0 alone runs the CPU port)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": workload_config("compat", 1.0),
