@@ -6,25 +6,31 @@ sphere of 873,620 triangles (frequency 209) over a ground quad, lit by a
 seeded 2048x1024 FP32 equirect sky (gradient + 0.5 degree sun lobe of peak
 5e4 + lognormal texel noise sigma 0.3), materials 60/20/20 Lambertian /
 mirror / dielectric per surface cluster, 4M photons per pass, alpha 0.7,
-photon and eye depth 12. Data are synthetic (seeded); nothing is downloaded.
+r1 = diag/64, photon and eye depth 12, canonical Knaus-Zwicker mode. Data
+are synthetic (seeded); nothing is downloaded.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--mode canonical|compat]
+                  [--mode canonical|compat] [--workload config2|config3|config4]
+                  [--case mlp_forward|mlp_train|render|subsurface|classic ...]
 
 --impl gb300 (default) times the hand-written sm_103a kernels through the C
-ABI: `value` is device time of K passes with every input resident in HBM;
-`e2e` is the same passes through pppm_render_pass + pppm_render_read into
-pinned host memory (the reference writes an image every pass). --impl
-reference times the reference algorithm on the host cores instead (the
-oracle port of oracle/pppm_port.cc, built from the reference's own algorithm
-and pinned bit-exact to it; the reference sources do not travel to the GPU
-machine) on a bounded sample of the workload. Multi-GPU runs are replicas
-(passes shard with no exchange until an image reduction, not timed here).
+ABI: `value` is the device time of passes W+1..W+K with every input resident
+in HBM; `e2e` replays the same passes (same indices, same radii) through
+pppm_render_pass + pppm_render_read into pinned host memory, wall clock.
+--impl reference times the CPU restatement of the same workload (the oracle
+port, oracle/pppm_port.cc: the reference's algorithm pinned bit-exact to the
+compiled reference in compat mode, with the same canonical gather as the GPU
+arm) on all host cores, passes W+1..W+K of the identical configuration.
+The default gb300 run also carries, as extra keys: the CPU baseline, a
+full-size compat-mode figure for both GPU and port, the subsurface (config3)
+and batched-jobs (config4) workloads, and the equal-time learned-vs-plain
+relMSE study. --case runs one small profiling case (kernel timings only).
+Multi-GPU runs are replicas (passes shard with no exchange until one image
+reduction, not timed here).
 """
 from __future__ import annotations
 
 import argparse
-import ctypes
 import json
 import os
 import pathlib
@@ -42,7 +48,6 @@ sys.path.insert(0, str(ROOT / "oracle"))
 
 METRIC = "Mphotons/s + equal-time relMSE, learned vs plain PPM-APA, 1080p, 1 GB300"
 UNIT = "Mphotons/s"
-# the headline workload and the subsurface one (measured on request)
 WORKLOADS = {
     "config2": dict(photons=4_000_000, depth=12, width=1920, height=1080, triangles=873_622,
                     desc="ppm-apa pass, 1920x1080, displaced icosphere 873,620 tris + ground, 2048x1024 sky env, "
@@ -57,8 +62,8 @@ WORKLOADS = {
                          "(refractive + BSSRDF) + ground, 1024x512 sky env, 2M photons/pass, depth 12, Poisson "
                          "irradiance points + octree rebuilt every pass"),
 }
-PHOTONS = WORKLOADS["config2"]["photons"]
-DEPTH = WORKLOADS["config2"]["depth"]
+# issue slots: 4 warp schedulers per SM, one warp instruction each per cycle
+SMS, SCHEDULERS_PER_SM = 152, 4
 
 
 def parse():
@@ -69,16 +74,25 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="canonical", choices=["canonical", "compat"])
     ap.add_argument("--cell-factor", type=float, default=1.0)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-study", action="store_true", help="skip the equal-time learned-vs-plain relMSE study")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the compat, config3, config4 and cold end-to-end extra keys")
+    ap.add_argument("--study-seeds", type=int, default=3)
     ap.add_argument("--no-graph", action="store_true", help="config4: run every pass through pppm_render_pass")
     ap.add_argument("--graph-lanes", type=int, default=0, help="config4: jobs at once inside the graph")
-    args = ap.parse_args()
-    global PHOTONS, DEPTH
-    PHOTONS = WORKLOADS[args.workload]["photons"]
-    DEPTH = WORKLOADS[args.workload]["depth"]
-    return args
+    ap.add_argument("--case", default=None, choices=["mlp_forward", "mlp_train", "render", "subsurface", "classic"],
+                    help="one small profiling case instead of the bench")
+    ap.add_argument("--photons", type=int, default=1_000_000, help="--case render/classic: photons per pass")
+    ap.add_argument("--width", type=int, default=960, help="--case render/classic: image width")
+    ap.add_argument("--height", type=int, default=540, help="--case render/classic: image height")
+    ap.add_argument("--passes", type=int, default=3, help="--case: passes per render")
+    ap.add_argument("--rows", type=int, default=4_000_000, help="--case mlp_forward: network rows")
+    ap.add_argument("--records", type=int, default=65536, help="--case mlp_train: training records")
+    ap.add_argument("--full", action="store_true", help="--case subsurface: the config3 sizes")
+    ap.add_argument("--count", action="store_true", help="--case render: a first render with traversal counting")
+    return ap.parse_args()
 
 
 def dist_env():
@@ -94,7 +108,16 @@ def workload_config(mode, cell_factor, workload="config2"):
             "triangles": w["triangles"], "photons_per_pass": w["photons"], "max_depth": w["depth"], "alpha": 0.7,
             "radius_scale": (1 / 64) if mode == "canonical" else 0.1, "cell_factor": cell_factor,
             "parallelism": "replicas",
-            "l2": "inputs larger than L2 (photon map, path queues and BVH ~1.5 GB per pass)"}
+            "l2": "inputs larger than L2 (photon map, path queues and BVH ~1.5 GB per pass), no flush"}
+
+
+def params_for(P, mode, workload, seed, threads, cell_factor=1.0, flags=0):
+    w = WORKLOADS[workload]
+    compat = mode == "compat"
+    return P.Context.make_params(mode=P.MODE_COMPAT if compat else P.MODE_CANONICAL, photons=w["photons"],
+                                 num_streams=threads, max_bounce_photon=w["depth"], max_bounce_eye=w["depth"],
+                                 radius_scale=0.1 if compat else 1 / 64, seed=seed, cell_factor=cell_factor,
+                                 flags=flags)
 
 
 class ClockSampler:
@@ -166,117 +189,126 @@ def measured_peak():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        return float(d["hbm_gbs"]), "measured", float(d.get("sm_max_mhz", 2070.0))
+    return 6800.0, "fallback", 2070.0
 
 
-def cpu_baseline(scene, sample_scale=16, threads=None):
-    """The reference algorithm (oracle port, compat semantics) on the host
-    cores over a bounded sample: photons and pixels divided by sample_scale."""
+def profile_json(name):
+    p = ROOT / "profiles" / name
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def port_passes(scene, mode, passes, threads, warm):
+    """Passes 1..passes of the oracle port on the host cores; returns the
+    wall time of passes warm+1..passes (photon trace + map build + eye paths
+    and gather, as the reference's pass loop times them) and the radii."""
     import port
     import pppm_gb300 as P
 
-    threads = threads or os.cpu_count() or 1
-    w, h = 1920 // int(sample_scale ** 0.5), 1080 // int(sample_scale ** 0.5)
     cam = P.Context.make_camera(scene.camera)
-    cam.width, cam.height = w, h
-    photons = PHOTONS // sample_scale
-    par = P.Context.make_params(mode=P.MODE_COMPAT, photons=photons, num_streams=threads, max_bounce_photon=DEPTH,
-                                max_bounce_eye=DEPTH)
+    par = params_for(P, mode, "config2", 1, threads)
     ps = port.PortScene(scene)
-    out = ps.render(cam, par, 1)
-    st = out["stats"][0]
-    sec = (st["ms_photon"] + st["ms_eye"]) / 1e3
-    return {"value": photons / sec / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"1 pass of {photons} photons at {w}x{h} on the same scene (1/{sample_scale} of the photons "
-                      f"and pixels), reference semantics, {threads} OpenMP threads; scene setup untimed"}
+    out = ps.render(cam, par, passes)
+    st = out["stats"][warm:]
+    return sum((s["ms_photon"] + s["ms_eye"]) / 1e3 for s in st), [s["radius"] for s in out["stats"]]
 
 
-def equal_time_study(ctx, scene, common, ref_passes=4096, budget_passes=64):
-    """relMSE of plain and learned-proposal renders against a ref_passes plain
-    render (relMSE = mean over pixels and channels of (x - r)^2 / (r^2 + 0.01)).
-    Plain renders budget_passes passes; their wall time is the budget. The
-    learned render runs whole passes until the budget is spent. Both images
-    are read at checkpoints (the reads are not counted in the wall times),
-    which gives the learned render's relMSE at equal time and the first
-    checkpoint at which it is at or below plain's final relMSE."""
+def cpu_baseline(scene, threads):
+    """The port on the host cores: passes 2-3 of the full workload (pass 1
+    untimed), canonical mode, all threads."""
+    sec, _ = port_passes(scene, "canonical", 3, threads, 1)
+    photons = WORKLOADS["config2"]["photons"]
+    return {"value": 2 * photons / sec / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"passes 2-3 (pass 1 untimed) of the full workload: 1920x1080, 4M photons, canonical, "
+                      f"r1 = diag/64, depth 12; oracle port on {threads} OpenMP threads; scene set-up untimed"}
+
+
+def compat_full_size(ctx, scene, threads):
+    """Full-size compat mode (the reference's semantics: kNN gather with
+    k = (int)r, growing radius, phantom photons, per-stream tapes) on the GPU
+    and on the port, passes 2-3 of the same render (pass 1 untimed)."""
+    import torch
+
     import pppm_gb300 as P
 
-    checkpoints = {2, 4, 6, 8, 10, 12, 14, 16, 20, 24, 28, 32, 40, 48, 56, 64, 80, 96, 128}
-    ref = None
-
-    def rel(x):
-        return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
-
-    def render(flags, seed, passes=None, budget=None, curve=None):
-        ctx.render_begin(scene.camera, P.Context.make_params(**dict(common, seed=seed, flags=flags)))
-        el = 0.0
-        t = 0
-        while True:
-            t += 1
-            t0 = time.perf_counter()
-            ctx.render_pass(t)
-            el += time.perf_counter() - t0
-            done = (passes is not None and t >= passes) or (budget is not None and el >= budget)
-            if curve is not None and (t in checkpoints or done):
-                curve.append({"passes": t, "seconds": round(el, 4), "relmse": rel(ctx.render_read() / t)})
-            if done:
-                break
-        return ctx.render_read() / t, t, el
-
-    ref, _, ref_s = render(0, 1000, passes=ref_passes)
-    cp, cl = [], []
-    plain, n_plain, budget = render(0, 7, passes=budget_passes, curve=cp)
-    e_plain = rel(plain)
-    ctx.learned_config(retrain_every=2, steps=2, batch=65536, lr=4e-3, floor_bsdf=0.3, max_log_kappa=7.0,
-                       guide_bounces=0)
-    learned, n_learned, el = render(P.FLAG_LEARNED, 7, budget=budget, curve=cl)
-    match = next((c for c in cl if c["relmse"] <= e_plain), None)
-    return {"reference_passes": ref_passes, "reference_s": ref_s, "budget_s": budget,
-            "plain": {"passes": n_plain, "relmse": e_plain, "curve": cp},
-            "learned": {"passes": n_learned, "seconds": el, "relmse": rel(learned), "curve": cl},
-            "relmse_learned_over_plain": rel(learned) / e_plain,
-            "learned_reaches_plain_relmse_at_s": match["seconds"] if match else None,
-            "time_ratio_plain_over_learned": budget / match["seconds"] if match else None,
-            "relmse": "mean((x - r)^2 / (r^2 + 0.01)) over pixels and channels",
-            "learned_settings": "environment direction proposed by the network (8 vMF lobes at the emission input), "
-                                "one-sample MIS with the reference's cell sampling at floor 0.3; retrain every 2 "
-                                "passes, 2 Adam steps x 65536 records, lr 4e-3, max log kappa 7; bounces not "
-                                "guided"}
+    photons = WORKLOADS["config2"]["photons"]
+    ctx.render_begin(scene.camera, params_for(P, "compat", "config2", 1, threads))
+    ctx.render_pass(1)
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for t in (2, 3):
+        ctx.render_pass(t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    gpu = 2 * photons / (e0.elapsed_time(e1) / 1e3) / 1e6
+    sec, radii = port_passes(scene, "compat", 3, threads, 1)
+    cpu = 2 * photons / sec / 1e6
+    return {"gpu": gpu, "port": cpu, "unit": UNIT, "gpu_over_port": gpu / cpu, "passes_timed": [2, 3],
+            "port_threads": threads, "num_streams": threads, "radii": radii,
+            "what": "compat mode at the full size (1920x1080, 4M photons, r1 = 0.1 diag, depth 12): the reference's "
+                    "own semantics; GPU device time vs the oracle port on all host cores, same passes"}
 
 
-def run_reference(args):
-    rank, world, local = dist_env()
-    if rank != 0:
-        return 0
-    import port
+def counted_passes(ctx, scene, common, warm, steps):
+    """Traversal and gather counters of passes warm+1..warm+steps (the timed
+    passes) from a separate counting render: canonical passes depend only on
+    their index, so the counting render skips to them."""
     import pppm_gb300 as P
 
-    scene = build_scene()
-    threads = os.cpu_count() or 1
-    scale = 16
-    w, h = 1920 // 4, 1080 // 4
-    photons = PHOTONS // scale
-    cam = P.Context.make_camera(scene.camera)
-    cam.width, cam.height = w, h
-    par = P.Context.make_params(mode=P.MODE_COMPAT, photons=photons, num_streams=threads, max_bounce_photon=DEPTH,
-                                max_bounce_eye=DEPTH)
-    ps = port.PortScene(scene)
-    out = ps.render(cam, par, args.warmup + args.steps)
-    timed = out["stats"][args.warmup:]
-    sec = sum((s["ms_photon"] + s["ms_eye"]) / 1e3 for s in timed)
-    value = photons * args.steps / sec / 1e6
-    sample = (f"each step: 1 pass of {photons} photons at {w}x{h} (1/{scale} of the photons and pixels of the "
-              f"workload), reference semantics (kNN gather, growing radius), {threads} OpenMP threads")
-    # n_gpus: the launch's N (rank 0 alone runs the CPU port)
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": workload_config("compat", 1.0),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-    return 0
+    par = P.Context.make_params(**dict(common, flags=P.FLAG_COUNT_TRAVERSAL))
+    ctx.render_begin(scene.camera, par)
+    if warm:
+        ctx.render_skip(warm)
+    keys = ("photon_rays", "photon_node_visits", "photon_tri_tests", "gather_pairs", "gather_inside",
+            "gather_queries", "eye_rays", "node_visits", "tri_tests")
+    tot = dict.fromkeys(keys, 0)
+    for t in range(warm + 1, warm + steps + 1):
+        st = ctx.render_pass(t)
+        for k in keys:
+            tot[k] += getattr(st, k)
+    return {k: v / steps for k, v in tot.items()}
+
+
+def rooflines(cnt, stats, clocks):
+    """Photon-pass roofline (survey byte model against the measured HBM copy
+    bandwidth, plus the DRAM fraction the ncu capture gives) and the gather's
+    issue-rate roofline (warp instructions per second against the SMs' issue
+    slots)."""
+    peak, peak_kind, sm_max = measured_peak()
+    ms_bounce = statistics.mean(s["ms_bounce"] for s in stats)
+    alg = cnt["photon_rays"] * 48 + cnt["photon_node_visits"] * 128 + cnt["photon_tri_tests"] * 48
+    achieved = alg / (ms_bounce / 1e3) / 1e9
+    traf = profile_json("photon_bounce_traffic.json")
+    traffic = traf.get("dram_bytes_per_pass")
+    photon = {"bound": "latency/divergence", "ceiling": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+              "frac": achieved / peak, "traffic": traffic, "kernel": "kPhotonPersistent (all photon bounces)",
+              "peak_kind": peak_kind, "algorithmic_bytes_per_pass": alg,
+              "model": "survey byte model: 48 B per ray + 128 B per BVH node visited + 48 B per triangle tested "
+                       "(counted live over the timed passes); most of these bytes are L1/L2 hits"}
+    if traffic:
+        photon["dram_achieved"] = traffic / (ms_bounce / 1e3) / 1e9
+        photon["dram_frac"] = photon["dram_achieved"] / peak
+    if "threads_per_inst" in traf:
+        photon["lanes_per_instruction"] = traf["threads_per_inst"]
+        photon["lanes_source"] = "smsp__thread_inst_executed / smsp__inst_executed of the committed capture"
+    gat = profile_json("gather_tiled_issue.json")
+    ms_gather = statistics.mean(s["ms_gather"] for s in stats)
+    mhz = (clocks or {}).get("sm_mhz") or sm_max
+    issue_peak = SMS * SCHEDULERS_PER_SM * mhz * 1e6 / 1e9
+    gather = {"bound": "issue", "kernel": "kGatherTiled (canonical gather, incl. its small set-up launches)",
+              "unit": "G warp-instructions/s", "peak": issue_peak,
+              "peak_model": f"{SMS} SMs x {SCHEDULERS_PER_SM} schedulers x 1 warp instruction per cycle at the "
+                            f"sampled SM clock {mhz:.0f} MHz",
+              "pairs_per_query": cnt["gather_pairs"] / max(cnt["gather_queries"], 1),
+              "inside_per_query": cnt["gather_inside"] / max(cnt["gather_queries"], 1),
+              "pair_tests_per_s": cnt["gather_pairs"] / (ms_gather / 1e3)}
+    if "warp_inst_per_pair" in gat:
+        ach = gat["warp_inst_per_pair"] * cnt["gather_pairs"] / (ms_gather / 1e3) / 1e9
+        gather.update({"achieved": ach, "frac": ach / issue_peak, "warp_inst_per_pair": gat["warp_inst_per_pair"],
+                       "traffic": gat.get("dram_bytes_per_launch")})
+    return photon, gather
 
 
 def run_gb300(args):
@@ -290,17 +322,19 @@ def run_gb300(args):
 
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
+    W = WORKLOADS[args.workload]
+    photons = W["photons"]
+    threads = os.cpu_count() or 1
     scene = build_scene(args.workload)
     ctx = P.Context(local)
     ctx.set_scene(scene)
     compat = args.mode == "compat"
-    common = dict(mode=P.MODE_COMPAT if compat else P.MODE_CANONICAL, photons=PHOTONS, num_streams=16,
-                  max_bounce_photon=DEPTH, max_bounce_eye=DEPTH, radius_scale=0.1 if compat else 1 / 64,
+    common = dict(mode=P.MODE_COMPAT if compat else P.MODE_CANONICAL, photons=photons, num_streams=16,
+                  max_bounce_photon=W["depth"], max_bounce_eye=W["depth"], radius_scale=0.1 if compat else 1 / 64,
                   seed=1 + rank, cell_factor=args.cell_factor)
 
-    # one untimed pass with traversal counting: algorithmic bytes per ray
-    ctx.render_begin(scene.camera, P.Context.make_params(**common, flags=P.FLAG_COUNT_TRAVERSAL))
-    cnt = ctx.render_pass(1)
+    # counters of the timed passes (untimed counting render)
+    cnt = counted_passes(ctx, scene, common, args.warmup, args.steps) if not compat else None
 
     ctx.render_begin(scene.camera, P.Context.make_params(**common))
     t = 1
@@ -326,39 +360,31 @@ def run_gb300(args):
         tt = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         ms = float(tt.item())
-    value = world * args.steps * PHOTONS / (ms / 1e3) / 1e6
+    value = world * args.steps * photons / (ms / 1e3) / 1e6
 
-    # end to end through the C ABI: pass + image readback into pinned memory
+    # end to end through the C ABI on the same passes: a fresh render, the
+    # warm-up passes untimed, then passes W+1..W+K each followed by the read
+    # of the accumulator into pinned host memory (the reference writes an
+    # image after every pass)
     host = torch.empty((scene.camera.height, scene.camera.width, 3), dtype=torch.float32, pin_memory=True)
     hp = host.numpy()
+    ctx.render_begin(scene.camera, P.Context.make_params(**common))
+    for t in range(1, args.warmup + 1):
+        ctx.render_pass(t)
     barrier()
     torch.cuda.synchronize()
     w0 = time.perf_counter()
-    for _ in range(args.steps):
+    for t in range(args.warmup + 1, args.warmup + args.steps + 1):
         ctx.render_pass(t)
-        t += 1
         ctx.render_read(hp)
     e2e_s = time.perf_counter() - w0
     if world > 1:
         tt = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(tt.item())
-    e2e = world * args.steps * PHOTONS / e2e_s / 1e6
+    e2e = world * args.steps * photons / e2e_s / 1e6
     h2d = (16 * 16) if compat else 0  # per-pass stream states (compat only)
     d2h = host.numel() * 4 + 2 * 112  # image + two counter readbacks
-
-    # roofline of the photon bounce kernels (traversal dominated): the
-    # algorithmic bytes of a traversal, 32 B ray + 16 B hit + 128 B per node
-    # visited + 48 B per triangle tested
-    ms_bounce = sum(s["ms_bounce"] for s in stats) / len(stats)
-    alg = cnt.photon_rays * 48 + cnt.photon_node_visits * 128 + cnt.photon_tri_tests * 48
-    peak, peak_kind = measured_peak()
-    achieved = alg / (ms_bounce / 1e3) / 1e9
-    traffic = None
-    tf = ROOT / "profiles" / "photon_bounce_traffic.json"
-    if tf.exists():
-        d = json.loads(tf.read_text())
-        traffic = d.get("dram_bytes_per_pass")
 
     line = None
     if rank == 0:
@@ -371,33 +397,277 @@ def run_gb300(args):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32 (f64 triangle test, exact)", "data": "synthetic (seeded)",
                 "config": cfg,
-                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "passes": [args.warmup + 1, args.warmup + args.steps],
+                        "note": "scene resident (uploaded once by pppm_scene_set / pppm_env_set before the timed "
+                                "region); per-pass upload = pass parameters only (by value); per-pass download = "
+                                "the W x H x 3 FP32 accumulator + pass counters; same pass indices as value"},
                 "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic, "kernel": "kPhotonPersistent (all photon bounces)",
-                             "peak_kind": peak_kind,
-                             "algorithmic_bytes_per_pass": alg},
                 "clocks": clocks,
-                "stage_ms": per,
-                "per_pass": {"photon_rays": cnt.photon_rays, "eye_rays": cnt.eye_rays,
-                             "stored": int(stats[-1]["photons_stored"]), "queries": int(stats[-1]["gather_queries"]),
-                             "node_visits_per_photon_ray": cnt.photon_node_visits / max(cnt.photon_rays, 1),
-                             "tri_tests_per_photon_ray": cnt.photon_tri_tests / max(cnt.photon_rays, 1),
-                             "gather_pairs_per_query": cnt.gather_pairs / max(cnt.gather_queries, 1),
-                             "gather_inside_per_query": cnt.gather_inside / max(cnt.gather_queries, 1),
-                             "sss_points": int(stats[-1]["sss_points"]), "sss_photons": int(stats[-1]["sss_photons"])}}
-        if world == 1 and not args.no_cpu_baseline and args.workload == "config2":
-            line["cpu_baseline"] = cpu_baseline(scene)
-        if world == 1 and not args.no_study and args.workload == "config2" and args.mode == "canonical":
-            line["equal_time_relmse"] = equal_time_study(ctx, scene, common)
+                "stage_ms": per}
+        if cnt is not None:
+            photon_roof, gather_roof = rooflines(cnt, stats, clocks)
+            line["roofline"] = photon_roof
+            line["roofline_gather"] = gather_roof
+            line["per_pass"] = {"photon_rays": cnt["photon_rays"], "eye_rays": cnt["eye_rays"],
+                                "stored": int(stats[-1]["photons_stored"]),
+                                "queries": int(stats[-1]["gather_queries"]),
+                                "node_visits_per_photon_ray": cnt["photon_node_visits"] / max(cnt["photon_rays"], 1),
+                                "tri_tests_per_photon_ray": cnt["photon_tri_tests"] / max(cnt["photon_rays"], 1),
+                                "mrays_per_s": (cnt["photon_rays"] + cnt["eye_rays"]) / (ms / args.steps / 1e3) / 1e6,
+                                "counters": "means over the timed passes (separate counting render)"}
+        full = world == 1 and args.workload == "config2" and not compat
+        if full and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(scene, threads)
+            line["passes_per_s"] = {"gpu": 1e3 / (ms / args.steps),
+                                    "cpu_port_all_cores": line["cpu_baseline"]["value"] / (photons / 1e6),
+                                    "what": "passes per second at the full workload; the target is >= 50x"}
+            line["passes_per_s"]["gpu_over_cpu"] = line["passes_per_s"]["gpu"] / line["passes_per_s"]["cpu_port_all_cores"]
+        if full and not args.no_extra:
+            line["e2e_cold"] = e2e_cold(ctx, scene, common, args.steps)
+            line["compat_full_size"] = compat_full_size(ctx, scene, threads)
+        if full and not args.no_study:
+            line["equal_time_relmse"] = equal_time_study(ctx, scene, common, seeds=args.study_seeds)
+        ctx.close()
+        if full and not args.no_extra:
+            line["config3"] = config3_line(local, args)
+            line["config4"] = run_batch(args, as_extra=True)
         print(json.dumps(line), flush=True)
-    ctx.close()
+    else:
+        ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
 
 
-def run_batch(args):
+def e2e_cold(ctx, scene, common, steps):
+    """The reference's render() call as a user makes it, from host buffers:
+    scene and env upload, BVH build, env tables, render set-up, `steps`
+    passes and the accumulator read, all inside the wall-clock region."""
+    import torch
+
+    import pppm_gb300 as P
+
+    host = torch.empty((scene.camera.height, scene.camera.width, 3), dtype=torch.float32, pin_memory=True)
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    ctx.set_scene(scene)
+    ctx.render_begin(scene.camera, P.Context.make_params(**common))
+    for t in range(1, steps + 1):
+        ctx.render_pass(t)
+    ctx.render_read(host.numpy())
+    sec = time.perf_counter() - w0
+    h2d = scene.tris.nbytes + scene.mat_id.nbytes + scene.mats.nbytes + scene.env.nbytes
+    return {"value": steps * common["photons"] / sec / 1e6, "unit": UNIT, "seconds": sec, "passes": [1, steps],
+            "h2d_bytes": int(h2d), "d2h_bytes": int(host.numel() * 4),
+            "what": "one pppm_scene_set + pppm_env_set (upload, host BVH build, env tables) + render_begin + "
+                    f"{steps} passes + one accumulator read, wall clock"}
+
+
+def config3_line(local, args):
+    """The subsurface workload (config 3): device time per pass."""
+    import torch
+
+    import pppm_gb300 as P
+
+    sc = build_scene("config3")
+    ctx = P.Context(local)
+    try:
+        ctx.set_scene(sc)
+        par = P.Context.make_params(mode=P.MODE_CANONICAL, photons=sc.photons, max_bounce_photon=12,
+                                    max_bounce_eye=12, radius_scale=1 / 64, seed=1)
+        ctx.render_begin(sc.camera, par)
+        warm, steps = 2, 8
+        for t in range(1, warm + 1):
+            ctx.render_pass(t)
+        stream = torch.cuda.ExternalStream(ctx.stream_ptr())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        stats = [ctx.render_pass(t).as_dict() for t in range(warm + 1, warm + steps + 1)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+    finally:
+        ctx.close()
+    keys = ("ms_subsurface", "ms_photon", "ms_eye", "ms_gather", "ms_grid")
+    return {"value": sc.photons / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_pass": ms, "passes": [warm + 1, warm + steps],
+            "config": workload_config("canonical", 1.0, "config3"),
+            "sss_points": int(stats[-1]["sss_points"]), "sss_photons": int(stats[-1]["sss_photons"]),
+            "stage_ms": {k: statistics.mean(s[k] for s in stats) for k in keys},
+            "note": "irradiance points follow the reference's areaRadius rule (ppm_probabilistic.cc:35-46)"}
+
+
+def run_reference(args):
+    """The CPU restatement (oracle port) of the identical workload and
+    configuration on all host cores: passes W+1..W+K timed, as the GPU arm."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    scene = build_scene()
+    sec, _ = port_passes(scene, args.mode, args.warmup + args.steps, threads, args.warmup)
+    photons = WORKLOADS["config2"]["photons"]
+    value = photons * args.steps / sec / 1e6
+    sample = (f"passes {args.warmup + 1}-{args.warmup + args.steps} of the full workload (warm-up passes untimed), "
+              f"{args.mode} mode, oracle port on {threads} OpenMP threads; per pass: photon trace + photon map "
+              f"build + eye paths and gather")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": workload_config(args.mode, args.cell_factor),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- learned vs plain
+def _stays_below(curve, target):
+    """Earliest checkpoint after which the curve never rises above target."""
+    at = None
+    for c in curve:
+        if c["relmse"] <= target:
+            if at is None:
+                at = c
+        else:
+            at = None
+    return at
+
+
+def _first_below(curve, target):
+    return next((c for c in curve if c["relmse"] <= target), None)
+
+
+def equal_time_study(ctx, scene, common, seeds=3, ref_passes=4096, budget_passes=64):
+    """relMSE of several samplers against a ref_passes plain render
+    (relMSE = mean over pixels and channels of (x - r)^2 / (r^2 + 0.01)),
+    at equal wall time. For each seed the plain render's budget_passes
+    passes set the time budget and the target (its final relMSE); every arm
+    runs whole passes until the budget is spent. One rule on every curve:
+    the time to the target is the earliest checkpoint after which the curve
+    stays at or below it (the first checkpoint at or below it is reported
+    too). Checkpoint reads are not counted in the wall times."""
+    import torch
+
+    import pppm_gb300 as P
+
+    checkpoints = set(range(2, 65, 2)) | {80, 96, 128}
+    H, Wd = scene.camera.height, scene.camera.width
+    img = torch.empty((H, Wd, 3), dtype=torch.float32, device="cuda")
+    ref = None
+
+    def read():
+        ctx.render_read(img)
+        ctx.sync()
+        return img
+
+    def rel(x, t):
+        y = x / t
+        return float(((y - ref) ** 2 / (ref ** 2 + 1e-2)).mean().item())
+
+    def render(flags, seed, passes=None, budget=None, curve=None):
+        ctx.render_begin(scene.camera, P.Context.make_params(**dict(common, seed=seed, flags=flags)))
+        el, t, train = 0.0, 0, 0.0
+        while True:
+            t += 1
+            t0 = time.perf_counter()
+            st = ctx.render_pass(t)
+            el += time.perf_counter() - t0
+            train += st.ms_train
+            done = (passes is not None and t >= passes) or (budget is not None and el >= budget)
+            if curve is not None and (t in checkpoints or done):
+                curve.append({"passes": t, "seconds": round(el, 4), "relmse": rel(read(), t)})
+            if done:
+                break
+        return t, el, train
+
+    render(0, 1000, passes=ref_passes)
+    ref = read().clone() / ref_passes
+    arms = {
+        "luminance": dict(exponent=1.0, learned=None),
+        "learned_config5": dict(exponent=2.0, learned=dict(retrain_every=4, steps=8, batch=65536, lr=1e-3,
+                                                             floor_bsdf=0.3, max_log_kappa=7.0, guide_bounces=0)),
+        "learned_tuned": dict(exponent=2.0, learned=dict(retrain_every=2, steps=2, batch=65536, lr=4e-3,
+                                                           floor_bsdf=0.3, max_log_kappa=7.0, guide_bounces=0)),
+        "learned_tuned_guided_bounces": dict(exponent=2.0, learned=dict(retrain_every=2, steps=2, batch=65536,
+                                                                          lr=4e-3, floor_bsdf=0.3, max_log_kappa=7.0,
+                                                                          guide_bounces=1)),
+        "learned_tuned_over_luminance": dict(exponent=1.0, learned=dict(retrain_every=2, steps=2, batch=65536,
+                                                                          lr=4e-3, floor_bsdf=0.3,
+                                                                          max_log_kappa=7.0, guide_bounces=0)),
+    }
+    per_seed = []
+    for s in range(seeds):
+        seed = 7 + s
+        cp = []
+        ctx.env_importance(2.0)
+        n_plain, budget, _ = render(0, seed, passes=budget_passes, curve=cp)
+        target = cp[-1]["relmse"]
+        row = {"seed": seed, "budget_s": budget, "target_relmse": target,
+               "plain": {"passes": n_plain, "relmse": target, "curve": cp,
+                         "stays_below_s": _stays_below(cp, target)["seconds"],
+                         "first_below_s": _first_below(cp, target)["seconds"]}}
+        for name, arm in arms.items():
+            ctx.env_importance(arm["exponent"])
+            flags = 0
+            if arm["learned"]:
+                ctx.learned_config(**arm["learned"])
+                flags = P.FLAG_LEARNED
+            cv = []
+            n, el, train = render(flags, seed, budget=budget, curve=cv)
+            sb, fb = _stays_below(cv, target), _first_below(cv, target)
+            row[name] = {"passes": n, "seconds": el, "train_ms": train, "relmse": cv[-1]["relmse"], "curve": cv,
+                         "stays_below_s": sb["seconds"] if sb else None,
+                         "first_below_s": fb["seconds"] if fb else None}
+        ctx.env_importance(2.0)
+        per_seed.append(row)
+
+    def ratio(num, den, key):
+        vals = [r[num][key] / r[den][key] for r in per_seed if r[num][key] and r[den][key]]
+        return {"mean": statistics.mean(vals) if vals else None, "per_seed": vals,
+                "seeds_reaching": len(vals)}
+
+    def rel_ratio(a, b):
+        vals = [r[a]["relmse"] / r[b]["relmse"] for r in per_seed]
+        return {"mean": statistics.mean(vals), "per_seed": vals}
+
+    summary = {}
+    for name in ["luminance", *[a for a in arms if a != "luminance"]]:
+        summary[name] = {"time_ratio_plain_over_arm": ratio("plain", name, "stays_below_s"),
+                         "time_ratio_plain_over_arm_first_below": ratio("plain", name, "first_below_s"),
+                         "relmse_arm_over_plain_at_equal_time": rel_ratio(name, "plain")}
+    summary["learned_config5_vs_luminance"] = {
+        "time_ratio_luminance_over_learned": ratio("luminance", "learned_config5", "stays_below_s"),
+        "relmse_learned_over_luminance_at_equal_time": rel_ratio("learned_config5", "luminance")}
+    summary["learned_tuned_vs_luminance"] = {
+        "time_ratio_luminance_over_learned": ratio("luminance", "learned_tuned", "stays_below_s"),
+        "relmse_learned_over_luminance_at_equal_time": rel_ratio("learned_tuned", "luminance")}
+    head = summary["learned_config5"]["time_ratio_plain_over_arm"]["mean"]
+    return {"reference_passes": ref_passes, "budget_passes_plain": budget_passes, "seeds": [r["seed"] for r in per_seed],
+            "time_ratio_plain_over_learned": head,
+            "headline": "learned_config5 (retrain every 4 passes, 8 Adam steps x 65,536 records, lr 1e-3, MIS floor "
+                        "0.3): mean over seeds of plain's time to its own final relMSE over the learned arm's, "
+                        "both by the stays-below rule",
+            "rule": "time to target = earliest checkpoint after which the curve stays <= target (the plain "
+                    "render's relMSE after 64 passes, per seed); first_below = first checkpoint <= target",
+            "relmse": "mean((x - r)^2 / (r^2 + 0.01)) over pixels and channels",
+            "arms": {"plain": "the reference's environment sampling (cell pdf ~ luminance^2)",
+                     "luminance": "plain with the cell pdf ~ luminance (pppm_env_importance(1)), no network",
+                     "learned_config5": "network proposes the environment direction (8 vMF lobes at the emission "
+                                        "input), one-sample MIS with the reference's cell draw at floor 0.3; "
+                                        "retrain every 4 passes, 8 steps, lr 1e-3",
+                     "learned_tuned": "same, retrain every 2 passes, 2 steps, lr 4e-3",
+                     "learned_tuned_guided_bounces": "learned_tuned + the network evaluated per photon at its "
+                                                     "Lambertian hit position and normal, proposing the bounce "
+                                                     "direction (MIS with the cosine lobe at floor 0.3)",
+                     "learned_tuned_over_luminance": "learned_tuned with the luminance cell pdf as the MIS "
+                                                     "defensive component"},
+            "summary": summary, "per_seed": per_seed}
+
+
+# ---------------------------------------------------------------- config 4
+def run_batch(args, as_extra=False):
     """Batched uneven jobs: aggregate Mrays/s over the whole batch and per-job
     pass latency p50/p99 (wall time of each pppm_render_pass)."""
     import pppm_gb300 as P
@@ -406,7 +676,7 @@ def run_batch(args):
     rank, world, local = dist_env()
     if rank != 0:
         return 0
-    jobs = S.config4_jobs(seed=4 + args.warmup)
+    jobs = S.config4_jobs(seed=4 + (3 if as_extra else args.warmup))
     b = P.Batch(local)
     b.config(use_graph=not args.no_graph, graph_lanes=args.graph_lanes)
     ids = []
@@ -436,13 +706,102 @@ def run_batch(args):
                       "graph_instantiate_s": stats[0]["batch_graph_instantiate_ms"] / 1e3,
                       "autotuned_shapes": shapes},
             "clocks": clk.summary()}
-    print(json.dumps(line), flush=True)
     b.close()
+    if as_extra:
+        return line
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- profiling cases
+def run_case(args):
+    """Small, seeded cases for kernel profiling (ncu) and timing: each builds
+    its inputs, runs the kernels a few times and prints one line of timings.
+    Inputs exceed the 129 MB L2 where the kernel streams memory and stay far
+    below the device capacity, so a capture of one or two launches ends
+    within seconds."""
+    import torch
+
+    import pppm_gb300 as P
+    import scenes as S
+
+    ctx = P.Context(0)
+    out = {"case": args.case}
+    if args.case == "mlp_forward":
+        rows = args.rows
+        rng = np.random.default_rng(0)
+        pos = torch.tensor(rng.uniform(-30, 30, (rows, 3)).astype(np.float32), device="cuda")
+        nrm = torch.nn.functional.normalize(torch.tensor(rng.normal(size=(rows, 3)).astype(np.float32), device="cuda"))
+        res = torch.empty((rows, 40), device="cuda")
+        params = torch.tensor(rng.normal(size=P.MLP_PARAMS).astype(np.float32) * 0.1, device="cuda")
+        bb = np.array([-50.0, -50.0, -50.0, 50.0, 50.0, 50.0])
+
+        def call():
+            return ctx.lib.pppm_mlp_forward(ctx.h, params.data_ptr(), pos.data_ptr(), nrm.data_ptr(), rows,
+                                            bb.ctypes.data, res.data_ptr())
+        for _ in range(3):
+            assert call() == P.OK
+        stream = torch.cuda.ExternalStream(ctx.stream_ptr())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(10):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 10
+        out.update(rows=rows, ms_per_call=ms, tflops=rows * 31.7e3 / (ms / 1e3) / 1e12)
+    elif args.case == "mlp_train":
+        rng = np.random.default_rng(1)
+        n = args.records
+        pos = rng.uniform(-30, 30, (n, 3))
+        nr = rng.normal(size=(n, 3))
+        nr /= np.linalg.norm(nr, axis=1, keepdims=True)
+        d = rng.normal(size=(n, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        w = rng.lognormal(size=(n, 1))
+        rec = np.concatenate([pos, nr, d, w], 1).astype(np.float32)
+        params = rng.normal(size=P.MLP_PARAMS).astype(np.float32) * 0.1
+        bb = np.array([-50.0, -50.0, -50.0, 50.0, 50.0, 50.0])
+        for _ in range(2):
+            ctx.mlp_grad(params, rec, bb)
+        t0 = time.perf_counter()
+        for _ in range(5):
+            loss, _g = ctx.mlp_grad(params, rec, bb)
+        out.update(records=n, ms_per_step_incl_host=(time.perf_counter() - t0) / 5 * 1e3, loss=loss)
+    elif args.case in ("render", "subsurface", "classic"):
+        if args.case == "render":
+            sc = S.config2(width=args.width, height=args.height)
+            par = dict(mode=P.MODE_CANONICAL, photons=args.photons, max_bounce_photon=12, max_bounce_eye=12,
+                       radius_scale=1 / 64, seed=1)
+        elif args.case == "subsurface":
+            sc = S.config3() if args.full else S.config3(width=640, height=360, photons=1_000_000, nu=250, nv=100)
+            par = dict(mode=P.MODE_CANONICAL, photons=sc.photons, max_bounce_photon=12, max_bounce_eye=12,
+                       radius_scale=1 / 64, seed=1)
+        else:
+            sc = S.config2(width=args.width, height=args.height, freq=96)
+            par = dict(mode=P.MODE_CLASSIC, photons=args.photons, num_streams=16, max_bounce_photon=12,
+                       max_bounce_eye=12)
+        ctx.set_scene(sc)
+        if args.count and args.case == "render":
+            ctx.render_begin(sc.camera, P.Context.make_params(**par, flags=P.FLAG_COUNT_TRAVERSAL))
+            out["counted"] = [{k: getattr(ctx.render_pass(t + 1), k) for k in
+                               ("photon_rays", "photon_node_visits", "photon_tri_tests", "gather_pairs",
+                                "gather_inside", "gather_queries")} for t in range(args.passes)]
+        ctx.render_begin(sc.camera, P.Context.make_params(**par))
+        res = [ctx.render_pass(t + 1).as_dict() for t in range(args.passes)]
+        keys = ("ms_subsurface", "ms_photon", "ms_bounce", "ms_grid", "ms_eye", "ms_gather", "photon_rays",
+                "eye_rays", "photons_stored", "sss_points")
+        out.update({k: res[-1][k] for k in keys}, photons=par["photons"], w=sc.camera.width, h=sc.camera.height)
+    ctx.close()
+    print(json.dumps(out), flush=True)
     return 0
 
 
 def main():
     args = parse()
+    if args.case:
+        return run_case(args)
     if args.workload == "config4" and args.impl == "gb300":
         return run_batch(args)
     if args.impl == "reference":

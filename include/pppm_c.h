@@ -172,6 +172,17 @@ int pppm_env_set(pppm_ctx* ctx, const float* rgb, int32_t w, int32_t h);
 /* Envmap importance tables (envmap.cc:88-163), 4096 doubles each. */
 int pppm_env_tables(pppm_ctx* ctx, double* pdf, double* cdf);
 
+/* Rebuilds the environment's 64x64 cell tables with cell weight
+ * luminance^exponent (0 <= exponent <= 8) in place of the reference's
+ * luminance^2 (envmap.cc:128-153; exponent 2 restores the reference's tables
+ * bit for bit). Photon fluxes follow the new pdf (area / (pdf * P)), so every
+ * exponent renders the same expectation; exponent 1 is the plain non-learned
+ * alternative to the reference's heuristic on skies with a small bright sun.
+ * Applies to passes rendered after the call; pppm_env_set restores 2; not
+ * part of a checkpoint. No counterpart in the reference (its exponent is
+ * fixed). */
+int pppm_env_importance(pppm_ctx* ctx, double exponent);
+
 /* Replaces Envmap::sampleFromDir (envmap.cc:47-60): nearest-texel radiance
  * for n unit directions (3 floats each, any memory) into rgb (n x 3). */
 int pppm_env_lookup(pppm_ctx* ctx, const float* dirs, int64_t n, float* rgb);
@@ -338,13 +349,15 @@ int pppm_halton(pppm_ctx* ctx, uint32_t seed, int32_t count, int32_t n, double* 
  * all device memory under a fixed budget, frame loops that must not stall on
  * cudaMalloc, or code that must not create a pppm context. It needs no
  * context and calls no cudaMalloc/cudaFree or allocating library routine.
- * Every array must already be device (or managed) memory; work runs on
- * `stream` (a cudaStream_t, NULL = the default stream) and the call waits
- * for it before returning. Scratch lives in one fixed device array of about
- * 6.6 MB that every GPU loading the library holds until exit; n above
- * PPPM_NOALLOC_MAX_PHOTONS returns PPPM_E_CAPACITY. The first call on a
- * device looks up that array's address (issue it before any stream
- * capture). Calls share the array, so calls that overlap on the GPU race.
+ * Every array must already be device memory of the current device (or
+ * managed memory); host memory and another GPU's memory return PPPM_E_ARG.
+ * Work runs on `stream` (a cudaStream_t, NULL = the default stream) and the
+ * call waits for it before returning. Scratch lives in one fixed device
+ * array of about 6.6 MB that every GPU loading the library holds until exit;
+ * n above PPPM_NOALLOC_MAX_PHOTONS returns PPPM_E_CAPACITY. The first call
+ * on a device looks up that array's address (issue it before any stream
+ * capture); resetting that device (cudaDeviceReset) afterwards is not
+ * supported. Calls share the array, so calls that overlap on the GPU race.
  * No counterpart in the reference. */
 #define PPPM_NOALLOC_MAX_PHOTONS (1 << 17)
 int pppm_knn_noalloc(const float* photon_pos, int64_t n, const float* queries, int64_t m, int32_t num_target_photons,

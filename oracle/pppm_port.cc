@@ -462,6 +462,30 @@ public:
         for (size_t i = 0; i < pts.size(); i++) v[i] = &pts[i];
         if (!pts.empty()) rec(v, 0, 0, (int)pts.size(), 0);
     }
+    // Canonical gather: the flux of every photon strictly inside the ball of
+    // radius r around q whose stored normal faces `on`. Same tree and the
+    // same pruning as knnRec (a subtree is visited when |delta| <= r), but
+    // the fluxes are summed in visiting order with no heap: the reference
+    // has no ball-only gather, and a heap of ~10^3 photons per query would
+    // make the CPU timing a measure of std::priority_queue.
+    V ballSum(V q, double r, V on) const {
+        V tot;
+        if (nodes_.empty()) return tot;
+        const Node* stack[64];
+        int sp = 0;
+        stack[sp++] = &nodes_[0];
+        while (sp > 0) {
+            const Node* nd = stack[--sp];
+            const V diff = nd->pt.p - q;
+            if (norm(diff) < r && dot(nd->pt.n, on) > 0.0) tot = tot + nd->pt.flux;
+            const double delta = q[nd->axis] - nd->pt.p[nd->axis];
+            const Node* nearC = delta < 0.0 ? nd->l : nd->r;
+            const Node* farC = delta < 0.0 ? nd->r : nd->l;
+            if (farC && std::abs(delta) <= r) stack[sp++] = farC;
+            if (nearC) stack[sp++] = nearC;
+        }
+        return tot;
+    }
     // knn: K_NEAREST | EPSILON_BALL with (epsilon, k); else EPSILON_BALL only.
     // Results farthest first (the max-heap's pop order).
     void query(V q, bool knn, int k, double eps, std::vector<const Photon*>* out) const {
@@ -566,11 +590,7 @@ struct Renderer {
     }
 
     V gatherCanonical(V q, V on, V refl, double roulette) const {
-        std::vector<const Photon*> ph;
-        kd.query(q, false, 0, radius, &ph);
-        V tot;
-        for (const Photon* p : ph)
-            if (dot(p->n, on) > 0.0) tot = tot + p->flux;
+        const V tot = kd.ballSum(q, radius, on);
         return refl * tot * kInvPi / (kPi * radius * radius * roulette);
     }
 
@@ -835,11 +855,7 @@ void port_gather_canonical(const double* ph9, int64_t n, const double* q12, int6
 #pragma omp parallel for schedule(dynamic, 64)
     for (int64_t j = 0; j < m; j++) {
         const double* q = q12 + 12 * j;
-        std::vector<const Photon*> res;
-        kd.query(V(q[0], q[1], q[2]), false, 0, radius, &res);
-        V tot;
-        for (const Photon* p : res)
-            if (dot(p->n, V(q[3], q[4], q[5])) > 0.0) tot = tot + p->flux;
+        const V tot = kd.ballSum(V(q[0], q[1], q[2]), radius, V(q[3], q[4], q[5]));
         const V L = V(q[6], q[7], q[8]) * V(q[9], q[10], q[11]) * tot * kInvPi / (kPi * radius * radius);
         out[3 * j] = L.x;
         out[3 * j + 1] = L.y;

@@ -275,6 +275,8 @@ int pppm_scene_set(pppm_ctx* c, const float* tri, int64_t ntri, const int32_t* m
     return PPPM_OK;
 }
 
+static int uploadEnvTables(pppm_ctx* c);
+
 int pppm_env_set(pppm_ctx* c, const float* rgb, int32_t w, int32_t h) {
     if (!c || !rgb || w <= 0 || h <= 0) return fail(c, PPPM_E_ARG, "env_set: bad arguments");
     // The 64x64 importance map divides by the texel area of each cell
@@ -287,6 +289,33 @@ int pppm_env_set(pppm_ctx* c, const float* rgb, int32_t w, int32_t h) {
     const size_t bytes = (size_t)w * h * 3 * sizeof(float);
     PPPM_CUDA(c, c->envRgb.ensure(bytes));
     PPPM_CUDA(c, cudaMemcpy(c->envRgb.p, rgb, bytes, cudaMemcpyHostToDevice));
+    c->envW = w;
+    c->envH = h;
+    const int r = uploadEnvTables(c);
+    if (r != PPPM_OK) return r;
+    c->hasEnv = true;
+    c->envExponent = 2.0;
+    return PPPM_OK;
+}
+
+int pppm_env_importance(pppm_ctx* c, double exponent) {
+    if (!c || !(exponent >= 0.0 && exponent <= 8.0)) return fail(c, PPPM_E_ARG, "env_importance: bad exponent");
+    if (!c->hasEnv) return fail(c, PPPM_E_STATE, "env_importance: no env map");
+    if (exponent == c->envExponent) return PPPM_OK;
+    cudaSetDevice(c->device);
+    std::vector<float> rgb((size_t)c->envW * c->envH * 3);
+    PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    PPPM_CUDA(c, cudaMemcpy(rgb.data(), c->envRgb.p, rgb.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    envImportance(rgb.data(), c->envW, c->envH, &c->envPdf, &c->envCdf, exponent);
+    const int r = uploadEnvTables(c);
+    if (r != PPPM_OK) return r;
+    c->envExponent = exponent;
+    return PPPM_OK;
+}
+
+// Device copies of the importance tables in c->envPdf / c->envCdf: pdf, cdf,
+// the integer cdf of the draw comparison, and a fresh flux-scale table.
+static int uploadEnvTables(pppm_ctx* c) {
     PPPM_CUDA(c, c->envPdfD.ensure(4096 * sizeof(double)));
     PPPM_CUDA(c, c->envCdfD.ensure(4096 * sizeof(double)));
     PPPM_CUDA(c, cudaMemcpy(c->envPdfD.p, c->envPdf.data(), 4096 * sizeof(double), cudaMemcpyHostToDevice));
@@ -300,9 +329,6 @@ int pppm_env_set(pppm_ctx* c, const float* rgb, int32_t w, int32_t h) {
     }
     PPPM_CUDA(c, c->envScaleD.ensure(4096 * 4));
     c->envScaleFor = -1.0;
-    c->envW = w;
-    c->envH = h;
-    c->hasEnv = true;
     return PPPM_OK;
 }
 

@@ -247,6 +247,7 @@ struct pppm_ctx {
     std::vector<double> envPdf, envCdf;
     pppm::DBuf envRgb, envPdfD, envCdfD, envUcdfD, envScaleD;
     double envScaleFor = -1.0;  // numPhotons the flux-scale table was built for
+    double envExponent = 2.0;   // cell weight = luminance^envExponent (2: the reference)
     // staging for host arguments
     pppm::DBuf stage[8];
     std::vector<void*> pinned;

@@ -172,7 +172,8 @@ void lookup(const float* rgb, int w, int h, double dx, double dy, double dz, dou
 }
 }  // namespace
 
-void envImportance(const float* rgb, int w, int h, std::vector<double>* pdf, std::vector<double>* cdf) {
+void envImportance(const float* rgb, int w, int h, std::vector<double>* pdf, std::vector<double>* cdf,
+                   double exponent) {
     const int W = 64, H = 64;
     pdf->assign(W * H, 0.0);
     cdf->assign(W * H, 0.0);
@@ -197,8 +198,9 @@ void envImportance(const float* rgb, int w, int h, std::vector<double>* pdf, std
                 }
             }
             const double l = acc[0] * 0.2126 + acc[1] * 0.7152 + acc[2] * 0.0722;
-            (*pdf)[iy * W + ix] = l * l;
-            total += l * l;
+            const double wgt = exponent == 2.0 ? l * l : std::pow(l, exponent);
+            (*pdf)[iy * W + ix] = wgt;
+            total += wgt;
         }
     }
     const double eps = 1.0e-12;

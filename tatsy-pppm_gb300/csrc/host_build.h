@@ -27,7 +27,11 @@ struct HostBvh {
 bool buildQbvh(const float* tri9, int64_t ntri, HostBvh* out, std::string* err);
 
 // Envmap::createImportanceMap (envmap.cc:88-163): pdf and cdf, 4096 each.
-void envImportance(const float* rgb, int w, int h, std::vector<double>* pdf, std::vector<double>* cdf);
+// Envmap::createImportanceMap (envmap.cc:88-163): 64x64 cell pdf/cdf over
+// super-sampled directions, cell weight luminance^exponent (2 in the
+// reference: l * l).
+void envImportance(const float* rgb, int w, int h, std::vector<double>* pdf, std::vector<double>* cdf,
+                   double exponent = 2.0);
 
 // Image::loadHdr (image.cc:296-434) on an in-memory file. Returns 0 or a
 // negative code; with rgb == nullptr only reports the size.

@@ -1,7 +1,6 @@
-// Radiance gathers over the photon hash grid.
+// The compat radiance gather over the photon hash grid (the canonical
+// gather is k_gather_tiled.cu).
 //
-// Canonical: every photon within the global radius r whose oriented normal
-// faces the query's oriented normal contributes refl/pi * flux / (pi r^2).
 // Compat: the reference's k-nearest search (k = (int)radius, epsilon =
 // gatherPhotons, kdtree_detail.h:90-132), its disc filter and its cone filter
 // with the flux/distance index mismatch (ppm_probabilistic.cc:300-335).
@@ -18,58 +17,6 @@ unsigned blocksFor(int64_t n, int bs) {
 
 __device__ __forceinline__ int64_t queryCount(const QueryView& qv) {
     return qv.count ? min((int64_t)*qv.count, qv.n) : qv.n;
-}
-
-template <bool kAccum>
-__global__ void __launch_bounds__(256) kGatherCanonical(GridDev g, QueryView qv, float r, float* __restrict__ out) {
-    const int64_t n = queryCount(qv);
-    const float r2 = r * r;
-    const float norm = 1.0f / (kPiF * kPiF * r2);
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float4 q0 = qv.q[3 * i], q1 = qv.q[3 * i + 1], q2 = qv.q[3 * i + 2];
-        const int lx = cellCoord(q0.x - r, g.ox, g.invCell, g.nx), hx = cellCoord(q0.x + r, g.ox, g.invCell, g.nx);
-        const int ly = cellCoord(q0.y - r, g.oy, g.invCell, g.ny), hy = cellCoord(q0.y + r, g.oy, g.invCell, g.ny);
-        const int lz = cellCoord(q0.z - r, g.oz, g.invCell, g.nz), hz = cellCoord(q0.z + r, g.oz, g.invCell, g.nz);
-        uint32_t keys[27];
-        int nk = 0;
-        for (int cz = lz; cz <= hz && cz <= lz + 2; cz++)
-            for (int cy = ly; cy <= hy && cy <= ly + 2; cy++)
-                for (int cx = lx; cx <= hx && cx <= lx + 2; cx++) {
-                    const uint32_t k = bucketOf(cx, cy, cz, g.mask);
-                    bool dup = false;
-                    for (int t = 0; t < nk; t++) dup |= keys[t] == k;
-                    if (!dup) keys[nk++] = k;
-                }
-        float sx = 0.f, sy = 0.f, sz = 0.f;
-        for (int t = 0; t < nk; t++) {
-            const uint32_t b0 = __ldg(&g.start[keys[t]]), b1 = __ldg(&g.start[keys[t] + 1]);
-            for (uint32_t j = b0; j < b1; j++) {
-                const float4 a = __ldg(&g.rec[2 * (int64_t)j]);
-                const float dx = a.x - q0.x, dy = a.y - q0.y, dz = a.z - q0.z;
-                const float d2 = dx * dx + dy * dy + dz * dz;
-                if (d2 < r2) {
-                    const f3 np = unpackNormal(__float_as_uint(a.w));
-                    if (np.x * q1.x + np.y * q1.y + np.z * q1.z > 0.0f) {
-                        const float4 b = __ldg(&g.rec[2 * (int64_t)j + 1]);
-                        sx += b.x;
-                        sy += b.y;
-                        sz += b.z;
-                    }
-                }
-            }
-        }
-        const float lx_ = q2.x * sx * norm, ly_ = q2.y * sy * norm, lz_ = q2.z * sz * norm;
-        if (kAccum) {
-            const int64_t px = __float_as_int(q0.w);
-            out[3 * px] += lx_;
-            out[3 * px + 1] += ly_;
-            out[3 * px + 2] += lz_;
-        } else {
-            out[3 * i] = lx_;
-            out[3 * i + 1] = ly_;
-            out[3 * i + 2] = lz_;
-        }
-    }
 }
 
 // Sorted (ascending) candidate list of the k nearest photons.
@@ -272,14 +219,6 @@ __global__ void kPackQueries(const float* __restrict__ in, int64_t m, float4* __
 __global__ void kSetCount(uint64_t* c, int64_t n) { *c = (uint64_t)n; }
 
 }  // namespace
-
-cudaError_t launchGatherCanonical(const GridDev& g, QueryView q, float radius, float* out, bool accumulate,
-                                  cudaStream_t st) {
-    const int bs = 256;
-    if (accumulate) kGatherCanonical<true><<<blocksFor(q.n, bs), bs, 0, st>>>(g, q, radius, out);
-    else kGatherCanonical<false><<<blocksFor(q.n, bs), bs, 0, st>>>(g, q, radius, out);
-    return cudaGetLastError();
-}
 
 cudaError_t launchGatherCompat(const GridDev& g, QueryView q, int k, float eps, float rlim, int64_t phantoms,
                                float* out, bool accumulate, cudaStream_t st) {

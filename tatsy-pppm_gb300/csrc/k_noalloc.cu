@@ -10,6 +10,7 @@
 #include <mutex>
 
 #include "kernels.h"
+#include "noalloc_check.h"
 
 namespace pppm {
 
@@ -133,19 +134,41 @@ unsigned naBlocks(int64_t n) {
 
 // Device address of gScratch per device ordinal, looked up once per device
 // with that device current. Host code may not use &gScratch as a device
-// address: on the host it names a host-side shadow of the symbol.
+// address: on the host it names a host-side shadow of the symbol. The
+// address belongs to the device's primary context as it was at the first
+// call; a cudaDeviceReset while the library is loaded discards that context
+// and the cached address with it, so resetting a device that has used this
+// entry point is not supported.
 std::mutex gScratchMutex;
 void* gScratchAddr[256] = {nullptr};
+
+static_assert(kNaUnregistered == (int)cudaMemoryTypeUnregistered && kNaHost == (int)cudaMemoryTypeHost &&
+                  kNaDevice == (int)cudaMemoryTypeDevice && kNaManaged == (int)cudaMemoryTypeManaged,
+              "NaMemoryType mirrors cudaMemoryType");
+
+// naPointerUsable on the pointer's attributes (noalloc_check.h).
+bool usableOn(const void* ptr, int device) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return naPointerUsable((int)a.type, a.device, device);
+}
+
+// Clears the pending CUDA error so that it does not surface in the
+// caller's next unrelated cudaGetLastError, and reports the failure.
+int cudaFailure() {
+    cudaGetLastError();
+    return PPPM_E_CUDA;
+}
 
 int scratchFor(int device, unsigned char** out) {
     if (device < 0 || device >= 256) return PPPM_E_ARG;
     std::lock_guard<std::mutex> lock(gScratchMutex);
     if (gScratchAddr[device] == nullptr) {
         void* ptr = nullptr;
-        if (cudaGetSymbolAddress(&ptr, gScratch) != cudaSuccess || ptr == nullptr) {
-            cudaGetLastError();
-            return PPPM_E_CUDA;
-        }
+        if (cudaGetSymbolAddress(&ptr, gScratch) != cudaSuccess || ptr == nullptr) return cudaFailure();
         gScratchAddr[device] = ptr;
     }
     *out = static_cast<unsigned char*>(gScratchAddr[device]);
@@ -168,15 +191,13 @@ extern "C" int pppm_knn_noalloc(const float* photon_pos, int64_t n, const float*
     if (k < 1) return PPPM_E_UNDEFINED;
     if (k > kMaxKnn) return PPPM_E_CAPACITY;
     if (m == 0) return PPPM_OK;
-    // nothing is staged: every array must already be device (or managed) memory
-    if ((n > 0 && !isDevicePtr(photon_pos)) || !isDevicePtr(queries) || !isDevicePtr(cnt) ||
-        (cap > 0 && !isDevicePtr(idx)))
-        return PPPM_E_ARG;
     int device = 0;
-    if (cudaGetDevice(&device) != cudaSuccess) {
-        cudaGetLastError();
-        return PPPM_E_CUDA;
-    }
+    if (cudaGetDevice(&device) != cudaSuccess) return cudaFailure();
+    // nothing is staged: every array must already be memory the current
+    // device reads directly (its own device memory, or managed memory)
+    if ((n > 0 && !usableOn(photon_pos, device)) || !usableOn(queries, device) || !usableOn(cnt, device) ||
+        (cap > 0 && !usableOn(idx, device)))
+        return PPPM_E_ARG;
     unsigned char* s = nullptr;
     const int r = scratchFor(device, &s);
     if (r) return r;
@@ -188,7 +209,7 @@ extern "C" int pppm_knn_noalloc(const float* photon_pos, int64_t n, const float*
     uint32_t* cursor = reinterpret_cast<uint32_t*>(s + NaLayout::cursor);
     uint32_t* tmp = reinterpret_cast<uint32_t*>(s + NaLayout::tmp);
     // the previous call's contents stay in the array: clear what starts at zero
-    if (cudaMemsetAsync(hist, 0, 4 * ((size_t)kNaTable + 1), st) != cudaSuccess) return PPPM_E_CUDA;
+    if (cudaMemsetAsync(hist, 0, 4 * ((size_t)kNaTable + 1), st) != cudaSuccess) return cudaFailure();
     kNaInit<<<1, 1, 0, st>>>(p);
     kNaBbox<<<naBlocks(n), 256, 0, st>>>(photon_pos, n, p);
     kNaParams<<<1, 1, 0, st>>>(p, n, k, sorted, hist);
@@ -196,20 +217,16 @@ extern "C" int pppm_knn_noalloc(const float* photon_pos, int64_t n, const float*
     // the bucket table size depends only on n (as in pppm_knn)
     uint32_t size = 1u << 12;
     while ((int64_t)size < 2 * n && size < kNaTable) size <<= 1;
-    if (exclusiveScan(hist, size, cursor, tmp, st) != cudaSuccess) return PPPM_E_CUDA;
+    if (exclusiveScan(hist, size, cursor, tmp, st) != cudaSuccess) return cudaFailure();
     kNaScatter<<<naBlocks(n), 256, 0, st>>>(photon_pos, n, keys, cursor, sorted);
     // the query kernel takes the grid description by value: read it back
     // into host stack memory (this waits for the stream)
     NaParams hp;
     if (cudaMemcpyAsync(&hp, p, sizeof(hp), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess) {
-        cudaGetLastError();
-        return PPPM_E_CUDA;
-    }
-    if (launchKnn(hp.grid, queries, m, k, (float)num_target_photons, idx, cnt, cap, st) != cudaSuccess) return PPPM_E_CUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) {
-        cudaGetLastError();
-        return PPPM_E_CUDA;
-    }
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return cudaFailure();
+    if (launchKnn(hp.grid, queries, m, k, (float)num_target_photons, idx, cnt, cap, st) != cudaSuccess)
+        return cudaFailure();
+    if (cudaStreamSynchronize(st) != cudaSuccess) return cudaFailure();
     return PPPM_OK;
 }

@@ -25,10 +25,6 @@ GridDev gridGeometry(const double* bbmin, const double* bbmax, double cell);
 cudaError_t gridBuild(GridBufs& g, const GridDev& view, const float4* rec, const uint64_t* dCount, int64_t capacity,
                       cudaStream_t st);
 
-// Canonical radius-ball gather. out: per query (accumulate=false, m x 3)
-// or accum[pixel] += (accumulate=true).
-cudaError_t launchGatherCanonical(const GridDev& g, QueryView q, float radius, float* out, bool accumulate,
-                                  cudaStream_t st);
 // Canonical gather with shared-memory staging of cell neighbourhoods
 // (queries counting-sorted by cell first). work: optional 2 counters.
 cudaError_t querySortLayout(QuerySortBufs& qs, int64_t maxQueries);

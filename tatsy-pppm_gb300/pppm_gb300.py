@@ -92,6 +92,7 @@ SIGNATURES = {
     "pppm_scene_set": ([_VP, _VP, ctypes.c_int64, _VP, _VP, ctypes.c_int32], ctypes.c_int),
     "pppm_env_set": ([_VP, _VP, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
     "pppm_env_tables": ([_VP, _VP, _VP], ctypes.c_int),
+    "pppm_env_importance": ([_VP, ctypes.c_double], ctypes.c_int),
     "pppm_env_lookup": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_emit_photons": ([_VP, _VP, ctypes.c_int64, ctypes.c_int64, _VP, _VP, _VP, _VP], ctypes.c_int),
     "pppm_hdr_decode": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
@@ -243,6 +244,10 @@ class Context:
         cdf = np.zeros(4096)
         self._check(self.lib.pppm_env_tables(self.h, pdf.ctypes.data, cdf.ctypes.data))
         return pdf, cdf
+
+    def env_importance(self, exponent=2.0):
+        """pppm_env_importance: environment cell weight luminance^exponent (2: the reference)."""
+        self._check(self.lib.pppm_env_importance(self.h, float(exponent)))
 
     def env_lookup(self, dirs):
         n = int(dirs.shape[0])

@@ -53,3 +53,34 @@ def test_null_and_bad_arguments_return_status():
     r = lib.pppm_create(-1, ctypes.byref(h))
     assert r == P.E_CUDA and not h.value
 
+
+def test_noalloc_pointer_rule(tmp_path):
+    """pppm_knn_noalloc stages nothing, so it takes only memory its kernels
+    read in place on the current device: that device's own memory or managed
+    memory. Another GPU's memory (an illegal address without peer access),
+    host and unregistered memory are refused. The rule is checked here on
+    the host with the memory types and device ordinals that
+    cudaPointerGetAttributes reports, so no GPU ever sees a foreign pointer."""
+    import shutil
+    import subprocess
+
+    if shutil.which("g++") is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / "rule.cc"
+    src.write_text(
+        '#include "noalloc_check.h"\n#include <cstdio>\nusing namespace pppm;\n'
+        "int main() {\n"
+        "  int bad = 0;\n"
+        "  bad += !naPointerUsable(kNaDevice, 0, 0);\n"
+        "  bad += !naPointerUsable(kNaDevice, 3, 3);\n"
+        "  bad += naPointerUsable(kNaDevice, 1, 0);\n"
+        "  bad += naPointerUsable(kNaDevice, 0, 1);\n"
+        "  bad += !naPointerUsable(kNaManaged, 0, 1);\n"
+        "  bad += !naPointerUsable(kNaManaged, -2, 0);\n"
+        "  bad += naPointerUsable(kNaHost, 0, 0);\n"
+        "  bad += naPointerUsable(kNaUnregistered, 0, 0);\n"
+        '  std::printf("%d\\n", bad);\n  return bad;\n}\n')
+    exe = tmp_path / "rule"
+    subprocess.run(["g++", "-std=c++17", "-I", str(P.HERE / "csrc"), str(src), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
