@@ -785,9 +785,10 @@ def run_case(args):
         ctx.set_scene(sc)
         if args.count and args.case == "render":
             ctx.render_begin(sc.camera, P.Context.make_params(**par, flags=P.FLAG_COUNT_TRAVERSAL))
-            out["counted"] = [{k: getattr(ctx.render_pass(t + 1), k) for k in
-                               ("photon_rays", "photon_node_visits", "photon_tri_tests", "gather_pairs",
-                                "gather_inside", "gather_queries")} for t in range(args.passes)]
+            keys = ("photon_rays", "photon_node_visits", "photon_tri_tests", "gather_pairs", "gather_inside",
+                    "gather_queries")
+            counted = [ctx.render_pass(t + 1) for t in range(args.passes)]
+            out["counted"] = [{k: getattr(st, k) for k in keys} for st in counted]
         ctx.render_begin(sc.camera, P.Context.make_params(**par))
         res = [ctx.render_pass(t + 1).as_dict() for t in range(args.passes)]
         keys = ("ms_subsurface", "ms_photon", "ms_bounce", "ms_grid", "ms_eye", "ms_gather", "photon_rays",

@@ -115,6 +115,9 @@ typedef struct {
                                  reference counterpart */
 #define PPPM_FLAG_LEARNED_FROZEN 0x4 /* with PPPM_FLAG_LEARNED: the same pipeline without training (the
                                         reference's sampling alone): the method without the network */
+#define PPPM_FLAG_SAMPLER_QMC 0x8 /* compat mode: the RANDOM_SAMPLER_QUASI_MONTE_CARLO sampler type of
+                                     ProgressivePhotonMappingProb::render (ppm_probabilistic.cc:58-73):
+                                     stream i is Halton(200, true, i) (halton.cc) instead of XorShift(i) */
 
 /* Per-pass statistics written by pppm_render_pass. */
 typedef struct {
@@ -242,12 +245,41 @@ int pppm_intersect(pppm_ctx* ctx, const float* rays, int64_t n, int32_t* tri, do
 int pppm_hash_points(pppm_ctx* ctx, const float* pts, int64_t n, int32_t hash_size, double scale,
                      const double* bbmin, uint32_t* out);
 
+/* Replaces HashGrid<T>::init(hash_size, scale, bbox) + add(item i, boxmin[i],
+ * boxmax[i]) for i = 0 .. n-1 (hash_grid_detail.h:26-52) and the bucket
+ * vectors operator[] returns: boxes are n x 3 doubles each (host or device),
+ * bbmin the 3 doubles of bbox.posMin(). Cell coordinates are
+ * |(int)((v - bbmin) * scale)| per axis, so boxes reaching below bbmin fold
+ * as in the reference. Output in CSR form: start (hash_size + 1 offsets) and
+ * items (item ids), each bucket in the reference's insertion order (add
+ * order; an item appears once per covered cell that hashes to the bucket).
+ * *count = the number of entries; start and items NULL: count only; items
+ * NULL: offsets only; cap < *count: PPPM_E_CAPACITY. At most 2^24 cells per
+ * box (PPPM_E_CAPACITY) and fewer than 2^32 entries in all. */
+int pppm_hashgrid_build(pppm_ctx* ctx, const double* boxmin, const double* boxmax, int64_t n, int32_t hash_size,
+                        double scale, const double* bbmin, uint32_t* start, int32_t* items, int64_t cap,
+                        int64_t* count);
+
 /* Replaces PhotonMap::findKNN (photon_map.cc:24-26) -> KdTree::knnSearch
  * (kdtree_detail.h:90-132) with the reference's argument order
  * (numTargetPhotons lands in epsilon, targetRadius in k). Results per query
  * in the reference's order (farthest first): idx (m x cap), cnt (m). */
 int pppm_knn(pppm_ctx* ctx, const float* photon_pos, int64_t n, const float* queries, int64_t m,
              int32_t num_target_photons, double target_radius, int32_t* idx, int32_t* cnt, int32_t cap);
+
+/* Replaces KdTree<T>::knnSearch(point, KnnQuery(type, epsilon, k), results)
+ * (kdtree.h:13-24, kdtree_detail.h:88-132) over n points (3 floats each):
+ * type is PPPM_KNN_EPSILON_BALL and/or PPPM_KNN_K_NEAREST as KnnSearchType;
+ * without EPSILON_BALL the ball is unbounded. K_NEAREST: the k nearest
+ * points strictly within epsilon (k <= 64 and <= cap); EPSILON_BALL alone:
+ * every point within epsilon, refused with PPPM_E_CAPACITY when a query has
+ * min(cap, 64) or more. Results per query farthest first (the max-heap's pop
+ * order): idx (m x cap point indices), cnt (m). k < 1 with K_NEAREST returns
+ * PPPM_E_UNDEFINED (the reference reads an empty queue). */
+#define PPPM_KNN_EPSILON_BALL 0x01
+#define PPPM_KNN_K_NEAREST 0x02
+int pppm_kdtree_knn(pppm_ctx* ctx, const float* points, int64_t n, const float* queries, int64_t m, int32_t type,
+                    double epsilon, int32_t k, int32_t* idx, int32_t* cnt, int32_t cap);
 
 /* Replaces the Lambertian gather of ProgressivePhotonMappingProb::radiance
  * (ppm_probabilistic.cc:300-335). photons: n records of 8 floats
@@ -295,6 +327,17 @@ int pppm_dipole_irradiance(pppm_ctx* ctx, const pppm_material* mat, const float*
  * host) and the total count. */
 int pppm_poisson_disk(pppm_ctx* ctx, const float* tri_xyz, int64_t ntri, double min_dist, uint32_t* rng_state,
                       float* pts, float* nrm, int64_t cap, int64_t* count);
+
+/* Replaces SubsurfaceIntegrator::buildPhotonMap (subsurface_integrator.cc:
+ * 240-327) as SubsurfaceIntegrator::initialize calls it: params->photons
+ * env-map photons from num_streams streams, seeded XorShift(sss_time + t - 1
+ * + i) in compat mode, up to 64 bounces, a record at every BSSRDF hit with
+ * roulette on the mean flux. out: the records (n x 8 floats: position,
+ * flux, packed normal, path index bits), *n their count (out NULL or cap
+ * too small: count only). Sets up the context for this stage alone: any
+ * active render of the context ends. The scene needs a BSSRDF material
+ * (else PPPM_E_STATE). */
+int pppm_subsurface_photons(pppm_ctx* ctx, const pppm_params* params, int32_t t, float* out, int64_t cap, int64_t* n);
 
 /* Replaces SubsurfaceIntegrator::irradianceWithPM (subsurface_integrator.cc:
  * 329-365) over an injected photon map: photons are n records of 8 floats
@@ -418,6 +461,15 @@ int pppm_render_read(pppm_ctx* ctx, float* accum);
  * accumulator. rgb8: w*h*3 bytes, host or device. */
 int pppm_render_image(pppm_ctx* ctx, int32_t tonemap, uint8_t* rgb8);
 
+/* The same output stage on an explicit accumulation buffer (w*h*3 floats,
+ * host or device, row y = camera row y, the sum of `passes` passes): the
+ * lines of ppm_probabilistic.cc:96-106 that fill _result and call
+ * Image::gamma(2.2, true), with Image::tonemap (image.cc:498-524) first
+ * when tonemap = 1, and Image::toByte (image.cc:530-533) as Image::savePng
+ * applies it. rgb8: w*h*3 bytes, host or device. */
+int pppm_image_bytes(pppm_ctx* ctx, const float* accum, int32_t w, int32_t h, int32_t passes, int32_t tonemap,
+                     uint8_t* rgb8);
+
 /* PNG file (8-bit RGB, no interlace) of w*h*3 bytes (host), in place of
  * stbi_write_png in Image::savePng (image.cc:484-495). The zlib stream holds
  * stored deflate blocks, one per row, so the file is larger than stb's but
@@ -442,8 +494,20 @@ int pppm_render_load(pppm_ctx* ctx, const uint8_t* in, int64_t size);
 int pppm_render(pppm_ctx* ctx, const pppm_camera* cam, const pppm_params* params, int32_t passes, float* accum);
 
 /* Photon records of the last pass: n x 8 floats (pos xyz, flux xyz, packed
- * normal, stream id as float bits of an int). Returns the count in *n. */
+ * normal, emitted path index as float bits of an int; in compat mode the
+ * reference's thread of the path is index / ceil(P/N)). The records of one
+ * path appear in bounce order. Returns the count in *n. */
 int pppm_render_photons(pppm_ctx* ctx, float* out, int64_t cap, int64_t* n);
+
+/* Gather queries (Lambertian hit points of the eye paths) of the last
+ * PPM-APA pass, the hit points that radiance() (ppm_probabilistic.cc:300-335)
+ * gathers at: n x 12 floats (position xyz, pixel index; oriented normal
+ * xyz, specular and refractive bounces before the hit; path weight *
+ * reflectance / roulette xyz, hit triangle id; the pixel index, bounces and
+ * triangle id as float bits of an int), in the order the eye kernel wrote
+ * them. Returns the count in *n. For parity checks of single hit points; no
+ * counterpart in the reference. */
+int pppm_render_queries(pppm_ctx* ctx, float* out, int64_t cap, int64_t* n);
 
 /* ------------------------------------------------------------- batch */
 /* Many uneven render jobs (each with its own scene, env map, camera and

@@ -486,6 +486,25 @@ public:
         }
         return tot;
     }
+    // Calls f(photon, |p - q|) for every photon strictly inside radius r of q
+    // (same traversal as ballSum).
+    template <class F>
+    void forBall(V q, double r, F&& f) const {
+        if (nodes_.empty()) return;
+        const Node* stack[64];
+        int sp = 0;
+        stack[sp++] = &nodes_[0];
+        while (sp > 0) {
+            const Node* nd = stack[--sp];
+            const double d = norm(nd->pt.p - q);
+            if (d < r) f(nd->pt, d);
+            const double delta = q[nd->axis] - nd->pt.p[nd->axis];
+            const Node* nearC = delta < 0.0 ? nd->l : nd->r;
+            const Node* farC = delta < 0.0 ? nd->r : nd->l;
+            if (farC && std::abs(delta) <= r) stack[sp++] = farC;
+            if (nearC) stack[sp++] = nearC;
+        }
+    }
     // knn: K_NEAREST | EPSILON_BALL with (epsilon, k); else EPSILON_BALL only.
     // Results farthest first (the max-heap's pop order).
     void query(V q, bool knn, int k, double eps, std::vector<const Photon*>* out) const {
@@ -520,6 +539,7 @@ struct Renderer {
     std::vector<XorShift> streams;
     KdTree kd;
     std::vector<double> buffer;
+    std::vector<double> queries;  // per pixel, 12 doubles (radiance's rec), when requested
     std::vector<Photon> lastPhotons;
     int64_t stored = 0, phantoms = 0;
     double msPhoton = 0.0, msEye = 0.0;
@@ -597,7 +617,11 @@ struct Renderer {
     // radiance (ppm_probabilistic.cc:246-344) without BSSRDF. The recursion
     // is unrolled into a loop; the per-bounce factors are applied innermost
     // first, (refl * L) / (pdf * roulette), as the recursive calls return.
-    V radiance(V o, V d, Tape& tp) const {
+    // rec (optional, 12 doubles): the gather query of this path, as the GPU
+    // library's eye kernel writes it: hit point, triangle id, oriented
+    // normal, specular bounces before the hit, path weight * refl /
+    // roulette, and rec[11] = 1 when the path gathered.
+    V radiance(V o, V d, Tape& tp, double* rec = nullptr) const {
         std::vector<std::pair<V, double>> stack;
         V inner;
         for (int b = 0;; b++) {
@@ -621,8 +645,16 @@ struct Renderer {
                 roul = 1.0;
             }
             if (m.type == PPPM_BSDF_LAMBERTIAN) {
-                inner = compat ? gatherCompat(hp, n, m.refl, roul)
-                               : gatherCanonical(hp, dot(n, d) < 0.0 ? n : -n, m.refl, roul);
+                const V on = dot(n, d) < 0.0 ? n : -n;
+                inner = compat ? gatherCompat(hp, n, m.refl, roul) : gatherCanonical(hp, on, m.refl, roul);
+                if (rec) {
+                    V w(1.0, 1.0, 1.0);
+                    for (const auto& f : stack) w = w * f.first / f.second;
+                    w = w * m.refl / roul;
+                    const double v[12] = {hp.x, hp.y, hp.z, (double)id, on.x, on.y, on.z, (double)stack.size(),
+                                          w.x, w.y, w.z, 1.0};
+                    std::memcpy(rec, v, sizeof(v));
+                }
                 break;
             }
             double pdf = 1.0;
@@ -693,7 +725,9 @@ struct Renderer {
                         tp.fill(streams[s]);
                         const double px = x + tp.pop() - 0.5;
                         const double py = y + tp.pop() - 0.5;
-                        const V L = radiance(cam.center, cam.ray(px, py), tp);
+                        double* rec = queries.empty() ? nullptr : &queries[12 * ((size_t)y * W + x)];
+                        if (rec) rec[11] = 0.0;
+                        const V L = radiance(cam.center, cam.ray(px, py), tp, rec);
                         double* p = &buffer[3 * ((size_t)y * W + x)];
                         p[0] += L.x; p[1] += L.y; p[2] += L.z;
                     }
@@ -707,7 +741,9 @@ struct Renderer {
                 tp.fill(x, true);
                 const double px = (pix % W) + tp.pop() - 0.5;
                 const double py = (pix / W) + tp.pop() - 0.5;
-                const V L = radiance(cam.center, cam.ray(px, py), tp);
+                double* rec = queries.empty() ? nullptr : &queries[12 * (size_t)pix];
+                if (rec) rec[11] = 0.0;
+                const V L = radiance(cam.center, cam.ray(px, py), tp, rec);
                 double* p = &buffer[3 * pix];
                 p[0] += L.x; p[1] += L.y; p[2] += L.z;
             }
@@ -784,8 +820,10 @@ void port_intersect(void* s, const float* rays, int64_t n, int32_t* tri, double*
 // Renders `passes` passes; accum: W*H*3 doubles (sum over passes), stats
 // per pass. photons (optional, cap records of 12 doubles) receives the
 // photon map of the last pass; returns the record count in *nphotons.
+// queries (optional, W*H records of 12 doubles) receives each pixel's gather
+// query of the last pass (radiance's rec; rec[11] = 0 where none).
 int port_render(void* s, const pppm_camera* cam, const pppm_params* par, int32_t passes, double* accum,
-                port_pass_stats* stats, double* photons, int64_t cap, int64_t* nphotons) {
+                port_pass_stats* stats, double* photons, int64_t cap, int64_t* nphotons, double* queries) {
     const Scene* sc = static_cast<Scene*>(s);
     if (sc->env.w == 0) return PPPM_E_STATE;
     Renderer R;
@@ -807,6 +845,7 @@ int port_render(void* s, const pppm_camera* cam, const pppm_params* par, int32_t
     R.cam.h = cam->height;
     R.buffer.assign((size_t)cam->width * cam->height * 3, 0.0);
     for (int t = 1; t <= passes; t++) {
+        if (queries && t == passes) R.queries.assign((size_t)cam->width * cam->height * 12, 0.0);
         if (R.compat && (int)R.radius < 1) return PPPM_E_UNDEFINED;
         const double r = R.radius;
         const int rc = R.pass(t);
@@ -814,6 +853,7 @@ int port_render(void* s, const pppm_camera* cam, const pppm_params* par, int32_t
         if (stats) stats[t - 1] = {r, R.stored, R.phantoms, R.msPhoton, R.msEye};
     }
     std::memcpy(accum, R.buffer.data(), R.buffer.size() * 8);
+    if (queries && !R.queries.empty()) std::memcpy(queries, R.queries.data(), R.queries.size() * 8);
     if (nphotons) {
         *nphotons = (int64_t)R.lastPhotons.size();
         for (int64_t i = 0; i < std::min<int64_t>(cap, *nphotons); i++) {
@@ -860,6 +900,57 @@ void port_gather_canonical(const double* ph9, int64_t n, const double* q12, int6
         out[3 * j] = L.x;
         out[3 * j + 1] = L.y;
         out[3 * j + 2] = L.z;
+    }
+}
+
+// Canonical gather bounds on explicit photons (9 doubles: pos, flux,
+// normal) and queries (12 doubles: pos, oriented normal, weight, as
+// port_gather_canonical with refl folded into the weight: refl = 1). A
+// photon is ambiguous when a float32 implementation may decide it the
+// other way: squared distance within d2band * r^2 of r^2, or normal dot
+// within nband of zero. lo sums the photons inside for certain, hi adds the
+// ambiguous ones, ref is the exact float64 gather; amb counts ambiguous
+// photons, inside the photons ref sums. All m x 3 (amb, inside m) and divided
+// by pi^2 r^2.
+void port_gather_bounds(const double* ph9, int64_t n, const double* q12, int64_t m, double radius, double d2band,
+                        double nband, double* lo, double* hi, double* ref, int64_t* amb, int64_t* inside) {
+    std::vector<Photon> ph((size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        const double* p = ph9 + 9 * i;
+        ph[i] = {V(p[0], p[1], p[2]), V(p[3], p[4], p[5]), V(), V(p[6], p[7], p[8])};
+    }
+    KdTree kd;
+    kd.build(ph);
+    const double r2 = radius * radius;
+    const double rq = radius * std::sqrt(1.0 + d2band);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t j = 0; j < m; j++) {
+        const double* q = q12 + 12 * j;
+        const V qp(q[0], q[1], q[2]), qn(q[3], q[4], q[5]);
+        V sure, maybe, exact;
+        int64_t na = 0, ni = 0;
+        kd.forBall(qp, rq, [&](const Photon& p, double d) {
+            const double d2 = d * d;
+            const double c = dot(p.n, qn);
+            const bool in = d2 < r2 * (1.0 - d2band) && c > nband;
+            const bool amb = !in && ((std::abs(d2 - r2) <= d2band * r2 && c > -nband) || std::abs(c) <= nband);
+            if (in) sure = sure + p.flux;
+            if (amb) {
+                maybe = maybe + p.flux;
+                na++;
+            }
+            if (d < radius && c > 0.0) {
+                exact = exact + p.flux;
+                ni++;
+            }
+        });
+        const V w = V(q[6], q[7], q[8]) * V(q[9], q[10], q[11]) * (1.0 / (kPi * kPi * r2));
+        const V a = w * sure, b = a + w * maybe, e = w * exact;
+        lo[3 * j] = a.x; lo[3 * j + 1] = a.y; lo[3 * j + 2] = a.z;
+        hi[3 * j] = b.x; hi[3 * j + 1] = b.y; hi[3 * j + 2] = b.z;
+        ref[3 * j] = e.x; ref[3 * j + 1] = e.y; ref[3 * j + 2] = e.z;
+        amb[j] = na;
+        inside[j] = ni;
     }
 }
 

@@ -334,6 +334,27 @@ int rh_knn(const float* ppos, int n, const float* q, int m, int numTargetPhotons
     return overflow ? -1 : 0;
 }
 
+// KdTree<Photon>::knnSearch (kdtree_detail.h:88-132) with KnnQuery(type,
+// epsilon, k) as given; ids travel in the direction field as in rh_knn.
+int rh_kdtree_knn(const float* ppos, int n, const float* q, int m, int type, double epsilon, int k, int32_t* out_idx,
+                  int32_t* out_cnt, int cap) {
+    std::vector<Photon> photons(n);
+    for (int i = 0; i < n; i++) photons[i] = Photon(v3(ppos + 3 * i), Vector3D(), Vector3D(i, 0, 0), Vector3D());
+    KdTree<Photon> tree;
+    tree.construct(photons);
+    int overflow = 0;
+    for (int j = 0; j < m; j++) {
+        std::vector<Photon> res;
+        tree.knnSearch(Photon(v3(q + 3 * j), Vector3D(), Vector3D(), Vector3D()), KnnQuery(type, epsilon, k), &res);
+        out_cnt[j] = (int)res.size();
+        for (size_t i = 0; i < res.size(); i++) {
+            if ((int)i < cap) out_idx[j * cap + i] = (int32_t)res[i].direction().x();
+            else overflow = 1;
+        }
+    }
+    return overflow ? -1 : 0;
+}
+
 // ---------------------------------------------------------------- gather
 // ProgressivePhotonMappingProb::radiance (ppm_probabilistic.cc:246-344) at
 // bounce 0 for rays hitting Lambertian surfaces, with the photon map built
@@ -377,6 +398,7 @@ struct PassJob {
     double gatherRadius;
     int npasses;
     unsigned int sssTime;  // time(NULL) seen by pass t's subsurface photon map: sssTime + t - 1
+    int sampler;           // rh_render_passes: 0 RANDOM_SAMPLER_PSEUDO_RANDOM, 1 RANDOM_SAMPLER_QUASI_MONTE_CARLO
 };
 
 static void collectKd(const KdTree<Photon>::KdTreeNode* node, std::vector<Photon>* out) {
@@ -414,8 +436,10 @@ int rh_render_passes(void* s, const PassJob* job, double* accum, double* radii, 
         ppm._integrator = new SubsurfaceIntegrator();
     }
 
+    // the samplers of render() (ppm_probabilistic.cc:58-73)
     RandomSampler* rs = new RandomSampler[OMP_NUM_CORE];
-    for (int i = 0; i < OMP_NUM_CORE; i++) rs[i] = Random::generateSampler(i);
+    for (int i = 0; i < OMP_NUM_CORE; i++)
+        rs[i] = job->sampler == 1 ? Halton::generateSampler(200, true, i) : Random::generateSampler(i);
     Image buffer(job->w, job->h);
     buffer.fill(Vector3D(0.0, 0.0, 0.0));
     std::streambuf* old = std::cout.rdbuf(nullptr);  // silence progress output
@@ -444,6 +468,28 @@ int rh_render_passes(void* s, const PassJob* job, double* accum, double* radii, 
         }
     }
     delete[] rs;
+    return 0;
+}
+
+// SubsurfaceIntegrator::buildPhotonMap (subsurface_integrator.cc:240-327)
+// with time(NULL) = sssTime: the photon map's records (12 doubles each,
+// read back from its kd-tree as rh_render_passes does).
+int rh_sss_photons(void* s, int photons, unsigned int sssTime, double* out, int cap, int* count) {
+    const Scene& sc = static_cast<HarnessScene*>(s)->scene;
+    SubsurfaceIntegrator integ;
+    gFakeTime = (time_t)sssTime;
+    std::streambuf* old = std::cout.rdbuf(nullptr);
+    integ.buildPhotonMap(sc, photons, 64);
+    std::cout.rdbuf(old);
+    std::vector<Photon> all;
+    if (integ.photonMap._kdtree._nodes) collectKd(&integ.photonMap._kdtree._nodes[0], &all);
+    *count = (int)all.size();
+    for (int i = 0; i < (int)all.size() && i < cap; i++) {
+        put3(out + 12 * i, static_cast<Vector3D>(all[i]));
+        put3(out + 12 * i + 3, all[i].flux());
+        put3(out + 12 * i + 6, all[i].direction());
+        put3(out + 12 * i + 9, all[i].normal());
+    }
     return 0;
 }
 
@@ -541,6 +587,35 @@ int rh_classic_passes(void* s, const PassJob* job, double* image) {
     }
     delete[] hals;
     return 0;
+}
+
+// The bytes a pass writes (ppm_probabilistic.cc:96-106) from an
+// accumulation buffer (w*h*3 doubles, row y = camera row y, not divided):
+// result.pixel(x, h - y - 1) = buffer(x, y) / t, optionally Image::tonemap
+// (image.cc:498-524), Image::gamma(2.2, true) (image.cc:202-213), then
+// Image::toByte per channel as Image::savePng does (image.cc:484-495).
+// vals (optional, w*h*3): the doubles toByte receives.
+void rh_image_bytes(const double* buffer, int w, int h, int t, int tonemap, unsigned char* out, double* vals) {
+    Image result(w, h);
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const double* b = buffer + 3 * ((size_t)y * w + x);
+            result.pixel(x, h - y - 1) = Vector3D(b[0], b[1], b[2]) / t;
+        }
+    if (tonemap) result.tonemap();
+    result.gamma(2.2, true);
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const Vector3D& c = result(x, y);
+            unsigned char* o = out + 3 * ((size_t)y * w + x);
+            o[0] = Image::toByte(c.x());
+            o[1] = Image::toByte(c.y());
+            o[2] = Image::toByte(c.z());
+            if (vals) {
+                double* v = vals + 3 * ((size_t)y * w + x);
+                v[0] = c.x(); v[1] = c.y(); v[2] = c.z();
+            }
+        }
 }
 
 // Halton::request (halton.cc:123-133): n numbers of `count` consecutive

@@ -85,6 +85,11 @@ def lib():
         _lib.rh_classic_passes.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _D]
         _lib.rh_path_trace.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _D]
         _lib.rh_halton.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.c_int, _D]
+        _lib.rh_sss_photons.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint, _D, ctypes.c_int, _I]
+        _lib.rh_kdtree_knn.argtypes = [_F, ctypes.c_int, _F, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_int, _I, _I, ctypes.c_int]
+        _lib.rh_kdtree_knn.restype = ctypes.c_int
+        _lib.rh_image_bytes.argtypes = [_D, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, _D]
         _lib.rh_irradiance_pm.argtypes = [_D, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_double, _D]
     return _lib
@@ -209,12 +214,21 @@ class RefScene:
         lib().rh_path_trace(self.h, ctypes.byref(job), _p(accum, _D))
         return accum
 
+    def sss_photons(self, photons, sss_time, cap=1 << 20):
+        """SubsurfaceIntegrator::buildPhotonMap with time(NULL) = sss_time:
+        its records, 12 doubles each (position, flux, direction, normal)."""
+        out = np.zeros((cap, 12))
+        cnt = np.zeros(1, np.int32)
+        lib().rh_sss_photons(self.h, int(photons), int(sss_time), _p(out, _D), cap, _p(cnt, _I))
+        return out[: min(int(cnt[0]), cap)]
+
     def render_passes(self, camera, photons, npasses, gather_photons=128, gather_radius=16.0, photon_cap=0,
-                      sss_time=0):
+                      sss_time=0, qmc=False):
         """Passes 1..npasses of ProgressivePhotonMappingProb::render. With a
         BSSRDF in the scene, pass t seeds its subsurface photon streams with
         time(NULL) = sss_time + t - 1 and the Poisson sampler continues the
-        process-wide RNG (reproducible in a fresh process only)."""
+        process-wide RNG (reproducible in a fresh process only). qmc: the
+        RANDOM_SAMPLER_QUASI_MONTE_CARLO sampler type (Halton(200, true, i))."""
         job = _PassJob()
         job.eye[:] = camera.eye
         job.dir[:] = camera.dir
@@ -226,6 +240,7 @@ class RefScene:
         job.gatherRadius = gather_radius
         job.npasses = npasses
         job.sssTime = int(sss_time)
+        job.sampler = 1 if qmc else 0
         accum = np.zeros((camera.height, camera.width, 3))
         radii = np.zeros(npasses)
         cnt = np.zeros(1, np.int32)
@@ -239,6 +254,18 @@ class RefScene:
         return out
 
 
+def image_bytes(buffer, t, tonemap=False):
+    """The reference's pass output bytes (rh_image_bytes) of an H x W x 3
+    accumulation buffer after t passes: H x W x 3 uint8, rows flipped, and
+    the doubles Image::toByte received."""
+    buf = np.ascontiguousarray(buffer, np.float64)
+    h, w = buf.shape[:2]
+    out = np.zeros((h, w, 3), np.uint8)
+    vals = np.zeros((h, w, 3))
+    lib().rh_image_bytes(_p(buf, _D), w, h, int(t), 1 if tonemap else 0, out.ctypes.data, _p(vals, _D))
+    return out, vals
+
+
 def halton(seed, count, n=200):
     out = np.zeros((count, n))
     lib().rh_halton(int(seed), int(count), int(n), _p(out, _D))
@@ -249,7 +276,7 @@ class _PassJob(ctypes.Structure):
     _fields_ = [("eye", ctypes.c_double * 3), ("dir", ctypes.c_double * 3), ("up", ctypes.c_double * 3),
                 ("fov", ctypes.c_double), ("w", ctypes.c_int), ("h", ctypes.c_int), ("photons", ctypes.c_int),
                 ("gatherPhotons", ctypes.c_int), ("gatherRadius", ctypes.c_double), ("npasses", ctypes.c_int),
-                ("sssTime", ctypes.c_uint)]
+                ("sssTime", ctypes.c_uint), ("sampler", ctypes.c_int)]
 
 
 def write_hdr(path, rgb):
@@ -341,6 +368,19 @@ def knn(photon_pos, queries, num_target_photons, target_radius, cap=512):
     cnt = np.zeros(q.shape[0], np.int32)
     r = lib().rh_knn(_p(pp, _F), pp.shape[0], _p(q, _F), q.shape[0], int(num_target_photons), float(target_radius),
                      _p(idx, _I), _p(cnt, _I), cap)
+    if r != 0:
+        raise RuntimeError("cap too small")
+    return idx, cnt
+
+
+def kdtree_knn(points, queries, type_, epsilon, k, cap=64):
+    """KdTree<Photon>::knnSearch with KnnQuery(type, epsilon, k): ids farthest first."""
+    p = np.ascontiguousarray(points, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    idx = np.full((len(q), cap), -1, np.int32)
+    cnt = np.zeros(len(q), np.int32)
+    r = lib().rh_kdtree_knn(_p(p, _F), len(p), _p(q, _F), len(q), int(type_), float(epsilon), int(k), _p(idx, _I),
+                            _p(cnt, _I), cap)
     if r != 0:
         raise RuntimeError("cap too small")
     return idx, cnt

@@ -167,6 +167,13 @@ struct GuideState {
 
 // Classic PPM (ProgressivePhotonMapping): render points, Halton tables,
 // render-point hash grid and photon-update events.
+// Scratch of pppm_hashgrid_build (k_hashgrid.cu).
+struct HashGridBufs {
+    DBuf offs, offsCursor, offsTmp;  // per item: first insertion index (scanned cell counts)
+    DBuf hist, cursor, tmp;          // per bucket: start offsets
+    DBuf order, flag;                // entries' insertion indices by bucket; oversize flag
+};
+
 struct ClassicState {
     DBuf pos, nrm, flux, weight, emission, r2, n, coeff;  // per render point (pixel), SoA, double where the reference is
     DBuf haltonPerm, haltonPrime, haltonOffset;          // permutation tables per stream, first 200 primes
@@ -203,6 +210,7 @@ struct RenderState {
     DBuf gatherWork;  // 2 counters: photon pairs tested, pairs within the radius
     int64_t depositCap = 0;
     int64_t storedLast = 0;
+    int64_t queriesLast = 0;  // gather queries written by the last pass
     int64_t storedMax = 0;     // most photons stored by one pass of this render
     HostPinned graphSlots;      // counters of captured passes (graph.cu)
     std::vector<double> graphRadius;  // radius of each captured pass
@@ -252,6 +260,7 @@ struct pppm_ctx {
     pppm::DBuf stage[8];
     std::vector<void*> pinned;
     pppm::RenderState rs;
+    pppm::HashGridBufs hashGrid;  // pppm_hashgrid_build
     std::vector<uint32_t> jumpTables;  // XorShift jump-ahead matrices (host copy)
     // scratch of the kNN / gather stage entry points
     pppm::DBuf stageRec, stageQ, stageCount;

@@ -145,6 +145,7 @@ int graphFinishPass(pppm_ctx* c, int slot, pppm_pass_stats* st, double* msPass) 
         return fail(c, PPPM_E_UNDEFINED, "render_graph: a photon draw fell past the env CDF");
     if (hc.undefinedEye) return fail(c, PPPM_E_CAPACITY, "render_graph: an eye path exceeded 4096 segments");
     rs.storedLast = (int64_t)hc.deposits;
+    rs.queriesLast = (int64_t)hc.queries;
     rs.storedMax = std::max(rs.storedMax, rs.storedLast);
     float ms = 0.0f;
     if (msPass) *msPass = cudaEventElapsedTime(&ms, e[0], e[3]) == cudaSuccess ? ms : 0.0;

@@ -104,30 +104,46 @@ using namespace pppm;
 
 extern "C" {
 
-int pppm_render_image(pppm_ctx* c, int32_t tonemap, uint8_t* rgb8) {
-    if (!c || !rgb8) return fail(c, PPPM_E_ARG, "render_image: bad arguments");
-    const RenderState& rs = c->rs;
-    if (!rs.active || rs.passesDone < 1) return fail(c, PPPM_E_STATE, "render_image: no pass rendered");
-    cudaSetDevice(c->device);
-    const int w = rs.cam.width, h = rs.cam.height;
+// The output bytes of a device accumulator acc (w*h*3 floats) after
+// `passes` passes into rgb8 (host or device).
+static int imageBytes(pppm_ctx* c, const float* acc, int w, int h, int passes, int32_t tonemap, uint8_t* rgb8) {
     const int64_t n = (int64_t)w * h;
     void* dout;
     int r;
     if ((r = stageOut(c, rgb8, (size_t)n * 3, 0, &dout))) return r;
-    const double invT = 1.0 / (double)rs.passesDone;
+    const double invT = 1.0 / (double)passes;
     PPPM_CUDA(c, c->stageCount.ensure(16));
     double* sumLog = c->stageCount.as<double>();
     unsigned long long* maxBits = reinterpret_cast<unsigned long long*>(sumLog + 1);
     if (tonemap) {
         PPPM_CUDA(c, cudaMemsetAsync(sumLog, 0, 16, c->stream));
-        kTonemapStats<<<152 * 4, 256, 0, c->stream>>>(rs.accum.as<float>(), n, invT, sumLog, maxBits);
+        kTonemapStats<<<152 * 4, 256, 0, c->stream>>>(acc, n, invT, sumLog, maxBits);
     }
-    kImage<<<152 * 8, 256, 0, c->stream>>>(rs.accum.as<float>(), w, h, invT, tonemap ? 1 : 0, sumLog, maxBits,
+    kImage<<<152 * 8, 256, 0, c->stream>>>(acc, w, h, invT, tonemap ? 1 : 0, sumLog, maxBits,
                                            static_cast<unsigned char*>(dout));
     PPPM_CUDA(c, cudaGetLastError());
     if ((r = finishOut(c, rgb8, dout, (size_t)n * 3))) return r;
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
     return PPPM_OK;
+}
+
+int pppm_render_image(pppm_ctx* c, int32_t tonemap, uint8_t* rgb8) {
+    if (!c || !rgb8) return fail(c, PPPM_E_ARG, "render_image: bad arguments");
+    const RenderState& rs = c->rs;
+    if (!rs.active || rs.passesDone < 1) return fail(c, PPPM_E_STATE, "render_image: no pass rendered");
+    cudaSetDevice(c->device);
+    return imageBytes(c, rs.accum.as<float>(), rs.cam.width, rs.cam.height, rs.passesDone, tonemap, rgb8);
+}
+
+int pppm_image_bytes(pppm_ctx* c, const float* accum, int32_t w, int32_t h, int32_t passes, int32_t tonemap,
+                     uint8_t* rgb8) {
+    if (!c || !accum || !rgb8 || w < 1 || h < 1 || passes < 1) return fail(c, PPPM_E_ARG, "image_bytes: bad arguments");
+    cudaSetDevice(c->device);
+    const void* dacc;
+    int r;
+    // staging slot 1: imageBytes writes through slot 0
+    if ((r = stageIn(c, accum, (size_t)w * h * 12, 1, &dacc))) return r;
+    return imageBytes(c, static_cast<const float*>(dacc), w, h, passes, tonemap, rgb8);
 }
 
 int pppm_png_encode(const uint8_t* rgb8, int32_t w, int32_t h, uint8_t* out, int64_t cap, int64_t* size) {

@@ -35,57 +35,7 @@ namespace pppm {
 
 namespace {
 
-constexpr int kHaltonDims = 200;
 constexpr double kPiD = 3.14159265358979323846;
-
-struct HaltonDev {
-    const uint16_t* perm;  // [stream][sum of bases]
-    const int* prime;      // 200
-    const int* offset;     // 200
-    int sum;
-};
-
-// Halton::radicalInverse (halton.cc:142-152) with its permutation.
-__device__ inline double haltonValue(const HaltonDev& h, int stream, unsigned long long n, int dim) {
-    const int base = h.prime[dim];
-    const uint16_t* p = h.perm + (size_t)stream * h.sum + h.offset[dim];
-    const double invBase = __drcp_rn((double)base);
-    double val = 0.0, invBi = invBase;
-    while (n > 0xFFFFFFFFull) {  // 64-bit digits only while the index needs them
-        const unsigned long long q = n / (unsigned)base;
-        const int d = p[n - q * base];
-        val = __dadd_rn(val, __dmul_rn((double)d, invBi));
-        invBi = __dmul_rn(invBi, invBase);
-        n = q;
-    }
-    for (uint32_t m = (uint32_t)n; m > 0;) {
-        const uint32_t q = m / (uint32_t)base;
-        const int d = p[m - q * (uint32_t)base];
-        val = __dadd_rn(val, __dmul_rn((double)d, invBi));
-        invBi = __dmul_rn(invBi, invBase);
-        m = q;
-    }
-    return val;
-}
-
-// One RandomSequence of 200 numbers (sample `index` of sampler `stream`).
-struct HaltonTape {
-    const HaltonDev* h;
-    int stream;
-    unsigned long long index;
-    int dim;
-    bool over;
-    __device__ inline double popd() {
-        if (dim >= kHaltonDims) {
-            over = true;  // RandomSequence::pop asserts (random_sequence.h:50-53)
-            return 0.0;
-        }
-        return haltonValue(*h, stream, index, dim++);
-    }
-    // a draw in [0, 1) as the 32-bit integer floor(r * 2^32): comparisons
-    // against 0.5 and float conversions keep their meaning
-    __device__ inline uint32_t popu() { return (uint32_t)fmin(popd() * 4294967296.0, 4294967295.0); }
-};
 
 struct RpView {
     double* pos;       // 3 per point
@@ -566,12 +516,11 @@ static bool haltonTables(int streams, std::vector<uint16_t>* perm, std::vector<i
     return true;
 }
 
-int classicBegin(pppm_ctx* c, int64_t pixels) {
+int haltonBegin(pppm_ctx* c, int streams) {
     ClassicState& s = c->rs.classic;
-    const int N = c->rs.par.num_streams;
     std::vector<uint16_t> perm;
     std::vector<int> primes, offs;
-    if (!haltonTables(N, &perm, &primes, &offs, &s.haltonSum))
+    if (!haltonTables(streams, &perm, &primes, &offs, &s.haltonSum))
         return fail(c, PPPM_E_UNDEFINED, "render_begin: a Halton permutation draws abs(INT_MIN) (undefined)");
     PPPM_CUDA(c, s.haltonPerm.ensure(perm.size() * 2));
     PPPM_CUDA(c, s.haltonPrime.ensure(primes.size() * 4));
@@ -579,6 +528,17 @@ int classicBegin(pppm_ctx* c, int64_t pixels) {
     PPPM_CUDA(c, cudaMemcpy(s.haltonPerm.p, perm.data(), perm.size() * 2, cudaMemcpyHostToDevice));
     PPPM_CUDA(c, cudaMemcpy(s.haltonPrime.p, primes.data(), primes.size() * 4, cudaMemcpyHostToDevice));
     PPPM_CUDA(c, cudaMemcpy(s.haltonOffset.p, offs.data(), offs.size() * 4, cudaMemcpyHostToDevice));
+    return PPPM_OK;
+}
+
+HaltonDev haltonDev(pppm_ctx* c) { return haltonView(c->rs.classic); }
+
+int classicBegin(pppm_ctx* c, int64_t pixels) {
+    ClassicState& s = c->rs.classic;
+    {
+        const int e = haltonBegin(c, c->rs.par.num_streams);
+        if (e) return e;
+    }
     const size_t P = (size_t)pixels;
     PPPM_CUDA(c, s.pos.ensure(P * 24));
     PPPM_CUDA(c, s.nrm.ensure(P * 12));

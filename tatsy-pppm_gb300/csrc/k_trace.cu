@@ -204,26 +204,37 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
     }
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < tp.numPaths;
          g += (int64_t)gridDim.x * blockDim.x) {
-        Tape tape;
-        tape.pos = 0;
-        tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
-        if (tp.mode == PPPM_MODE_COMPAT) {
-            const uint4 s = *reinterpret_cast<const uint4*>(photonStates + 4 * g);
-            tape.x.s[0] = s.x; tape.x.s[1] = s.y; tape.x.s[2] = s.z; tape.x.s[3] = s.w;
-        } else {
-            seedCanonical(tp.seed, tp.pass, (uint64_t)g, tape.x);
-        }
         f3 d, dir, flux;
-        const bool ok = learned ? emitPhotonMis(env, tape, mix, gv.emitFloor, gv.emitK, &d, &dir, &flux)
-                                : emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux, tp.sssPass != 0);
-        if (!ok) atomicAdd(&ctr->undefinedEmit, 1ull);
+        bool ok;
         PathState p;
+        if (tp.qmc) {
+            // photon round i of thread s draws sample i of the pass from
+            // sampler s (tracePhotons, ppm_probabilistic.cc:131-135)
+            const int s = (int)(g / tp.taskPerThread);
+            HaltonTape tape{&tp.halton, s, qmcIndex(tp, s, g % tp.taskPerThread), 0, false};
+            ok = emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux, false);
+            if (tape.over) ok = false;
+            storeTape(tape, p);
+        } else {
+            Tape tape;
+            tape.pos = 0;
+            tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
+            if (tp.mode == PPPM_MODE_COMPAT) {
+                const uint4 s = *reinterpret_cast<const uint4*>(photonStates + 4 * g);
+                tape.x.s[0] = s.x; tape.x.s[1] = s.y; tape.x.s[2] = s.z; tape.x.s[3] = s.w;
+            } else {
+                seedCanonical(tp.seed, tp.pass, (uint64_t)g, tape.x);
+            }
+            ok = learned ? emitPhotonMis(env, tape, mix, gv.emitFloor, gv.emitK, &d, &dir, &flux)
+                         : emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux, tp.sssPass != 0);
+            storeTape(tape, p);
+        }
+        if (!ok) atomicAdd(&ctr->undefinedEmit, 1ull);
         p.ox = 50.0 * (double)d.x;  // R * dir with R = 50 (envmap.cc:63,85)
         p.oy = 50.0 * (double)d.y;
         p.oz = 50.0 * (double)d.z;
         p.dx = dir.x; p.dy = dir.y; p.dz = dir.z;
         p.fx = ok ? flux.x : 0.f; p.fy = ok ? flux.y : 0.f; p.fz = ok ? flux.z : 0.f;
-        p.rng[0] = tape.x.s[0]; p.rng[1] = tape.x.s[1]; p.rng[2] = tape.x.s[2]; p.rng[3] = tape.x.s[3];
         p.id = (int)g;
         p.bounce = 0;
         p.pad[0] = -1;  // no pending bounce record
@@ -266,14 +277,12 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
 // 262-320): three draws from the path's tape, the deposit (store, da, db) on
 // Lambertian (subsurface pass: BSSRDF) surfaces, Russian roulette, and the
 // next ray in p. alive turns false when the path ends here.
-template <bool kSss>
+template <bool kSss, class TapeT = Tape>
 __device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView& sc, PathState& p, int slot, double best,
                                           bool& alive, bool& store, float4& da, float4& db) {
-    Tape tape;
-    tape.pos = 0;
-    tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
-    tape.x.s[0] = p.rng[0]; tape.x.s[1] = p.rng[1]; tape.x.s[2] = p.rng[2]; tape.x.s[3] = p.rng[3];
-    const uint32_t r0 = tape.popu(), r1 = tape.popu(), r2 = tape.popu();
+    TapeT tape;
+    loadTape(tp, p, tape);
+    const auto r0 = tape.draw(), r1 = tape.draw(), r2 = tape.draw();
     const float4 a = sc.tris[3 * slot], b = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
     const int tid = __float_as_int(a.w);
     const DevMaterial& m = sc.mats[sc.matId[tid]];
@@ -292,10 +301,10 @@ __device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView
                              __uint_as_float(packNormal(on)));
             db = make_float4(flux.x, flux.y, flux.z, __int_as_float(p.id));
             const float prob = (flux.x + flux.y + flux.z) / 3.0f;
-            if (!(u32ToFloat(r0) < prob)) alive = false;  // rands[0] >= probability: break
+            if (!(r0.f() < prob)) alive = false;  // rands[0] >= probability: break
         }
         if (alive) {
-            const float pdf = bsdfSample(m, din, nrm, r1, r2, &nd);
+            const float pdf = bsdfSample(m, din, nrm, r1.u, r2.u, &nd);
             flux = flux * refl * (1.0f / pdf);
         }
     } else if (m.type & PPPM_BSDF_LAMBERTIAN) {
@@ -311,25 +320,25 @@ __device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView
                 tp.guide.rec[er - 1].w +=
                     (0.2126f * flux.x + 0.7152f * flux.y + 0.0722f * flux.z) * __ldg(&tp.guide.imp[v]);
         }
-        if ((unsigned long long)r0 < m.rrCeil) {  // rands[0] < probability
+        if (r0.lt(m.rrCeil, m.rr_photon)) {  // rands[0] < probability
             if (tp.guided && tp.guide.guideBounces) {
                 nd = on;  // kGuideResolve draws the direction around the normal
                 p.pad[1] |= kPathNeedsDir;
             } else {
-                bsdfSample(m, din, on, r1, r2, &nd);
+                bsdfSample(m, din, on, r1.u, r2.u, &nd);
             }
             flux = flux * refl * m.invRr;
         } else {
             alive = false;
         }
     } else {
-        const float pdf = bsdfSample(m, din, on, r0, r1, &nd);
+        const float pdf = bsdfSample(m, din, on, r0.u, r1.u, &nd);
         flux = flux * refl * (1.0f / pdf);
     }
     p.ox = hp[0]; p.oy = hp[1]; p.oz = hp[2];
     p.dx = nd.x; p.dy = nd.y; p.dz = nd.z;
     p.fx = flux.x; p.fy = flux.y; p.fz = flux.z;
-    p.rng[0] = tape.x.s[0]; p.rng[1] = tape.x.s[1]; p.rng[2] = tape.x.s[2]; p.rng[3] = tape.x.s[3];
+    storeTape(tape, p);
     p.bounce += 1;
 }
 
@@ -439,7 +448,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(T
 // left after the first bounces are long chains (inside refractive and
 // mirrored geometry) that leave most of a per-bounce launch idle; here each
 // warp carries its paths to the end (no queue output, `out` unused).
-template <bool kSss, bool kTail>
+template <bool kSss, bool kTail, class TapeT = Tape>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(TraceParams tp, SceneView sc, int bounce, const PathState* __restrict__ in,
                                                      PathState* __restrict__ out, int64_t maxPaths,
                                                      float4* __restrict__ dep, int64_t depCap, PassCounters* ctr) {
@@ -496,7 +505,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
             if (slot < 0) {
                 alive = false;
             } else {
-                photonHit<kSss>(tp, sc, p, slot, best, alive, store, da, db);
+                photonHit<kSss, TapeT>(tp, sc, p, slot, best, alive, store, da, db);
                 if (kTail && alive)
                     alive = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
             }
@@ -541,7 +550,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
 #endif
 constexpr bool kEyeTiles = PPPM_EYE_TILES != 0;
 
-template <bool kSss, bool kPT>
+template <bool kSss, bool kPT, class TapeT = Tape>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TraceParams tp, SceneView sc, EnvDev env, CameraDev cam,
                                                  OctView oct, const uint32_t* __restrict__ pixelStates,
                                                  float* __restrict__ accum, float4* __restrict__ queries,
@@ -578,16 +587,26 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
         // every lane of the warp stays in the bounce loop until all paths end
         // (the traversal is warp-cooperative)
         bool alive = pix < np;
-        Tape tape;
-        tape.pos = 0;
-        tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
-        tape.x.s[0] = tape.x.s[1] = tape.x.s[2] = tape.x.s[3] = 1u;
+        TapeT tape;
+        if constexpr (TapeT::kExact32) {
+            tape.pos = 0;
+            tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
+            tape.x.s[0] = tape.x.s[1] = tape.x.s[2] = tape.x.s[3] = 1u;
+        } else {
+            tape = HaltonTape{&tp.halton, 0, 0, 0, false};
+        }
         f3 d = {0.f, 0.f, 1.f};
         double o[3] = {cam.ex, cam.ey, cam.ez};
         f3 w = {1.f, 1.f, 1.f}, L = {0.f, 0.f, 0.f};
         if (alive) {
             const int x = (int)(pix % cam.w), y = (int)(pix / cam.w);
-            if (tp.mode == PPPM_MODE_COMPAT || tp.mode == PPPM_MODE_PATH_TRACING) {
+            if constexpr (!TapeT::kExact32) {
+                // pixel x of the stream's k-th row: sample taskPerThread + k w + x
+                // of sampler y % N (traceRays, ppm_probabilistic.cc:214-229)
+                const int s = y % tp.numStreams;
+                tape.stream = s;
+                tape.index = qmcIndex(tp, s, tp.taskPerThread + (int64_t)(y / tp.numStreams) * cam.w + x);
+            } else if (tp.mode == PPPM_MODE_COMPAT || tp.mode == PPPM_MODE_PATH_TRACING) {
                 const uint4 s = *reinterpret_cast<const uint4*>(pixelStates + 4 * pix);
                 tape.x.s[0] = s.x; tape.x.s[1] = s.y; tape.x.s[2] = s.z; tape.x.s[3] = s.w;
             } else {
@@ -624,7 +643,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
                 alive = false;
                 continue;
             }
-            const uint32_t r0 = tape.popu(), r1 = tape.popu(), r2 = tape.popu();
+            const auto r0 = tape.draw(), r1 = tape.draw(), r2 = tape.draw();
             const float4 a = sc.tris[3 * slot], bb = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
             const DevMaterial& m = sc.mats[sc.matId[__float_as_int(a.w)]];
             double hp[3];
@@ -633,7 +652,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
             float roul = m.roulette;
             if (bnc >= 3) {
                 // rands[0] > roulette: the path ends and contributes nothing more
-                if ((unsigned long long)r0 > m.roulFloor) {
+                if (r0.gt(m.roulFloor, (double)m.roulette)) {
                     alive = false;
                     continue;
                 }
@@ -652,7 +671,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
                     if (s.total) {
                         d = s.rdir;
                         bnc++;
-                    } else if (r1 < 0x80000000u) {  // rands[1] < 0.5: reflect, same bounce count
+                    } else if (r1.lt(0x80000000ull, 0.5)) {  // rands[1] < 0.5: reflect, same bounce count
                         w = w * refl * (s.Re / 0.5f);
                         d = s.rdir;
                     } else {  // transmit: diffuse subsurface radiance
@@ -684,14 +703,17 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
                 const f3 wq = w * refl * (1.0f / roul);
                 q0 = make_float4(__double2float_rn(hp[0]), __double2float_rn(hp[1]), __double2float_rn(hp[2]),
                                  __int_as_float((int)pix));
-                q1 = make_float4(on.x, on.y, on.z, 0.f);
-                q2 = make_float4(wq.x, wq.y, wq.z, 0.f);
+                // .w: the specular/refractive bounces before this hit and the
+                // hit triangle's id (int bits), for parity checks of single
+                // hit points; the gathers read neither
+                q1 = make_float4(on.x, on.y, on.z, __int_as_float(bnc));
+                q2 = make_float4(wq.x, wq.y, wq.z, a.w);
                 query = true;
                 alive = false;
                 continue;
             }
             f3 nd;
-            const float pdf = bsdfSample(m, d, nrm, r1, r2, &nd);
+            const float pdf = bsdfSample(m, d, nrm, r1.u, r2.u, &nd);
             w = w * refl * (1.0f / (pdf * roul));
             o[0] = hp[0]; o[1] = hp[1]; o[2] = hp[2];
             d = nd;
@@ -699,7 +721,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
         }
         // a compat tape holds 200 numbers (ppm_probabilistic.cc:222); the
         // reference aborts when a path pops more
-        if ((tp.mode == PPPM_MODE_COMPAT || tp.mode == PPPM_MODE_PATH_TRACING) && tape.pos > 200)
+        if ((tp.mode == PPPM_MODE_COMPAT || tp.mode == PPPM_MODE_PATH_TRACING) && tape.exhausted())
             atomicAdd(&ctr->undefinedEye, 1ull);
         if (onImage) {
             accum[3 * pix] += L.x;
@@ -812,6 +834,9 @@ cudaError_t launchPhotonBounce(const TraceParams& tp, const SceneView& sc, int b
     const unsigned blocks = blocksFor(maxPaths, 128, 152 * tp.bouncePerSm);
     if (tp.sssPass)
         kPhotonBounce<true, false><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths, deposits, depositCap, ctr);
+    else if (tp.qmc)
+        kPhotonBounce<false, false, HaltonTape><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths, deposits,
+                                                                         depositCap, ctr);
     else
         kPhotonBounce<false, false><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, out, maxPaths, deposits, depositCap, ctr);
     return cudaGetLastError();
@@ -836,6 +861,9 @@ cudaError_t launchPhotonTail(const TraceParams& tp, const SceneView& sc, int bou
     if (tp.sssPass)
         kPhotonBounce<true, true><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, nullptr, maxPaths, deposits, depositCap,
                                                            ctr);
+    else if (tp.qmc)
+        kPhotonBounce<false, true, HaltonTape><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, nullptr, maxPaths, deposits,
+                                                                        depositCap, ctr);
     else
         kPhotonBounce<false, true><<<blocks, 128, 0, st>>>(tp, sc, bounce, in, nullptr, maxPaths, deposits, depositCap,
                                                             ctr);
@@ -847,7 +875,13 @@ cudaError_t launchEyeTrace(const TraceParams& tp, const SceneView& sc, const Env
                            float4* sssQ, int64_t sssCap, PassCounters* ctr, cudaStream_t st, bool pathTrace) {
     const unsigned blocks = blocksFor((int64_t)cam.w * cam.h, 128, 152 * tp.eyePerSm);
     const bool sss = oct.numNodes > 0 || tp.hasSss;
-    if (pathTrace && sss)
+    if (tp.qmc && !pathTrace && sss)
+        kEyeTrace<true, false, HaltonTape><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries,
+                                                                    sssQ, sssCap, ctr);
+    else if (tp.qmc && !pathTrace)
+        kEyeTrace<false, false, HaltonTape><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries,
+                                                                     sssQ, sssCap, ctr);
+    else if (pathTrace && sss)
         kEyeTrace<true, true><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap, ctr);
     else if (pathTrace)
         kEyeTrace<false, true><<<blocks, 128, 0, st>>>(tp, sc, env, cam, oct, pixelStates, accum, queries, sssQ, sssCap,

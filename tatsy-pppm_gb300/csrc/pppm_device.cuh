@@ -134,7 +134,29 @@ __host__ __device__ inline uint32_t mix32(uint32_t x) {
 // and polar draw, which folds all photons of one small bright env cell onto
 // one curve of directions). Compat mode keeps the raw outputs, as the
 // reference does.
+//
+// A draw of a tape, with the comparisons the shading code makes against
+// double thresholds. A XorShift draw x stands for x * 2^-32 exactly, so the
+// comparisons run on integers: x * 2^-32 < p <=> x < ceil(p * 2^32) and
+// x * 2^-32 > p <=> x > floor(p * 2^32) (the thresholds are precomputed).
+struct Draw32 {
+    uint32_t u;
+    __device__ inline bool lt(unsigned long long ceilThr, double) const { return u < ceilThr; }
+    __device__ inline bool gt(unsigned long long floorThr, double) const { return u > floorThr; }
+    __device__ inline float f() const { return u32ToFloat(u); }
+};
+// A draw of an arbitrary double in [0, 1) (the permuted Halton sampler):
+// compared in double; u = floor(d * 2^32) feeds the float conversions.
+struct DrawD {
+    uint32_t u;
+    double d;
+    __device__ inline bool lt(unsigned long long, double thr) const { return d < thr; }
+    __device__ inline bool gt(unsigned long long, double thr) const { return d > thr; }
+    __device__ inline float f() const { return (float)d; }
+};
+
 struct Tape {
+    static constexpr bool kExact32 = true;  // every draw is x * 2^-32
     XorShift x;
     int pos;
     uint32_t scramble = 0;
@@ -145,16 +167,85 @@ struct Tape {
     __device__ inline double popd() { pos++; return u32ToReal(next()); }
     __device__ inline float popf() { pos++; return u32ToFloat(next()); }
     __device__ inline uint32_t popu() { pos++; return next(); }
+    __device__ inline Draw32 draw() { return Draw32{popu()}; }
+    __device__ inline bool exhausted() const { return pos > 200; }
 };
 
 // A tape given explicitly (stage tests feed the reference's own numbers).
 struct ArrayTape {
+    static constexpr bool kExact32 = true;
     const double* v;
     int pos;
     __device__ inline double popd() { return v[pos++]; }
     __device__ inline float popf() { return (float)popd(); }
     // tape values are x * 2^-32 with x < 2^32, so this is exact
     __device__ inline uint32_t popu() { return (uint32_t)(v[pos++] * 4294967296.0); }
+    __device__ inline Draw32 draw() { return Draw32{popu()}; }
+};
+
+// ------------------------------------------------------------------ Halton
+// Halton(200, true, seed) (halton.cc:88-152), the reference's
+// RANDOM_SAMPLER_QUASI_MONTE_CARLO sampler: dimension j of sample n is the
+// radical inverse of n in the j-th prime base with that base's digits
+// permuted per sampler. Tables: permutations [stream][sum of bases], the
+// first 200 primes and each base's offset in a stream's table.
+constexpr int kHaltonDims = 200;
+
+struct HaltonDev {
+    const uint16_t* perm;
+    const int* prime;
+    const int* offset;
+    int sum;
+};
+
+// Halton::radicalInverse (halton.cc:142-152) with its permutation, in
+// double with the reference's operation order.
+__device__ inline double haltonValue(const HaltonDev& h, int stream, unsigned long long n, int dim) {
+    const int base = h.prime[dim];
+    const uint16_t* p = h.perm + (size_t)stream * h.sum + h.offset[dim];
+    const double invBase = __drcp_rn((double)base);
+    double val = 0.0, invBi = invBase;
+    while (n > 0xFFFFFFFFull) {  // 64-bit digits only while the index needs them
+        const unsigned long long q = n / (unsigned)base;
+        const int d = p[n - q * base];
+        val = __dadd_rn(val, __dmul_rn((double)d, invBi));
+        invBi = __dmul_rn(invBi, invBase);
+        n = q;
+    }
+    for (uint32_t m = (uint32_t)n; m > 0;) {
+        const uint32_t q = m / (uint32_t)base;
+        const int d = p[m - q * (uint32_t)base];
+        val = __dadd_rn(val, __dmul_rn((double)d, invBi));
+        invBi = __dmul_rn(invBi, invBase);
+        m = q;
+    }
+    return val;
+}
+
+// One RandomSequence of 200 numbers: sample `index` of sampler `stream`.
+struct HaltonTape {
+    static constexpr bool kExact32 = false;
+    const HaltonDev* h;
+    int stream;
+    unsigned long long index;
+    int dim;
+    bool over;
+    __device__ inline double popd() {
+        if (dim >= kHaltonDims) {
+            over = true;  // RandomSequence::pop asserts (random_sequence.h:50-53)
+            return 0.0;
+        }
+        return haltonValue(*h, stream, index, dim++);
+    }
+    __device__ inline float popf() { return (float)popd(); }
+    // a draw in [0, 1) as the 32-bit integer floor(r * 2^32): comparisons
+    // against 0.5 and float conversions keep their meaning
+    __device__ inline uint32_t popu() { return (uint32_t)fmin(popd() * 4294967296.0, 4294967295.0); }
+    __device__ inline DrawD draw() {
+        const double d = popd();
+        return DrawD{(uint32_t)fmin(d * 4294967296.0, 4294967295.0), d};
+    }
+    __device__ inline bool exhausted() const { return over || dim > kHaltonDims; }
 };
 
 // ------------------------------------------------------------------ vectors
@@ -834,11 +925,19 @@ __device__ inline f3 envLookup(const EnvDev& e, f3 d) {
 // i.e. uniform in solid angle (y is linear in v). *index = 4096 past the CDF.
 template <class TapeT>
 __device__ inline f3 envCellDraw(const EnvDev& e, TapeT& tp, int* index) {
-    const unsigned long long r = tp.popu();
-    int lo = 0, hi = 4096;  // first index with cdf[i] >= r * 2^-32
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (__ldg(&e.ucdf[mid]) < r) lo = mid + 1; else hi = mid;
+    int lo = 0, hi = 4096;  // first index with cdf[i] >= r
+    if constexpr (TapeT::kExact32) {
+        const unsigned long long r = tp.popu();  // r * 2^-32 exactly: compare on integers
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(&e.ucdf[mid]) < r) lo = mid + 1; else hi = mid;
+        }
+    } else {
+        const double r = tp.popd();
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(&e.cdf[mid]) < r) lo = mid + 1; else hi = mid;
+        }
     }
     *index = lo;
     const int ix = lo % 64, iy = lo / 64;

@@ -100,6 +100,10 @@ void passSetup(pppm_ctx* c, int t, int64_t paths, TraceParams* tp, CameraDev* cd
     tp->eyePerSm = rs.eyePerSm;
     tp->guided = rs.guide.enabled ? 1 : 0;
     tp->guide = guideView(c, 3 * paths);
+    tp->qmc = (par.mode == PPPM_MODE_COMPAT && (par.flags & PPPM_FLAG_SAMPLER_QMC)) ? 1 : 0;
+    if (tp->qmc) tp->halton = haltonDev(c);
+    tp->width = W;
+    tp->height = H;
     {
         const double ex = rs.cam.eye[0], ey = rs.cam.eye[1], ez = rs.cam.eye[2];
         const double dx = rs.cam.dir[0], dy = rs.cam.dir[1], dz = rs.cam.dir[2];
@@ -191,16 +195,10 @@ int ptPass(pppm_ctx* c, int t, const TraceParams& tp, const SceneView& sv, const
 
 extern "C" {
 
-int pppm_knn(pppm_ctx* c, const float* photonPos, int64_t n, const float* queries, int64_t m, int32_t numTarget,
-             double targetRadius, int32_t* idx, int32_t* cnt, int32_t cap) {
-    if (!c || n < 0 || m < 0 || cap < 0 || (n > 0 && !photonPos) || (m > 0 && (!queries || !cnt || (cap > 0 && !idx))))
-        return fail(c, PPPM_E_ARG, "knn: bad arguments");
-    // KnnQuery(type, epsilon, k) receives (numTargetPhotons, targetRadius):
-    // k = (int)targetRadius, epsilon = numTargetPhotons (photon_map.cc:25, kdtree.h:17)
-    const int k = (int)targetRadius;
-    const float eps = (float)numTarget;
-    if (k < 1) return fail(c, PPPM_E_UNDEFINED, "knn: k = (int)radius < 1 pops an empty queue in the reference");
-    if (k > kMaxKnn) return fail(c, PPPM_E_CAPACITY, "knn: k above 64");
+// The k nearest of n points within distance eps of each query (k <= 64),
+// farthest first: KdTree::knnSearch (kdtree_detail.h:88-132) on the hash grid.
+static int knnRun(pppm_ctx* c, const float* photonPos, int64_t n, const float* queries, int64_t m, int k, float eps,
+                  int32_t* idx, int32_t* cnt, int32_t cap) {
     if (m == 0) return PPPM_OK;
     cudaSetDevice(c->device);
     std::vector<float> hp;
@@ -225,6 +223,49 @@ int pppm_knn(pppm_ctx* c, const float* photonPos, int64_t n, const float* querie
     if ((r = finishOut(c, idx, didx, (size_t)m * cap * 4))) return r;
     if ((r = finishOut(c, cnt, dcnt, (size_t)m * 4))) return r;
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PPPM_OK;
+}
+
+int pppm_knn(pppm_ctx* c, const float* photonPos, int64_t n, const float* queries, int64_t m, int32_t numTarget,
+             double targetRadius, int32_t* idx, int32_t* cnt, int32_t cap) {
+    if (!c || n < 0 || m < 0 || cap < 0 || (n > 0 && !photonPos) || (m > 0 && (!queries || !cnt || (cap > 0 && !idx))))
+        return fail(c, PPPM_E_ARG, "knn: bad arguments");
+    // KnnQuery(type, epsilon, k) receives (numTargetPhotons, targetRadius):
+    // k = (int)targetRadius, epsilon = numTargetPhotons (photon_map.cc:25, kdtree.h:17)
+    const int k = (int)targetRadius;
+    const float eps = (float)numTarget;
+    if (k < 1) return fail(c, PPPM_E_UNDEFINED, "knn: k = (int)radius < 1 pops an empty queue in the reference");
+    if (k > kMaxKnn) return fail(c, PPPM_E_CAPACITY, "knn: k above 64");
+    return knnRun(c, photonPos, n, queries, m, k, eps, idx, cnt, cap);
+}
+
+int pppm_kdtree_knn(pppm_ctx* c, const float* points, int64_t n, const float* queries, int64_t m, int32_t type,
+                    double epsilon, int32_t k, int32_t* idx, int32_t* cnt, int32_t cap) {
+    if (!c || n < 0 || m < 0 || cap < 0 || (n > 0 && !points) || (m > 0 && (!queries || !cnt || (cap > 0 && !idx))) ||
+        (type & ~(PPPM_KNN_EPSILON_BALL | PPPM_KNN_K_NEAREST)) != 0 || !(epsilon >= 0.0))
+        return fail(c, PPPM_E_ARG, "kdtree_knn: bad arguments");
+    // without EPSILON_BALL the ball is unbounded (knnSearch sets INFTY)
+    const float eps = (type & PPPM_KNN_EPSILON_BALL) ? (float)std::min(epsilon, 1e30) : 1e30f;
+    if (type & PPPM_KNN_K_NEAREST) {
+        // k = 0 pops the queue's only element at once, then reads the top of
+        // an empty queue (kdtree_detail.h:110-113)
+        if (k < 1) return fail(c, PPPM_E_UNDEFINED, "kdtree_knn: k < 1 reads an empty queue in the reference");
+        if (k > kMaxKnn || k > cap) return fail(c, PPPM_E_CAPACITY, "kdtree_knn: k above 64 or above cap");
+        return knnRun(c, points, n, queries, m, k, eps, idx, cnt, cap);
+    }
+    // EPSILON_BALL alone: every point within epsilon. Searched as the cap
+    // nearest (cap <= 64); a query that fills cap may have more: refused.
+    const int kk = std::min<int32_t>(cap, kMaxKnn);
+    if (kk < 1) return fail(c, PPPM_E_CAPACITY, "kdtree_knn: cap < 1");
+    const int r = knnRun(c, points, n, queries, m, kk, eps, idx, cnt, cap);
+    if (r) return r;
+    if (m > 0) {
+        std::vector<int32_t> hc((size_t)m);
+        if (isDevicePtr(cnt)) PPPM_CUDA(c, cudaMemcpy(hc.data(), cnt, (size_t)m * 4, cudaMemcpyDeviceToHost));
+        else std::memcpy(hc.data(), cnt, (size_t)m * 4);
+        for (int32_t v : hc)
+            if (v >= kk) return fail(c, PPPM_E_CAPACITY, "kdtree_knn: more than min(cap, 64) points within epsilon");
+    }
     return PPPM_OK;
 }
 
@@ -284,6 +325,9 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
         return fail(c, PPPM_E_ARG, "render_begin: unknown mode");
     if ((par->mode == PPPM_MODE_CLASSIC || par->mode == PPPM_MODE_PATH_TRACING) && (par->flags & PPPM_FLAG_LEARNED))
         return fail(c, PPPM_E_ARG, "render_begin: the learned proposal needs canonical mode");
+    if ((par->flags & PPPM_FLAG_SAMPLER_QMC) && par->mode != PPPM_MODE_COMPAT)
+        return fail(c, PPPM_E_ARG, "render_begin: the Halton sampler belongs to compat mode (the reference's sampler "
+                                   "types); classic PPM always uses it");
     if (par->num_streams < 1 || par->num_streams > 4096 || par->photons < 1 || cam->width < 1 || cam->height < 1 ||
         par->max_bounce_photon < 0 || par->max_bounce_eye < 0 || !(par->alpha > 0.0) || !(par->radius_scale > 0.0))
         return fail(c, PPPM_E_ARG, "render_begin: bad parameters");
@@ -336,6 +380,10 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
         const int e = envFluxScale(c, (double)par->photons);
         if (e) return e;
     }
+    if (par->flags & PPPM_FLAG_SAMPLER_QMC) {
+        const int e = haltonBegin(c, N);
+        if (e) return e;
+    }
     if (par->mode == PPPM_MODE_CLASSIC) {
         // classic PPM has no subsurface stage for these materials (its test is
         // type == BSSRDF, progressive_photon_mapping.cc:42) and no proposal
@@ -354,6 +402,7 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
     rs.passesDone = 0;
     rs.storedLast = 0;
+    rs.queriesLast = 0;
     rs.storedMax = 0;
     rs.phantomsLast = 0;
     rs.active = true;
@@ -407,7 +456,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         if (e) return e;
     }
     PPPM_CUDA(c, cudaEventRecord(c->ev[7], c->stream));
-    if (compat) {
+    if (compat && !tp.qmc) {
         std::vector<uint32_t> ss((size_t)N * 4);
         for (int s = 0; s < N; s++) std::memcpy(&ss[4 * s], rs.streams[s].s, 16);
         PPPM_CUDA(c, cudaMemcpyAsync(rs.streamStatesD.p, ss.data(), ss.size() * 4, cudaMemcpyHostToDevice, c->stream));
@@ -470,7 +519,8 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         // per-bounce launches while the queue is wide, then one tail launch
         // (guided bounces need every bounce as a queue step)
         const bool guideBounces = tp.guided && rs.guide.guideBounces;
-        const bool persistent = kPersistentPhotons && !guideBounces;
+        // the Halton photons run on the per-bounce kernels
+        const bool persistent = kPersistentPhotons && !guideBounces && !tp.qmc;
         const uint32_t* perm = nullptr;
         const PathState* traced = nullptr;
         {
@@ -643,6 +693,7 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
         }
     }
     rs.storedLast = stored;
+    rs.queriesLast = (int64_t)hc.queries;
     rs.storedMax = std::max(rs.storedMax, stored);
     rs.phantomsLast = phantoms;
     rs.passesDone = t;
@@ -733,6 +784,25 @@ int pppm_render_photons(pppm_ctx* c, float* out, int64_t cap, int64_t* n) {
         if ((r = stageOut(c, out, (size_t)m * 32, 0, &dout))) return r;
         PPPM_CUDA(c, launchUnpackRecords(c->rs.photons.as<float4>(), m, (float*)dout, c->stream));
         if ((r = finishOut(c, out, dout, (size_t)m * 32))) return r;
+        PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return PPPM_OK;
+}
+
+int pppm_render_queries(pppm_ctx* c, float* out, int64_t cap, int64_t* n) {
+    if (!c || !n || cap < 0 || (cap > 0 && !out)) return fail(c, PPPM_E_ARG, "render_queries: bad arguments");
+    if (!c->rs.active) return fail(c, PPPM_E_STATE, "render_queries: no render");
+    const int64_t cnt = std::min<int64_t>(c->rs.queriesLast, (int64_t)c->rs.cam.width * c->rs.cam.height);
+    *n = cnt;
+    const int64_t m = std::min(cnt, cap);
+    if (m > 0) {
+        // 3 float4 per query as the eye kernel wrote them: (position, pixel
+        // as int bits), (oriented normal, 0), (path weight * refl / roulette, 0)
+        void* dout;
+        int r;
+        if ((r = stageOut(c, out, (size_t)m * 48, 0, &dout))) return r;
+        PPPM_CUDA(c, cudaMemcpyAsync(dout, c->rs.queries.p, (size_t)m * 48, cudaMemcpyDeviceToDevice, c->stream));
+        if ((r = finishOut(c, out, dout, (size_t)m * 48))) return r;
         PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     return PPPM_OK;

@@ -110,18 +110,19 @@ int sssBegin(pppm_ctx* c) {
     return PPPM_OK;
 }
 
-int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv, const EnvDev& ev, int64_t* launches) {
-    SssState& s = c->rs.sss;
+// Kernel parameters and photon tape states of pass t's subsurface photon set
+// (SubsurfaceIntegrator::buildPhotonMap, subsurface_integrator.cc:240-327).
+static int sssPhotonSetup(pppm_ctx* c, int t, const TraceParams& base, TraceParams* tpOut, uint32_t** statesOut,
+                          int64_t* launches) {
     RenderState& rs = c->rs;
     const pppm_params& par = rs.par;
     // the path tracer's subsurface stage is the reference's, as in compat mode
     const bool compat = par.mode == PPPM_MODE_COMPAT || par.mode == PPPM_MODE_PATH_TRACING;
     const int N = par.num_streams;
-    const int64_t paths = base.numPaths;
-
     TraceParams tp = base;
     if (compat) tp.mode = PPPM_MODE_COMPAT;
     tp.sssPass = 1;
+    tp.qmc = 0;  // its streams are XorShift(time + i) whatever sampler the eye paths use
     tp.maxBouncePhoton = kSssBounceLimit;
     // the subsurface photon set keeps the reference's own sampling
     tp.guided = 0;
@@ -142,17 +143,41 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
                                       photonStates, nullptr, c->stream));
         *launches += 1;
     }
+    *tpOut = tp;
+    *statesOut = photonStates;
+    return PPPM_OK;
+}
+
+// Emission and every bounce of the subsurface photons into s.photons.
+static int sssPhotonLaunch(pppm_ctx* c, const TraceParams& tp, const SceneView& sv, const EnvDev& ev,
+                           const uint32_t* photonStates, PassCounters* ctr, int64_t* launches) {
+    SssState& s = c->rs.sss;
+    PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
+    const uint32_t* perm = nullptr;
+    const PathState* traced = nullptr;
+    int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, kPersistentPhotons, &traced, &perm, launches);
+    if (!e) e = tracePhotonsTo(c, tp, sv, tp.numPaths, s.photons.as<float4>(), s.cap, ctr, launches, traced, perm);
+    return e;
+}
+
+int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv, const EnvDev& ev, int64_t* launches) {
+    SssState& s = c->rs.sss;
+    RenderState& rs = c->rs;
+    const pppm_params& par = rs.par;
+    const int64_t paths = base.numPaths;
+    TraceParams tp;
+    uint32_t* photonStates = nullptr;
+    {
+        const int e = sssPhotonSetup(c, t, base, &tp, &photonStates, launches);
+        if (e) return e;
+    }
     PassCounters* ctr = rs.photonCount.as<PassCounters>();
     if (s.cap == 0) s.cap = std::max<int64_t>(paths, 1 << 16);
     PPPM_CUDA(c, s.photons.ensure((size_t)s.cap * 32));
 
     // the subsurface photon pass
-    PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
     {
-        const uint32_t* perm = nullptr;
-        const PathState* traced = nullptr;
-        int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, kPersistentPhotons, &traced, &perm, launches);
-        if (!e) e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches, traced, perm);
+        const int e = sssPhotonLaunch(c, tp, sv, ev, photonStates, ctr, launches);
         if (e) return e;
     }
 
@@ -177,12 +202,8 @@ int sssPrepare(pppm_ctx* c, int t, const TraceParams& base, const SceneView& sv,
         // grow and trace the same photons again (tapes and keys are unchanged)
         s.cap = (int64_t)(hc.deposits * 1.25) + 1024;
         PPPM_CUDA(c, s.photons.ensure((size_t)s.cap * 32));
-        PPPM_CUDA(c, cudaMemsetAsync(ctr, 0, sizeof(PassCounters), c->stream));
         {
-            const uint32_t* perm = nullptr;
-            const PathState* traced = nullptr;
-            int e = emitPhotonPaths(c, tp, ev, photonStates, ctr, kPersistentPhotons, &traced, &perm, launches);
-            if (!e) e = tracePhotonsTo(c, tp, sv, paths, s.photons.as<float4>(), s.cap, ctr, launches, traced, perm);
+            const int e = sssPhotonLaunch(c, tp, sv, ev, photonStates, ctr, launches);
             if (e) return e;
         }
         PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
@@ -240,6 +261,58 @@ OctView sssView(const pppm_ctx* c) {
 using namespace pppm;
 
 extern "C" {
+
+int pppm_subsurface_photons(pppm_ctx* c, const pppm_params* par, int32_t t, float* out, int64_t cap, int64_t* n) {
+    if (!c || !par || !n || t < 1 || cap < 0 || (cap > 0 && !out))
+        return fail(c, PPPM_E_ARG, "subsurface_photons: bad arguments");
+    if (par->mode != PPPM_MODE_COMPAT && par->mode != PPPM_MODE_CANONICAL)
+        return fail(c, PPPM_E_ARG, "subsurface_photons: compat or canonical mode");
+    pppm_params p = *par;
+    p.flags &= ~(PPPM_FLAG_LEARNED | PPPM_FLAG_LEARNED_FROZEN | PPPM_FLAG_SAMPLER_QMC);
+    const pppm_camera cam{{0.f, 0.f, 0.f}, {0.f, 0.f, 1.f}, {0.f, 1.f, 0.f}, 1.0f, 1, 1};
+    int r = pppm_render_begin(c, &cam, &p);
+    if (r) return r;
+    RenderState& rs = c->rs;
+    rs.active = false;  // a set-up for this stage only: no render pass follows
+    SssState& s = rs.sss;
+    if (!s.enabled) return fail(c, PPPM_E_STATE, "subsurface_photons: the scene has no BSSRDF material");
+    TraceParams base, tp;
+    CameraDev cd;
+    const int64_t paths = p.mode == PPPM_MODE_COMPAT ? rs.taskPerThread * p.num_streams : p.photons;
+    passSetup(c, t, paths, &base, &cd);
+    int64_t launches = 0;
+    uint32_t* photonStates = nullptr;
+    if ((r = sssPhotonSetup(c, t, base, &tp, &photonStates, &launches))) return r;
+    PassCounters* ctr = rs.photonCount.as<PassCounters>();
+    if (s.cap == 0) s.cap = std::max<int64_t>(paths, 1 << 16);
+    const SceneView sv = sceneView(c);
+    const EnvDev ev = envView(c);
+    for (int attempt = 0;; attempt++) {
+        PPPM_CUDA(c, s.photons.ensure((size_t)s.cap * 32));
+        if ((r = sssPhotonLaunch(c, tp, sv, ev, photonStates, ctr, &launches))) return r;
+        PassCounters hc;
+        PPPM_CUDA(c, cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
+        PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (hc.undefinedEmit)
+            return fail(c, PPPM_E_UNDEFINED, "subsurface_photons: a photon draw fell past the env CDF");
+        if ((int64_t)hc.deposits <= s.cap) {
+            s.stored = (int64_t)hc.deposits;
+            break;
+        }
+        if (attempt > 0) return fail(c, PPPM_E_CAPACITY, "subsurface_photons: photon overflow");
+        s.cap = (int64_t)(hc.deposits * 1.25) + 1024;
+    }
+    *n = s.stored;
+    const int64_t m = std::min(s.stored, cap);
+    if (m > 0) {
+        void* dout;
+        if ((r = stageOut(c, out, (size_t)m * 32, 0, &dout))) return r;
+        PPPM_CUDA(c, launchUnpackRecords(s.photons.as<float4>(), m, (float*)dout, c->stream));
+        if ((r = finishOut(c, out, dout, (size_t)m * 32))) return r;
+        PPPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return PPPM_OK;
+}
 
 int pppm_poisson_disk(pppm_ctx* c, const float* tri_xyz, int64_t ntri, double min_dist, uint32_t* rng_state,
                       float* pts, float* nrm, int64_t cap, int64_t* count) {

@@ -111,7 +111,47 @@ struct TraceParams {
     int eyePerSm = 16;     // eye kernel: blocks per SM (tunable)
     int guided;   // 1: learned proposal (emission direction; Lambertian bounces through kGuideResolve)
     GuideView guide;
+    // compat mode with the reference's RANDOM_SAMPLER_QUASI_MONTE_CARLO
+    // sampler: each stream s is Halton(200, true, s); per pass it serves its
+    // taskPerThread photons, then the pixels of its rows y = s, s + N, ...
+    int qmc = 0;
+    HaltonDev halton = {};
+    int width = 0, height = 0;  // image size (sample indices of the QMC streams)
 };
+
+// Halton sample index of pass tp.pass for stream s: the samples of earlier
+// passes (taskPerThread photons + the pixels of the stream's rows each),
+// then `offset` (photon round i, or taskPerThread + row k * width + x).
+__host__ __device__ inline unsigned long long qmcIndex(const TraceParams& tp, int s, int64_t offset) {
+    const int64_t rows = s < tp.height ? (tp.height - 1 - s) / tp.numStreams + 1 : 0;
+    return (unsigned long long)(tp.pass - 1) * (unsigned long long)(tp.taskPerThread + rows * tp.width) +
+           (unsigned long long)offset;
+}
+
+// The tape of a photon path between bounces, held in PathState.rng:
+// XorShift, the four state words; Halton, the sample index (two words), the
+// next dimension and the stream.
+__device__ __forceinline__ void loadTape(const TraceParams& tp, const PathState& p, Tape& t) {
+    t.pos = 0;
+    t.scramble = tp.mode == PPPM_MODE_CANONICAL;
+    t.x.s[0] = p.rng[0]; t.x.s[1] = p.rng[1]; t.x.s[2] = p.rng[2]; t.x.s[3] = p.rng[3];
+}
+__device__ __forceinline__ void loadTape(const TraceParams& tp, const PathState& p, HaltonTape& t) {
+    t.h = &tp.halton;
+    t.stream = (int)p.rng[3];
+    t.index = (unsigned long long)p.rng[0] | ((unsigned long long)p.rng[1] << 32);
+    t.dim = (int)p.rng[2];
+    t.over = false;
+}
+__device__ __forceinline__ void storeTape(const Tape& t, PathState& p) {
+    p.rng[0] = t.x.s[0]; p.rng[1] = t.x.s[1]; p.rng[2] = t.x.s[2]; p.rng[3] = t.x.s[3];
+}
+__device__ __forceinline__ void storeTape(const HaltonTape& t, PathState& p) {
+    p.rng[0] = (uint32_t)t.index;
+    p.rng[1] = (uint32_t)(t.index >> 32);
+    p.rng[2] = (uint32_t)t.dim;
+    p.rng[3] = (uint32_t)t.stream;
+}
 
 // PerspectiveCamera::getRay (perspective_camera.cc:42-46) in FP32.
 __device__ __forceinline__ void cameraRay(const CameraDev& c, float px, float py, f3* d) {
@@ -250,6 +290,10 @@ int guideEndPass(pppm_ctx* c, int t);
 
 // Classic PPM (k_classic.cu).
 int classicBegin(pppm_ctx* c, int64_t pixels);
+// Halton(200, true, s) tables of samplers s < streams (permutations, primes,
+// offsets) on the device, and their view (k_classic.cu).
+int haltonBegin(pppm_ctx* c, int streams);
+HaltonDev haltonDev(pppm_ctx* c);
 int classicPass(pppm_ctx* c, int t, const TraceParams& tp, const SceneView& sv, const EnvDev& ev, const CameraDev& cd,
                 pppm_pass_stats* stats);
 int classicRead(pppm_ctx* c, float* out);

@@ -307,12 +307,26 @@ public:
     const Hitpoint& hitpoint() const { return hp; }
 };
 
+namespace pppm {
+// A context of its own (device memory, stream, render state), released
+// with the last owner.
+inline std::shared_ptr<pppm_ctx> newContext() {
+    pppm_ctx* c = nullptr;
+    check(pppm_create(0, &c), nullptr, "pppm_create");
+    return std::shared_ptr<pppm_ctx>(c, [](pppm_ctx* x) { pppm_destroy(x); });
+}
+}  // namespace pppm
+
 class Scene {  // scene.h:23-56, scene.cc
     std::vector<float> tris_;
     std::vector<int32_t> matId_;
     std::vector<pppm_material> mats_;
     Envmap env_;
     bool accel_ = false;
+    // every Scene owns its GPU context: its triangles, BVH and env map live
+    // there, and integrators render a scene in the scene's own context, so
+    // several scenes coexist in one program (copies share the context)
+    std::shared_ptr<pppm_ctx> ctx_;
 
 public:
     template <class T>
@@ -328,14 +342,29 @@ public:
     }
     void setEnvmap(const Envmap& e) { env_ = e; }
     void setAccelerator() {
-        pppm_ctx* c = pppm::context();
+        if (!ctx_) ctx_ = pppm::newContext();
+        pppm_ctx* c = ctx_.get();
         pppm::check(pppm_scene_set(c, tris_.data(), (int64_t)matId_.size(), matId_.data(), mats_.data(),
                                    (int32_t)mats_.size()), c, "Scene::setAccelerator");
         if (!env_.rgb.empty())
             pppm::check(pppm_env_set(c, env_.rgb.data(), env_.width, env_.height), c, "Scene::setEnvmap");
         accel_ = true;
     }
+    // The scene's context (after setAccelerator; integrators render there).
+    pppm_ctx* context() const {
+        if (!accel_) throw pppm::Error(PPPM_E_STATE, "the scene has no accelerator: call setAccelerator first");
+        return ctx_.get();
+    }
     size_t numTriangles() const { return matId_.size(); }
+    Triangle getTriangle(int id) const {  // scene.h:52
+        const float* t = &tris_[9 * (size_t)id];
+        return Triangle(Vector3D(t[0], t[1], t[2]), Vector3D(t[3], t[4], t[5]), Vector3D(t[6], t[7], t[8]));
+    }
+    BSDF getBsdf(int id) const {  // scene.h:53
+        BSDF b;
+        b.m = mats_[(size_t)matId_[(size_t)id]];
+        return b;
+    }
     // Scene::intersect -> QBVHAccel::intersect (scene.cc:40-47)
     bool intersect(const Ray& ray, Intersection& isect) const {
         if (!accel_) throw pppm::Error(PPPM_E_STATE, "Scene::intersect before setAccelerator");
@@ -344,13 +373,75 @@ public:
         int32_t tri;
         double t;
         float pos[3], nrm[3];
-        pppm_ctx* c = pppm::context();
+        pppm_ctx* c = context();
         pppm::check(pppm_intersect(c, r, 1, &tri, &t, pos, nrm), c, "Scene::intersect");
         isect.id = tri;
         isect.hp.distance_ = t;
         isect.hp.position_ = Vector3D(pos[0], pos[1], pos[2]);
         isect.hp.normal_ = Vector3D(nrm[0], nrm[1], nrm[2]);
         return tri != -1;
+    }
+    // Many rays in one GPU call (the single-ray form waits for the GPU per ray).
+    void intersect(const std::vector<Ray>& rays, std::vector<Intersection>* out) const {
+        std::vector<float> r(rays.size() * 6);
+        for (size_t i = 0; i < rays.size(); i++)
+            for (int d = 0; d < 3; d++) {
+                r[6 * i + d] = (float)rays[i].origin()[d];
+                r[6 * i + 3 + d] = (float)rays[i].direction()[d];
+            }
+        std::vector<int32_t> tri(rays.size());
+        std::vector<double> t(rays.size());
+        std::vector<float> pos(rays.size() * 3), nrm(rays.size() * 3);
+        pppm_ctx* c = context();
+        pppm::check(pppm_intersect(c, r.data(), (int64_t)rays.size(), tri.data(), t.data(), pos.data(), nrm.data()), c,
+                    "Scene::intersect");
+        out->resize(rays.size());
+        for (size_t i = 0; i < rays.size(); i++) {
+            Intersection& x = (*out)[i];
+            x.id = tri[i];
+            x.hp.distance_ = t[i];
+            x.hp.position_ = Vector3D(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+            x.hp.normal_ = Vector3D(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+        }
+    }
+};
+
+// --------------------------------------------------------------- QBVH
+class QBVHAccel {  // qbvh_accel.h:24-67: construct + closest hit, on the GPU
+    std::shared_ptr<pppm_ctx> ctx_;
+    bool built_ = false;
+
+public:
+    // QBVHAccel::construct (qbvh_accel.cc:139-203): the reference's 4-wide
+    // topology, built on the host and uploaded to this accelerator's context.
+    void construct(const std::vector<Triangle>& triangles) {
+        if (!ctx_) ctx_ = pppm::newContext();
+        std::vector<float> tri(triangles.size() * 9);
+        for (size_t i = 0; i < triangles.size(); i++)
+            for (int k = 0; k < 3; k++)
+                for (int d = 0; d < 3; d++) tri[9 * i + 3 * k + d] = (float)triangles[i].p(k)[d];
+        const std::vector<int32_t> mid(triangles.size(), 0);
+        const pppm_material m = LambertianBRDF::factory(Vector3D(0.5, 0.5, 0.5)).m;
+        pppm::check(pppm_scene_set(ctx_.get(), tri.data(), (int64_t)triangles.size(), mid.data(), &m, 1), ctx_.get(),
+                    "QBVHAccel::construct");
+        built_ = true;
+    }
+    // QBVHAccel::intersect (qbvh_accel.cc:205-285): the closest triangle's
+    // index, or -1; hitpoint receives distance, position and normal.
+    int intersect(const Ray& ray, Hitpoint* hitpoint) const {
+        if (!built_) throw pppm::Error(PPPM_E_STATE, "QBVHAccel::intersect before construct");
+        const float r[6] = {(float)ray.origin().x(), (float)ray.origin().y(), (float)ray.origin().z(),
+                            (float)ray.direction().x(), (float)ray.direction().y(), (float)ray.direction().z()};
+        int32_t tri;
+        double t;
+        float pos[3], nrm[3];
+        pppm::check(pppm_intersect(ctx_.get(), r, 1, &tri, &t, pos, nrm), ctx_.get(), "QBVHAccel::intersect");
+        if (tri >= 0 && hitpoint) {
+            hitpoint->distance_ = t;
+            hitpoint->position_ = Vector3D(pos[0], pos[1], pos[2]);
+            hitpoint->normal_ = Vector3D(nrm[0], nrm[1], nrm[2]);
+        }
+        return tri;
     }
 };
 
@@ -387,6 +478,11 @@ public:
 };
 
 // --------------------------------------------------------------- integrator
+enum RandomSamplerType {  // random_sampler.h
+    RANDOM_SAMPLER_PSEUDO_RANDOM = 0,
+    RANDOM_SAMPLER_QUASI_MONTE_CARLO = 1
+};
+
 class ProgressivePhotonMappingProb {  // ppm_probabilistic.h:23-42
     std::vector<float> result_;
     int w_ = 0, h_ = 0, passes_ = 0;
@@ -400,13 +496,18 @@ public:
     // resultDirectory + "%03d.png", as the reference does with RESULT_DIRECTORY.
     std::string resultDirectory;
 
-    // ProgressivePhotonMappingProb::render (ppm_probabilistic.cc:24-121): the
-    // reference writes a PNG per pass; here the linear buffer stays on the
-    // GPU and result() returns buffer / passes after the call.
-    void render(const Scene& /*scene*/, const Camera& camera, const RenderParameters& params) {
-        pppm_ctx* ctx = pppm::context();
+    // ProgressivePhotonMappingProb::render (ppm_probabilistic.cc:24-121) in
+    // the scene's context: the reference writes a PNG per pass; here the
+    // linear buffer stays on the GPU and result() returns buffer / passes
+    // after the call. randomSamplerType as the reference's (:58-73): the
+    // quasi-Monte Carlo type gives stream i the sampler Halton(200, true, i)
+    // (compat mode only, as the reference has no canonical mode).
+    void render(const Scene& scene, const Camera& camera, const RenderParameters& params,
+                RandomSamplerType randomSamplerType = RANDOM_SAMPLER_PSEUDO_RANDOM) {
+        pppm_ctx* ctx = scene.context();
         pppm_params p{};
         p.mode = mode;
+        if (randomSamplerType == RANDOM_SAMPLER_QUASI_MONTE_CARLO) p.flags |= PPPM_FLAG_SAMPLER_QMC;
         p.num_streams = numStreams;
         p.photons = params.photons();
         p.gather_photons = params.gatherPhotons();
@@ -457,8 +558,8 @@ public:
 
     // ProgressivePhotonMapping::render (progressive_photon_mapping.cc:31-119):
     // result() returns the last pass's image.
-    void render(const Scene& /*scene*/, const Camera& camera, const RenderParameters& params) {
-        pppm_ctx* ctx = pppm::context();
+    void render(const Scene& scene, const Camera& camera, const RenderParameters& params) {
+        pppm_ctx* ctx = scene.context();
         pppm_params p{};
         p.mode = PPPM_MODE_CLASSIC;
         p.num_streams = numStreams;
@@ -493,11 +594,6 @@ public:
     int height() const { return h_; }
 };
 
-enum RandomSamplerType {  // random_sampler.h
-    RANDOM_SAMPLER_PSEUDO_RANDOM = 0,
-    RANDOM_SAMPLER_QUASI_MONTE_CARLO = 1
-};
-
 class PathTracing {  // path_tracing.h:20-37
     std::vector<float> result_;
     int w_ = 0, h_ = 0, passes_ = 0;
@@ -512,11 +608,11 @@ public:
     // PathTracing::render (path_tracing.cc:23-127) with the pseudo-random
     // sampler (the quasi-Monte Carlo one is not provided: PPPM_E_ARG);
     // bounceLimit 64 as executePathTracing's default.
-    void render(const Scene& /*scene*/, const Camera& camera, const RenderParameters& params,
+    void render(const Scene& scene, const Camera& camera, const RenderParameters& params,
                 RandomSamplerType randomSamplerType = RANDOM_SAMPLER_PSEUDO_RANDOM) {
         if (randomSamplerType != RANDOM_SAMPLER_PSEUDO_RANDOM)
             throw pppm::Error(PPPM_E_ARG, "PathTracing: only the pseudo-random sampler");
-        pppm_ctx* ctx = pppm::context();
+        pppm_ctx* ctx = scene.context();
         pppm_params p{};
         p.mode = PPPM_MODE_PATH_TRACING;
         p.num_streams = numStreams;
@@ -549,6 +645,119 @@ public:
     }
     int width() const { return w_; }
     int height() const { return h_; }
+};
+
+// --------------------------------------------------------------- subsurface
+namespace pppm {
+// The state of sampler::poissonDisk's process-wide XorShift (sampler.cc:
+// its static Random), XorShift(0) at program start (random.h:23-31).
+inline uint32_t* poissonRngState() {
+    static uint32_t st[4] = {0, 0, 0, 0};
+    static bool init = false;
+    if (!init) {
+        uint32_t v = 0;
+        for (int i = 1; i <= 4; i++) {
+            v = 1812433253u * (v ^ (v >> 30)) + (uint32_t)i;
+            st[i - 1] = v;
+        }
+        init = true;
+    }
+    return st;
+}
+}  // namespace pppm
+
+class SubsurfaceIntegrator {  // subsurface_integrator.h:40-130
+    std::vector<float> ipts_;  // per irradiance point: position, normal, area, irradiance (10 floats)
+    double maxError_ = 0.05;
+
+public:
+    // numStreams is the reference's OMP_NUM_CORE (the subsurface photon
+    // streams XorShift(time(NULL) + i)); sssTime, when non-zero, stands for
+    // time(NULL) so that a run can be repeated.
+    int numStreams = 8;
+    uint32_t sssTime = 0;
+
+    // SubsurfaceIntegrator::initialize (subsurface_integrator.cc:179-204) in
+    // the scene's context: Poisson-disc points on the BSSRDF triangles with
+    // the process-wide sampler state (sampler.cc:36-101), the subsurface
+    // photon map (buildPhotonMap, :240-327, streams seeded time(NULL) + i),
+    // the irradiance at the points (irradianceWithPM, :329-365). The octree
+    // over the points is built where irradiance() is evaluated. Resets any
+    // render active in the scene's context.
+    void initialize(const Scene& scene, const RenderParameters& params, double areaRadius, double maxError = 0.05) {
+        pppm_ctx* c = scene.context();
+        std::vector<float> tri;
+        double area4 = 0.0;
+        for (int i = 0; i < (int)scene.numTriangles(); i++) {
+            if (!(scene.getBsdf(i).type() & BSDF_TYPE_BSSRDF)) continue;
+            const Triangle t = scene.getTriangle(i);
+            for (int k = 0; k < 3; k++)
+                for (int d = 0; d < 3; d++) tri.push_back((float)t.p(k)[d]);
+            const Vector3D cr = Vector3D::cross(t.p(1) - t.p(0), t.p(2) - t.p(1));
+            area4 += std::ceil(4.0 * 0.5 * cr.norm() / (areaRadius * areaRadius));
+        }
+        if (tri.empty()) throw pppm::Error(PPPM_E_STATE, "The scene does not have subsurface scattering object!!");
+        const int64_t ntri = (int64_t)tri.size() / 9;
+        const int64_t cap = (int64_t)area4 + ntri + 16;
+        std::vector<float> pts((size_t)cap * 3), nrm((size_t)cap * 3);
+        int64_t m = 0;
+        pppm::check(pppm_poisson_disk(c, tri.data(), ntri, areaRadius, pppm::poissonRngState(), pts.data(), nrm.data(),
+                                      cap, &m), c, "SubsurfaceIntegrator::initialize");
+        maxError_ = maxError;
+        pppm_params p{};
+        p.mode = PPPM_MODE_COMPAT;
+        p.num_streams = numStreams;
+        p.photons = params.photons();
+        p.gather_photons = params.gatherPhotons();
+        p.gather_radius = params.gatherRadius();
+        p.max_bounce_photon = 64;
+        p.max_bounce_eye = 64;
+        p.alpha = 0.7;
+        p.radius_scale = 0.1;
+        p.cell_factor = 1.0f;
+        p.sss_time = sssTime ? sssTime : (uint32_t)std::time(nullptr);
+        int64_t np = 0;
+        pppm::check(pppm_subsurface_photons(c, &p, 1, nullptr, 0, &np), c, "SubsurfaceIntegrator::initialize");
+        std::vector<float> ph((size_t)std::max<int64_t>(np, 1) * 8);
+        pppm::check(pppm_subsurface_photons(c, &p, 1, ph.data(), np, &np), c, "SubsurfaceIntegrator::initialize");
+        std::vector<float> q6((size_t)m * 6), irad((size_t)m * 3);
+        for (int64_t i = 0; i < m; i++)
+            for (int d = 0; d < 3; d++) {
+                q6[6 * i + d] = pts[3 * i + d];
+                q6[6 * i + 3 + d] = nrm[3 * i + d];
+            }
+        if (m > 0)
+            pppm::check(pppm_subsurface_photon_irradiance(c, ph.data(), np, q6.data(), m, params.photons(),
+                                                          params.gatherRadius(), params.gatherPhotons(), irad.data()),
+                        c, "SubsurfaceIntegrator::initialize");
+        const double dA = (0.5 * areaRadius) * (0.5 * areaRadius) * 3.14159265358979323846;  // :199
+        ipts_.assign((size_t)m * 10, 0.0f);
+        for (int64_t i = 0; i < m; i++) {
+            float* o = &ipts_[10 * (size_t)i];
+            for (int d = 0; d < 3; d++) {
+                o[d] = pts[3 * i + d];
+                o[3 + d] = nrm[3 * i + d];
+                o[7 + d] = irad[3 * i + d];
+            }
+            o[6] = (float)dA;
+        }
+    }
+    size_t numPoints() const { return ipts_.size() / 10; }
+    // SubsurfaceIntegrator::irradiance (:234-238): (1/pi)(1 - Fdr) times the
+    // octree sum of Rd(d^2) E A (subsurface_integrator.cc:147-167).
+    Vector3D irradiance(const Vector3D& p, const BSDF& bsdf) const { return irradiance(std::vector<Vector3D>{p}, bsdf)[0]; }
+    std::vector<Vector3D> irradiance(const std::vector<Vector3D>& ps, const BSDF& bsdf) const {
+        if (!bsdf.m.has_bssrdf) throw pppm::Error(PPPM_E_ARG, "Specified object does not have BSSRDF!!");
+        std::vector<float> q(ps.size() * 3), rgb(ps.size() * 3);
+        for (size_t i = 0; i < ps.size(); i++)
+            for (int d = 0; d < 3; d++) q[3 * i + d] = (float)ps[i][d];
+        pppm_ctx* c = pppm::context();
+        pppm::check(pppm_dipole_irradiance(c, &bsdf.m, ipts_.data(), (int64_t)numPoints(), maxError_, q.data(),
+                                           (int64_t)ps.size(), rgb.data()), c, "SubsurfaceIntegrator::irradiance");
+        std::vector<Vector3D> out;
+        for (size_t i = 0; i < ps.size(); i++) out.emplace_back(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+        return out;
+    }
 };
 
 // --------------------------------------------------------------- photon map / hash grid
@@ -585,19 +794,118 @@ public:
     }
 };
 
+enum KnnSearchType {  // kdtree.h:8-11
+    EPSILON_BALL = PPPM_KNN_EPSILON_BALL,
+    K_NEAREST = PPPM_KNN_K_NEAREST
+};
+
+struct KnnQuery {  // kdtree.h:13-24
+    KnnSearchType type;
+    double epsilon;
+    int k;
+    KnnQuery(int type_, double epsilon_, int k_) : type(static_cast<KnnSearchType>(type_)), epsilon(epsilon_), k(k_) {}
+};
+
 template <class T>
-class HashGrid {  // hash_grid.h:8-37: bucket selection on the GPU
+class KdTree {  // kdtree.h:26-88: the search runs on the GPU over the hash grid
+    std::vector<T> points_;
+    std::vector<float> pos_;
+
+public:
+    void construct(const std::vector<T>& points) {  // kdtree_detail.h:53-87
+        points_ = points;
+        pos_.clear();
+        pos_.reserve(points.size() * 3);
+        for (const T& p : points)
+            for (int d = 0; d < 3; d++) pos_.push_back((float)p[d]);
+    }
+    void release() {
+        points_.clear();
+        pos_.clear();
+    }
+    // KdTree::knnSearch (kdtree_detail.h:88-132): the reference's result
+    // order (farthest first). At most 64 results per query; an
+    // EPSILON_BALL-only query with more points in its ball throws
+    // (PPPM_E_CAPACITY) instead of returning a partial set.
+    void knnSearch(const T& point, const KnnQuery& query, std::vector<T>* results) const {
+        const float q[3] = {(float)point[0], (float)point[1], (float)point[2]};
+        const int cap = 64;
+        std::vector<int32_t> idx(cap);
+        int32_t cnt = 0;
+        pppm_ctx* c = pppm::context();
+        pppm::check(pppm_kdtree_knn(c, pos_.data(), (int64_t)points_.size(), q, 1, (int32_t)query.type, query.epsilon,
+                                    query.k, idx.data(), &cnt, cap), c, "KdTree::knnSearch");
+        for (int i = 0; i < cnt && i < cap; i++) results->push_back(points_[(size_t)idx[i]]);
+    }
+};
+
+template <class T>
+class HashGrid {  // hash_grid.h:8-37; buckets built on the GPU (pppm_hashgrid_build)
     int size_ = -1;
     double scale_ = 0.0;
     double bbmin_[3] = {0, 0, 0};
+    std::vector<T> items_;
+    std::vector<double> lo_, hi_;
+    std::vector<std::vector<T>> data_;
+    bool built_ = false;
+
+    void build() {
+        pppm_ctx* c = pppm::context();
+        const int64_t n = (int64_t)items_.size();
+        int64_t cnt = 0;
+        pppm::check(pppm_hashgrid_build(c, lo_.data(), hi_.data(), n, size_, scale_, bbmin_, nullptr, nullptr, 0, &cnt),
+                    c, "HashGrid::add");
+        std::vector<uint32_t> start((size_t)size_ + 1);
+        std::vector<int32_t> ids((size_t)std::max<int64_t>(cnt, 1));
+        pppm::check(pppm_hashgrid_build(c, lo_.data(), hi_.data(), n, size_, scale_, bbmin_, start.data(), ids.data(),
+                                        cnt, &cnt), c, "HashGrid::add");
+        data_.assign((size_t)size_, {});
+        for (int b = 0; b < size_; b++)
+            for (uint32_t k = start[b]; k < start[(size_t)b + 1]; k++) data_[(size_t)b].push_back(items_[(size_t)ids[k]]);
+        built_ = true;
+    }
 
 public:
-    void init(int hashSize, double hashScale, const Vector3D& bbMin) {
+    // HashGrid::init (hash_grid_detail.h:26-31)
+    void init(int hashSize, double hashScale, const BBox& bbox) {
         size_ = hashSize;
         scale_ = hashScale;
-        for (int d = 0; d < 3; d++) bbmin_[d] = bbMin[d];
+        for (int d = 0; d < 3; d++) bbmin_[d] = bbox.posMin()[d];
+        clear();
     }
-    // bucket index of HashGrid::operator[] for each point
+    // HashGrid::add (hash_grid_detail.h:34-52): p enters every bucket of the
+    // cells the box covers; the buckets are formed on the GPU at the next
+    // operator[] after adds.
+    void add(const T& p, const Vector3D& boxMin, const Vector3D& boxMax) {
+        items_.push_back(p);
+        for (int d = 0; d < 3; d++) {
+            lo_.push_back(boxMin[d]);
+            hi_.push_back(boxMax[d]);
+        }
+        built_ = false;
+    }
+    void clear() {  // hash_grid_detail.h:54-57
+        items_.clear();
+        lo_.clear();
+        hi_.clear();
+        data_.clear();
+        built_ = false;
+    }
+    // HashGrid::operator[] (hash_grid_detail.h:65-72): the bucket of v's cell,
+    // items in the reference's insertion order
+    std::vector<T>& operator[](const Vector3D& v) {
+        if (size_ <= 0) throw pppm::Error(PPPM_E_STATE, "hash size is not initialized");
+        if (!built_) build();
+        return data_[(size_t)bucket(v)];
+    }
+    // The bucket of v's cell: |(int)((v - bbMin) * scale)| per axis and the
+    // reference's hash, in double like operator[] (hash_grid_detail.h:60-72).
+    uint32_t bucket(const Vector3D& v) const {
+        int c[3];
+        for (int d = 0; d < 3; d++) c[d] = std::abs(static_cast<int>((v[d] - bbmin_[d]) * scale_));
+        return ((uint32_t)c[0] * 73856093u ^ (uint32_t)c[1] * 19349663u ^ (uint32_t)c[2] * 83492791u) % (uint32_t)size_;
+    }
+    // buckets of many points (rounded to FP32) in one GPU call
     std::vector<uint32_t> buckets(const std::vector<Vector3D>& pts) const {
         std::vector<float> p;
         for (const auto& v : pts)

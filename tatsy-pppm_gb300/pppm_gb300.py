@@ -21,6 +21,8 @@ MODE_COMPAT, MODE_CANONICAL, MODE_CLASSIC, MODE_PATH_TRACING = 0, 1, 2, 3
 FLAG_COUNT_TRAVERSAL = 0x1
 FLAG_LEARNED = 0x2
 FLAG_LEARNED_FROZEN = 0x4
+FLAG_SAMPLER_QMC = 0x8  # compat mode: the reference's QMC sampler type (permuted Halton)
+KNN_EPSILON_BALL, KNN_K_NEAREST = 0x01, 0x02
 NOALLOC_MAX_PHOTONS = 1 << 17  # PPPM_NOALLOC_MAX_PHOTONS
 MLP_PARAMS = 16104  # PPPM_MLP_PARAMS
 
@@ -105,10 +107,15 @@ SIGNATURES = {
     "pppm_hash_points": ([_VP, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP], ctypes.c_int),
     "pppm_knn": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP,
                   ctypes.c_int32], ctypes.c_int),
+    "pppm_kdtree_knn": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
+                         ctypes.c_int32, _VP, _VP, ctypes.c_int32], ctypes.c_int),
+    "pppm_hashgrid_build": ([_VP, _VP, _VP, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _VP, _VP, _VP,
+                             ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_dipole_rd": ([_VP, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_render_graph": ([_VP, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_render_skip": ([_VP, ctypes.c_int32], ctypes.c_int),
     "pppm_render_image": ([_VP, ctypes.c_int32, _VP], ctypes.c_int),
+    "pppm_image_bytes": ([_VP, _VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_png_encode": ([_VP, ctypes.c_int32, ctypes.c_int32, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_render_save": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_render_load": ([_VP, _VP, ctypes.c_int64], ctypes.c_int),
@@ -117,6 +124,7 @@ SIGNATURES = {
                                ctypes.c_int),
     "pppm_poisson_disk": ([_VP, _VP, ctypes.c_int64, ctypes.c_double, _VP, _VP, _VP, ctypes.c_int64, _VP],
                           ctypes.c_int),
+    "pppm_subsurface_photons": ([_VP, _VP, ctypes.c_int32, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_subsurface_photon_irradiance": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int64,
                                            ctypes.c_double, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_halton": ([_VP, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32, _VP], ctypes.c_int),
@@ -133,6 +141,7 @@ SIGNATURES = {
     "pppm_render_read": ([_VP, _VP], ctypes.c_int),
     "pppm_render": ([_VP, _VP, _VP, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_render_photons": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
+    "pppm_render_queries": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_render_tune": ([_VP, ctypes.c_float, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
     "pppm_batch_create": ([ctypes.c_int, ctypes.POINTER(_VP)], ctypes.c_int),
     "pppm_batch_destroy": ([_VP], ctypes.c_int),
@@ -283,6 +292,31 @@ class Context:
                                               _ptr(out)))
         return out
 
+    def kdtree_knn(self, points, queries, type_, epsilon, k, cap=64):
+        """pppm_kdtree_knn: KdTree::knnSearch with KnnQuery(type, epsilon, k)."""
+        n, m = int(points.shape[0]), int(queries.shape[0])
+        idx = _empty_like_kind(queries, (m, cap), np.int32)
+        cnt = _empty_like_kind(queries, (m,), np.int32)
+        self._check(self.lib.pppm_kdtree_knn(self.h, _ptr(points), n, _ptr(queries), m, int(type_), float(epsilon),
+                                             int(k), _ptr(idx), _ptr(cnt), cap))
+        return idx, cnt
+
+    def hashgrid_build(self, boxmin, boxmax, hash_size, scale, bbmin):
+        """pppm_hashgrid_build (HashGrid::init + add over boxes): (start, items)
+        CSR bucket contents in the reference's insertion order."""
+        lo = np.ascontiguousarray(boxmin, np.float64).reshape(-1, 3)
+        hi = np.ascontiguousarray(boxmax, np.float64).reshape(-1, 3)
+        bm = np.ascontiguousarray(bbmin, np.float64).reshape(3)
+        n = ctypes.c_int64()
+        self._check(self.lib.pppm_hashgrid_build(self.h, lo.ctypes.data, hi.ctypes.data, len(lo), int(hash_size),
+                                                 float(scale), bm.ctypes.data, None, None, 0, ctypes.byref(n)))
+        start = np.zeros(int(hash_size) + 1, np.uint32)
+        items = np.zeros(max(n.value, 1), np.int32)
+        self._check(self.lib.pppm_hashgrid_build(self.h, lo.ctypes.data, hi.ctypes.data, len(lo), int(hash_size),
+                                                 float(scale), bm.ctypes.data, start.ctypes.data, items.ctypes.data,
+                                                 n.value, ctypes.byref(n)))
+        return start, items[: n.value]
+
     def knn(self, photon_pos, queries, num_target_photons, target_radius, cap=64):
         n, m = int(photon_pos.shape[0]), int(queries.shape[0])
         idx = _empty_like_kind(queries, (m, cap), np.int32)
@@ -350,6 +384,15 @@ class Context:
         self._check(self.lib.pppm_mlp_grad(self.h, prm.ctypes.data, rec.ctypes.data, rec.shape[0], bb.ctypes.data,
                                            grad.ctypes.data, ctypes.byref(loss)))
         return loss.value, grad
+
+    def subsurface_photons(self, params, t=1):
+        """pppm_subsurface_photons: the subsurface photon map (n x 8 floats)."""
+        n = ctypes.c_int64()
+        self._check(self.lib.pppm_subsurface_photons(self.h, ctypes.byref(params), int(t), None, 0, ctypes.byref(n)))
+        out = np.zeros((max(n.value, 1), 8), np.float32)
+        self._check(self.lib.pppm_subsurface_photons(self.h, ctypes.byref(params), int(t), out.ctypes.data, n.value,
+                                                     ctypes.byref(n)))
+        return out[: n.value]
 
     def subsurface_photon_irradiance(self, photons8, points6, num_photons, gather_radius, gather_photons):
         ph = np.ascontiguousarray(photons8, np.float32).reshape(-1, 8)
@@ -429,6 +472,15 @@ class Context:
         self._check(self.lib.pppm_render_image(self.h, 1 if tonemap else 0, out.ctypes.data))
         return out
 
+    def image_bytes(self, accum, passes, tonemap=False):
+        """pppm_image_bytes: the reference's output bytes of an explicit H x W x 3 accumulator."""
+        acc = np.ascontiguousarray(accum, np.float32)
+        h, w = acc.shape[:2]
+        out = np.zeros((h, w, 3), np.uint8)
+        self._check(self.lib.pppm_image_bytes(self.h, acc.ctypes.data, w, h, int(passes), 1 if tonemap else 0,
+                                              out.ctypes.data))
+        return out
+
     def render_save(self):
         """pppm_render_save: the checkpoint as bytes."""
         n = ctypes.c_int64()
@@ -464,6 +516,15 @@ class Context:
         out = np.zeros((cap, 8), np.float32)
         n = ctypes.c_int64()
         self._check(self.lib.pppm_render_photons(self.h, out.ctypes.data, cap, ctypes.byref(n)))
+        return out[: n.value]
+
+    def render_queries(self):
+        """pppm_render_queries: the last pass's gather queries, n x 12 floats
+        (position, pixel bits, oriented normal, 0, weight, 0)."""
+        n = ctypes.c_int64()
+        self._check(self.lib.pppm_render_queries(self.h, None, 0, ctypes.byref(n)))
+        out = np.zeros((max(n.value, 1), 12), np.float32)
+        self._check(self.lib.pppm_render_queries(self.h, out.ctypes.data, n.value, ctypes.byref(n)))
         return out[: n.value]
 
 

@@ -125,6 +125,26 @@ def gen_hash():
     save("hash", **out)
 
 
+def gen_hash_boxes():
+    """HashGrid<int>::add over boxes (hash_grid_detail.h:34-52): bucket
+    contents in insertion order, from the reference. Boxes of render-point
+    size, boxes reaching below bbmin (|(int)x| folding, empty axes), single
+    cells and a table small enough that one item's cells share buckets."""
+    rng = np.random.default_rng(9)
+    out = {}
+    for k, (size, scale, n, half) in enumerate([(4096, 0.5, 3000, 1.5), (65536, 1.0 / 0.37, 5000, 0.4),
+                                                  (97, 2.0, 400, 1.2), (256 * 256, 1.0 / 1.6, 2000, 0.0)]):
+        bbmin = rng.uniform(-30, -10, 3)
+        bbmax = rng.uniform(10, 30, 3)
+        c = rng.uniform(bbmin - 3.0, bbmax, (n, 3))
+        h = rng.uniform(0, half, (n, 3)) if half > 0 else np.zeros((n, 3))
+        lo, hi = c - h, c + h
+        start, items = rh.hash_add_boxes(size, scale, bbmin, bbmax, lo, hi)
+        out.update({f"bbmin{k}": bbmin, f"size{k}": np.array(size), f"scale{k}": np.array(scale), f"lo{k}": lo,
+                    f"hi{k}": hi, f"start{k}": start, f"items{k}": items})
+    save("hash_boxes", **out)
+
+
 def gen_rng():
     out = {}
     for s in (0, 1, 7, 123456789):
@@ -187,6 +207,21 @@ def gen_knn():
     save("knn", **out)
 
 
+def gen_kdtree_knn():
+    """KdTree::knnSearch (kdtree_detail.h:88-132) with each KnnQuery type:
+    K_NEAREST | EPSILON_BALL, K_NEAREST alone (unbounded ball) and
+    EPSILON_BALL alone (every point within epsilon), on surface photons."""
+    rng = np.random.default_rng(12)
+    pos = surface_photons(rng, 30000)[0]
+    q = (pos[rng.integers(0, len(pos), 3000)] + rng.normal(size=(3000, 3)) * 0.3).astype(np.float32)
+    out = {"pos": pos, "queries": q}
+    for k, (t, eps, kk) in enumerate([(3, 2.5, 12), (2, 0.0, 20), (1, 0.35, 0), (3, 0.8, 64)]):
+        idx, cnt = rh.kdtree_knn(pos, q, t, eps, kk, cap=64)
+        out.update({f"type{k}": np.array(t), f"eps{k}": np.array(eps), f"k{k}": np.array(kk), f"idx{k}": idx,
+                    f"cnt{k}": cnt})
+    save("kdtree_knn", **out)
+
+
 def gen_gather():
     """radiance() at bounce 0 on a Lambertian ground plane (y = -5): rays
     straight down from y = 10 hit at float-exact points (x, -5, z), so the
@@ -242,6 +277,17 @@ def gen_render():
          photon_count=np.array(res["photon_count"]), eye=np.array(cam.eye), dir=np.array(cam.dir), up=np.array(cam.up),
          fov=np.array(cam.fov), wh=np.array([cam.width, cam.height]), nphotons=np.array(sc.photons),
          threads=np.array(rh.num_threads()))
+
+
+def gen_render_qmc():
+    """The same two passes with the QMC sampler type (Halton(200, true, i)
+    per thread, ppm_probabilistic.cc:58-73)."""
+    sc = S.small_test_scene(seed=3, subdiv=3, width=64, height=48, photons=20000)
+    sc.env = quantize_env(sc.env)
+    R = rh.RefScene(sc)
+    res = R.render_passes(sc.camera, sc.photons, 2, photon_cap=200000, qmc=True)
+    save("render_qmc", accum=res["accum"], radii=res["radii"], photons=res["photons"],
+         photon_count=np.array(res["photon_count"]), threads=np.array(rh.num_threads()))
 
 
 def gen_dipole():
@@ -345,6 +391,17 @@ def gen_sss_render():
          nphotons=np.array(sc.photons), threads=np.array(rh.num_threads()), sss_time=np.array(1234567))
 
 
+def gen_sss_photons():
+    """SubsurfaceIntegrator::buildPhotonMap alone, with time(NULL) = 7654321
+    (its photon streams are XorShift(time + i)), N = 8."""
+    sc = S.small_sss_scene()
+    sc.env = quantize_env(sc.env)
+    R = rh.RefScene(sc)
+    ph = R.sss_photons(sc.photons, 7654321)
+    save("sss_photons", photons=ph, nphotons=np.array(sc.photons), sss_time=np.array(7654321),
+         threads=np.array(rh.num_threads()))
+
+
 def gen_classic():
     """Classic PPM (ProgressivePhotonMapping) with one OpenMP thread: with
     more threads its render-point updates run under a lock in an order that
@@ -388,6 +445,27 @@ def gen_path_trace_sss():
     save("path_trace_sss", **a, accum=acc, eye=np.array(cam.eye), dir=np.array(cam.dir), up=np.array(cam.up),
          fov=np.array(cam.fov), wh=np.array([cam.width, cam.height]), nphotons=np.array(sc.photons),
          threads=np.array(rh.num_threads()), sss_time=np.array(1234567))
+
+
+def gen_image():
+    """The reference's output bytes (Image::tonemap / gamma(2.2, true) /
+    toByte through rh_image_bytes) of fixed FP32 accumulation buffers:
+    rendered-like lognormal values, zeros, saturating values, values right at
+    byte boundaries and, for the gamma-only path, negatives, NaN and inf."""
+    rng = np.random.default_rng(21)
+    h, w, t = 40, 56, 3
+    acc = (rng.lognormal(-1.0, 1.2, (h, w, 3)) * t).astype(np.float32)
+    acc[:4] = 0.0
+    acc[4:6] = np.float32(t * 1.5)  # above 1 after division: saturates
+    # exact byte boundaries k / 255 before gamma correction: (k/255)^2.2 * t
+    k = rng.integers(1, 255, (2, w, 3))
+    acc[6:8] = ((k / 255.0) ** 2.2 * t).astype(np.float32)
+    tone = acc.copy()
+    acc[8, :8, 0] = [-1.0, -0.0, np.nan, np.inf, -np.inf, 1e-30, 3e38, 1e-45]
+    ref_gamma, val_gamma = rh.image_bytes(acc.astype(np.float64), t, tonemap=False)
+    ref_tone, val_tone = rh.image_bytes(tone.astype(np.float64), t, tonemap=True)
+    save("image", acc_gamma=acc, bytes_gamma=ref_gamma, vals_gamma=val_gamma, acc_tonemap=tone,
+         bytes_tonemap=ref_tone, vals_tonemap=val_tone, passes=np.array(t))
 
 
 def ply_bytes(verts, faces, counts=None, header_extra=(), vertex_props=("x", "y", "z"), trailer=b""):
@@ -460,7 +538,9 @@ def gen_ply():
 
 
 GENERATORS.update({"knn": gen_knn, "gather": gen_gather, "render": gen_render, "dipole": gen_dipole,
-                   "sss_irradiance": gen_sss_irradiance, "path_trace": gen_path_trace, "ply": gen_ply})
+                   "sss_irradiance": gen_sss_irradiance, "path_trace": gen_path_trace, "ply": gen_ply,
+                   "image": gen_image, "render_qmc": gen_render_qmc, "hash_boxes": gen_hash_boxes,
+                   "kdtree_knn": gen_kdtree_knn, "sss_photons": gen_sss_photons})
 # generators that need a fresh process (process-wide reference RNG state)
 FRESH = {"poisson": gen_poisson, "render_sss": gen_sss_render, "classic": gen_classic,
          "path_trace_sss": gen_path_trace_sss}

@@ -1,0 +1,173 @@
+"""Element-wise parity of one PPM-APA pass (GPU library against the oracle
+port at the same inputs and random numbers), shared by the whole-pass tests.
+
+The two sides follow the same random numbers; FP32 shading (GPU) and FP64
+shading (port) differ only in rounding. Every element gets a bound, and
+every element outside 1e-5 is listed with its cause:
+
+* photon records: each GPU record is matched to the port record at the same
+  position (1e-3); its flux must agree within 1e-5. Causes listed:
+  - "diverged": a path whose ray crossed a triangle edge differently on the
+    two sides leaves the port's path from that bounce on; all its later
+    records are unmatched (a record unmatched while a later record of the
+    same path matches again would be an error: none are allowed);
+  - "emission texel edge": a path whose emission direction lies on an
+    environment texel edge takes the neighbouring texel's radiance in FP32,
+    so every record of the path carries the same flux factor against the
+    port (checked: one factor per path, for all its records).
+* eye queries (the Lambertian hit point each pixel gathers at): per pixel,
+  position within 1e-4 relative, normal within the FP32 cross product's
+  error for the hit triangle (8 u |v|max |e|max / |e1 x e2|, u = 2^-24), and
+  path weight within 1e-5 (1 + b), b = specular/refractive bounces before
+  the hit (each adds FP32 Fresnel and direction rounding). Pixels where only
+  one side gathers, or both at different points, are "eye diverged".
+* per-hit-point radiance: every GPU query's radiance (its pixel in the
+  one-pass image) against the float64 gather of the GPU's own photon map at
+  the GPU's own query: within max(1e-5, gamma_n) relative, gamma_n = n u /
+  (1 - n u) the bound of an FP32 sum of the n photons gathered, where no
+  photon is ambiguous (on the sphere within 1e-5 relative in r^2, or a
+  normal within 1e-3 of perpendicular); else between the certain and the
+  certain + ambiguous sums. No other exception is allowed.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+PHOTON_RTOL = 1e-5
+QUERY_RTOL = 1e-5
+RADIANCE_RTOL = 1e-5
+U32 = 2.0 ** -24
+
+
+def unpack_normals(bits):
+    """Photon record normals (2 x 16-bit octahedral, as the GPU unpacks them)."""
+    p = np.asarray(bits, np.float32).view(np.uint32)
+    u = (p & 0xFFFF).astype(np.float32) / np.float32(65535.0) * np.float32(2.0) - np.float32(1.0)
+    v = (p >> 16).astype(np.float32) / np.float32(65535.0) * np.float32(2.0) - np.float32(1.0)
+    z = np.float32(1.0) - np.abs(u) - np.abs(v)
+    neg = z < 0
+    ou = u.copy()
+    u = np.where(neg, (1 - np.abs(v)) * np.where(ou >= 0, 1, -1), u).astype(np.float32)
+    v = np.where(neg, (1 - np.abs(ou)) * np.where(v >= 0, 1, -1), v).astype(np.float32)
+    n = np.stack([u, v, z], 1).astype(np.float64)
+    return n / np.linalg.norm(n, axis=1, keepdims=True)
+
+
+def photon_parity(gpu, ref_ph):
+    """gpu: n x 8 GPU records (pos, flux, packed normal, path id bits) in
+    buffer order (each path's records in bounce order); ref_ph: port records
+    (pos, flux, ...). Returns counts by cause; 'unexplained' and
+    'isolated_mismatches' must be 0."""
+    from scipy.spatial import cKDTree
+
+    tree = cKDTree(ref_ph[:, :3])
+    dist, j = tree.query(gpu[:, :3].astype(np.float64))
+    rflux = ref_ph[j, 3:6]
+    pos_ok = dist < 1e-3
+    ferr = np.max(np.abs(gpu[:, 3:6] - rflux) / np.maximum(np.abs(rflux), 1e-30), axis=1)
+    flux_ok = ferr <= PHOTON_RTOL
+    ok = pos_ok & flux_ok
+    pid = gpu[:, 7].view(np.int32).astype(np.int64)
+    order = np.lexsort((np.arange(len(gpu)), pid))  # bounce order within each path
+    ps, pos_ok_o = pid[order], pos_ok[order]
+    start = np.r_[True, ps[1:] != ps[:-1]]
+    seg = np.cumsum(start) - 1
+    # diverged: the first record at another position; every later record of
+    # the path must be elsewhere too
+    bad = ~pos_ok_o
+    big = np.iinfo(np.int64).max
+    first_bad = np.full(seg[-1] + 1 if len(seg) else 0, big)
+    np.minimum.at(first_bad, seg[bad], np.flatnonzero(bad))
+    isolated = np.flatnonzero((np.arange(len(order)) > first_bad[seg]) & pos_ok_o)
+    # emission texel edge: all records of the path at the same positions, all
+    # carrying one flux factor (per channel) against the port
+    off = pos_ok & ~flux_ok
+    ratio = gpu[:, 3:6].astype(np.float64) / np.maximum(np.abs(rflux), 1e-30) * np.sign(rflux)
+    texel, unexplained = [], []
+    for path in np.unique(pid[off]):
+        recs = np.flatnonzero(pid == path)
+        rr = ratio[recs][pos_ok[recs]]
+        same = np.all(np.abs(rr - rr[0]) <= 1e-5 * np.abs(rr[0]) + 1e-12)
+        whole = np.all(~flux_ok[recs][pos_ok[recs]])
+        (texel if same and whole else unexplained).append(int(path))
+    return {"records": len(gpu), "port_records": len(ref_ph), "matched_within_1e-5": int(ok.sum()),
+            "diverged": int((~pos_ok).sum()), "paths_diverged": int((first_bad < big).sum()),
+            "emission_texel_edge_records": int((off & np.isin(pid, texel)).sum()),
+            "emission_texel_edge_paths": len(texel), "unexplained_paths": unexplained[:20],
+            "unexplained": len(unexplained), "isolated_mismatches": int(isolated.size),
+            "flux_err_max_matched": float(ferr[ok].max()) if ok.any() else 0.0}
+
+
+def _normal_bound(tris9, tri_id):
+    """FP32 error of a unit normal from the cross product of float edges."""
+    t = tris9[tri_id].astype(np.float64).reshape(-1, 3, 3)
+    e1, e2 = t[:, 1] - t[:, 0], t[:, 2] - t[:, 0]
+    cr = np.linalg.norm(np.cross(e1, e2), axis=1)
+    emax = np.maximum(np.linalg.norm(e1, axis=1), np.linalg.norm(e2, axis=1))
+    vmax = np.abs(t).reshape(-1, 9).max(1)
+    return 8.0 * U32 * vmax * emax / np.maximum(cr, 1e-300) + 1e-6
+
+
+def query_parity(gq, port_q, width, height, tris9):
+    """gq: GPU queries (n x 12 floats); port_q: H*W x 12 doubles (flag at 11).
+    Returns counts by cause and the mask of GPU queries whose eye paths match."""
+    pix = gq[:, 3].view(np.int32).astype(np.int64)
+    bounces = gq[:, 7].view(np.int32).astype(np.int64)
+    tri = gq[:, 11].view(np.int32).astype(np.int64)
+    has_port = port_q[:, 11] > 0
+    has_gpu = np.zeros(width * height, bool)
+    has_gpu[pix] = True
+    pq = port_q[pix]
+    same_pos = pq[:, 11] > 0
+    same_pos &= np.all(np.abs(gq[:, :3] - pq[:, :3]) <= 1e-4 * np.maximum(1.0, np.abs(pq[:, :3])), axis=1)
+    werr = np.max(np.abs(gq[:, 8:11] - pq[:, 8:11]) / np.maximum(np.abs(pq[:, 8:11]), 1e-30), axis=1)
+    nerr = np.max(np.abs(gq[:, 4:7] - pq[:, 4:7]), axis=1)
+    nbound = _normal_bound(tris9, tri)
+    w_exact, n_exact = werr <= QUERY_RTOL, nerr <= 1e-5
+    w_ok = werr <= QUERY_RTOL * (1 + bounces)
+    n_ok = nerr <= np.maximum(nbound, 1e-5)
+    same = same_pos & (pq[:, 3].astype(np.int64) == tri) & (pq[:, 7].astype(np.int64) == bounces)
+    match = same & w_ok & n_ok
+    res = {"pixels": width * height, "gpu_queries": len(gq), "port_queries": int(has_port.sum()),
+           "matched": int(match.sum()), "matched_within_1e-5": int((same & w_exact & n_exact).sum()),
+           "weight_within_bounce_bound": int((same & w_ok & ~w_exact).sum()),
+           "normal_within_triangle_bound": int((same & n_ok & ~n_exact).sum()),
+           "eye_diverged_gpu_only": int((has_gpu & ~has_port).sum()),
+           "eye_diverged_port_only": int((~has_gpu & has_port).sum()),
+           "eye_diverged_other_hit_point": int((pq[:, 11] > 0).sum() - same.sum()),
+           "outside_bounds": int((same & ~(w_ok & n_ok)).sum()),
+           "outside_detail": [(float(werr[i]), int(bounces[i]), float(nerr[i]), float(nbound[i]))
+                              for i in np.flatnonzero(same & ~(w_ok & n_ok))[:20]]}
+    return res, match
+
+
+def radiance_parity(img, gq, gpu_ph, radius):
+    """Per-hit-point radiance of a one-pass image: every GPU query's pixel
+    against the float64 gather bounds of the GPU's own photon map at that
+    query (oracle port, port_gather_bounds). Returns counts; 'outside_bound'
+    must be 0."""
+    import port
+
+    pix = gq[:, 3].view(np.int32).astype(np.int64)
+    ph9 = np.zeros((len(gpu_ph), 9))
+    ph9[:, :6] = gpu_ph[:, :6]
+    ph9[:, 6:9] = unpack_normals(gpu_ph[:, 6])
+    q12 = np.zeros((len(gq), 12))
+    q12[:, :3] = gq[:, :3]
+    q12[:, 3:6] = gq[:, 4:7]
+    q12[:, 6:9] = gq[:, 8:11]
+    q12[:, 9:12] = 1.0
+    lo, hi, ref, amb, inside = port.gather_bounds(ph9, q12, radius)
+    out = img.reshape(-1, 3)[pix].astype(np.float64)
+    # FP32 sum of n photons, the normalisation and the weight product
+    nu = (inside + amb + 4).astype(np.float64)[:, None] * U32
+    rtol = np.maximum(RADIANCE_RTOL, nu / (1.0 - nu))
+    floor = 1e-6 * max(np.abs(ref).max(), 1e-30)
+    within = np.all((out >= lo - rtol * np.abs(lo) - floor) & (out <= hi + rtol * np.abs(hi) + floor), axis=1)
+    exact = np.all(np.abs(out - ref) <= RADIANCE_RTOL * np.abs(ref) + floor, axis=1)
+    summed = np.all(np.abs(out - ref) <= rtol * np.abs(ref) + floor, axis=1)
+    return {"queries": len(gq), "within_1e-5": int(exact.sum()),
+            "within_fp32_sum_bound": int((~exact & summed).sum()),
+            "within_ambiguity_bound": int((~summed & within).sum()),
+            "outside_bound": int((~within).sum()), "queries_with_ambiguous_photons": int((amb > 0).sum()),
+            "max_photons_gathered": int(inside.max()) if len(inside) else 0}

@@ -127,3 +127,31 @@ def test_render_sss_rejects_small_gather_radius():
         assert e.value.code == P.E_UNDEFINED
     finally:
         c.close()
+
+
+def test_subsurface_photons_match_reference(ctx, golden):
+    """pppm_subsurface_photons (SubsurfaceIntegrator::buildPhotonMap, the
+    stage the host mirror's SubsurfaceIntegrator::initialize calls) against
+    the reference's photon map with the same time(NULL): the same records
+    but where FP32 shading moves a photon path across an edge."""
+    from scipy.spatial import cKDTree
+
+    g = golden("render_sss")
+    q = golden("sss_photons")
+    mats = g["mats"].reshape(-1).view(S.MATERIAL_DTYPE)
+    cam = S.Camera(tuple(g["eye"]), tuple(g["dir"]), tuple(g["up"]), float(g["fov"]), int(g["wh"][0]), int(g["wh"][1]))
+    sc = S.Scene("sss", g["tris"], g["mat_id"], mats, g["env"], cam, photons=int(q["nphotons"]))
+    ctx.set_scene(sc)
+    par = P.Context.make_params(mode=P.MODE_COMPAT, photons=sc.photons, num_streams=int(q["threads"]),
+                                sss_time=int(q["sss_time"]))
+    gpu = ctx.subsurface_photons(par)
+    ref = q["photons"]
+    assert abs(len(gpu) - len(ref)) <= 0.02 * len(ref)
+    dist, j = cKDTree(ref[:, :3]).query(gpu[:, :3].astype(np.float64))
+    rflux = ref[j, 3:6]
+    match = (dist < 1e-3) & np.all(np.abs(gpu[:, 3:6] - rflux) <= 1e-4 * np.abs(rflux) + 1e-12, axis=1)
+    print(f"subsurface photons: {len(gpu)} vs {len(ref)}, matched {match.mean():.4f}")
+    assert match.mean() > 0.98
+    # the stage ended any render of the context: a pass now needs render_begin
+    with pytest.raises(P.PppmError):
+        ctx.render_pass(1)

@@ -168,6 +168,63 @@ def _canonical_np(ph8, nrm, q12, r):
     return out
 
 
+# A photon is ambiguous for a query when the FP32 test may legitimately
+# decide it the other way than the float64 restatement: its squared
+# distance within 1e-5 relative of r^2 (FP32 rounding of the distance), or
+# its normal within 1e-3 of perpendicular to the query's (the photon record
+# stores the normal in 2 x 16-bit octahedral form, error ~1e-4).
+D2_BAND, NORMAL_BAND = 1e-5, 1e-3
+
+
+def _canonical_bounds(ph8, nrm, q12, r):
+    """float64 bounds of each query's canonical gather: lo sums the photons
+    that are inside for certain, hi adds the ambiguous ones (fluxes are
+    non-negative). Also the exact restatement and the ambiguous count."""
+    m = len(q12)
+    lo, hi, ref = np.zeros((m, 3)), np.zeros((m, 3)), np.zeros((m, 3))
+    amb = np.zeros(m, np.int64)
+    pos, flux = ph8[:, :3].astype(np.float64), ph8[:, 3:6].astype(np.float64)
+    r2 = r * r
+    for i in range(m):
+        d2 = ((pos - q12[i, :3].astype(np.float64)) ** 2).sum(1)
+        c = nrm @ q12[i, 3:6].astype(np.float64)
+        sure = (d2 < r2 * (1 - D2_BAND)) & (c > NORMAL_BAND)
+        maybe = (np.abs(d2 - r2) <= D2_BAND * r2) & (c > -NORMAL_BAND) | (d2 < r2 * (1 + D2_BAND)) & (
+            np.abs(c) <= NORMAL_BAND)
+        maybe &= ~sure
+        w = q12[i, 6:9].astype(np.float64) * q12[i, 9:12] / (np.pi * np.pi * r2)
+        lo[i] = w * flux[sure].sum(0)
+        hi[i] = lo[i] + w * flux[maybe].sum(0)
+        ref[i] = w * flux[(d2 < r2) & (c > 0)].sum(0)
+        amb[i] = int(maybe.sum())
+    return lo, hi, ref, amb
+
+
+def check_canonical_gather(out, ph8, nrm, q12, r, name=""):
+    """Per-query bound (no blanket allowance): a query with no ambiguous
+    photon must match the float64 restatement within RTOL (plus an absolute
+    floor of 1e-6 of the largest value for float sums of ~zero); a query with
+    ambiguous photons must lie between its certain-photon sum and that sum
+    plus every ambiguous photon, within the same tolerance. Every query
+    that differs from the restatement is listed with its cause."""
+    lo, hi, ref, amb = _canonical_bounds(ph8, nrm, q12, r)
+    out = np.asarray(out, np.float64)
+    floor = 1e-6 * max(np.abs(ref).max(), 1e-30)
+    tol_lo = RTOL * np.abs(lo) + floor
+    tol_hi = RTOL * np.abs(hi) + floor
+    within = np.all((out >= lo - tol_lo) & (out <= hi + tol_hi), axis=1)
+    exact = np.all(np.abs(out - ref) <= RTOL * np.abs(ref) + floor, axis=1)
+    bad = np.flatnonzero(~within)
+    assert bad.size == 0, (name, bad[:10], out[bad[:3]], lo[bad[:3]], hi[bad[:3]])
+    clean_off = np.flatnonzero(~exact & (amb == 0))
+    assert clean_off.size == 0, (name, clean_off[:10])
+    listed = np.flatnonzero(~exact)
+    print(f"canonical gather {name}: {len(out)} queries, {listed.size} differ from the float64 restatement, "
+          f"each within its bound by ambiguous photons (boundary distance or perpendicular normal): "
+          f"{listed[:20].tolist()}")
+    return listed
+
+
 def pack_normals(n):
     """Octahedral 2x16-bit packing used by photon records (pppm_device.cuh)."""
     n = n / np.abs(n).sum(1, keepdims=True)
@@ -196,8 +253,44 @@ def test_gather_canonical(ctx, golden, r):
     qn /= np.linalg.norm(qn, axis=1, keepdims=True)
     q = np.concatenate([qp, qn, rng.uniform(0.2, 0.9, (m, 3)), rng.uniform(0.5, 2, (m, 3))], 1).astype(np.float32)
     out = ctx.gather(1, ph8, q, r)
-    ref = _canonical_np(ph8, ph12[:, 9:12].astype(np.float64), q, r)
-    scale = np.abs(ref).max()
-    ok = np.all(np.abs(out - ref) <= RTOL * np.abs(ref) + 1e-6 * scale, axis=1)
-    # boundary photons (|d - r| < 1e-5 r) or normals within the packing error of perpendicular may flip
-    assert ok.mean() > 0.99, ok.mean()
+    check_canonical_gather(out, ph8, ph12[:, 9:12].astype(np.float64), q, r, f"golden photons r={r}")
+
+
+@pytest.mark.parametrize("case", [0, 1, 2, 3])
+def test_hashgrid_add_matches_reference(ctx, golden, case):
+    """HashGrid::init + add over boxes (hash_grid_detail.h:26-52): every
+    bucket's items, in the reference's insertion order, bit for bit."""
+    g = golden("hash_boxes")
+    start, items = ctx.hashgrid_build(g[f"lo{case}"], g[f"hi{case}"], int(g[f"size{case}"]), float(g[f"scale{case}"]),
+                                      g[f"bbmin{case}"])
+    assert np.array_equal(start.astype(np.int64), g[f"start{case}"].astype(np.int64))
+    assert np.array_equal(items, g[f"items{case}"])
+
+
+@pytest.mark.parametrize("case", [0, 1, 2, 3])
+def test_kdtree_knn_matches_reference(ctx, golden, case):
+    """KdTree::knnSearch with KnnQuery(type, epsilon, k) (kdtree_detail.h:
+    88-132): the same sets in the same (farthest-first) order, except
+    near-equal distances at the k-th neighbour or at epsilon (FP32 against
+    the reference's double distances), which are listed."""
+    g = golden("kdtree_knn")
+    pos, q = g["pos"], g["queries"]
+    t, eps, k = int(g[f"type{case}"]), float(g[f"eps{case}"]), int(g[f"k{case}"])
+    idx, cnt = ctx.kdtree_knn(pos, q, t, eps, k, cap=64)
+    ref_idx, ref_cnt = g[f"idx{case}"], g[f"cnt{case}"]
+    listed = []
+    for i in range(len(q)):
+        a, b = idx[i, :cnt[i]], ref_idx[i, :ref_cnt[i]]
+        if cnt[i] == ref_cnt[i] and np.array_equal(a, b):
+            continue
+        dd = np.linalg.norm(pos.astype(np.float64) - q[i].astype(np.float64), axis=1)
+        sa, sb = set(a.tolist()), set(b.tolist())
+        if sa == sb:  # same set, order swapped only among equal distances
+            assert np.allclose(dd[a], dd[b], rtol=1e-5), i
+        else:
+            edge = np.sort(dd[list(sb)])[-1] if (t & P.KNN_K_NEAREST) and sb else eps
+            sym = list(sa ^ sb)
+            assert np.all(np.abs(dd[sym] - edge) <= 1e-5 * max(edge, 1e-30)), (i, dd[sym], edge)
+        listed.append(i)
+    print(f"kdtree knn type {t} eps {eps} k {k}: {len(listed)} near-tie queries: {listed[:20]}")
+    assert len(listed) <= 0.002 * len(q)
