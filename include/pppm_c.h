@@ -172,6 +172,18 @@ int pppm_scene_set(pppm_ctx* ctx, const float* tri_xyz, int64_t ntri, const int3
  * 64x64 importance pdf/cdf (envmap.cc:88-163) in double on the host. */
 int pppm_env_set(pppm_ctx* ctx, const float* rgb, int32_t w, int32_t h);
 
+/* Makes material mat_id (of the scene set last) emit radiance rgb (3
+ * floats >= 0) from the front side of its triangles (the side of
+ * (p1 - p0) x (p2 - p0)). No counterpart in the reference, whose only light
+ * is the environment map. With emitters in the scene every photon leaves an
+ * emitter: the emitter by area, a uniform point of it, a cosine direction
+ * about its normal, flux Le * pi * (total emitter area) / photons; eye paths
+ * add Le where they meet a front side. A scene with emitters needs no
+ * environment map (eye rays that miss then see black) and renders in
+ * canonical mode or with the path tracer (other modes: PPPM_E_ARG at
+ * pppm_render_begin). pppm_scene_set clears all emission. */
+int pppm_material_emission(pppm_ctx* ctx, int32_t mat_id, const float* rgb);
+
 /* Envmap importance tables (envmap.cc:88-163), 4096 doubles each. */
 int pppm_env_tables(pppm_ctx* ctx, double* pdf, double* cdf);
 

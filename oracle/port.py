@@ -29,6 +29,7 @@ def lib():
         _lib.port_scene_create.argtypes = [_VP, ctypes.c_int64, _VP, _VP, ctypes.c_int32, _VP, ctypes.c_int32,
                                            ctypes.c_int32]
         _lib.port_scene_destroy.argtypes = [_VP]
+        _lib.port_scene_emission.argtypes = [_VP, ctypes.c_int32, _VP]
         _lib.port_env_tables.argtypes = [_VP, _VP, _VP]
         _lib.port_intersect.argtypes = [_VP, _VP, ctypes.c_int64, _VP, _VP]
         _lib.port_render.argtypes = [_VP, _VP, _VP, ctypes.c_int32, _VP, _VP, _VP, ctypes.c_int64, _VP, _VP]
@@ -52,6 +53,9 @@ class PortScene:
                                      self._keep[2].ctypes.data, self._keep[2].shape[0],
                                      env.ctypes.data if env is not None else None,
                                      env.shape[1] if env is not None else 0, env.shape[0] if env is not None else 0)
+        for mid, rgb in (getattr(scene, "emission", None) or {}).items():
+            e = np.ascontiguousarray(rgb, np.float32).reshape(3)
+            L.port_scene_emission(self.h, int(mid), e.ctypes.data)
 
     def __del__(self):
         try:
@@ -80,7 +84,7 @@ class PortScene:
         w, h = cam_struct.width, cam_struct.height
         accum = np.zeros((h, w, 3))
         stats = (PassStats * max(passes, 1))()
-        ph = np.zeros((max(photon_cap, 1), 12))
+        ph = np.zeros((max(photon_cap, 1), 13))
         qr = np.zeros((h * w, 12)) if queries else None
         n = ctypes.c_int64()
         r = lib().port_render(self.h, ctypes.byref(cam_struct), ctypes.byref(params), passes, accum.ctypes.data, stats,

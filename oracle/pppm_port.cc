@@ -332,6 +332,7 @@ struct Env {
     std::vector<V> img;
     std::vector<double> pdf, cdf;
     V lookup(V d) const {
+        if (w == 0) return V();  // no environment map
         const double th = std::acos(d.y);
         double ph = std::atan2(d.z, d.x);
         if (ph < 0.0) ph += 2.0 * kPi;
@@ -404,6 +405,7 @@ struct Camera {
 // ------------------------------------------------------------------ photon map
 struct Photon {
     V p, flux, dir, n;
+    int64_t path = -1;  // emitted path index (the GPU library's numbering: s * T + i in compat mode)
 };
 
 class KdTree {
@@ -527,6 +529,14 @@ struct Scene {
     Env env;
     Qbvh bvh;
     double bmin[3], bmax[3];
+    // emissive materials (the GPU library's pppm_material_emission; the
+    // reference has none): emission per material, the emitting triangles,
+    // their area CDF (last entry 1) and summed area
+    std::vector<V> emit;
+    std::vector<int> lightTris;
+    std::vector<double> lightCdf;
+    double lightArea = 0.0;
+    bool emissive(int mat) const { return emit[mat].x > 0.0 || emit[mat].y > 0.0 || emit[mat].z > 0.0; }
 };
 
 struct Renderer {
@@ -547,9 +557,33 @@ struct Renderer {
     V envLookup(V d) const { return sc->env.lookup(d); }
 
     // tracePhotons (ppm_probabilistic.cc:123-208) for one path.
-    void tracePath(Tape& tp, std::vector<Photon>* out, int pass) {
+    // A photon from the emissive triangles, in the GPU library's draw order:
+    // the emitter by area (first CDF entry >= the draw), u = sqrt(r1) and
+    // barycentrics (1 - u, u (1 - r2), u r2), a cosine direction about the
+    // normal e1 x e2, flux Le * pi * area / photons.
+    bool lightEmit(Tape& tp, V* pos, V* dir, V* flux) const {
+        const double r = tp.pop();
+        const int k = (int)(std::lower_bound(sc->lightCdf.begin(), sc->lightCdf.end(), r) - sc->lightCdf.begin());
+        if (k >= (int)sc->lightCdf.size()) return false;
+        const Tri& t = sc->tris[sc->lightTris[k]];
+        const double r1 = tp.pop(), r2 = tp.pop();
+        const double su = std::sqrt(r1);
+        const V e1 = t.p1 - t.p0, e2 = t.p2 - t.p0;
+        *pos = t.p0 + (su * (1.0 - r2)) * e1 + (su * r2) * e2;
+        const V n = normalized(cross(e1, e2));
+        const double a0 = tp.pop(), a1 = tp.pop();
+        onHemisphere(n, a0, a1, dir);
+        *flux = sc->emit[sc->matId[sc->lightTris[k]]] * (kPi * sc->lightArea / (double)par.photons);
+        return true;
+    }
+
+    void tracePath(Tape& tp, std::vector<Photon>* out, int pass, int64_t pathId) {
         V pos, d, flux;
-        if (!sc->env.emit(tp, (double)par.photons, &pos, &d, &flux)) return;
+        if (!sc->lightTris.empty()) {
+            if (!lightEmit(tp, &pos, &d, &flux)) return;
+        } else if (!sc->env.emit(tp, (double)par.photons, &pos, &d, &flux)) {
+            return;
+        }
         V o = pos;
         for (int b = 0;; b++) {
             if (b >= par.max_bounce_photon || std::max(flux.x, std::max(flux.y, flux.z)) <= 0.0) break;
@@ -564,7 +598,7 @@ struct Renderer {
             V nd;
             double pdf = 1.0;
             if (m.type == PPPM_BSDF_LAMBERTIAN) {
-                out->push_back({hp, flux, d, compat ? n : on});
+                out->push_back({hp, flux, d, compat ? n : on, pathId});
                 const double prob = (m.refl.x + m.refl.y + m.refl.z) / 3.0;
                 if (r0 < prob) {
                     bsdfSample(m, d, on, r1, r2, &nd, &pdf);
@@ -624,6 +658,9 @@ struct Renderer {
     V radiance(V o, V d, Tape& tp, double* rec = nullptr) const {
         std::vector<std::pair<V, double>> stack;
         V inner;
+        // emitters met on the way (none in the reference's scenes), weighted
+        // by the path throughput so far
+        V emitted, wfwd(1.0, 1.0, 1.0);
         for (int b = 0;; b++) {
             double t;
             const int id = b >= par.max_bounce_eye ? -1 : sc->bvh.intersect(o, d, &t);
@@ -635,6 +672,8 @@ struct Renderer {
             const Mat& m = sc->mats[sc->matId[id]];
             const V hp = o + t * d;
             const V n = sc->tris[id].normal();
+            if (!sc->lightTris.empty() && sc->emissive(sc->matId[id]) && dot(n, d) < 0.0)
+                emitted = emitted + wfwd * sc->emit[sc->matId[id]];
             double roul = std::max(m.refl.x, std::max(m.refl.y, m.refl.z));
             if (b >= 3) {
                 if (r0 > roul) {
@@ -661,11 +700,12 @@ struct Renderer {
             V nd;
             bsdfSample(m, d, n, r1, r2, &nd, &pdf);
             stack.push_back({m.refl, pdf * roul});
+            wfwd = wfwd * m.refl / (pdf * roul);
             o = hp;
             d = nd;
         }
         for (size_t j = stack.size(); j-- > 0;) inner = stack[j].first * inner / stack[j].second;
-        return inner;
+        return sc->lightTris.empty() ? inner : inner + emitted;
     }
 
     int pass(int t) {
@@ -679,7 +719,7 @@ struct Renderer {
                 for (int s = 0; s < N; s++) {
                     Tape tp;
                     tp.fill(streams[s]);
-                    tracePath(tp, &ph[s], t);
+                    tracePath(tp, &ph[s], t, (int64_t)s * T + i);
                 }
             }
         } else {
@@ -690,7 +730,7 @@ struct Renderer {
                 Tape tp;
                 XorShift x = seedCanonical(par.seed, t, (uint64_t)g);
                 tp.fill(x, true);
-                tracePath(tp, &loc[omp_get_thread_num()], t);
+                tracePath(tp, &loc[omp_get_thread_num()], t, g);
             }
             for (auto& v : loc) ph[0].insert(ph[0].end(), v.begin(), v.end());
         }
@@ -797,7 +837,34 @@ void* port_scene_create(const float* tri9, int64_t ntri, const int32_t* matId, c
         s->env.build();
     }
     s->bvh.build(s->tris);
+    s->emit.assign((size_t)nmat, V());
     return s;
+}
+
+// Material mat emits rgb from the front side of its triangles; rebuilds the
+// emitter list (scene order) and its area CDF as the GPU library does (edges
+// subtracted in float, the cross product in double).
+void port_scene_emission(void* sp, int32_t mat, const float* rgb) {
+    Scene* s = static_cast<Scene*>(sp);
+    s->emit[mat] = V(rgb[0], rgb[1], rgb[2]);
+    s->lightTris.clear();
+    s->lightCdf.clear();
+    double total = 0.0;
+    for (size_t i = 0; i < s->tris.size(); i++) {
+        if (!s->emissive(s->matId[i])) continue;
+        const Tri& t = s->tris[i];
+        const float e1[3] = {(float)t.p1.x - (float)t.p0.x, (float)t.p1.y - (float)t.p0.y, (float)t.p1.z - (float)t.p0.z};
+        const float e2[3] = {(float)t.p2.x - (float)t.p0.x, (float)t.p2.y - (float)t.p0.y, (float)t.p2.z - (float)t.p0.z};
+        const double cx = (double)e1[1] * e2[2] - (double)e1[2] * e2[1];
+        const double cy = (double)e1[2] * e2[0] - (double)e1[0] * e2[2];
+        const double cz = (double)e1[0] * e2[1] - (double)e1[1] * e2[0];
+        total += 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+        s->lightTris.push_back((int)i);
+        s->lightCdf.push_back(total);
+    }
+    s->lightArea = total;
+    for (double& c : s->lightCdf) c /= total;
+    if (!s->lightCdf.empty()) s->lightCdf.back() = 1.0;
 }
 
 void port_scene_destroy(void* s) { delete static_cast<Scene*>(s); }
@@ -818,14 +885,16 @@ void port_intersect(void* s, const float* rays, int64_t n, int32_t* tri, double*
 }
 
 // Renders `passes` passes; accum: W*H*3 doubles (sum over passes), stats
-// per pass. photons (optional, cap records of 12 doubles) receives the
-// photon map of the last pass; returns the record count in *nphotons.
+// per pass. photons (optional, cap records of 13 doubles: position, flux,
+// direction, normal, emitted path index or -1 for a phantom slot) receives
+// the photon map of the last pass (each path's records in bounce order);
+// returns the record count in *nphotons.
 // queries (optional, W*H records of 12 doubles) receives each pixel's gather
 // query of the last pass (radiance's rec; rec[11] = 0 where none).
 int port_render(void* s, const pppm_camera* cam, const pppm_params* par, int32_t passes, double* accum,
                 port_pass_stats* stats, double* photons, int64_t cap, int64_t* nphotons, double* queries) {
     const Scene* sc = static_cast<Scene*>(s);
-    if (sc->env.w == 0) return PPPM_E_STATE;
+    if (sc->env.w == 0 && sc->lightTris.empty()) return PPPM_E_STATE;
     Renderer R;
     R.sc = sc;
     R.par = *par;
@@ -858,9 +927,9 @@ int port_render(void* s, const pppm_camera* cam, const pppm_params* par, int32_t
         *nphotons = (int64_t)R.lastPhotons.size();
         for (int64_t i = 0; i < std::min<int64_t>(cap, *nphotons); i++) {
             const Photon& p = R.lastPhotons[i];
-            const double v[12] = {p.p.x, p.p.y, p.p.z, p.flux.x, p.flux.y, p.flux.z,
-                                  p.dir.x, p.dir.y, p.dir.z, p.n.x, p.n.y, p.n.z};
-            std::memcpy(photons + 12 * i, v, sizeof(v));
+            const double v[13] = {p.p.x, p.p.y, p.p.z, p.flux.x, p.flux.y, p.flux.z,
+                                  p.dir.x, p.dir.y, p.dir.z, p.n.x, p.n.y, p.n.z, (double)p.path};
+            std::memcpy(photons + 13 * i, v, sizeof(v));
         }
     }
     return PPPM_OK;

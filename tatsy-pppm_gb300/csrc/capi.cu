@@ -247,6 +247,10 @@ int pppm_scene_set(pppm_ctx* c, const float* tri, int64_t ntri, const int32_t* m
         c->lambertArea += 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
     }
     c->hostTri.assign(tri, tri + 9 * ntri);
+    c->hostMatId.assign(matId, matId + ntri);
+    c->matEmit.assign((size_t)nmat * 3, 0.0f);
+    c->numLights = 0;
+    c->lightArea = 0.0;
     c->bssrdfTris.clear();
     c->bssrdfArea = 0.0;
     for (int64_t i = 0; i < ntri; i++) {
@@ -276,6 +280,65 @@ int pppm_scene_set(pppm_ctx* c, const float* tri, int64_t ntri, const int32_t* m
 }
 
 static int uploadEnvTables(pppm_ctx* c);
+
+int pppm_material_emission(pppm_ctx* c, int32_t mat_id, const float* rgb) {
+    if (!c || !rgb) return fail(c, PPPM_E_ARG, "material_emission: bad arguments");
+    if (!c->hasScene) return fail(c, PPPM_E_STATE, "material_emission: no scene");
+    if (mat_id < 0 || (size_t)mat_id >= c->mats.size()) return fail(c, PPPM_E_ARG, "material_emission: bad material id");
+    for (int k = 0; k < 3; k++)
+        if (!(rgb[k] >= 0.0f) || !std::isfinite(rgb[k]))
+            return fail(c, PPPM_E_ARG, "material_emission: emission must be finite and >= 0");
+    cudaSetDevice(c->device);
+    c->rs.active = false;
+    for (int k = 0; k < 3; k++) c->matEmit[3 * (size_t)mat_id + k] = rgb[k];
+    DevMaterial d = toDevMaterial(c->mats[(size_t)mat_id]);
+    for (int k = 0; k < 3; k++) d.emit[k] = rgb[k];
+    d.emissive = (rgb[0] > 0.0f || rgb[1] > 0.0f || rgb[2] > 0.0f) ? 1 : 0;
+    PPPM_CUDA(c, cudaMemcpy(c->devMats.as<DevMaterial>() + mat_id, &d, sizeof(d), cudaMemcpyHostToDevice));
+    // the emitter list: triangles of emissive materials in scene order, with
+    // their areas 0.5 |e1 x e2| in double
+    std::vector<float> tri;
+    std::vector<float> le;
+    std::vector<double> cdf;
+    double total = 0.0;
+    for (size_t i = 0; i < c->hostMatId.size(); i++) {
+        const float* e = &c->matEmit[3 * (size_t)c->hostMatId[i]];
+        if (!(e[0] > 0.0f || e[1] > 0.0f || e[2] > 0.0f)) continue;
+        const float* p = &c->hostTri[9 * i];
+        const float e1[3] = {p[3] - p[0], p[4] - p[1], p[5] - p[2]};
+        const float e2[3] = {p[6] - p[0], p[7] - p[1], p[8] - p[2]};
+        float idBits;
+        std::memcpy(&idBits, &c->hostMatId[i], 4);
+        const float row[12] = {p[0], p[1], p[2], idBits, e1[0], e1[1], e1[2], 0.0f, e2[0], e2[1], e2[2], 0.0f};
+        tri.insert(tri.end(), row, row + 12);
+        le.insert(le.end(), e, e + 3);
+        const double cx = (double)e1[1] * e2[2] - (double)e1[2] * e2[1];
+        const double cy = (double)e1[2] * e2[0] - (double)e1[0] * e2[2];
+        const double cz = (double)e1[0] * e2[1] - (double)e1[1] * e2[0];
+        total += 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+        cdf.push_back(total);
+    }
+    c->numLights = (int)cdf.size();
+    c->lightArea = total;
+    if (c->numLights == 0) return PPPM_OK;
+    if (!(total > 0.0)) return fail(c, PPPM_E_ARG, "material_emission: the emitting triangles have zero area");
+    std::vector<unsigned long long> u(cdf.size());
+    for (size_t i = 0; i < cdf.size(); i++) {
+        cdf[i] /= total;
+        u[i] = (unsigned long long)std::floor(cdf[i] * 4294967296.0);
+    }
+    cdf.back() = 1.0;
+    u.back() = 4294967296ull;  // every draw x < 2^32 selects an emitter
+    PPPM_CUDA(c, c->lightTri.ensure(tri.size() * 4));
+    PPPM_CUDA(c, c->lightLe.ensure(le.size() * 4));
+    PPPM_CUDA(c, c->lightCdf.ensure(cdf.size() * 8));
+    PPPM_CUDA(c, c->lightUcdf.ensure(u.size() * 8));
+    PPPM_CUDA(c, cudaMemcpy(c->lightTri.p, tri.data(), tri.size() * 4, cudaMemcpyHostToDevice));
+    PPPM_CUDA(c, cudaMemcpy(c->lightLe.p, le.data(), le.size() * 4, cudaMemcpyHostToDevice));
+    PPPM_CUDA(c, cudaMemcpy(c->lightCdf.p, cdf.data(), cdf.size() * 8, cudaMemcpyHostToDevice));
+    PPPM_CUDA(c, cudaMemcpy(c->lightUcdf.p, u.data(), u.size() * 8, cudaMemcpyHostToDevice));
+    return PPPM_OK;
+}
 
 int pppm_env_set(pppm_ctx* c, const float* rgb, int32_t w, int32_t h) {
     if (!c || !rgb || w <= 0 || h <= 0) return fail(c, PPPM_E_ARG, "env_set: bad arguments");

@@ -242,6 +242,13 @@ struct pppm_ctx {
     pppm::DBuf nodes, tris, matId, devMats, triE;
     double lambertArea = 0.0;  // summed area of Lambertian triangles
     std::vector<float> hostTri;        // triangle soup (9 floats each), for the Poisson sampler
+    std::vector<int32_t> hostMatId;    // material of each triangle
+    // emissive materials (pppm_material_emission) and their triangles
+    std::vector<float> matEmit;        // 3 per material
+    pppm::DBuf lightTri, lightCdf, lightUcdf, lightLe;
+    int numLights = 0;
+    double lightArea = 0.0;            // summed area of the emitters
+    float lightFluxScale = 0.0f;       // pi * lightArea / photons of the active render
     std::vector<int64_t> bssrdfTris;   // triangles with a BSSRDF, in scene order
     double bssrdfArea = 0.0;           // their summed Triangle::area, in scene order
     // sampler.cc's static Random (seeded 0) of the Poisson-disc sampler; it
@@ -345,8 +352,14 @@ inline EnvDev envView(const pppm_ctx* c) {
     e.pdf = c->envPdfD.as<double>();
     e.ucdf = c->envUcdfD.as<unsigned long long>();
     e.fluxScale = c->envScaleD.as<float>();
-    e.w = c->envW;
-    e.h = c->envH;
+    e.w = c->hasEnv ? c->envW : 0;
+    e.h = c->hasEnv ? c->envH : 0;
+    e.lightTri = c->lightTri.as<float4>();
+    e.lightCdf = c->lightCdf.as<double>();
+    e.lightUcdf = c->lightUcdf.as<unsigned long long>();
+    e.lightLe = c->lightLe.as<float>();
+    e.numLights = c->numLights;
+    e.lightFluxScale = c->lightFluxScale;
     return e;
 }
 // Fills the per-CDF-cell photon flux scale for numPhotons.

@@ -207,7 +207,23 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
         f3 d, dir, flux;
         bool ok;
         PathState p;
-        if (tp.qmc) {
+        double org[3];
+        bool fromLight = false;
+        if (env.numLights > 0) {
+            // emissive triangles: the scene's light instead of the environment
+            Tape tape;
+            tape.pos = 0;
+            tape.scramble = tp.mode == PPPM_MODE_CANONICAL;
+            if (tp.mode == PPPM_MODE_COMPAT) {
+                const uint4 s = *reinterpret_cast<const uint4*>(photonStates + 4 * g);
+                tape.x.s[0] = s.x; tape.x.s[1] = s.y; tape.x.s[2] = s.z; tape.x.s[3] = s.w;
+            } else {
+                seedCanonical(tp.seed, tp.pass, (uint64_t)g, tape.x);
+            }
+            ok = emitFromLights(env, tape, org, &dir, &flux, &d);
+            fromLight = true;
+            storeTape(tape, p);
+        } else if (tp.qmc) {
             // photon round i of thread s draws sample i of the pass from
             // sampler s (tracePhotons, ppm_probabilistic.cc:131-135)
             const int s = (int)(g / tp.taskPerThread);
@@ -230,9 +246,13 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
             storeTape(tape, p);
         }
         if (!ok) atomicAdd(&ctr->undefinedEmit, 1ull);
-        p.ox = 50.0 * (double)d.x;  // R * dir with R = 50 (envmap.cc:63,85)
-        p.oy = 50.0 * (double)d.y;
-        p.oz = 50.0 * (double)d.z;
+        if (fromLight) {
+            p.ox = org[0]; p.oy = org[1]; p.oz = org[2];
+        } else {
+            p.ox = 50.0 * (double)d.x;  // R * dir with R = 50 (envmap.cc:63,85)
+            p.oy = 50.0 * (double)d.y;
+            p.oz = 50.0 * (double)d.z;
+        }
         p.dx = dir.x; p.dy = dir.y; p.dz = dir.z;
         p.fx = ok ? flux.x : 0.f; p.fy = ok ? flux.y : 0.f; p.fz = ok ? flux.z : 0.f;
         p.id = (int)g;
@@ -649,6 +669,9 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
             double hp[3];
             hitPosition(o[0], o[1], o[2], d.x, d.y, d.z, best, hp);
             const f3 nrm = triNormalF(a, bb, c);
+            // an emissive surface seen from its front side (no counterpart in
+            // the reference, which has no emitters)
+            if (m.emissive && dot(nrm, d) < 0.0f) L = L + w * mk(m.emit[0], m.emit[1], m.emit[2]);
             float roul = m.roulette;
             if (bnc >= 3) {
                 // rands[0] > roulette: the path ends and contributes nothing more

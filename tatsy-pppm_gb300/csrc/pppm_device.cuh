@@ -17,7 +17,10 @@ constexpr double kEps = 1.0e-12;    // EPS (common.h:13)
 constexpr double kInfty = 1.0e20;   // INFTY (common.h:12)
 constexpr float kPiF = 3.14159265358979323846f;
 constexpr double kPi = 3.14159265358979323846;
-constexpr int kStackSize = 64;      // traversal stack; the builder caps depth at 20
+#ifndef PPPM_STACK_SIZE
+#define PPPM_STACK_SIZE 64
+#endif
+constexpr int kStackSize = PPPM_STACK_SIZE;  // traversal stack; the builder caps depth at 20
 constexpr int kMaxBvhDepth = 20;
 
 // ------------------------------------------------------------------ layouts
@@ -58,6 +61,8 @@ struct DevMaterial {
     float invRr;     // 1 / rr_photon for the flux update
     float pad0;
     DipoleDev dip;   // valid when type has the BSSRDF bit
+    float emit[3];   // emitted radiance of the front side (pppm_material_emission); 0 for the reference's materials
+    int emissive;    // emit != 0
 };
 
 struct EnvDev {
@@ -70,7 +75,18 @@ struct EnvDev {
     // per CDF cell: (float)(area / (pdf * numPhotons)) (envmap.cc:80-83),
     // filled per render because numPhotons is a render parameter
     const float* fluxScale;
-    int w, h;
+    int w, h;         // 0 x 0: no environment map (eye rays that miss see black)
+    // emissive triangles (no counterpart in the reference, whose only light
+    // is the environment): per emitter 3 float4 (p0, p1 - p0, p2 - p0; w of
+    // the first: emitter material), the area CDF in double and as the
+    // integer comparison values floor(cdf * 2^32), and the flux scale
+    // pi * total area / photons. numLights > 0: every photon leaves an emitter.
+    const float4* lightTri;
+    const double* lightCdf;
+    const unsigned long long* lightUcdf;
+    const float* lightLe;   // 3 per emitter
+    int numLights;
+    float lightFluxScale;
 };
 
 // ------------------------------------------------------------------ RNG
@@ -909,6 +925,7 @@ __device__ inline float bsdfSample(const DevMaterial& m, f3 in, f3 normal, uint3
 
 // Envmap::sampleFromDir (envmap.cc:11-17,47-60), nearest texel.
 __device__ inline f3 envLookup(const EnvDev& e, f3 d) {
+    if (e.w == 0) return {0.f, 0.f, 0.f};  // no environment map
     const float theta = acosf(fminf(fmaxf(d.y, -1.0f), 1.0f));
     float phi = atan2f(d.z, d.x);
     if (phi < 0.0f) phi += 2.0f * kPiF;
@@ -958,6 +975,46 @@ __device__ inline int envCellOf(f3 d) {
     const int ix = min(max((int)(phi * (64.0f / (2.0f * kPiF))), 0), 63);
     const int iy = min(max((int)((1.0f - d.y) * 0.5f * 64.0f), 0), 63);
     return iy * 64 + ix;
+}
+
+// A photon from the emissive triangles (no counterpart in the reference):
+// the emitter by area (first CDF entry >= the draw), a uniform point of it
+// (u = sqrt(r1): barycentrics (1 - u, u (1 - r2), u r2)), a cosine direction
+// about its geometric normal (e1 x e2, the emitting side), and the flux
+// Le * pi * total area / photons (area pdf 1 / A, direction pdf cos / pi).
+// o: the point in double. Returns false past the last CDF entry.
+template <class TapeT>
+__device__ inline bool emitFromLights(const EnvDev& e, TapeT& tp, double* o, f3* dir, f3* flux, f3* normal) {
+    int lo = 0, hi = e.numLights;
+    if constexpr (TapeT::kExact32) {
+        const unsigned long long r = tp.popu();
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(&e.lightUcdf[mid]) < r) lo = mid + 1; else hi = mid;
+        }
+    } else {
+        const double r = tp.popd();
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(&e.lightCdf[mid]) < r) lo = mid + 1; else hi = mid;
+        }
+    }
+    const bool ok = lo < e.numLights;
+    const int k = min(lo, e.numLights - 1);
+    const float r1 = tp.popf(), r2 = tp.popf();
+    const float su = sqrtf(r1);
+    const double b1 = (double)(su * (1.0f - r2)), b2 = (double)(su * r2);
+    const float4 p0 = e.lightTri[3 * k], e1 = e.lightTri[3 * k + 1], e2 = e.lightTri[3 * k + 2];
+    o[0] = (double)p0.x + b1 * (double)e1.x + b2 * (double)e2.x;
+    o[1] = (double)p0.y + b1 * (double)e1.y + b2 * (double)e2.y;
+    o[2] = (double)p0.z + b1 * (double)e1.z + b2 * (double)e2.z;
+    const f3 n = normalized(cross(mk(e1.x, e1.y, e1.z), mk(e2.x, e2.y, e2.z)));
+    const float a0 = tp.popf(), a1 = tp.popf();
+    *dir = onHemisphere(n, a0, a1);
+    *normal = n;
+    const float* le = e.lightLe + 3 * k;
+    *flux = mk(le[0], le[1], le[2]) * e.lightFluxScale;
+    return ok;
 }
 
 // Envmap::samplePhoton (envmap.cc:62-86) followed by the cosine hemisphere

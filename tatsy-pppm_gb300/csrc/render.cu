@@ -318,8 +318,15 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     if (!c || !cam || !par) return fail(c, PPPM_E_ARG, "render_begin: null argument");
     if (!c->hasScene) return fail(c, PPPM_E_STATE, "render_begin: no scene");
     // The default Scene env map has no importance tables (scene.cc:11-12):
-    // photon emission would read an empty CDF.
-    if (!c->hasEnv) return fail(c, PPPM_E_STATE, "render_begin: no env map (the only light of the reference)");
+    // photon emission would read an empty CDF. Emissive triangles light a
+    // scene without one.
+    if (!c->hasEnv && c->numLights == 0)
+        return fail(c, PPPM_E_STATE, "render_begin: no env map (the only light of the reference) and no emitter");
+    if (c->numLights > 0 && par->mode != PPPM_MODE_CANONICAL && par->mode != PPPM_MODE_PATH_TRACING)
+        return fail(c, PPPM_E_ARG, "render_begin: emissive materials have no reference semantics; canonical mode and "
+                                   "the path tracer render them");
+    if (c->numLights > 0 && (par->flags & PPPM_FLAG_LEARNED))
+        return fail(c, PPPM_E_ARG, "render_begin: the learned proposal proposes environment directions");
     if (par->mode != PPPM_MODE_COMPAT && par->mode != PPPM_MODE_CANONICAL && par->mode != PPPM_MODE_CLASSIC &&
         par->mode != PPPM_MODE_PATH_TRACING)
         return fail(c, PPPM_E_ARG, "render_begin: unknown mode");
@@ -376,10 +383,12 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     PPPM_CUDA(c, rs.streamStatesD.ensure((size_t)N * 16));
     PPPM_CUDA(c, querySortLayout(rs.qsort, pixels));
     PPPM_CUDA(c, rs.gatherWork.ensure(16));
-    {
+    if (c->hasEnv) {
         const int e = envFluxScale(c, (double)par->photons);
         if (e) return e;
     }
+    // emitter photons: Le * pi * area / P (area pdf 1/A, cosine pdf cos/pi)
+    c->lightFluxScale = (float)(3.14159265358979323846 * c->lightArea / (double)par->photons);
     if (par->flags & PPPM_FLAG_SAMPLER_QMC) {
         const int e = haltonBegin(c, N);
         if (e) return e;

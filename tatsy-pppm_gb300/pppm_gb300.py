@@ -95,6 +95,7 @@ SIGNATURES = {
     "pppm_env_set": ([_VP, _VP, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
     "pppm_env_tables": ([_VP, _VP, _VP], ctypes.c_int),
     "pppm_env_importance": ([_VP, ctypes.c_double], ctypes.c_int),
+    "pppm_material_emission": ([_VP, ctypes.c_int32, _VP], ctypes.c_int),
     "pppm_env_lookup": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_emit_photons": ([_VP, _VP, ctypes.c_int64, ctypes.c_int64, _VP, _VP, _VP, _VP], ctypes.c_int),
     "pppm_hdr_decode": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, _VP, _VP], ctypes.c_int),
@@ -242,7 +243,14 @@ class Context:
                                             mats.shape[0]))
         if scene.env is not None:
             self.set_env(scene.env)
+        for mid, rgb in (getattr(scene, "emission", None) or {}).items():
+            self.material_emission(mid, rgb)
         self.scene = scene
+
+    def material_emission(self, mat_id, rgb):
+        """pppm_material_emission: material mat_id emits rgb from its front side."""
+        e = np.ascontiguousarray(rgb, np.float32).reshape(3)
+        self._check(self.lib.pppm_material_emission(self.h, int(mat_id), e.ctypes.data))
 
     def set_env(self, rgb):
         rgb = np.ascontiguousarray(rgb, np.float32)

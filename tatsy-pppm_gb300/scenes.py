@@ -72,6 +72,9 @@ class Scene:
     max_depth: int = 64
     alpha: float = 0.7
     radius_scale: float = 0.1
+    # material id -> emitted RGB radiance of its triangles' front side
+    # (pppm_material_emission); the reference's scenes have none
+    emission: dict | None = None
 
     @property
     def ntri(self):
@@ -281,6 +284,26 @@ def config1a(seed=1, width=256, height=256, photons=200_000, passes=16, subdiv=5
     env = sky_env(env_w, env_h, seed, sun_peak=50.0, sun_deg=8.0)
     cam = look_camera((0.0, 2.0, -55.0), (0.0, 0.0, 0.0), 0.75, width, height)
     return _assemble("config1a", [(box, 0), (sph, 1)], mats, env, cam, photons=photons, passes=passes, max_depth=8)
+
+
+def config1(seed=1, width=256, height=256, photons=200_000, passes=16, subdiv=5, emission=12.0):
+    """The CPU-runnable configuration as written: the open box of 10 wall
+    triangles (side 40) with a 2-triangle area light (10 x 10, just below
+    the ceiling, facing down, emission `emission` RGB) around a
+    noise-displaced icosphere (subdivision `subdiv`, 20*4^subdiv triangles,
+    amplitude 5% of the radius); Lambertian albedos uniform in [0.2, 0.8]^3
+    per object; no environment map (the light is the only source)."""
+    rng = np.random.default_rng(seed)
+    box = open_box(20.0)
+    sph = displace_sphere(geodesic_sphere(2 ** subdiv), 8.0, 0.05, seed, center=(0, -12.0 + 8.0 * 1.0, 4.0))
+    light = quad((-5.0, 19.5, -5.0), (5.0, 19.5, -5.0), (5.0, 19.5, 5.0), (-5.0, 19.5, 5.0))  # normal -y
+    mats = [material(LAMBERTIAN, rng.uniform(0.2, 0.8, 3)), material(LAMBERTIAN, rng.uniform(0.2, 0.8, 3)),
+            material(LAMBERTIAN, rng.uniform(0.2, 0.8, 3))]
+    cam = look_camera((0.0, 2.0, -55.0), (0.0, 0.0, 0.0), 0.75, width, height)
+    sc = _assemble("config1", [(box, 0), (sph, 1), (light, 2)], mats, None, cam, photons=photons, passes=passes,
+                   max_depth=8)
+    sc.emission = {2: (emission, emission, emission)}
+    return sc
 
 
 def config2(seed=2, width=1920, height=1080, photons=4_000_000, passes=64, freq=209, env_w=2048, env_h=1024,

@@ -171,7 +171,7 @@ int main(int argc, char** argv) {
         std::vector<Vector3D> at;
         std::vector<double> atf;
         for (int i = 0; i < 64; i++) {
-            const Vector3D v(uniform(-3, 3), uniform(-1, 3), uniform(-3, 3));
+            const Vector3D v(uniform(-3, 3), uniform(-4.5, 0.5), uniform(-12, -6));
             at.push_back(v);
             const double xyz[3] = {v.x(), v.y(), v.z()};
             atf.insert(atf.end(), xyz, xyz + 3);

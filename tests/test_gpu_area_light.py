@@ -1,0 +1,83 @@
+"""Emissive triangles (the configuration with a 2-triangle area light of
+emission 12 in an open box around a displaced icosphere, 256x256, 200k
+photons, 16 passes, depth 8).
+
+The reference has no emissive surfaces (its only light is the environment
+map), so parity here is against the CPU restatement alone: the oracle port
+with the same emitter draw (area CDF, uniform point, cosine direction, flux
+Le * pi * area / photons) and the same counter-seeded random numbers. The
+path tracer renders the same scene without photons and must agree with the
+photon-mapped image on the mean, an estimator-independent check of the
+emitter's flux convention.
+"""
+import numpy as np
+import pytest
+
+import pppm_gb300 as P
+import scenes as S
+from pass_parity import photon_parity
+
+pytestmark = pytest.mark.gpu
+
+
+def _params(mode=P.MODE_CANONICAL, depth=8, **kw):
+    return P.Context.make_params(mode=mode, photons=200_000, max_bounce_photon=depth, max_bounce_eye=depth,
+                                 radius_scale=1 / 64, seed=3, num_streams=16, **kw)
+
+
+def test_config1_area_light_matches_port(ctx):
+    import port
+
+    sc = S.config1()
+    passes = 16
+    ctx.set_scene(sc)
+    ctx.render_begin(sc.camera, _params())
+    st = [ctx.render_pass(t) for t in range(1, passes + 1)]
+    img = ctx.render_read().astype(np.float64)
+    gpu = ctx.render_photons(1 << 21)
+    out = port.PortScene(sc).render(P.Context.make_camera(sc.camera), _params(), passes, photon_cap=1 << 21)
+    assert [s.radius for s in st] == [s["radius"] for s in out["stats"]]
+    pr = photon_parity(gpu, out["photons"])
+    ref = out["accum"]
+    rel = np.abs(img - ref) / np.maximum(np.abs(ref), 1e-3)
+    close = np.all(rel < 1e-3, axis=2).mean()
+    relmse = float(np.mean((img - ref) ** 2) / np.mean(ref ** 2))
+    lit = (ref / passes).max(2) > 10.0  # pixels that see the emitter itself
+    print(f"area light: photon records {pr}; pixels within 1e-3 {close:.4f}, relMSE {relmse:.3e}, "
+          f"emitter pixels {lit.mean():.4f}")
+    assert pr["isolated_mismatches"] == 0 and pr["unexplained"] == 0, pr
+    assert pr["matched_within_1e-5"] >= 0.99 * pr["records"], pr
+    assert close > 0.9 and relmse < 1e-3
+    # the emitter seen directly: Le = 12 per pass (plus its own gathered light)
+    assert lit.mean() > 0.005
+    assert np.all(np.abs(img[lit] / passes - 12.0) < 0.5)
+
+
+def test_config1_path_tracer_agrees_on_the_mean(ctx):
+    """Photon mapping and path tracing of the emitter-lit box converge to the
+    same image: their mean radiance agrees within the Monte Carlo error of
+    16 passes (path length 64 on both sides)."""
+    sc = S.config1()
+    ctx.set_scene(sc)
+    means = {}
+    for name, mode in (("ppm", P.MODE_CANONICAL), ("pt", P.MODE_PATH_TRACING)):
+        ctx.render_begin(sc.camera, _params(mode=mode, depth=64))
+        for t in range(1, 17):
+            ctx.render_pass(t)
+        img = ctx.render_read().astype(np.float64) / 16
+        means[name] = float(img[(img.max(2) < 10.0)].mean())  # without the emitter's own pixels
+    print(f"mean radiance off the emitter: ppm {means['ppm']:.4f}, path tracing {means['pt']:.4f}")
+    assert abs(means["ppm"] - means["pt"]) <= 0.05 * means["pt"]
+
+
+def test_emitters_need_canonical_or_path_tracing(ctx):
+    sc = S.config1(width=16, height=16, photons=1000)
+    ctx.set_scene(sc)
+    for par in (_params(mode=P.MODE_COMPAT), _params(mode=P.MODE_CLASSIC), _params(flags=P.FLAG_LEARNED)):
+        with pytest.raises(P.PppmError) as e:
+            ctx.render_begin(sc.camera, par)
+        assert e.value.code == P.E_ARG
+    with pytest.raises(P.PppmError):
+        ctx.material_emission(99, (1.0, 1.0, 1.0))
+    with pytest.raises(P.PppmError):
+        ctx.material_emission(2, (-1.0, 1.0, 1.0))

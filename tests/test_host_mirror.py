@@ -146,7 +146,8 @@ def test_mirror_classes_match_c_abi(tmp_path, golden):
     sph = S.displace_sphere(S.geodesic_sphere(4), 4.0, 0.05, 3).reshape(-1, 9)
     a_tris = np.concatenate([sph, S.ground(-5.0, 15.0).reshape(-1, 9)]).astype(np.float32)
     b_tris = S.torus(6.0, 2.0, 40, 20, 0.05, 4, center=(0.0, 2.0, 3.0)).reshape(-1, 9).astype(np.float32)
-    c_tris = S.displace_sphere(S.geodesic_sphere(5), 2.0, 0.05, 5, center=(0.0, 1.0, 0.0)).reshape(-1, 9)
+    # the subsurface sphere in front of scene A's sphere, above its ground
+    c_tris = S.displace_sphere(S.geodesic_sphere(5), 2.5, 0.05, 5, center=(0.0, -2.0, -9.0)).reshape(-1, 9)
     c_tris = c_tris.astype(np.float32)
     for name, t in (("a", a_tris), ("b", b_tris), ("c", c_tris)):
         S.write_ply(tmp_path / f"{name}.ply", t)
