@@ -297,23 +297,25 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
 // 262-320): three draws from the path's tape, the deposit (store, da, db) on
 // Lambertian (subsurface pass: BSSRDF) surfaces, Russian roulette, and the
 // next ray in p. alive turns false when the path ends here.
+// The ray is given as (ox, oy, oz, din); the next ray leaves through hp and
+// nd. p supplies and receives everything else of the path (flux, tape,
+// bounce, records): callers that keep the ray in their traversal state do
+// not hold a second copy of it in p.
 template <bool kSss, class TapeT = Tape>
-__device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView& sc, PathState& p, int slot, double best,
-                                          bool& alive, bool& store, float4& da, float4& db) {
+__device__ __forceinline__ void photonHitRay(const TraceParams& tp, const SceneView& sc, PathState& p, int slot,
+                                             double best, double ox, double oy, double oz, const f3 din, bool& alive,
+                                             bool& store, float4& da, float4& db, double* hp, f3& nd) {
     TapeT tape;
     loadTape(tp, p, tape);
     const auto r0 = tape.draw(), r1 = tape.draw(), r2 = tape.draw();
     const float4 a = sc.tris[3 * slot], b = sc.tris[3 * slot + 1], c = sc.tris[3 * slot + 2];
     const int tid = __float_as_int(a.w);
     const DevMaterial& m = sc.mats[sc.matId[tid]];
-    double hp[3];
-    hitPosition(p.ox, p.oy, p.oz, p.dx, p.dy, p.dz, best, hp);
+    hitPosition(ox, oy, oz, din.x, din.y, din.z, best, hp);
     const f3 nrm = triNormalF(a, b, c);
-    const f3 din = {p.dx, p.dy, p.dz};
     const f3 on = dot(nrm, din) < 0.0f ? nrm : -nrm;
     f3 flux = {p.fx, p.fy, p.fz};
     const f3 refl = {m.refl[0], m.refl[1], m.refl[2]};
-    f3 nd;
     if (kSss) {
         if (kSss && (m.type & PPPM_BSDF_BSSRDF)) {
             store = true;
@@ -355,11 +357,21 @@ __device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView
         const float pdf = bsdfSample(m, din, on, r0.u, r1.u, &nd);
         flux = flux * refl * (1.0f / pdf);
     }
-    p.ox = hp[0]; p.oy = hp[1]; p.oz = hp[2];
-    p.dx = nd.x; p.dy = nd.y; p.dz = nd.z;
     p.fx = flux.x; p.fy = flux.y; p.fz = flux.z;
     storeTape(tape, p);
     p.bounce += 1;
+}
+
+// photonHitRay for a path that carries its ray in p.
+template <bool kSss, class TapeT = Tape>
+__device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView& sc, PathState& p, int slot, double best,
+                                          bool& alive, bool& store, float4& da, float4& db) {
+    double hp[3];
+    f3 nd;
+    photonHitRay<kSss, TapeT>(tp, sc, p, slot, best, p.ox, p.oy, p.oz, mk(p.dx, p.dy, p.dz), alive, store, da, db, hp,
+                              nd);
+    p.ox = hp[0]; p.oy = hp[1]; p.oz = hp[2];
+    p.dx = nd.x; p.dy = nd.y; p.dz = nd.z;
 }
 
 // Every bounce of every emitted photon path in one launch. Warps stay
@@ -432,11 +444,15 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(T
             if (s.hit < 0) {
                 alive = false;
             } else {
-                photonHit<kSss>(tp, sc, p, s.hit, s.best, alive, store, da, db);
+                // the ray lives in the traversal state only
+                double hp[3];
+                f3 nd;
+                photonHitRay<kSss>(tp, sc, p, s.hit, s.best, s.odx, s.ody, s.odz, mk(s.dx, s.dy, s.dz), alive, store,
+                                   da, db, hp, nd);
                 if (alive) alive = p.bounce < tp.maxBouncePhoton && fmaxf(p.fx, fmaxf(p.fy, p.fz)) > 0.0f;
+                if (alive) s.begin(sc.rootCode, hp[0], hp[1], hp[2], nd.x, nd.y, nd.z);
             }
-            if (alive) s.begin(sc.rootCode, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz);
-            else has = false;
+            if (!alive) has = false;
         }
         const unsigned long long di = warpAppend(store, &ctr->deposits);
         if (store && (int64_t)di < depCap) {
