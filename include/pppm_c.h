@@ -169,7 +169,10 @@ int pppm_scene_set(pppm_ctx* ctx, const float* tri_xyz, int64_t ntri, const int3
 
 /* Replaces Envmap::Envmap(file) (envmap.cc:28-36): rgb is w*h*3 floats of
  * the decoded equirect image (row 0 = top, as Image stores it); builds the
- * 64x64 importance pdf/cdf (envmap.cc:88-163) in double on the host. */
+ * 64x64 importance pdf/cdf (envmap.cc:88-163) in double on the host.
+ * The map stays with the context across pppm_scene_set; rgb = NULL with
+ * w = h = 0 removes it (a Scene without setEnvmap: rays that leave the
+ * scene see black, scene.cc:11-12). */
 int pppm_env_set(pppm_ctx* ctx, const float* rgb, int32_t w, int32_t h);
 
 /* Makes material mat_id (of the scene set last) emit radiance rgb (3

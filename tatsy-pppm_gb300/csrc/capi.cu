@@ -341,6 +341,13 @@ int pppm_material_emission(pppm_ctx* c, int32_t mat_id, const float* rgb) {
 }
 
 int pppm_env_set(pppm_ctx* c, const float* rgb, int32_t w, int32_t h) {
+    if (c && !rgb && w == 0 && h == 0) {
+        // no environment map: rays that leave the scene see black (the
+        // reference's default Envmap, scene.cc:11-12)
+        c->hasEnv = false;
+        c->envExponent = 2.0;
+        return PPPM_OK;
+    }
     if (!c || !rgb || w <= 0 || h <= 0) return fail(c, PPPM_E_ARG, "env_set: bad arguments");
     // The 64x64 importance map divides by the texel area of each cell
     // (envmap.cc:104-113); below 64 texels per axis that area is zero and

@@ -135,8 +135,8 @@ int pppm_render_save(pppm_ctx* c, uint8_t* out, int64_t cap, int64_t* size) {
         h.bbmin[d] = c->bbmin[d];
         h.bbmax[d] = c->bbmax[d];
     }
-    h.envW = c->envW;
-    h.envH = c->envH;
+    h.envW = c->hasEnv ? c->envW : 0;  // 0 x 0: no environment map
+    h.envH = c->hasEnv ? c->envH : 0;
     std::memcpy(h.poissonRng, c->poissonRng, 16);
     h.numStreams = (int32_t)rs.streams.size();
     h.classic = classic ? 1 : 0;
@@ -188,7 +188,8 @@ int pppm_render_load(pppm_ctx* c, const uint8_t* in, int64_t size) {
     std::memcpy(&h, in, sizeof(h));
     if (std::memcmp(h.magic, kMagic, 8) != 0 || h.version != 1 || h.headerBytes != sizeof(CkHeader))
         return fail(c, PPPM_E_ARG, "render_load: not a checkpoint of this library version");
-    bool same = c->hasScene && c->hasEnv && h.ntri == c->ntri && h.envW == c->envW && h.envH == c->envH;
+    bool same = c->hasScene && h.ntri == c->ntri && h.envW == (c->hasEnv ? c->envW : 0) &&
+                h.envH == (c->hasEnv ? c->envH : 0);
     for (int d = 0; d < 3 && same; d++) same = h.bbmin[d] == c->bbmin[d] && h.bbmax[d] == c->bbmax[d];
     if (!same) return fail(c, PPPM_E_STATE, "render_load: the context holds another scene or environment map");
     int r = pppm_render_begin(c, &h.cam, &h.par);

@@ -241,8 +241,8 @@ class Context:
         mats = np.ascontiguousarray(scene.mats)
         self._check(self.lib.pppm_scene_set(self.h, tris.ctypes.data, tris.shape[0], mid.ctypes.data, mats.ctypes.data,
                                             mats.shape[0]))
-        if scene.env is not None:
-            self.set_env(scene.env)
+        # a scene without a map replaces the previous scene's map by none
+        self.set_env(scene.env)
         for mid, rgb in (getattr(scene, "emission", None) or {}).items():
             self.material_emission(mid, rgb)
         self.scene = scene
@@ -253,6 +253,10 @@ class Context:
         self._check(self.lib.pppm_material_emission(self.h, int(mat_id), e.ctypes.data))
 
     def set_env(self, rgb):
+        """pppm_env_set: the equirect map (H x W x 3), or None for no map."""
+        if rgb is None:
+            self._check(self.lib.pppm_env_set(self.h, None, 0, 0))
+            return
         rgb = np.ascontiguousarray(rgb, np.float32)
         self._check(self.lib.pppm_env_set(self.h, rgb.ctypes.data, rgb.shape[1], rgb.shape[0]))
 

@@ -48,9 +48,13 @@ def test_config1_area_light_matches_port(ctx):
     assert pr["isolated_mismatches"] == 0 and pr["unexplained"] == 0, pr
     assert pr["matched_within_1e-5"] >= 0.99 * pr["records"], pr
     assert close > 0.9 and relmse < 1e-3
-    # the emitter seen directly: Le = 12 per pass (plus its own gathered light)
+    # the emitter seen directly: Le = 12 per pass plus the light its surface
+    # reflects (photons from the floor below); pixels on its outline see it
+    # in some passes only, so the bound holds for most, and the port
+    # comparison covers every one
     assert lit.mean() > 0.005
-    assert np.all(np.abs(img[lit] / passes - 12.0) < 0.5)
+    assert np.median(img[lit].max(1) / passes) >= 12.0
+    assert np.allclose(img[lit], ref[lit], rtol=1e-3)
 
 
 def test_config1_path_tracer_agrees_on_the_mean(ctx):
@@ -81,3 +85,31 @@ def test_emitters_need_canonical_or_path_tracing(ctx):
         ctx.material_emission(99, (1.0, 1.0, 1.0))
     with pytest.raises(P.PppmError):
         ctx.material_emission(2, (-1.0, 1.0, 1.0))
+
+
+def test_scene_without_env_map_sees_black(ctx):
+    """set_scene of a scene without an environment map removes the map of
+    the scene set before: the path tracer's image is the one a fresh
+    context renders (paths that leave the open box see black, not the
+    previous sky)."""
+    sc = S.config1(width=32, height=32, subdiv=2, photons=1000)
+    par = _params(mode=P.MODE_PATH_TRACING, depth=16)
+
+    def render(c):
+        c.render_begin(sc.camera, par)
+        for t in (1, 2):
+            c.render_pass(t)
+        return c.render_read()
+
+    fresh = P.Context(0)
+    try:
+        fresh.set_scene(sc)
+        want = render(fresh)
+    finally:
+        fresh.close()
+    ctx.set_scene(S.small_test_scene(seed=3, subdiv=2, width=16, height=16, photons=1000))
+    ctx.set_scene(sc)
+    with pytest.raises(P.PppmError) as e:
+        ctx.env_tables()
+    assert e.value.code == P.E_STATE
+    np.testing.assert_array_equal(render(ctx), want)
