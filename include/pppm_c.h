@@ -463,6 +463,33 @@ int pppm_render_skip(pppm_ctx* ctx, int32_t count);
  * counterpart in the reference. */
 int pppm_render_tune(pppm_ctx* ctx, float cell_factor, int32_t bounce_blocks_per_sm, int32_t eye_blocks_per_sm);
 
+/* Every launch-shape knob of a render. No field changes what a pass
+ * computes (the same photon paths, deposits, eye paths and gather sets):
+ * each only moves work between launches, lanes or tiles, and so may change
+ * the order in which deposits are appended and the gather sums them. */
+typedef struct pppm_tune {
+    float cell_factor;             /* hash-grid cell edge / radius, >= 1 */
+    int32_t bounce_blocks_per_sm;  /* photon kernel grid cap, 1..64 */
+    int32_t eye_blocks_per_sm;     /* eye kernel grid cap, 1..64 */
+    int32_t refill;                /* persistent photon kernel: lanes of a warp with their closest hit
+                                      before the warp shades them and takes new paths, 1..32 */
+    int32_t exact_batch;           /* lanes waiting for double-precision triangle tests before a
+                                      warp runs them together, 1..32 */
+    int32_t gather_stage;          /* canonical gather: photons per warp tile, a multiple of 32 in
+                                      32..256 */
+    int32_t query_sub_bits;        /* canonical gather: query sort key with 2^bits sub-cells per
+                                      axis, 0..3 */
+} pppm_tune;
+
+/* Sets the knobs of an active render from the next pass on; a field < 0
+ * (cell_factor <= 0) keeps its current value, a value out of range is
+ * PPPM_E_ARG and changes nothing. render_begin restores the defaults
+ * (1, 64, 64, 24, 12, 128, 1). No counterpart in the reference. */
+int pppm_render_tune_ex(pppm_ctx* ctx, const pppm_tune* tune);
+
+/* The knobs the next pass of the active render will use. */
+int pppm_render_get_tune(pppm_ctx* ctx, pppm_tune* out);
+
 /* The linear accumulation buffer after the last pass (not divided by the
  * pass count, not flipped): w*h*3 floats, row y = camera pixel row y. */
 int pppm_render_read(pppm_ctx* ctx, float* accum);
@@ -555,6 +582,12 @@ typedef struct {
     double batch_graph_ms;        /* capture, instantiation and run of the batch graph */
     double batch_graph_capture_ms;     /* of which recording the passes */
     double batch_graph_instantiate_ms; /* of which cudaGraphInstantiate */
+    int32_t refill;               /* the other knobs chosen (pppm_tune) */
+    int32_t exact_batch;
+    int32_t gather_stage;
+    int32_t query_sub_bits;
+    int32_t tune_passes;          /* passes spent on tuning (real passes of the render) */
+    int32_t tune_candidate;       /* index of the candidate kept, -1 without tuning */
 } pppm_job_stats;
 
 int pppm_batch_create(int device, pppm_batch** out);
@@ -563,16 +596,19 @@ const char* pppm_batch_last_error(const pppm_batch* batch);
 /* Copies nothing it does not need: the scene and env map are uploaded and
  * the BVH built here. */
 int pppm_batch_submit(pppm_batch* batch, const pppm_job* job, int32_t* job_id);
-/* use_graph = 1 (the default): pppm_batch_run records the passes that
- * follow the tuning passes of every canonical job without subsurface
- * scattering or learned proposal into one CUDA graph (one branch per job,
- * the branches chained into graph_lanes lanes; 0 = 2 x max_concurrent) and
- * launches it once; 0 runs every pass through pppm_render_pass. */
+/* use_graph = 1 (the default): pppm_batch_run records the passes after the
+ * first of every canonical job without subsurface scattering or learned
+ * proposal into two CUDA graphs, each launched once: the tuning passes of
+ * all jobs, then the remaining passes with each job's chosen knobs (one
+ * branch per job, the branches chained into graph_lanes lanes; 0 = 2 x
+ * max_concurrent); 0 runs every pass through pppm_render_pass. */
 int pppm_batch_config(pppm_batch* batch, int32_t use_graph, int32_t graph_lanes);
 /* Runs every job's passes: up to max_concurrent jobs at once (one host
- * worker and one stream each, longest first), then the batch graph (see
- * pppm_batch_config). autotune = 1 times the first passes of each job under
- * different launch shapes and keeps the fastest. */
+ * worker and one stream each, longest first), then the batch graphs (see
+ * pppm_batch_config). autotune = 1: a job of P passes tries up to
+ * min(6, (P - 2) / 3) candidate settings of every pppm_tune knob, three
+ * interleaved passes each, and renders its remaining passes with the one of
+ * lowest median device time per pass (jobs under 8 passes are not tuned). */
 int pppm_batch_run(pppm_batch* batch, int32_t autotune, int32_t max_concurrent);
 /* A job's accumulation buffer (as pppm_render_read) and statistics. */
 int pppm_batch_result(pppm_batch* batch, int32_t job_id, float* accum, pppm_job_stats* stats);

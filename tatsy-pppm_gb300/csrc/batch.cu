@@ -1,13 +1,23 @@
 // Batched uneven render jobs: each job owns a context (scene, BVH, env map,
 // render state, stream); worker threads drive up to max_concurrent jobs at a
-// time, so their kernels overlap on the GPU, longest jobs first. With
-// autotune on, a job's first passes each run a different launch shape (hash
-// cell factor, photon-bounce and eye blocks per SM; results do not depend on
-// them) and the remaining passes use the fastest. Then the remaining passes
-// of every job that can be captured (canonical, no subsurface stage, no
-// learned proposal) are recorded into one CUDA graph, one branch per job,
-// and launched once. Per-pass latencies are recorded per job. No
-// counterpart in the reference (its render() handles one scene at a time).
+// time, so their kernels overlap on the GPU, longest jobs first.
+//
+// Autotuning: a job's passes after the first try the launch shapes of a
+// candidate table (every pppm_tune knob: hash cell factor, photon and eye
+// blocks per SM, refill threshold, exact-test batch, gather tile, query
+// sort sub-cells; no knob changes a result), each candidate for kRounds
+// passes in interleaved rounds (forward, backward, forward, so that the
+// shrinking radius favours no candidate), and the rest of the job runs the
+// candidate with the lowest median device time per pass. The tuning passes
+// are real passes of the render.
+//
+// Jobs that can be captured (canonical, no subsurface stage, no learned
+// proposal) run everything after their first pass in two CUDA graphs, one
+// branch per job: the first holds the tuning passes of all jobs (each
+// captured with its candidate's knobs, timed by the graph's event nodes),
+// the second the remaining passes with each job's choice. Other jobs tune
+// eagerly. Per-pass latencies are recorded per job. No counterpart in the
+// reference (its render() handles one scene at a time).
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -32,8 +42,11 @@ struct pppm_batch {
         int64_t rays = 0;
         float cell = 1.0f;
         int bounceBlocks = 16, eyeBlocks = 16;
-        bool graph = false;  // remaining passes go into the batch graph
-        int graphPasses = 0;
+        pppm_tune tune{};         // knobs after the tuning
+        std::vector<int> plan;    // candidate of each tuning pass
+        int chosen = -1;          // candidate kept (-1: no tuning)
+        bool graph = false;       // passes after the first go into the batch graphs
+        int graphPasses = 0;      // of which plan.size() in the tuning graph
         int status = PPPM_OK;
         std::string err;
     };
@@ -54,36 +67,90 @@ int jobFail(pppm_batch::Job& j, int code) {
     return code;
 }
 
-// Launch shapes tried over the first passes: (cell factor, bounce, eye).
-struct Shape {
-    float cell;
-    int bounce, eye;
+// Candidate launch shapes: the defaults first, then variants along every
+// knob (cell factor, bounce and eye blocks per SM, refill, exact batch,
+// gather tile, query sub-cell bits). A job with P passes tries the first
+// min(6, (P - 2) / kRounds) of them.
+const pppm_tune kCandidates[] = {
+    {1.0f, 64, 64, 24, 12, 128, 1}, {1.25f, 64, 64, 24, 12, 256, 2}, {1.0f, 32, 32, 16, 8, 128, 1},
+    {1.0f, 64, 64, 32, 16, 64, 0},  {1.5f, 64, 64, 24, 12, 256, 2},  {1.0f, 16, 16, 24, 12, 128, 1},
 };
-const Shape kShapes[] = {{1.0f, 64, 64}, {1.0f, 16, 16}, {1.0f, 32, 32}, {1.25f, 64, 64}, {1.5f, 64, 64}};
+constexpr int kNumCandidates = (int)(sizeof(kCandidates) / sizeof(kCandidates[0]));
+constexpr int kRounds = 3;  // timed passes per candidate
+
+// The knobs of candidate k for a render of this mode: compat renders keep
+// their cell size (it follows k) and use the kNN gather (no tiles).
+pppm_tune candidate(int k, bool canonical) {
+    pppm_tune t = kCandidates[k];
+    if (!canonical) {
+        t.cell_factor = 0.0f;
+        t.gather_stage = -1;
+        t.query_sub_bits = -1;
+    }
+    return t;
+}
+
+// Tuning passes of a job with `passes` passes: candidates in rounds of
+// alternating order, kRounds passes each; none when the job is too short.
+std::vector<int> tuningPlan(int passes, bool autotune) {
+    std::vector<int> plan;
+    const int k = autotune ? std::min(kNumCandidates, std::max(0, (passes - 2) / kRounds)) : 0;
+    if (k < 2) return plan;
+    for (int r = 0; r < kRounds; r++)
+        for (int i = 0; i < k; i++) plan.push_back((r & 1) ? k - 1 - i : i);
+    return plan;
+}
+
+// The candidate with the lowest median device time over its tuning passes
+// (ms[i]: device time of tuning pass i).
+int bestCandidate(const std::vector<int>& plan, const std::vector<double>& ms) {
+    int best = 0;
+    double bestMs = 1e300;
+    for (int k = 0; k < kNumCandidates; k++) {
+        std::vector<double> v;
+        for (size_t i = 0; i < plan.size() && i < ms.size(); i++)
+            if (plan[i] == k) v.push_back(ms[i]);
+        if (v.empty()) continue;
+        std::sort(v.begin(), v.end());
+        const double m = v[v.size() / 2];
+        if (m < bestMs) {
+            bestMs = m;
+            best = k;
+        }
+    }
+    return best;
+}
+
+void recordShape(pppm_batch::Job& j) {
+    pppm_render_get_tune(j.ctx, &j.tune);
+    j.cell = j.tune.cell_factor;
+    j.bounceBlocks = j.tune.bounce_blocks_per_sm;
+    j.eyeBlocks = j.tune.eye_blocks_per_sm;
+}
 
 int runJob(pppm_batch::Job& j, bool autotune, bool useGraph) {
     pppm_ctx* c = j.ctx;
     int r = pppm_render_begin(c, &j.cam, &j.par);
     if (r) return jobFail(j, r);
     const bool canonical = j.par.mode == PPPM_MODE_CANONICAL;
-    const int nShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
-    // pass 1 pays the allocations (default shape); passes 2 .. 1 + trials
-    // try one shape each; compat renders tune only the launch shapes (their
-    // cell size follows k)
-    const int trials = autotune ? std::min(std::max(j.passes - 2, 0), canonical ? nShapes : 3) : 0;
-    // passes run here; with the graph, the rest are captured after the tuning
-    j.graph = useGraph && graphEligible(c) && j.passes > 1 + trials;
-    const int eager = j.graph ? 1 + trials : j.passes;
+    j.plan = tuningPlan(j.passes, autotune);
+    j.chosen = -1;
+    // pass 1 pays the allocations (default shape); with the graphs, every
+    // later pass (tuning included) is captured
+    j.graph = useGraph && graphEligible(c) && j.passes > 1;
+    const int eager = j.graph ? 1 : j.passes;
     j.graphPasses = j.passes - eager;
-    double best = 1e300;
-    Shape bestShape = kShapes[0];
+    const int nPlan = (int)j.plan.size();
+    std::vector<double> dev;
     for (int t = 1; t <= eager; t++) {
-        const int trial = t - 2;  // index of the shape this pass tries
-        if (trial >= 0 && trial < trials) {
-            const Shape& s = kShapes[trial];
-            pppm_render_tune(c, canonical ? s.cell : 0.0f, s.bounce, s.eye);
-        } else if (trials > 0 && trial == trials) {
-            pppm_render_tune(c, canonical ? bestShape.cell : 0.0f, bestShape.bounce, bestShape.eye);
+        const int i = t - 2;  // tuning pass index
+        if (i >= 0 && i < nPlan) {
+            const pppm_tune s = candidate(j.plan[i], canonical);
+            pppm_render_tune_ex(c, &s);
+        } else if (nPlan > 0 && i == nPlan) {
+            j.chosen = bestCandidate(j.plan, dev);
+            const pppm_tune s = candidate(j.chosen, canonical);
+            pppm_render_tune_ex(c, &s);
         }
         pppm_pass_stats st;
         const auto t0 = std::chrono::steady_clock::now();
@@ -92,33 +159,28 @@ int runJob(pppm_batch::Job& j, bool autotune, bool useGraph) {
         if (r) return jobFail(j, r);
         j.passMs.push_back(ms);
         j.rays += st.photon_rays + st.eye_rays;
-        if (trial >= 0 && trial < trials) {
-            // device time of the stages the shapes affect
-            const double dev = st.ms_photon + st.ms_grid + st.ms_eye + st.ms_gather;
-            if (dev < best) {
-                best = dev;
-                bestShape = kShapes[trial];
-            }
-        }
+        // device time of the stages the knobs affect
+        if (i >= 0 && i < nPlan) dev.push_back(st.ms_photon + st.ms_grid + st.ms_eye + st.ms_gather);
     }
-    if (j.graph && trials > 0)
-        pppm_render_tune(c, canonical ? bestShape.cell : 0.0f, bestShape.bounce, bestShape.eye);
-    j.cell = c->rs.par.cell_factor;
-    j.bounceBlocks = c->rs.bouncePerSm;
-    j.eyeBlocks = c->rs.eyePerSm;
+    recordShape(j);
     return PPPM_OK;
 }
 
-// The remaining passes of the graph jobs: one capture on `origin`, one
-// launch. Each job is a branch (its context stream and side stream); the
-// branches form `lanes` chains. Jobs go, longest first, to the chain with the
-// least work so far (the work of a job: its remaining passes times the median
-// of its tuned passes), so at most `lanes` jobs run at once and the chains
-// end close together.
-int runGraph(pppm_batch* b, std::vector<pppm_batch::Job*>& gj, int lanes) {
+// Passes of the graph jobs: one capture on `origin`, one launch. tuning:
+// each job's tuning passes, each captured with its candidate's knobs; else
+// the passes after them. Each job is a branch (its context stream); the
+// branches form `lanes` chains. Jobs go, longest first, to the chain with
+// the least work so far (the work of a job: its passes in this graph times
+// the median of its passes so far), so at most `lanes` jobs run at once and
+// the chains end close together.
+int passesIn(const pppm_batch::Job& j, bool tuning) {
+    return tuning ? (int)j.plan.size() : j.graphPasses - (int)j.plan.size();
+}
+
+int runGraph(pppm_batch* b, std::vector<pppm_batch::Job*>& gj, int lanes, bool tuning) {
     cudaSetDevice(b->device);
     for (auto* j : gj) {
-        const int r = graphPrepare(j->ctx, j->graphPasses);
+        const int r = graphPrepare(j->ctx, passesIn(*j, tuning));
         if (r) return jobFail(*j, r);
         if (cudaStreamSynchronize(j->ctx->stream) != cudaSuccess) return jobFail(*j, PPPM_E_CUDA);
     }
@@ -154,7 +216,7 @@ int runGraph(pppm_batch* b, std::vector<pppm_batch::Job*>& gj, int lanes) {
     for (size_t k = 0; k < gj.size(); k++) {
         std::vector<double> s(gj[k]->passMs.begin() + std::min<size_t>(1, gj[k]->passMs.size()), gj[k]->passMs.end());
         std::sort(s.begin(), s.end());
-        est[k] = (s.empty() ? 1.0 : s[s.size() / 2]) * gj[k]->graphPasses;
+        est[k] = (s.empty() ? 1.0 : s[s.size() / 2]) * passesIn(*gj[k], tuning);
     }
     std::vector<size_t> order(gj.size());
     for (size_t k = 0; k < order.size(); k++) order[k] = k;
@@ -169,7 +231,12 @@ int runGraph(pppm_batch* b, std::vector<pppm_batch::Job*>& gj, int lanes) {
         laneWork[l] += est[k];
         laneLast[l] = (int)k;
         const int first = c->rs.passesDone + 1;
-        for (int i = 0; i < gj[k]->graphPasses; i++) {
+        const bool canonical = gj[k]->par.mode == PPPM_MODE_CANONICAL;
+        for (int i = 0; i < passesIn(*gj[k], tuning); i++) {
+            if (tuning) {
+                const pppm_tune s = candidate(gj[k]->plan[i], canonical);
+                pppm_render_tune_ex(c, &s);
+            }
             const int r = graphEnqueuePass(c, first + i, i, false);
             if (r) {
                 graphAbort(origin);
@@ -185,12 +252,15 @@ int runGraph(pppm_batch* b, std::vector<pppm_batch::Job*>& gj, int lanes) {
         cudaGetLastError();
         return failAll("batch graph: the capture failed");
     }
-    b->graphCaptureMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    const int r = graphRun(gj[0]->ctx, g, origin, &b->graphInstantiateMs);
-    b->graphMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    b->graphCaptureMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    double instMs = 0.0;
+    const int r = graphRun(gj[0]->ctx, g, origin, &instMs);
+    b->graphInstantiateMs += instMs;
+    b->graphMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (r) return failAll(std::string("batch graph: ") + pppm_last_error(gj[0]->ctx));
     for (auto* j : gj) {
-        for (int i = 0; i < j->graphPasses; i++) {
+        std::vector<double> dev;
+        for (int i = 0; i < passesIn(*j, tuning); i++) {
             pppm_pass_stats st;
             double ms = 0.0;
             const int e = graphFinishPass(j->ctx, i, &st, &ms);
@@ -199,7 +269,15 @@ int runGraph(pppm_batch* b, std::vector<pppm_batch::Job*>& gj, int lanes) {
                 break;
             }
             j->passMs.push_back(ms);
+            dev.push_back(ms);
             j->rays += st.photon_rays + st.eye_rays;
+        }
+        if (tuning && j->status == PPPM_OK) {
+            // the remaining passes run the fastest candidate
+            j->chosen = bestCandidate(j->plan, dev);
+            const pppm_tune s = candidate(j->chosen, j->par.mode == PPPM_MODE_CANONICAL);
+            pppm_render_tune_ex(j->ctx, &s);
+            recordShape(*j);
         }
     }
     cleanup();
@@ -279,13 +357,16 @@ int pppm_batch_run(pppm_batch* b, int32_t autotune, int32_t max_concurrent) {
     std::vector<std::thread> pool;
     for (int w = 0; w < nw; w++) pool.emplace_back(worker);
     for (auto& t : pool) t.join();
-    b->graphMs = 0.0;
-    std::vector<pppm_batch::Job*> gj;
-    for (auto& j : b->jobs)
-        if (j.status == PPPM_OK && j.graph && j.graphPasses > 0) gj.push_back(&j);
-    // inside the graph no host thread bounds the jobs in flight: twice as
+    b->graphMs = b->graphCaptureMs = b->graphInstantiateMs = 0.0;
+    // inside the graphs no host thread bounds the jobs in flight: twice as
     // many as the eager phase measured best on the batched workload
-    if (!gj.empty()) runGraph(b, gj, b->graphLanes > 0 ? b->graphLanes : 2 * max_concurrent);
+    const int lanes = b->graphLanes > 0 ? b->graphLanes : 2 * max_concurrent;
+    for (const bool tuning : {true, false}) {
+        std::vector<pppm_batch::Job*> gj;
+        for (auto& j : b->jobs)
+            if (j.status == PPPM_OK && j.graph && passesIn(j, tuning) > 0) gj.push_back(&j);
+        if (!gj.empty()) runGraph(b, gj, lanes, tuning);
+    }
     b->wallMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     for (auto& j : b->jobs)
         if (j.status) {
@@ -320,6 +401,12 @@ int pppm_batch_result(pppm_batch* b, int32_t id, float* accum, pppm_job_stats* s
         stats->batch_graph_ms = b->graphMs;
         stats->batch_graph_capture_ms = b->graphCaptureMs;
         stats->batch_graph_instantiate_ms = b->graphInstantiateMs;
+        stats->refill = j.tune.refill;
+        stats->exact_batch = j.tune.exact_batch;
+        stats->gather_stage = j.tune.gather_stage;
+        stats->query_sub_bits = j.tune.query_sub_bits;
+        stats->tune_passes = (int32_t)j.plan.size();
+        stats->tune_candidate = j.chosen;
     }
     return PPPM_OK;
 }

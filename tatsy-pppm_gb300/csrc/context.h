@@ -51,9 +51,22 @@ struct GridBufs {
 };
 
 // Counting sort of gather queries by grid cell (tiled gather).
+// Canonical gather shape (tunable per render; neither changes a result):
+// photons per warp tile (a multiple of 32, 32..256) and sub-cells per axis
+// of the query sort key (2^bits, bits 0..3).
+#ifndef PPPM_GATHER_WSTAGE
+#define PPPM_GATHER_WSTAGE 128
+#endif
+#ifndef PPPM_GATHER_SUBBITS
+#define PPPM_GATHER_SUBBITS 1
+#endif
+constexpr int kGatherStageMax = 256;
+
 struct QuerySortBufs {
     DBuf hist, cursor, tmp, keys, sorted;
     uint32_t size = 0;
+    int stage = PPPM_GATHER_WSTAGE;
+    int subBits = PPPM_GATHER_SUBBITS;
 };
 
 // Pinned host buffer (grown on demand).
@@ -219,9 +232,12 @@ struct RenderState {
     SssState sss;
     GuideState guide;
     ClassicState classic;
-    // launch shapes the autotuner may change between passes
+    // launch shapes the autotuner may change between passes (with
+    // qsort.stage and qsort.subBits)
     int bouncePerSm = 16;
     int eyePerSm = 16;
+    int refill = kRefill;
+    int exactBatch = kExactBatch;
 };
 
 }  // namespace pppm

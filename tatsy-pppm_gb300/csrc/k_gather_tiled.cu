@@ -4,7 +4,7 @@
 // takes 64 consecutive sorted queries. For every distinct cell among them
 // the warp stages the photons of the cell's 3x3x3 neighbourhood (cell edge
 // >= radius, so the neighbourhood covers every photon within the radius of
-// any query in the cell) into its shared-memory tile in rounds of kWStage
+// any query in the cell) into its shared-memory tile in rounds of `stage`
 // photons, and each query of that cell tests every staged photon. The
 // photons of a neighbourhood are read from L2/HBM once per warp instead of
 // once per query; hundreds of eye hit points typically share a cell.
@@ -20,17 +20,12 @@ constexpr int kTileQ = 128;  // threads per block
 #endif
 constexpr int kQ = PPPM_GATHER_QPT;  // queries per thread
 constexpr int kWarps = kTileQ / 32;
-#ifndef PPPM_GATHER_WSTAGE
-#define PPPM_GATHER_WSTAGE 128
-#endif
-constexpr int kWStage = PPPM_GATHER_WSTAGE;  // photons per warp tile
-#ifndef PPPM_GATHER_SUBBITS
-#define PPPM_GATHER_SUBBITS 1
-#endif
-constexpr int kSubBits = PPPM_GATHER_SUBBITS;  // query sort: sub-cells per axis = 2^kSubBits
 #ifndef PPPM_GATHER_MINBLOCKS
 #define PPPM_GATHER_MINBLOCKS 7
 #endif
+
+// dynamic shared memory of a gather block with tiles of `stage` photons
+size_t gatherSmem(int stage) { return (size_t)kWarps * stage * (2 * sizeof(float4) + sizeof(float)); }
 
 unsigned blocksFor(int64_t n, int bs, int cap = 152 * 32) {
     const int64_t want = (n + bs - 1) / bs;
@@ -42,20 +37,19 @@ __device__ __forceinline__ int64_t queryCount(const QueryView& qv) {
 }
 
 // Sort key of a query: its cell's bucket, then the Morton index of its
-// sub-cell (2^kSubBits per axis), so that the 64 queries of a warp lie close
+// sub-cell (2^subBits per axis), so that the 64 queries of a warp lie close
 // together and the photons it stages can be culled against their bounding
 // box.
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+__device__ __forceinline__ uint32_t spread3(uint32_t v, int subBits) {
     uint32_t r = 0;
-#pragma unroll
-    for (int b = 0; b < kSubBits; b++) r |= ((v >> b) & 1u) << (3 * b);
+    for (int b = 0; b < subBits; b++) r |= ((v >> b) & 1u) << (3 * b);
     return r;
 }
 
-__global__ void kQueryKeys(QueryView qv, GridDev g, uint32_t qmask, uint32_t* __restrict__ keys,
+__global__ void kQueryKeys(QueryView qv, GridDev g, uint32_t qmask, int subBits, uint32_t* __restrict__ keys,
                            uint32_t* __restrict__ hist) {
     const int64_t n = queryCount(qv);
-    constexpr int kSub = 1 << kSubBits;
+    const int kSub = 1 << subBits;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float4 q0 = qv.q[3 * i];
         const float fx = (q0.x - g.ox) * g.invCell, fy = (q0.y - g.oy) * g.invCell, fz = (q0.z - g.oz) * g.invCell;
@@ -64,8 +58,8 @@ __global__ void kQueryKeys(QueryView qv, GridDev g, uint32_t qmask, uint32_t* __
         const uint32_t sx = (uint32_t)min(max(__float2int_rd((fx - (float)cx) * kSub), 0), kSub - 1);
         const uint32_t sy = (uint32_t)min(max(__float2int_rd((fy - (float)cy) * kSub), 0), kSub - 1);
         const uint32_t sz = (uint32_t)min(max(__float2int_rd((fz - (float)cz) * kSub), 0), kSub - 1);
-        const uint32_t k = (bucketOf(cx, cy, cz, qmask >> (3 * kSubBits)) << (3 * kSubBits)) | spread3(sx) |
-                           (spread3(sy) << 1) | (spread3(sz) << 2);
+        const uint32_t k = (bucketOf(cx, cy, cz, qmask >> (3 * subBits)) << (3 * subBits)) | spread3(sx, subBits) |
+                           (spread3(sy, subBits) << 1) | (spread3(sz, subBits) << 2);
         keys[i] = k;
         atomicAdd(&hist[k], 1u);
     }
@@ -84,25 +78,28 @@ __global__ void kQueryScatter(QueryView qv, const uint32_t* __restrict__ keys, u
 
 // Each warp owns 32 * kQ consecutive sorted queries (kQ per lane, usually of
 // one cell) and stages the photons of its cell's 3x3x3 neighbourhood in its
-// own shared-memory tile, synchronising with __syncwarp only: warps whose
-// queries lie in different cells work on their neighbourhoods side by side
-// instead of waiting for one another at block barriers. Every staged photon
-// is read from shared memory once for kQ tests per lane.
+// own shared-memory tile of `stage` photons (dynamic shared memory,
+// gatherSmem(stage) bytes per block), synchronising with __syncwarp only:
+// warps whose queries lie in different cells work on their neighbourhoods
+// side by side instead of waiting for one another at block barriers. Every
+// staged photon is read from shared memory once for kQ tests per lane. The
+// tile size changes only how often a warp flushes its tile, not which
+// photons a query sums or in which order.
 template <bool kAccum, bool kCount>
 __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(GridDev g, const float4* __restrict__ sq,
                                                        const uint32_t* __restrict__ qcount, int64_t qcap, float r,
-                                                       float* __restrict__ out, unsigned long long* __restrict__ work) {
-    __shared__ float4 sA[kWarps][kWStage];  // pos.xyz, normal.x
-    __shared__ float4 sB[kWarps][kWStage];  // flux.xyz, normal.y
-    __shared__ float sC[kWarps][kWStage];   // normal.z
+                                                       int stage, float* __restrict__ out,
+                                                       unsigned long long* __restrict__ work) {
+    // per warp: pos.xyz|normal.x, flux.xyz|normal.y, normal.z of `stage` photons
+    extern __shared__ float4 gatherTile[];
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t n = qcount ? min((int64_t)*qcount, qcap) : qcap;
     const int64_t base = ((int64_t)blockIdx.x * kWarps + warp) * (32 * kQ);
     if (base >= n) return;  // uniform for the warp; the kernel has no block barrier
-    float4* wA = sA[warp];
-    float4* wB = sB[warp];
-    float* wC = sC[warp];
+    float4* wA = gatherTile + (size_t)warp * stage;
+    float4* wB = gatherTile + (size_t)(kWarps + warp) * stage;
+    float* wC = reinterpret_cast<float*>(gatherTile + (size_t)2 * kWarps * stage) + (size_t)warp * stage;
     // position and normal of each query stay in registers; its weight and
     // pixel are read again for the final write
     float3 q0[kQ], q1[kQ];
@@ -239,7 +236,7 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
             segs &= segs - 1;
             const uint32_t sb = __shfl_sync(0xffffffffu, b0, sgi), sn = __shfl_sync(0xffffffffu, nc, sgi);
             for (uint32_t i = 0; i < sn; i += 32) {
-                if (fill > (uint32_t)kWStage - 32) {
+                if (fill > (uint32_t)stage - 32) {
                     testTile(fill);
                     fill = 0;
                 }
@@ -315,7 +312,8 @@ cudaError_t querySortLayout(QuerySortBufs& qs, int64_t maxQueries) {
 cudaError_t querySort(const GridDev& g, QueryView qv, QuerySortBufs& qs, cudaStream_t st) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(qs.hist.p, 0, ((size_t)qs.size + 1) * 4, st)) != cudaSuccess) return e;
-    kQueryKeys<<<blocksFor(qv.n, 256), 256, 0, st>>>(qv, g, qs.size - 1, qs.keys.as<uint32_t>(), qs.hist.as<uint32_t>());
+    kQueryKeys<<<blocksFor(qv.n, 256), 256, 0, st>>>(qv, g, qs.size - 1, qs.subBits, qs.keys.as<uint32_t>(),
+                                                     qs.hist.as<uint32_t>());
     if ((e = exclusiveScan(qs.hist.as<uint32_t>(), qs.size, qs.cursor.as<uint32_t>(), qs.tmp.as<uint32_t>(), st)) !=
         cudaSuccess)
         return e;
@@ -338,10 +336,16 @@ cudaError_t launchGatherSorted(const GridDev& g, QueryView qv, QuerySortBufs& qs
     const uint32_t* total = qs.hist.as<uint32_t>() + qs.size;
     const unsigned blocks = (unsigned)std::max<int64_t>(1, (qv.n + kTileQ * kQ - 1) / (kTileQ * kQ));
     const float4* sq = qs.sorted.as<float4>();
-    if (accumulate && work) kGatherTiled<true, true><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, out, work);
-    else if (accumulate) kGatherTiled<true, false><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, out, work);
-    else if (work) kGatherTiled<false, true><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, out, work);
-    else kGatherTiled<false, false><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, out, work);
+    const int stage = qs.stage;
+    const size_t smem = gatherSmem(stage);
+    if (accumulate && work)
+        kGatherTiled<true, true><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
+    else if (accumulate)
+        kGatherTiled<true, false><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
+    else if (work)
+        kGatherTiled<false, true><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
+    else
+        kGatherTiled<false, false><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
     return cudaGetLastError();
 }
 

@@ -376,16 +376,12 @@ __device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView
 
 // Every bounce of every emitted photon path in one launch. Warps stay
 // resident and keep their lanes busy: the warp advances its lanes'
-// traversals together until at least kRefill of them have found their hit
+// traversals together until at least tp.refill of them have found their hit
 // (or all have), shades those (photonHit: deposit, roulette, next ray), and
 // lanes whose path ended take the next path of the emitted queue (one
 // atomic per warp). A path's own random numbers and traversal are those of
 // the per-bounce kernels; only the order in which paths are processed and
 // deposits appended changes.
-#ifndef PPPM_REFILL
-#define PPPM_REFILL 24
-#endif
-constexpr int kRefill = PPPM_REFILL;
 
 template <bool kSss>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(TraceParams tp, SceneView sc,
@@ -434,7 +430,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(T
             if (__any_sync(0xffffffffu, !has) && b + __popc(empty) < (unsigned long long)n) continue;
         }
         if (!__any_sync(0xffffffffu, has)) break;
-        warpTravRun(s, has, kRefill, sc.nodes, sc.tris, order, sTop, &visits, &tests, sc.triE);
+        warpTravRun(s, has, tp.refill, sc.nodes, sc.tris, order, sTop, &visits, &tests, sc.triE, tp.exactBatch);
         const bool fin = has && s.done();
         bool store = false;
         float4 da, db;
@@ -522,7 +518,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
         do {
         double best;
         const int slot = traverseExactWarp(sc.nodes, sc.tris, sc.rootCode, alive, p.ox, p.oy, p.oz, p.dx, p.dy, p.dz,
-                                           order, sTop, &best, &visits, &tests, sc.triE);
+                                           order, sTop, &best, &visits, &tests, sc.triE, tp.exactBatch);
         if (alive) {
             traced++;
             if (tp.guided && p.pad[0] >= 0) {
@@ -671,7 +667,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TracePara
             }
             double best;
             const int slot = traverseExactWarp(sc.nodes, sc.tris, sc.rootCode, doTrace, o[0], o[1], o[2], d.x, d.y,
-                                               d.z, order, sTop, &best, &visits, &tests, sc.triE);
+                                               d.z, order, sTop, &best, &visits, &tests, sc.triE, tp.exactBatch);
             if (!doTrace) continue;
             traced++;
             if (slot < 0) {

@@ -527,13 +527,20 @@ __device__ __forceinline__ int traverseExact(const QNode* __restrict__ nodes, co
 #ifndef PPPM_EXACT_BATCH
 #define PPPM_EXACT_BATCH 12
 #endif
-constexpr int kExactBatch = PPPM_EXACT_BATCH;
+constexpr int kExactBatch = PPPM_EXACT_BATCH;  // default; a render may tune it (1..32)
+// persistent photon kernel: lanes of a warp that must have their closest
+// hit before the warp shades them and refills (default; tunable, 1..32)
+#ifndef PPPM_REFILL
+#define PPPM_REFILL 24
+#endif
+constexpr int kRefill = PPPM_REFILL;
 
 __device__ __forceinline__ int traverseExactWarp(const QNode* __restrict__ nodes, const float4* __restrict__ tris,
                                                  int rootCode, bool active, double odx, double ody, double odz,
                                                  float dx, float dy, float dz, const int* orderTab,
                                                  const QNode* sTop, double* bestOut, int* nodeVisits,
-                                                 int* triTests, const double* __restrict__ triE = nullptr) {
+                                                 int* triTests, const double* __restrict__ triE = nullptr,
+                                                 int exactBatch = kExactBatch) {
     const float ox = __double2float_rn(odx), oy = __double2float_rn(ody), oz = __double2float_rn(odz);
     const float idx = dx == 0.0f ? 1.0e20f : __frcp_rn(dx);
     const float idy = dy == 0.0f ? 1.0e20f : __frcp_rn(dy);
@@ -553,7 +560,7 @@ __device__ __forceinline__ int traverseExactWarp(const QNode* __restrict__ nodes
         const unsigned runMask = __ballot_sync(0xffffffffu, canRun);
         const unsigned pendMask = __ballot_sync(0xffffffffu, ncand > 0);
         if ((runMask | pendMask) == 0) break;
-        if (pendMask != 0 && (__popc(pendMask) >= kExactBatch || runMask == 0)) {
+        if (pendMask != 0 && (__popc(pendMask) >= exactBatch || runMask == 0)) {
             if (ncand > 0) {
                 const double ddx = dx, ddy = dy, ddz = dz;
                 for (int c = 0; c < ncand; c++) {
@@ -681,14 +688,15 @@ struct WarpTrav {
 // in the warp votes). All 32 lanes call it.
 __device__ __forceinline__ void warpTravRun(WarpTrav& s, bool live, int minDone, const QNode* __restrict__ nodes,
                                             const float4* __restrict__ tris, const int* orderTab, const QNode* sTop,
-                                            int* nodeVisits, int* triTests, const double* __restrict__ triE = nullptr) {
+                                            int* nodeVisits, int* triTests, const double* __restrict__ triE = nullptr,
+                                            int exactBatch = kExactBatch) {
     for (;;) {
         const bool canRun = live && s.sp > 0 && s.ncand == 0;
         const unsigned runMask = __ballot_sync(0xffffffffu, canRun);
         const unsigned pendMask = __ballot_sync(0xffffffffu, live && s.ncand > 0);
         if ((runMask | pendMask) == 0) break;
         if (__popc(__ballot_sync(0xffffffffu, live && s.done())) >= minDone) break;
-        if (pendMask != 0 && (__popc(pendMask) >= kExactBatch || runMask == 0)) {
+        if (pendMask != 0 && (__popc(pendMask) >= exactBatch || runMask == 0)) {
             if (live && s.ncand > 0) {
                 const double ddx = s.dx, ddy = s.dy, ddz = s.dz;
                 for (int c = 0; c < s.ncand; c++) {

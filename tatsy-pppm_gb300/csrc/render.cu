@@ -98,6 +98,8 @@ void passSetup(pppm_ctx* c, int t, int64_t paths, TraceParams* tp, CameraDev* cd
     tp->hasSss = rs.sss.enabled ? 1 : 0;
     tp->bouncePerSm = rs.bouncePerSm;
     tp->eyePerSm = rs.eyePerSm;
+    tp->refill = rs.refill;
+    tp->exactBatch = rs.exactBatch;
     tp->guided = rs.guide.enabled ? 1 : 0;
     tp->guide = guideView(c, 3 * paths);
     tp->qmc = (par.mode == PPPM_MODE_COMPAT && (par.flags & PPPM_FLAG_SAMPLER_QMC)) ? 1 : 0;
@@ -349,6 +351,10 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     // fastest on the 1080p workload (16: +4% pass time)
     rs.bouncePerSm = 64;
     rs.eyePerSm = 64;
+    rs.refill = kRefill;
+    rs.exactBatch = kExactBatch;
+    rs.qsort.stage = PPPM_GATHER_WSTAGE;
+    rs.qsort.subBits = PPPM_GATHER_SUBBITS;
     const double dx = c->bbmax[0] - c->bbmin[0], dy = c->bbmax[1] - c->bbmin[1], dz = c->bbmax[2] - c->bbmin[2];
     rs.bboxDiag = std::sqrt(dx * dx + dy * dy + dz * dz);
     rs.radius = rs.bboxDiag * par->radius_scale;  // ppm_probabilistic.cc:51-55
@@ -755,6 +761,40 @@ int pppm_render_tune(pppm_ctx* c, float cell_factor, int32_t bounce_blocks_per_s
     }
     if (bounce_blocks_per_sm > 0) c->rs.bouncePerSm = std::min(bounce_blocks_per_sm, 64);
     if (eye_blocks_per_sm > 0) c->rs.eyePerSm = std::min(eye_blocks_per_sm, 64);
+    return PPPM_OK;
+}
+
+int pppm_render_tune_ex(pppm_ctx* c, const pppm_tune* t) {
+    if (!c || !t) return fail(c, PPPM_E_ARG, "render_tune_ex: null argument");
+    if (!c->rs.active) return fail(c, PPPM_E_STATE, "render_tune_ex: no render");
+    auto in = [](int32_t v, int lo, int hi) { return v < 0 || (v >= lo && v <= hi); };
+    if ((t->cell_factor > 0.0f && !(t->cell_factor >= 1.0f)) || !in(t->bounce_blocks_per_sm, 1, 64) ||
+        !in(t->eye_blocks_per_sm, 1, 64) || !in(t->refill, 1, 32) || !in(t->exact_batch, 1, 32) ||
+        !in(t->gather_stage, 32, kGatherStageMax) || (t->gather_stage > 0 && t->gather_stage % 32 != 0) ||
+        !in(t->query_sub_bits, 0, 3))
+        return fail(c, PPPM_E_ARG, "render_tune_ex: a knob out of range");
+    RenderState& rs = c->rs;
+    if (t->cell_factor > 0.0f) rs.par.cell_factor = t->cell_factor;
+    if (t->bounce_blocks_per_sm > 0) rs.bouncePerSm = t->bounce_blocks_per_sm;
+    if (t->eye_blocks_per_sm > 0) rs.eyePerSm = t->eye_blocks_per_sm;
+    if (t->refill > 0) rs.refill = t->refill;
+    if (t->exact_batch > 0) rs.exactBatch = t->exact_batch;
+    if (t->gather_stage > 0) rs.qsort.stage = t->gather_stage;
+    if (t->query_sub_bits >= 0) rs.qsort.subBits = t->query_sub_bits;
+    return PPPM_OK;
+}
+
+int pppm_render_get_tune(pppm_ctx* c, pppm_tune* out) {
+    if (!c || !out) return fail(c, PPPM_E_ARG, "render_get_tune: null argument");
+    if (!c->rs.active) return fail(c, PPPM_E_STATE, "render_get_tune: no render");
+    const RenderState& rs = c->rs;
+    out->cell_factor = rs.par.cell_factor;
+    out->bounce_blocks_per_sm = rs.bouncePerSm;
+    out->eye_blocks_per_sm = rs.eyePerSm;
+    out->refill = rs.refill;
+    out->exact_batch = rs.exactBatch;
+    out->gather_stage = rs.qsort.stage;
+    out->query_sub_bits = rs.qsort.subBits;
     return PPPM_OK;
 }
 

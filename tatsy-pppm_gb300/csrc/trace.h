@@ -109,6 +109,8 @@ struct TraceParams {
     int hasSss;   // 1: the scene has BSSRDF materials
     int bouncePerSm = 16;  // photon bounce kernel: blocks per SM (tunable)
     int eyePerSm = 16;     // eye kernel: blocks per SM (tunable)
+    int refill = kRefill;  // persistent photon kernel: lanes done before a warp shades (tunable)
+    int exactBatch = kExactBatch;  // lanes waiting before a warp runs the double tests (tunable)
     int guided;   // 1: learned proposal (emission direction; Lambertian bounces through kGuideResolve)
     GuideView guide;
     // compat mode with the reference's RANDOM_SAMPLER_QUASI_MONTE_CARLO

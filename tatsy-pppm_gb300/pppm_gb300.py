@@ -67,6 +67,16 @@ class PassStats(ctypes.Structure):
 _VP = ctypes.c_void_p
 
 
+class Tune(ctypes.Structure):
+    """pppm_tune: the launch-shape knobs of a render (none changes a result)."""
+    _fields_ = [("cell_factor", ctypes.c_float), ("bounce_blocks_per_sm", ctypes.c_int32),
+                ("eye_blocks_per_sm", ctypes.c_int32), ("refill", ctypes.c_int32), ("exact_batch", ctypes.c_int32),
+                ("gather_stage", ctypes.c_int32), ("query_sub_bits", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Job(ctypes.Structure):
     _fields_ = [("tri_xyz", ctypes.c_void_p), ("ntri", ctypes.c_int64), ("mat_id", ctypes.c_void_p),
                 ("mats", ctypes.c_void_p), ("nmat", ctypes.c_int32), ("env_rgb", ctypes.c_void_p),
@@ -80,7 +90,9 @@ class JobStats(ctypes.Structure):
                 ("ms_total", ctypes.c_double), ("ms_pass_p50", ctypes.c_double), ("ms_pass_p99", ctypes.c_double),
                 ("batch_wall_ms", ctypes.c_double), ("graph_passes", ctypes.c_int32),
                 ("batch_graph_ms", ctypes.c_double), ("batch_graph_capture_ms", ctypes.c_double),
-                ("batch_graph_instantiate_ms", ctypes.c_double)]
+                ("batch_graph_instantiate_ms", ctypes.c_double), ("refill", ctypes.c_int32),
+                ("exact_batch", ctypes.c_int32), ("gather_stage", ctypes.c_int32), ("query_sub_bits", ctypes.c_int32),
+                ("tune_passes", ctypes.c_int32), ("tune_candidate", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -144,6 +156,8 @@ SIGNATURES = {
     "pppm_render_photons": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_render_queries": ([_VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
     "pppm_render_tune": ([_VP, ctypes.c_float, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+    "pppm_render_tune_ex": ([_VP, _VP], ctypes.c_int),
+    "pppm_render_get_tune": ([_VP, _VP], ctypes.c_int),
     "pppm_batch_create": ([ctypes.c_int, ctypes.POINTER(_VP)], ctypes.c_int),
     "pppm_batch_destroy": ([_VP], ctypes.c_int),
     "pppm_batch_last_error": ([_VP], ctypes.c_char_p),
@@ -508,6 +522,21 @@ class Context:
         # the checkpoint header: magic (8 bytes), version, header size, camera
         self._cam = Camera.from_buffer_copy(bytes(blob[16:16 + ctypes.sizeof(Camera)]))
 
+    def render_tune(self, **knobs):
+        """pppm_render_tune_ex: set launch-shape knobs (Tune field names) from the next pass on."""
+        t = Tune(0.0, -1, -1, -1, -1, -1, -1)
+        for k, v in knobs.items():
+            if k not in dict(Tune._fields_):
+                raise TypeError(f"unknown knob {k}")
+            setattr(t, k, v)
+        self._check(self.lib.pppm_render_tune_ex(self.h, ctypes.byref(t)))
+
+    def get_tune(self):
+        """pppm_render_get_tune: the knobs of the next pass, as a dict."""
+        t = Tune()
+        self._check(self.lib.pppm_render_get_tune(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
     def render_skip(self, count):
         """pppm_render_skip: advance the render by `count` passes without rendering them."""
         self._check(self.lib.pppm_render_skip(self.h, int(count)))
@@ -587,7 +616,8 @@ class Batch:
         return jid.value
 
     def config(self, use_graph=True, graph_lanes=0):
-        """pppm_batch_config: capture the passes after tuning into one CUDA graph."""
+        """pppm_batch_config: capture the passes after each job's first into two CUDA graphs
+        (the tuning passes, then the rest)."""
         self._check(self.lib.pppm_batch_config(self.h, 1 if use_graph else 0, int(graph_lanes)))
 
     def run(self, autotune=True, max_concurrent=8):
