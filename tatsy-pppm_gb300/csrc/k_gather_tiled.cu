@@ -85,13 +85,23 @@ __global__ void kQueryScatter(QueryView qv, const uint32_t* __restrict__ keys, u
 // staged photon is read from shared memory once for kQ tests per lane. The
 // tile size changes only how often a warp flushes its tile, not which
 // photons a query sums or in which order.
-template <bool kAccum, bool kCount>
+// kStage > 0: tiles of kStage photons in static shared memory (the default
+// shape); 0: tiles of `stageRt` photons in dynamic shared memory.
+template <bool kAccum, bool kCount, int kStage>
 __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(GridDev g, const float4* __restrict__ sq,
                                                        const uint32_t* __restrict__ qcount, int64_t qcap, float r,
-                                                       int stage, float* __restrict__ out,
+                                                       int stageRt, float* __restrict__ out,
                                                        unsigned long long* __restrict__ work) {
     // per warp: pos.xyz|normal.x, flux.xyz|normal.y, normal.z of `stage` photons
-    extern __shared__ float4 gatherTile[];
+    const int stage = kStage > 0 ? kStage : stageRt;
+    float4* gatherTile;
+    if constexpr (kStage > 0) {
+        __shared__ float4 tileFixed[2 * kWarps * kStage + (kWarps * kStage + 3) / 4];
+        gatherTile = tileFixed;
+    } else {
+        extern __shared__ float4 tileDynamic[];
+        gatherTile = tileDynamic;
+    }
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t n = qcount ? min((int64_t)*qcount, qcap) : qcap;
@@ -337,15 +347,27 @@ cudaError_t launchGatherSorted(const GridDev& g, QueryView qv, QuerySortBufs& qs
     const unsigned blocks = (unsigned)std::max<int64_t>(1, (qv.n + kTileQ * kQ - 1) / (kTileQ * kQ));
     const float4* sq = qs.sorted.as<float4>();
     const int stage = qs.stage;
+    if (stage == PPPM_GATHER_WSTAGE) {
+        constexpr int S = PPPM_GATHER_WSTAGE;
+        if (accumulate && work)
+            kGatherTiled<true, true, S><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, S, out, work);
+        else if (accumulate)
+            kGatherTiled<true, false, S><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, S, out, work);
+        else if (work)
+            kGatherTiled<false, true, S><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, S, out, work);
+        else
+            kGatherTiled<false, false, S><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, S, out, work);
+        return cudaGetLastError();
+    }
     const size_t smem = gatherSmem(stage);
     if (accumulate && work)
-        kGatherTiled<true, true><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
+        kGatherTiled<true, true, 0><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
     else if (accumulate)
-        kGatherTiled<true, false><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
+        kGatherTiled<true, false, 0><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
     else if (work)
-        kGatherTiled<false, true><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
+        kGatherTiled<false, true, 0><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
     else
-        kGatherTiled<false, false><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
+        kGatherTiled<false, false, 0><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
     return cudaGetLastError();
 }
 

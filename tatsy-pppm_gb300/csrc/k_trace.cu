@@ -381,9 +381,9 @@ __device__ __forceinline__ void photonHit(const TraceParams& tp, const SceneView
 // lanes whose path ended take the next path of the emitted queue (one
 // atomic per warp). A path's own random numbers and traversal are those of
 // the per-bounce kernels; only the order in which paths are processed and
-// deposits appended changes.
-
-template <bool kSss>
+// deposits appended changes. kFixed: the default refill and exact-test
+// thresholds as constants (the tuned values are read from tp otherwise).
+template <bool kSss, bool kFixed>
 __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(TraceParams tp, SceneView sc,
                                                                                const PathState* __restrict__ in,
                                                                                int64_t maxPaths, float4* __restrict__ dep,
@@ -430,7 +430,8 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonPersistent(T
             if (__any_sync(0xffffffffu, !has) && b + __popc(empty) < (unsigned long long)n) continue;
         }
         if (!__any_sync(0xffffffffu, has)) break;
-        warpTravRun(s, has, tp.refill, sc.nodes, sc.tris, order, sTop, &visits, &tests, sc.triE, tp.exactBatch);
+        warpTravRun(s, has, kFixed ? kRefill : tp.refill, sc.nodes, sc.tris, order, sTop, &visits, &tests, sc.triE,
+                    kFixed ? kExactBatch : tp.exactBatch);
         const bool fin = has && s.done();
         bool store = false;
         float4 da, db;
@@ -881,11 +882,14 @@ cudaError_t launchPhotonPersistent(const TraceParams& tp, const SceneView& sc, c
                                    float4* deposits, int64_t depositCap, PassCounters* ctr, cudaStream_t st,
                                    const uint32_t* perm) {
     // resident warps only: every block stays until the queue is drained
-    const unsigned blocks = 152 * PPPM_TRACE_MINBLOCKS;
+    const unsigned blocks = 152 * std::max(1, std::min(tp.bouncePerSm, PPPM_TRACE_MINBLOCKS));
+    const bool fixed = tp.refill == kRefill && tp.exactBatch == kExactBatch;
     if (tp.sssPass)
-        kPhotonPersistent<true><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr, perm);
+        kPhotonPersistent<true, false><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr, perm);
+    else if (fixed)
+        kPhotonPersistent<false, true><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr, perm);
     else
-        kPhotonPersistent<false><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr, perm);
+        kPhotonPersistent<false, false><<<blocks, 128, 0, st>>>(tp, sc, in, maxPaths, deposits, depositCap, ctr, perm);
     return cudaGetLastError();
 }
 

@@ -94,7 +94,8 @@ def test_batch_graph_matches_batch_without_graph():
             for i in ids:
                 img, st = b.result(i)
                 assert st["passes"] == 10 and st["rays"] > 0
-                assert st["graph_passes"] == (4 if use_graph else 0)
+                # every pass after the first, the 6 tuning passes (2 candidates) included
+                assert st["graph_passes"] == (9 if use_graph else 0) and st["tune_passes"] == 6
                 imgs.setdefault(i, []).append(img)
         finally:
             b.close()
