@@ -94,22 +94,26 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
                                                        unsigned long long* __restrict__ work) {
     // per warp: pos.xyz|normal.x, flux.xyz|normal.y, normal.z of `stage` photons
     const int stage = kStage > 0 ? kStage : stageRt;
-    float4* gatherTile;
-    if constexpr (kStage > 0) {
-        __shared__ float4 tileFixed[2 * kWarps * kStage + (kWarps * kStage + 3) / 4];
-        gatherTile = tileFixed;
-    } else {
-        extern __shared__ float4 tileDynamic[];
-        gatherTile = tileDynamic;
-    }
-
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t n = qcount ? min((int64_t)*qcount, qcap) : qcap;
     const int64_t base = ((int64_t)blockIdx.x * kWarps + warp) * (32 * kQ);
     if (base >= n) return;  // uniform for the warp; the kernel has no block barrier
-    float4* wA = gatherTile + (size_t)warp * stage;
-    float4* wB = gatherTile + (size_t)(kWarps + warp) * stage;
-    float* wC = reinterpret_cast<float*>(gatherTile + (size_t)2 * kWarps * stage) + (size_t)warp * stage;
+    float4* wA;
+    float4* wB;
+    float* wC;
+    if constexpr (kStage > 0) {
+        __shared__ float4 sA[kWarps][kStage > 0 ? kStage : 1];
+        __shared__ float4 sB[kWarps][kStage > 0 ? kStage : 1];
+        __shared__ float sC[kWarps][kStage > 0 ? kStage : 1];
+        wA = sA[warp];
+        wB = sB[warp];
+        wC = sC[warp];
+    } else {
+        extern __shared__ float4 tileDynamic[];
+        wA = tileDynamic + (size_t)warp * stage;
+        wB = tileDynamic + (size_t)(kWarps + warp) * stage;
+        wC = reinterpret_cast<float*>(tileDynamic + (size_t)2 * kWarps * stage) + (size_t)warp * stage;
+    }
     // position and normal of each query stay in registers; its weight and
     // pixel are read again for the final write
     float3 q0[kQ], q1[kQ];
@@ -307,6 +311,29 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
 
 }  // namespace
 
+namespace {
+
+// Tiles of kStage photons in static shared memory (64, 128, 256), or of
+// `stage` photons in dynamic shared memory (kStage 0). Static tiles let the
+// compiler address them as shared memory directly: the same kernel with its
+// tiles behind a generic pointer ran 4 % slower.
+template <int kStage>
+cudaError_t gatherLaunch(const GridDev& g, const float4* sq, const uint32_t* total, int64_t n, float radius, int stage,
+                         float* out, bool accumulate, unsigned long long* work, unsigned blocks, cudaStream_t st) {
+    const size_t smem = kStage > 0 ? 0 : gatherSmem(stage);
+    if (accumulate && work)
+        kGatherTiled<true, true, kStage><<<blocks, kTileQ, smem, st>>>(g, sq, total, n, radius, stage, out, work);
+    else if (accumulate)
+        kGatherTiled<true, false, kStage><<<blocks, kTileQ, smem, st>>>(g, sq, total, n, radius, stage, out, work);
+    else if (work)
+        kGatherTiled<false, true, kStage><<<blocks, kTileQ, smem, st>>>(g, sq, total, n, radius, stage, out, work);
+    else
+        kGatherTiled<false, false, kStage><<<blocks, kTileQ, smem, st>>>(g, sq, total, n, radius, stage, out, work);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t querySortLayout(QuerySortBufs& qs, int64_t maxQueries) {
     uint32_t size = 1u << 10;
     while ((int64_t)size < 2 * maxQueries && size < (1u << 26)) size <<= 1;
@@ -346,29 +373,12 @@ cudaError_t launchGatherSorted(const GridDev& g, QueryView qv, QuerySortBufs& qs
     const uint32_t* total = qs.hist.as<uint32_t>() + qs.size;
     const unsigned blocks = (unsigned)std::max<int64_t>(1, (qv.n + kTileQ * kQ - 1) / (kTileQ * kQ));
     const float4* sq = qs.sorted.as<float4>();
-    const int stage = qs.stage;
-    if (stage == PPPM_GATHER_WSTAGE) {
-        constexpr int S = PPPM_GATHER_WSTAGE;
-        if (accumulate && work)
-            kGatherTiled<true, true, S><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, S, out, work);
-        else if (accumulate)
-            kGatherTiled<true, false, S><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, S, out, work);
-        else if (work)
-            kGatherTiled<false, true, S><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, S, out, work);
-        else
-            kGatherTiled<false, false, S><<<blocks, kTileQ, 0, st>>>(g, sq, total, qv.n, radius, S, out, work);
-        return cudaGetLastError();
+    switch (qs.stage) {
+        case 64: return gatherLaunch<64>(g, sq, total, qv.n, radius, 64, out, accumulate, work, blocks, st);
+        case 128: return gatherLaunch<128>(g, sq, total, qv.n, radius, 128, out, accumulate, work, blocks, st);
+        case 256: return gatherLaunch<256>(g, sq, total, qv.n, radius, 256, out, accumulate, work, blocks, st);
+        default: return gatherLaunch<0>(g, sq, total, qv.n, radius, qs.stage, out, accumulate, work, blocks, st);
     }
-    const size_t smem = gatherSmem(stage);
-    if (accumulate && work)
-        kGatherTiled<true, true, 0><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
-    else if (accumulate)
-        kGatherTiled<true, false, 0><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
-    else if (work)
-        kGatherTiled<false, true, 0><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
-    else
-        kGatherTiled<false, false, 0><<<blocks, kTileQ, smem, st>>>(g, sq, total, qv.n, radius, stage, out, work);
-    return cudaGetLastError();
 }
 
 }  // namespace pppm
