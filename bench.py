@@ -669,7 +669,8 @@ def equal_time_study(ctx, scene, common, seeds=3, ref_passes=4096, budget_passes
 # ---------------------------------------------------------------- config 4
 def run_batch(args, as_extra=False):
     """Batched uneven jobs: aggregate Mrays/s over the whole batch and per-job
-    pass latency p50/p99 (wall time of each pppm_render_pass)."""
+    pass latency p50/p99 (device time of each pass inside the batch graphs;
+    wall time of the eager first pass)."""
     import pppm_gb300 as P
     import scenes as S
 
@@ -691,7 +692,9 @@ def run_batch(args, as_extra=False):
     rays = sum(s["rays"] for s in stats)
     shapes = {}
     for s in stats:
-        k = f'cell {s["cell_factor"]:.2f} bounce {s["bounce_blocks_per_sm"]} eye {s["eye_blocks_per_sm"]}'
+        k = (f'candidate {s["tune_candidate"]}: cell {s["cell_factor"]:.2f} bounce {s["bounce_blocks_per_sm"]} '
+             f'eye {s["eye_blocks_per_sm"]} refill {s["refill"]} exact {s["exact_batch"]} '
+             f'stage {s["gather_stage"]} sub {s["query_sub_bits"]}')
         shapes[k] = shapes.get(k, 0) + 1
     line = {"metric": "aggregate Mrays/s over 64 batched uneven jobs (config 4)", "value": rays / wall / 1e6,
             "unit": "Mrays/s", "n_gpus": 1, "steps": 16, "warmup": 0, "ms_per_step": wall * 1e3 / 16,
@@ -704,7 +707,10 @@ def run_batch(args, as_extra=False):
                       "graph_s": stats[0]["batch_graph_ms"] / 1e3,
                       "graph_capture_s": stats[0]["batch_graph_capture_ms"] / 1e3,
                       "graph_instantiate_s": stats[0]["batch_graph_instantiate_ms"] / 1e3,
-                      "autotuned_shapes": shapes},
+                      "autotuned_shapes": shapes,
+                      "tuning": (f"{stats[0]['tune_passes']} of 16 passes per job: {stats[0]['tune_passes'] // 3} "
+                                 "candidate settings of every pppm_tune knob, 3 interleaved passes each, captured "
+                                 "in the first batch graph; the rest of the job runs the lowest median")},
             "clocks": clk.summary()}
     b.close()
     if as_extra:
