@@ -4,9 +4,13 @@
 // encoding of 128 rows, and runs the four GEMMs as tcgen05.mma (M=128,
 // N=64/48, K=16 steps) with the FP32 accumulator in TMEM. After each layer
 // the four warps read their 32 rows back with tcgen05.ld, add the bias,
-// apply ReLU, and write the FP16 activations as the next A operand. Every
-// mbarrier wait is bounded; on a timeout the CTA records an error, waits for
-// its MMAs to drain and frees its TMEM.
+// apply ReLU, and write the FP16 activations as the next A operand. The
+// last layer's outputs go through the (then free) A buffer so that the
+// tile's 20 KB of results leave in coalesced 16-byte stores, and each
+// thread loads its row of the next tile before the current tile's GEMMs so
+// that the input latency overlaps them. Every mbarrier wait is bounded; on a
+// timeout the CTA records an error, waits for its MMAs to drain and frees
+// its TMEM.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -30,7 +34,7 @@ constexpr int kSmemTotal = kSmemW + kSmemBias + kSmemA + 64 + 1024;  // + barrie
 
 __global__ void __launch_bounds__(128) kMlpForward(MlpInputs in, const uint8_t* __restrict__ blob, int64_t cap,
                                                    const unsigned long long* count, float* __restrict__ out,
-                                                   int* __restrict__ err) {
+                                                   int* __restrict__ err, bool vecOut) {
     const int64_t n = count ? min((int64_t)*count, cap) : cap;
     extern __shared__ uint8_t smemRaw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~(uintptr_t)1023);
@@ -62,13 +66,24 @@ __global__ void __launch_bounds__(128) kMlpForward(MlpInputs in, const uint8_t* 
     uint32_t phase = 0;
     bool ok = true;
 
+    float cur[6];
+    {
+        const int64_t row0 = (int64_t)blockIdx.x * kMlpRows + tid;
+        mlpLoadRow(in, row0 < n ? row0 : -1, cur);
+    }
     for (int64_t tile = blockIdx.x; ok && tile * kMlpRows < n; tile += gridDim.x) {
         const int64_t row = tile * kMlpRows + tid;
         {
             float f[kMlpIn];
-            mlpFeatures(in, row < n ? row : -1, f);
+            mlpFeaturesOf(in, cur, row < n, f);
 #pragma unroll
             for (int c = 0; c < kMlpIn / 8; c++) storeChunk(sA, mlpCanon(tid, 8 * c, kMlpIn), f + 8 * c);
+        }
+        // the next tile's row, in flight during this tile's GEMMs
+        float nxt[6];
+        {
+            const int64_t nrow = (tile + gridDim.x) * kMlpRows + tid;
+            mlpLoadRow(in, nrow < n ? nrow : -1, nxt);
         }
         asyncProxyFence();
         tcFenceBefore();
@@ -107,12 +122,27 @@ __global__ void __launch_bounds__(128) kMlpForward(MlpInputs in, const uint8_t* 
                 asyncProxyFence();
                 tcFenceBefore();
                 __syncthreads();
-            } else if (row < n) {
-                float* o = out + row * kMlpOut;
+            } else {
+                // the tile's outputs, row-major in the A buffer (its MMAs are done)
+                float4* sOut = reinterpret_cast<float4*>(sA);
 #pragma unroll
-                for (int j = 0; j < kMlpOut; j++) o[j] = v[j] + bias[j];
+                for (int c = 0; c < kMlpOut / 4; c++)
+                    sOut[tid * (kMlpOut / 4) + c] = make_float4(v[4 * c] + bias[4 * c], v[4 * c + 1] + bias[4 * c + 1],
+                                                                v[4 * c + 2] + bias[4 * c + 2], v[4 * c + 3] + bias[4 * c + 3]);
+                __syncthreads();
+                const int rows = (int)min((int64_t)kMlpRows, n - tile * kMlpRows);
+                if (vecOut) {
+                    float4* o = reinterpret_cast<float4*>(out + tile * kMlpRows * kMlpOut);
+                    for (int i = tid; i < rows * (kMlpOut / 4); i += blockDim.x) o[i] = sOut[i];
+                } else {
+                    float* o = out + tile * kMlpRows * kMlpOut;
+                    const float* so = reinterpret_cast<const float*>(sOut);
+                    for (int i = tid; i < rows * kMlpOut; i += blockDim.x) o[i] = so[i];
+                }
             }
         }
+#pragma unroll
+        for (int i = 0; i < 6; i++) cur[i] = nxt[i];
         tcFenceBefore();
         __syncthreads();
     }
@@ -141,8 +171,9 @@ cudaError_t launchMlpForward(const MlpInputs& in, const uint8_t* blob, int64_t n
     }
     if (n <= 0) return cudaSuccess;
     const int64_t tiles = (n + kMlpRows - 1) / kMlpRows;
-    const unsigned grid = (unsigned)std::min<int64_t>(tiles, 152 * 3);
-    kMlpForward<<<grid, 128, kSmemTotal, st>>>(in, blob, n, count, out, err);
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, 152 * 4);  // 4 CTAs per SM fit the shared memory
+    const bool vecOut = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    kMlpForward<<<grid, 128, kSmemTotal, st>>>(in, blob, n, count, out, err, vecOut);
     return cudaGetLastError();
 }
 

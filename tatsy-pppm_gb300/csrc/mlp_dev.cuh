@@ -35,18 +35,27 @@ inline MlpInputs mlpInputs(const double* bbox, const float* pos, const float* nr
 
 // features[a*24 + 2k] = sin(2^k pi x_a), [a*24 + 2k + 1] = cos(2^k pi x_a),
 // x_a the normalised coordinate; [72..74] = normal; [75..79] = 0.
+// Every fourth frequency is evaluated directly (sincospif of 2^k x_a, an
+// exact argument); the three above it by the double-angle identities
+// sin 2t = 2 sin t cos t, cos 2t = (cos t - sin t)(cos t + sin t), each of
+// which at most doubles the absolute error: under 1e-6 after three steps,
+// far below the FP16 rounding (2^-11) the features then go through.
 __device__ __forceinline__ void mlpEncode(float x, float y, float z, float nx, float ny, float nz, float* f) {
     const float c[3] = {x, y, z};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        float s = c[a];
 #pragma unroll
-        for (int k = 0; k < kMlpFreqs; k++) {
+        for (int k0 = 0; k0 < kMlpFreqs; k0 += 4) {
             float sn, cs;
-            sincospif(s, &sn, &cs);
-            f[a * 24 + 2 * k] = sn;
-            f[a * 24 + 2 * k + 1] = cs;
-            s *= 2.0f;
+            sincospif(c[a] * (float)(1 << k0), &sn, &cs);
+#pragma unroll
+            for (int k = k0; k < k0 + 4 && k < kMlpFreqs; k++) {
+                f[a * 24 + 2 * k] = sn;
+                f[a * 24 + 2 * k + 1] = cs;
+                const float s2 = 2.0f * sn * cs;
+                cs = (cs - sn) * (cs + sn);
+                sn = s2;
+            }
         }
     }
     f[72] = nx;
@@ -54,6 +63,33 @@ __device__ __forceinline__ void mlpEncode(float x, float y, float z, float nx, f
     f[74] = nz;
 #pragma unroll
     for (int i = 75; i < kMlpIn; i++) f[i] = 0.0f;
+}
+
+// The 6 input floats of a row (position, normal), or zeros for row < 0.
+__device__ __forceinline__ void mlpLoadRow(const MlpInputs& in, int64_t row, float* r) {
+    if (row < 0) {
+#pragma unroll
+        for (int i = 0; i < 6; i++) r[i] = 0.0f;
+        return;
+    }
+    const float* p = in.pos + 3 * row;
+    const float* n = in.nrm + 3 * row;
+    r[0] = __ldg(p);
+    r[1] = __ldg(p + 1);
+    r[2] = __ldg(p + 2);
+    r[3] = __ldg(n);
+    r[4] = __ldg(n + 1);
+    r[5] = __ldg(n + 2);
+}
+
+// Features of a row loaded by mlpLoadRow (valid = false: all zero).
+__device__ __forceinline__ void mlpFeaturesOf(const MlpInputs& in, const float* r, bool valid, float* f) {
+    if (!valid) {
+#pragma unroll
+        for (int i = 0; i < kMlpIn; i++) f[i] = 0.0f;
+        return;
+    }
+    mlpEncode((r[0] - in.ox) * in.sx, (r[1] - in.oy) * in.sy, (r[2] - in.oz) * in.sz, r[3], r[4], r[5], f);
 }
 
 __device__ __forceinline__ void mlpFeatures(const MlpInputs& in, int64_t row, float* f) {
