@@ -97,6 +97,24 @@ __device__ float vmfLossGrad(const float* raw, float dx, float dy, float dz, flo
     return -s * logq;
 }
 
+// Column sums of a warp's 64 x 32 values (t[j] of lane i: column j, record
+// i): five halving steps with shuffles; afterwards lane i holds in t[0] and
+// t[1] the sums of columns c and c + 1, c = 32 b4 + 16 b3 + 8 b2 + 4 b1 + 2 b0
+// for the bits b4..b0 of i. t[2..63] are left undefined.
+__device__ __forceinline__ void warpColumnSums(float* t) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int half = 32, off = 16; half >= 2; half >>= 1, off >>= 1) {
+        const bool upper = (lane & off) != 0;
+#pragma unroll
+        for (int j = 0; j < half; j++) {
+            const float send = upper ? t[j] : t[j + half];
+            const float keep = upper ? t[j + half] : t[j];
+            t[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128, 1) kMlpTrain(const MlpRecord* __restrict__ rec, int64_t n, const float* invSumW,
                                                     MlpInputs box, const uint8_t* __restrict__ blob,
                                                     float* __restrict__ grad, float* __restrict__ loss,
@@ -238,9 +256,19 @@ __global__ void __launch_bounds__(128, 1) kMlpTrain(const MlpRecord* __restrict_
 #pragma unroll
                 for (int c = 0; c < Kout / 8; c++) storeChunk(sA, mlpCanon(tid, 8 * c, Kout), g + 8 * c);
             }
-            const int bOff = l * kMlpHidden;
-            for (int o = 0; o < nOut; o++)
-                if (g[o] != 0.0f) atomicAdd(&sBg[bOff + o], g[o]);
+            // bias gradient: the column sums of dZ over the warp's 32 records by
+            // recursive halving (each step a lane keeps half of its columns and
+            // adds its partner's copy of them), then one shared atomic per lane
+            // and column pair instead of one per record and column
+            warpColumnSums(g);
+            {
+                const int lane = tid & 31;
+                const int col = ((lane >> 4) & 1) * 32 + ((lane >> 3) & 1) * 16 + ((lane >> 2) & 1) * 8 +
+                                ((lane >> 1) & 1) * 4 + (lane & 1) * 2;
+                const int bOff = l * kMlpHidden;
+                if (col < nOut && g[0] != 0.0f) atomicAdd(&sBg[bOff + col], g[0]);
+                if (col + 1 < nOut && g[1] != 0.0f) atomicAdd(&sBg[bOff + col + 1], g[1]);
+            }
             syncForMma();
             if (tid == 0) {
                 tcFenceAfter();
