@@ -484,7 +484,9 @@ typedef struct pppm_tune {
 /* Sets the knobs of an active render from the next pass on; a field < 0
  * (cell_factor <= 0) keeps its current value, a value out of range is
  * PPPM_E_ARG and changes nothing. render_begin restores the defaults
- * (1, 64, 64, 24, 12, 128, 1). No counterpart in the reference. */
+ * (1, 64, 64, 24, 12, 128, and 3 query sub-cell bits where the query sort
+ * keeps 4096 cell buckets with them, 1080p and up; fewer for smaller
+ * images, at least 1). No counterpart in the reference. */
 int pppm_render_tune_ex(pppm_ctx* ctx, const pppm_tune* tune);
 
 /* The knobs the next pass of the active render will use. */

@@ -42,6 +42,7 @@ struct pppm_batch {
         int64_t rays = 0;
         float cell = 1.0f;
         int bounceBlocks = 16, eyeBlocks = 16;
+        pppm_tune base{};         // knobs the render began with
         pppm_tune tune{};         // knobs after the tuning
         std::vector<int> plan;    // candidate of each tuning pass
         int chosen = -1;          // candidate kept (-1: no tuning)
@@ -71,17 +72,20 @@ int jobFail(pppm_batch::Job& j, int code) {
 // knob (cell factor, bounce and eye blocks per SM, refill, exact batch,
 // gather tile, query sub-cell bits). A job with P passes tries the first
 // min(6, (P - 2) / kRounds) of them.
+// query_sub_bits -1: the render's own choice (set by the image size)
 const pppm_tune kCandidates[] = {
-    {1.0f, 64, 64, 24, 12, 128, 1}, {1.25f, 64, 64, 24, 12, 256, 2}, {1.0f, 32, 32, 16, 8, 128, 1},
-    {1.0f, 64, 64, 32, 16, 64, 0},  {1.5f, 64, 64, 24, 12, 256, 2},  {1.0f, 5, 32, 24, 12, 128, 1},
+    {1.0f, 64, 64, 24, 12, 128, -1}, {1.25f, 64, 64, 24, 12, 256, 2}, {1.0f, 32, 32, 16, 8, 128, 3},
+    {1.0f, 64, 64, 32, 16, 64, 1},   {1.5f, 64, 64, 24, 12, 256, 2},  {1.0f, 5, 32, 24, 12, 128, -1},
 };
 constexpr int kNumCandidates = (int)(sizeof(kCandidates) / sizeof(kCandidates[0]));
 constexpr int kRounds = 3;  // timed passes per candidate
 
-// The knobs of candidate k for a render of this mode: compat renders keep
-// their cell size (it follows k) and use the kNN gather (no tiles).
-pppm_tune candidate(int k, bool canonical) {
+// The knobs of candidate k for a render of this mode (base: the knobs the
+// render began with): compat renders keep their cell size (it follows k)
+// and use the kNN gather (no tiles).
+pppm_tune candidate(int k, bool canonical, const pppm_tune& base) {
     pppm_tune t = kCandidates[k];
+    if (t.query_sub_bits < 0) t.query_sub_bits = base.query_sub_bits;
     if (!canonical) {
         t.cell_factor = 0.0f;
         t.gather_stage = -1;
@@ -132,6 +136,7 @@ int runJob(pppm_batch::Job& j, bool autotune, bool useGraph) {
     pppm_ctx* c = j.ctx;
     int r = pppm_render_begin(c, &j.cam, &j.par);
     if (r) return jobFail(j, r);
+    pppm_render_get_tune(c, &j.base);
     const bool canonical = j.par.mode == PPPM_MODE_CANONICAL;
     j.plan = tuningPlan(j.passes, autotune);
     j.chosen = -1;
@@ -145,11 +150,11 @@ int runJob(pppm_batch::Job& j, bool autotune, bool useGraph) {
     for (int t = 1; t <= eager; t++) {
         const int i = t - 2;  // tuning pass index
         if (i >= 0 && i < nPlan) {
-            const pppm_tune s = candidate(j.plan[i], canonical);
+            const pppm_tune s = candidate(j.plan[i], canonical, j.base);
             pppm_render_tune_ex(c, &s);
         } else if (nPlan > 0 && i == nPlan) {
             j.chosen = bestCandidate(j.plan, dev);
-            const pppm_tune s = candidate(j.chosen, canonical);
+            const pppm_tune s = candidate(j.chosen, canonical, j.base);
             pppm_render_tune_ex(c, &s);
         }
         pppm_pass_stats st;
@@ -234,7 +239,7 @@ int runGraph(pppm_batch* b, std::vector<pppm_batch::Job*>& gj, int lanes, bool t
         const bool canonical = gj[k]->par.mode == PPPM_MODE_CANONICAL;
         for (int i = 0; i < passesIn(*gj[k], tuning); i++) {
             if (tuning) {
-                const pppm_tune s = candidate(gj[k]->plan[i], canonical);
+                const pppm_tune s = candidate(gj[k]->plan[i], canonical, gj[k]->base);
                 pppm_render_tune_ex(c, &s);
             }
             const int r = graphEnqueuePass(c, first + i, i, false);
@@ -275,7 +280,7 @@ int runGraph(pppm_batch* b, std::vector<pppm_batch::Job*>& gj, int lanes, bool t
         if (tuning && j->status == PPPM_OK) {
             // the remaining passes run the fastest candidate
             j->chosen = bestCandidate(j->plan, dev);
-            const pppm_tune s = candidate(j->chosen, j->par.mode == PPPM_MODE_CANONICAL);
+            const pppm_tune s = candidate(j->chosen, j->par.mode == PPPM_MODE_CANONICAL, j->base);
             pppm_render_tune_ex(j->ctx, &s);
             recordShape(*j);
         }

@@ -53,12 +53,14 @@ struct GridBufs {
 // Counting sort of gather queries by grid cell (tiled gather).
 // Canonical gather shape (tunable per render; neither changes a result):
 // photons per warp tile (a multiple of 32, 32..256) and sub-cells per axis
-// of the query sort key (2^bits, bits 0..3).
+// of the query sort key (2^bits, bits 0..3). querySortLayout sets the bits
+// to the most, up to PPPM_GATHER_SUBBITS, that leave the sort at least 4096
+// cell buckets (3 at 1080p; 1 for images of up to ~64k pixels).
 #ifndef PPPM_GATHER_WSTAGE
 #define PPPM_GATHER_WSTAGE 128
 #endif
 #ifndef PPPM_GATHER_SUBBITS
-#define PPPM_GATHER_SUBBITS 1
+#define PPPM_GATHER_SUBBITS 3
 #endif
 constexpr int kGatherStageMax = 256;
 

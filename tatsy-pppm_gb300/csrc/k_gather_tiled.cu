@@ -338,6 +338,11 @@ cudaError_t querySortLayout(QuerySortBufs& qs, int64_t maxQueries) {
     uint32_t size = 1u << 10;
     while ((int64_t)size < 2 * maxQueries && size < (1u << 26)) size <<= 1;
     qs.size = size;
+    // sub-cell bits: the most (up to the default) that keep 4096 cell
+    // buckets; at least 1
+    int bits = 1;
+    while (bits < PPPM_GATHER_SUBBITS && (size >> (3 * (bits + 1))) >= 4096u) bits++;
+    qs.subBits = bits;
     cudaError_t e;
     if ((e = qs.hist.ensure(((size_t)size + 1) * 4)) != cudaSuccess) return e;
     if ((e = qs.cursor.ensure(((size_t)size + 1) * 4)) != cudaSuccess) return e;

@@ -353,8 +353,7 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     rs.eyePerSm = 64;
     rs.refill = kRefill;
     rs.exactBatch = kExactBatch;
-    rs.qsort.stage = PPPM_GATHER_WSTAGE;
-    rs.qsort.subBits = PPPM_GATHER_SUBBITS;
+    rs.qsort.stage = PPPM_GATHER_WSTAGE;  // (querySortLayout below sets the sub-cell bits)
     const double dx = c->bbmax[0] - c->bbmin[0], dy = c->bbmax[1] - c->bbmin[1], dz = c->bbmax[2] - c->bbmin[2];
     rs.bboxDiag = std::sqrt(dx * dx + dy * dy + dz * dz);
     rs.radius = rs.bboxDiag * par->radius_scale;  // ppm_probabilistic.cc:51-55
