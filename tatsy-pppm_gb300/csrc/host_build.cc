@@ -25,22 +25,35 @@ struct TempNode {
     int sep;
 };
 
-struct Builder {
-    const float* tri9;
-    std::vector<Item> items;
+// Nodes and leaf slots of a subtree, as the serial construction would lay
+// them out: the subtree's root first, then its children's subtrees in
+// child order (depth-first); leaf slots in the same order.
+struct Part {
     std::vector<TempNode> nodes;
     std::vector<float> slots;
     int maxDepth = 0;
+};
 
-    int makeLeaf(int lo, int hi) {
-        const int first = (int)(slots.size() / 12);
+// Subtrees of at least this many triangles, above this depth, are built as
+// OpenMP tasks into parts of their own and appended in child order, which
+// reproduces the serial layout exactly (the sorts of disjoint ranges are
+// independent; each range is sorted by the same std::sort call).
+constexpr int kTaskTris = 1 << 14;
+constexpr int kTaskDepth = 6;
+
+struct Builder {
+    const float* tri9;
+    std::vector<Item> items;
+
+    int makeLeaf(Part& P, int lo, int hi) const {
+        const int first = (int)(P.slots.size() / 12);
         for (int i = lo; i < hi; i++) {
             const float* t = tri9 + 9 * (int64_t)items[i].id;
             float idbits;
             const int id = items[i].id;
             std::memcpy(&idbits, &id, 4);
             const float rec[12] = {t[0], t[1], t[2], idbits, t[3], t[4], t[5], 0.0f, t[6], t[7], t[8], 0.0f};
-            slots.insert(slots.end(), rec, rec + 12);
+            P.slots.insert(P.slots.end(), rec, rec + 12);
         }
         return ~((first << 2) | (hi - lo));
     }
@@ -64,15 +77,31 @@ struct Builder {
                   [dim](const Item& x, const Item& y) { return x.g[dim] < y.g[dim]; });
     }
 
-    // constructRec (qbvh_accel.cc:150-203) on items[lo, hi).
-    int rec(int lo, int hi, int dim, int depth) {
+    // a child code of a part appended at (nodeOff, slotOff) of another
+    static int shift(int code, int nodeOff, int slotOff) {
+        if (code >= 0) return code + nodeOff;
+        const int lc = ~code;
+        return ~((((lc >> 2) + slotOff) << 2) | (lc & 3));
+    }
+
+    // constructRec (qbvh_accel.cc:150-203) on items[lo, hi), into P.
+    int rec(Part& P, int lo, int hi, int dim, int depth) {
         const int n = hi - lo;
-        if (n <= 3) return makeLeaf(lo, hi);
-        maxDepth = std::max(maxDepth, depth + 1);
+        if (n <= 3) return makeLeaf(P, lo, hi);
+        P.maxDepth = std::max(P.maxDepth, depth + 1);
         sortRange(lo, hi, dim);
         const int mid = n / 2;
-        sortRange(lo, lo + mid, (dim + 1) % 3);
-        sortRange(lo + mid, hi, (dim + 1) % 3);
+        const bool par = n >= kTaskTris && depth < kTaskDepth;
+        if (par) {
+#pragma omp task default(shared)
+            sortRange(lo, lo + mid, (dim + 1) % 3);
+#pragma omp task default(shared)
+            sortRange(lo + mid, hi, (dim + 1) % 3);
+#pragma omp taskwait
+        } else {
+            sortRange(lo, lo + mid, (dim + 1) % 3);
+            sortRange(lo + mid, hi, (dim + 1) % 3);
+        }
         const int cut[5] = {lo, lo + mid / 2, lo + mid, lo + mid + mid / 2, hi};
         TempNode nd;
         for (int c = 0; c < 4; c++) {
@@ -81,11 +110,31 @@ struct Builder {
             for (int d = 0; d < 3; d++) { nd.bmin[d][c] = mn[d]; nd.bmax[d][c] = mx[d]; }
         }
         nd.sep = dim | (((dim + 1) % 3) << 2) | (((dim + 1) % 3) << 4);
-        const int self = (int)nodes.size();
-        nodes.push_back(nd);
+        const int self = (int)P.nodes.size();
+        P.nodes.push_back(nd);
+        if (!par) {
+            for (int c = 0; c < 4; c++) {
+                const int code = rec(P, cut[c], cut[c + 1], (dim + 2) % 3, depth + 1);
+                P.nodes[self].child[c] = code;
+            }
+            return self;
+        }
+        Part sub[4];
+        int code[4];
         for (int c = 0; c < 4; c++) {
-            const int code = rec(cut[c], cut[c + 1], (dim + 2) % 3, depth + 1);
-            nodes[self].child[c] = code;
+#pragma omp task default(shared) firstprivate(c)
+            code[c] = rec(sub[c], cut[c], cut[c + 1], (dim + 2) % 3, depth + 1);
+        }
+#pragma omp taskwait
+        for (int c = 0; c < 4; c++) {
+            const int nodeOff = (int)P.nodes.size(), slotOff = (int)(P.slots.size() / 12);
+            for (TempNode t : sub[c].nodes) {
+                for (int k = 0; k < 4; k++) t.child[k] = shift(t.child[k], nodeOff, slotOff);
+                P.nodes.push_back(t);
+            }
+            P.slots.insert(P.slots.end(), sub[c].slots.begin(), sub[c].slots.end());
+            P.nodes[self].child[c] = shift(code[c], nodeOff, slotOff);
+            P.maxDepth = std::max(P.maxDepth, sub[c].maxDepth);
         }
         return self;
     }
@@ -110,36 +159,40 @@ bool buildQbvh(const float* tri9, int64_t ntri, HostBvh* out, std::string* err) 
         }
         b.items[i].id = (int)i;
     }
-    const int rootTemp = b.rec(0, (int)ntri, 0, 0);
-    if (b.maxDepth > 20) {
+    Part all;
+    int rootTemp = 0;
+#pragma omp parallel
+#pragma omp single
+    rootTemp = b.rec(all, 0, (int)ntri, 0, 0);
+    if (all.maxDepth > 20) {
         *err = "QBVH deeper than 20 levels";
         return false;
     }
-    out->tris.swap(b.slots);
-    out->depth = b.maxDepth;
+    out->tris.swap(all.slots);
+    out->depth = all.maxDepth;
     out->nodes.clear();
     if (rootTemp < 0) {
         out->rootCode = rootTemp;
         return true;
     }
     // BFS renumbering: top levels become contiguous from index 0.
-    std::vector<int> newIndex(b.nodes.size(), -1);
+    std::vector<int> newIndex(all.nodes.size(), -1);
     std::deque<int> q;
     q.push_back(rootTemp);
     int next = 0;
     std::vector<int> order;
-    order.reserve(b.nodes.size());
+    order.reserve(all.nodes.size());
     while (!q.empty()) {
         const int v = q.front();
         q.pop_front();
         newIndex[v] = next++;
         order.push_back(v);
         for (int c = 0; c < 4; c++)
-            if (b.nodes[v].child[c] >= 0) q.push_back(b.nodes[v].child[c]);
+            if (all.nodes[v].child[c] >= 0) q.push_back(all.nodes[v].child[c]);
     }
     out->nodes.resize(order.size());
     for (size_t k = 0; k < order.size(); k++) {
-        const TempNode& t = b.nodes[order[k]];
+        const TempNode& t = all.nodes[order[k]];
         HostQNode& h = out->nodes[k];
         std::memcpy(h.bmin, t.bmin, sizeof(h.bmin));
         std::memcpy(h.bmax, t.bmax, sizeof(h.bmax));
@@ -179,7 +232,9 @@ void envImportance(const float* rgb, int w, int h, std::vector<double>* pdf, std
     cdf->assign(W * H, 0.0);
     const int superX = w / W, superY = h / H;
     const double inv = 1.0 / (double)(superX * superY);
-    double total = 0.0;
+    // cells in parallel (each computed exactly as alone), then the total in
+    // the reference's cell order
+#pragma omp parallel for schedule(dynamic, 1)
     for (int iy = 0; iy < H; iy++) {
         for (int ix = 0; ix < W; ix++) {
             double acc[3] = {0.0, 0.0, 0.0};
@@ -200,9 +255,10 @@ void envImportance(const float* rgb, int w, int h, std::vector<double>* pdf, std
             const double l = acc[0] * 0.2126 + acc[1] * 0.7152 + acc[2] * 0.0722;
             const double wgt = exponent == 2.0 ? l * l : std::pow(l, exponent);
             (*pdf)[iy * W + ix] = wgt;
-            total += wgt;
         }
     }
+    double total = 0.0;
+    for (int i = 0; i < W * H; i++) total += (*pdf)[i];
     const double eps = 1.0e-12;
     (*pdf)[0] /= (total + eps);
     (*cdf)[0] = (*pdf)[0];
