@@ -19,21 +19,48 @@ __device__ __forceinline__ int64_t queryCount(const QueryView& qv) {
     return qv.count ? min((int64_t)*qv.count, qv.n) : qv.n;
 }
 
-// Sorted (ascending) candidate list of the k nearest photons.
+// Strict order of kNN candidates: squared distance, then (for the rare
+// exact FP32 ties) the photon's path id, position, flux and normal bits, so
+// that the selected set and its order do not depend on the order in which
+// deposits reached the photon map (atomic appends). Ties are not only
+// equidistant photons: a path whose next ray starts at its hit point (the
+// reference offsets nothing) can hit the same surface again at t ~ 1e-10
+// and deposit twice at the same position with another flux. id < 0: a
+// phantom record at the origin (all alike), after real photons at the same
+// distance.
+__device__ __forceinline__ bool knnBefore(float da, int ia, float db, int ib, const float4* __restrict__ rec) {
+    if (da != db) return da < db;
+    if (ia == ib || (ia < 0 && ib < 0)) return false;
+    if (ia < 0 || ib < 0) return ib < 0;
+    const uint32_t pa = __float_as_uint(__ldg(&rec[2 * (int64_t)ia + 1]).w);
+    const uint32_t pb = __float_as_uint(__ldg(&rec[2 * (int64_t)ib + 1]).w);
+    if (pa != pb) return pa < pb;
+    const float4 a = __ldg(&rec[2 * (int64_t)ia]), b = __ldg(&rec[2 * (int64_t)ib]);
+    const float4 fa = __ldg(&rec[2 * (int64_t)ia + 1]), fb = __ldg(&rec[2 * (int64_t)ib + 1]);
+    const uint32_t ka[7] = {__float_as_uint(a.x), __float_as_uint(a.y), __float_as_uint(a.z), __float_as_uint(fa.x),
+                            __float_as_uint(fa.y), __float_as_uint(fa.z), __float_as_uint(a.w)};
+    const uint32_t kb[7] = {__float_as_uint(b.x), __float_as_uint(b.y), __float_as_uint(b.z), __float_as_uint(fb.x),
+                            __float_as_uint(fb.y), __float_as_uint(fb.z), __float_as_uint(b.w)};
+    for (int i = 0; i < 7; i++)
+        if (ka[i] != kb[i]) return ka[i] < kb[i];
+    return false;  // identical records: either order gives the same list
+}
+
+// Sorted (ascending, knnBefore) candidate list of the k nearest photons.
 struct KnnList {
     float d2[kMaxKnn];
     int idx[kMaxKnn];
     int cnt;
-    __device__ __forceinline__ bool insert(float d, int id, int k) {
+    __device__ __forceinline__ bool insert(float d, int id, int k, const float4* __restrict__ rec) {
         int pos;
         if (cnt < k) {
             pos = cnt++;
-        } else if (d < d2[k - 1]) {
+        } else if (knnBefore(d, id, d2[k - 1], idx[k - 1], rec)) {
             pos = k - 1;
         } else {
             return false;
         }
-        while (pos > 0 && d2[pos - 1] > d) {
+        while (pos > 0 && knnBefore(d, id, d2[pos - 1], idx[pos - 1], rec)) {
             d2[pos] = d2[pos - 1];
             idx[pos] = idx[pos - 1];
             pos--;
@@ -61,7 +88,7 @@ __device__ __forceinline__ void knnVisit(const GridDev& g, int cx, int cy, int c
             continue;
         const float dx = qx - a.x, dy = qy - a.y, dz = qz - a.z;
         const float d2 = dx * dx + dy * dy + dz * dz;
-        if (d2 < eps2) L.insert(d2, (int)j, k);
+        if (d2 < eps2) L.insert(d2, (int)j, k, g.rec);
     }
 }
 
@@ -112,7 +139,7 @@ __device__ void knnSearch(const GridDev& g, float qx, float qy, float qz, int k,
         if (d2 < eps2) {
             const int64_t np = phantoms < k ? phantoms : k;
             for (int64_t t = 0; t < np; t++)
-                if (!L.insert(d2, -1, k)) break;
+                if (!L.insert(d2, -1, k, g.rec)) break;
         }
     }
 }

@@ -241,3 +241,21 @@ def test_full_size_compat_pass_matches_port():
     16 XorShift streams, kNN gather, phantom slots), against the port that
     the golden fixtures pin to the reference."""
     _full_size_pass(P.MODE_COMPAT)
+
+
+def test_compat_render_is_reproducible(ctx):
+    """Compat renders repeat bit for bit: deposits reach the photon map in a
+    different order every run (atomic appends), and the k-nearest search
+    orders exact distance ties by the photon's path and position, not by
+    that order."""
+    sc = S.small_test_scene(seed=7, subdiv=3, width=96, height=64, photons=60_000)
+    ctx.set_scene(sc)
+    par = P.Context.make_params(mode=P.MODE_COMPAT, photons=60_000, num_streams=8, seed=2)
+    imgs = []
+    for _ in range(3):
+        ctx.render_begin(sc.camera, par)
+        for t in range(1, 5):
+            ctx.render_pass(t)
+        imgs.append(ctx.render_read().copy())
+    np.testing.assert_array_equal(imgs[0], imgs[1])
+    np.testing.assert_array_equal(imgs[0], imgs[2])
