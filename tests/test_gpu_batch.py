@@ -59,3 +59,30 @@ def test_short_jobs_are_not_tuned():
         assert st["tune_passes"] == 0 and st["tune_candidate"] == -1 and st["passes"] == 7
     finally:
         b.close()
+
+
+def test_batch_tunes_compat_jobs_eagerly():
+    """A compat job cannot be captured: it tunes through pppm_render_pass
+    over the knobs its gather has (blocks, refill, exact batch) and keeps
+    the reference's cell size; its image is the stand-alone render's."""
+    sc, alpha = S.config4_jobs(seed=13, n=1, min_side=64, max_side=64, min_tris=3_000, max_tris=3_000,
+                               min_photons=30_000, max_photons=30_000)[0]
+    par = P.Context.make_params(mode=P.MODE_COMPAT, photons=sc.photons, num_streams=8, max_bounce_photon=8,
+                                max_bounce_eye=8, alpha=alpha)
+    b = P.Batch(0)
+    c = P.Context(0)
+    try:
+        i = b.submit(sc, par, 10)
+        b.run(autotune=True, max_concurrent=1)
+        img, st = b.result(i)
+        assert st["graph_passes"] == 0 and st["tune_passes"] == 6 and 0 <= st["tune_candidate"] < 2, st
+        assert st["cell_factor"] == 1.0
+        c.set_scene(sc)
+        c.render_begin(sc.camera, par)
+        for t in range(1, 11):
+            c.render_pass(t)
+        # compat renders repeat bit for bit, whatever the launch shapes
+        np.testing.assert_array_equal(img, c.render_read())
+    finally:
+        c.close()
+        b.close()
