@@ -43,6 +43,8 @@ struct GridBufs {
     DBuf sorted;   // float4 x 2 per photon, bucket order
     DBuf keys;     // uint32 bucket per photon
     DBuf scanTmp;  // scan partials
+    DBuf owner;    // uint64 per bucket: the cell of its photons (GridDev::owner)
+    bool hasOwner = false;  // the last build recorded owner
     uint32_t size = 0;   // buckets (power of two)
     float cell = 0.0f;   // cell edge
     float invCell = 0.0f;

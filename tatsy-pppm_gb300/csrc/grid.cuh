@@ -19,7 +19,19 @@ struct GridDev {
     float ox, oy, oz;        // origin
     float invCell, cell;
     int nx, ny, nz;          // cells per axis
+    // per bucket the one cell its photons lie in (cellCode), kBucketMixed
+    // when photons of several cells share it, kBucketEmpty when it has none;
+    // nullptr when the build did not record it
+    const unsigned long long* owner = nullptr;
 };
+
+constexpr unsigned long long kBucketEmpty = ~0ull;
+constexpr unsigned long long kBucketMixed = ~0ull - 1;
+
+// cell coordinates (each below 2^20) packed into one 64-bit code
+__host__ __device__ __forceinline__ unsigned long long cellCode(int cx, int cy, int cz) {
+    return (unsigned long long)cx | ((unsigned long long)cy << 21) | ((unsigned long long)cz << 42);
+}
 
 __device__ __forceinline__ uint32_t bucketOf(int cx, int cy, int cz, uint32_t mask) {
     const uint32_t h = ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u) ^ ((uint32_t)cz * 83492791u);

@@ -80,11 +80,21 @@ struct KnnList {
 __device__ __forceinline__ void knnVisit(const GridDev& g, int cx, int cy, int cz, float qx, float qy, float qz,
                                          float eps2, int k, KnnList& L) {
     const uint32_t key = bucketOf(cx, cy, cz, g.mask);
+    // a bucket whose photons all lie in one cell: this cell's (no per-photon
+    // test) or another's (nothing to visit)
+    bool pure = false;
+    if (g.owner) {
+        const unsigned long long own = __ldg(&g.owner[key]);
+        if (own != kBucketMixed) {
+            if (own != cellCode(cx, cy, cz)) return;
+            pure = true;
+        }
+    }
     const uint32_t b0 = __ldg(&g.start[key]), b1 = __ldg(&g.start[key + 1]);
     for (uint32_t j = b0; j < b1; j++) {
         const float4 a = __ldg(&g.rec[2 * (int64_t)j]);
-        if (cellCoord(a.x, g.ox, g.invCell, g.nx) != cx || cellCoord(a.y, g.oy, g.invCell, g.ny) != cy ||
-            cellCoord(a.z, g.oz, g.invCell, g.nz) != cz)
+        if (!pure && (cellCoord(a.x, g.ox, g.invCell, g.nx) != cx || cellCoord(a.y, g.oy, g.invCell, g.ny) != cy ||
+                      cellCoord(a.z, g.oz, g.invCell, g.nz) != cz))
             continue;
         const float dx = qx - a.x, dy = qy - a.y, dz = qz - a.z;
         const float d2 = dx * dx + dy * dy + dz * dz;

@@ -12,8 +12,11 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanChunk = kScanThreads * kScanItems;  // 2048 counts per block
 
+// kOwner: also records each bucket's cell (first photon's cell by
+// compare-and-swap; a photon of another cell marks the bucket mixed)
+template <bool kOwner>
 __global__ void kKeys(const float4* __restrict__ rec, const uint64_t* __restrict__ count, int64_t capacity, GridDev g,
-                      uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
+                      uint32_t* __restrict__ keys, uint32_t* __restrict__ hist, unsigned long long* __restrict__ owner) {
     const int64_t n = min((int64_t)*count, capacity);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float4 a = rec[2 * i];
@@ -23,6 +26,11 @@ __global__ void kKeys(const float4* __restrict__ rec, const uint64_t* __restrict
         const uint32_t k = bucketOf(cx, cy, cz, g.mask);
         keys[i] = k;
         atomicAdd(&hist[k], 1u);
+        if (kOwner) {
+            const unsigned long long code = cellCode(cx, cy, cz);
+            const unsigned long long old = atomicCAS(&owner[k], kBucketEmpty, code);
+            if (old != kBucketEmpty && old != code && old != kBucketMixed) atomicExch(&owner[k], kBucketMixed);
+        }
     }
 }
 
@@ -197,11 +205,12 @@ GridDev gridView(const GridBufs& g, const double* bbmin, const double* bbmax) {
     d.nx = cellsAlong(bbmax[0], g.origin[0], g.invCell);
     d.ny = cellsAlong(bbmax[1], g.origin[1], g.invCell);
     d.nz = cellsAlong(bbmax[2], g.origin[2], g.invCell);
+    d.owner = g.hasOwner ? g.owner.as<unsigned long long>() : nullptr;
     return d;
 }
 
 cudaError_t gridBuild(GridBufs& g, const GridDev& view, const float4* rec, const uint64_t* dCount, int64_t capacity,
-                      cudaStream_t st) {
+                      cudaStream_t st, bool withOwner) {
     cudaError_t e;
     if ((e = g.keys.ensure((size_t)std::max<int64_t>(capacity, 1) * 4)) != cudaSuccess) return e;
     if ((e = g.sorted.ensure((size_t)std::max<int64_t>(capacity, 1) * 32)) != cudaSuccess) return e;
@@ -209,7 +218,16 @@ cudaError_t gridBuild(GridBufs& g, const GridDev& view, const float4* rec, const
     if ((e = cudaMemsetAsync(hist, 0, ((size_t)g.size + 1) * 4, st)) != cudaSuccess) return e;
     GridDev v = view;
     const int bs = 256;
-    kKeys<<<gridFor(capacity, bs), bs, 0, st>>>(rec, dCount, capacity, v, g.keys.as<uint32_t>(), hist);
+    g.hasOwner = withOwner;
+    if (withOwner) {
+        if ((e = g.owner.ensure((size_t)g.size * 8)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(g.owner.p, 0xFF, (size_t)g.size * 8, st)) != cudaSuccess) return e;
+        kKeys<true><<<gridFor(capacity, bs), bs, 0, st>>>(rec, dCount, capacity, v, g.keys.as<uint32_t>(), hist,
+                                                          g.owner.as<unsigned long long>());
+    } else {
+        kKeys<false><<<gridFor(capacity, bs), bs, 0, st>>>(rec, dCount, capacity, v, g.keys.as<uint32_t>(), hist,
+                                                           nullptr);
+    }
     cudaError_t se = exclusiveScan(hist, (int64_t)g.size, g.cursor.as<uint32_t>(), g.scanTmp.as<uint32_t>(), st);
     if (se != cudaSuccess) return se;
     kScatter<<<gridFor(capacity, bs), bs, 0, st>>>(rec, dCount, capacity, g.keys.as<uint32_t>(), g.cursor.as<uint32_t>(),

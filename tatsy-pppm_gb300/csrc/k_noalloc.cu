@@ -38,6 +38,7 @@ struct NaParams {
     int bbmax[3];
     GridDev grid;
 };
+static_assert(sizeof(NaParams) <= NaLayout::sorted, "the parameters must fit their scratch region");
 
 // float <-> int mapping that preserves order, for atomicMin/atomicMax
 __device__ __forceinline__ int orderedInt(float f) {
@@ -104,6 +105,7 @@ __global__ void kNaParams(NaParams* p, int64_t n, int k, float4* sorted, uint32_
     g.nx = max(1, (int)ceil((mx[0] - g.ox) * g.invCell) + 1);
     g.ny = max(1, (int)ceil((mx[1] - g.oy) * g.invCell) + 1);
     g.nz = max(1, (int)ceil((mx[2] - g.oz) * g.invCell) + 1);
+    g.owner = nullptr;  // no bucket owners recorded: the search tests every photon's cell
 }
 
 __global__ void kNaKeys(const float* __restrict__ pos, int64_t n, const NaParams* p, uint32_t* __restrict__ keys,

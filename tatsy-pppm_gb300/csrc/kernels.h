@@ -23,7 +23,7 @@ GridDev gridView(const GridBufs& g, const double* bbmin, const double* bbmax);
 // Origin, cell edge and cells per axis of the grid gridLayout would give.
 GridDev gridGeometry(const double* bbmin, const double* bbmax, double cell);
 cudaError_t gridBuild(GridBufs& g, const GridDev& view, const float4* rec, const uint64_t* dCount, int64_t capacity,
-                      cudaStream_t st);
+                      cudaStream_t st, bool withOwner = false);
 
 // Canonical gather with shared-memory staging of cell neighbourhoods
 // (queries counting-sorted by cell first). work: optional 2 counters.

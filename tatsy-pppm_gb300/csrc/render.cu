@@ -219,7 +219,8 @@ static int knnRun(pppm_ctx* c, const float* photonPos, int64_t n, const float* q
     PPPM_CUDA(c, launchPackPositions((const float*)dp, n, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), c->stream));
     PPPM_CUDA(c, gridLayout(c->stageGrid, mn, mx, knnCell(mn, mx, n, k), n));
     GridDev gv = gridView(c->stageGrid, mn, mx);
-    PPPM_CUDA(c, gridBuild(c->stageGrid, gv, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), n, c->stream));
+    PPPM_CUDA(c, gridBuild(c->stageGrid, gv, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), n, c->stream,
+                           true));
     gv = gridView(c->stageGrid, mn, mx);
     PPPM_CUDA(c, launchKnn(gv, (const float*)dq, m, k, eps, (int32_t*)didx, (int32_t*)dcnt, cap, c->stream));
     if ((r = finishOut(c, idx, didx, (size_t)m * cap * 4))) return r;
@@ -301,7 +302,8 @@ int pppm_gather(pppm_ctx* c, int32_t mode, const float* photons, int64_t n, int6
     const double cell = mode == PPPM_MODE_CANONICAL ? radius : knnCell(mn, mx, n, k);
     PPPM_CUDA(c, gridLayout(c->stageGrid, mn, mx, cell, n));
     GridDev gv = gridView(c->stageGrid, mn, mx);
-    PPPM_CUDA(c, gridBuild(c->stageGrid, gv, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), n, c->stream));
+    PPPM_CUDA(c, gridBuild(c->stageGrid, gv, c->stageRec.as<float4>(), c->stageCount.as<uint64_t>(), n, c->stream,
+                           mode != PPPM_MODE_CANONICAL));
     gv = gridView(c->stageGrid, mn, mx);
     QueryView qv{c->stageQ.as<float4>(), nullptr, m};
     if (mode == PPPM_MODE_CANONICAL) {
@@ -611,8 +613,10 @@ int pppm_render_pass(pppm_ctx* c, int32_t t, pppm_pass_stats* stats) {
     }
     PPPM_CUDA(c, gridLayout(rs.grid, c->bbmin, c->bbmax, cell, stored));
     GridDev gv = gridView(rs.grid, c->bbmin, c->bbmax);
+    // the k-nearest search (compat) skips buckets of other cells and the
+    // per-photon cell test in buckets of one cell
     PPPM_CUDA(c, gridBuild(rs.grid, gv, rs.photons.as<float4>(), reinterpret_cast<const uint64_t*>(&ctr->deposits),
-                           rs.depositCap, c->stream));
+                           rs.depositCap, c->stream, compat));
     gv = gridView(rs.grid, c->bbmin, c->bbmax);
     launches += 5;
     PPPM_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
