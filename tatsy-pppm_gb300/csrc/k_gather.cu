@@ -51,7 +51,9 @@ struct KnnList {
     float d2[kMaxKnn];
     int idx[kMaxKnn];
     int cnt;
+    float kd = 3.4e38f;  // d2[k - 1] once the list is full: most candidates stop at this register
     __device__ __forceinline__ bool insert(float d, int id, int k, const float4* __restrict__ rec) {
+        if (d > kd) return false;  // farther than the k-th: cannot enter
         int pos;
         if (cnt < k) {
             pos = cnt++;
@@ -67,6 +69,7 @@ struct KnnList {
         }
         d2[pos] = d;
         idx[pos] = id;
+        if (cnt == k) kd = d2[k - 1];
         return true;
     }
 };
@@ -112,6 +115,7 @@ __device__ __forceinline__ float sideGap(float q, float o, float cell, int c0, i
 __device__ void knnSearch(const GridDev& g, float qx, float qy, float qz, int k, float eps, int64_t phantoms,
                           KnnList& L) {
     L.cnt = 0;
+    L.kd = 3.4e38f;
     const float eps2 = eps * eps;
     const int c0x = cellCoord(qx, g.ox, g.invCell, g.nx);
     const int c0y = cellCoord(qy, g.oy, g.invCell, g.ny);
