@@ -8,6 +8,8 @@
 // photons, and each query of that cell tests every staged photon. The
 // photons of a neighbourhood are read from L2/HBM once per warp instead of
 // once per query; hundreds of eye hit points typically share a cell.
+#include <type_traits>
+
 #include "kernels.h"
 
 namespace pppm {
@@ -24,8 +26,24 @@ constexpr int kWarps = kTileQ / 32;
 #define PPPM_GATHER_MINBLOCKS 7
 #endif
 
+// distance tests in coordinates relative to the centre of the warp's cell:
+// the tile holds p - c and |p - c|^2, so that a test is three FMAs and a
+// compare, |p'|^2 - 2 p'.q' < r^2 - |q'|^2 (1: default; 0: the difference
+// vector's squared length, seven instructions). With |p'|, |q'| a few radii
+// at most, the rounding of d^2 - r^2 stays below 2e-6 r^2 for cells up to
+// 2r (4e-6 r^2 at 4r), inside the 1e-5 r^2 band in which the float64
+// restatement treats a photon as on the sphere. The centre depends only on
+// the query's own cell, so a query's sum does not depend on which queries
+// share its warp.
+#ifndef PPPM_GATHER_LOCAL
+#define PPPM_GATHER_LOCAL 1
+#endif
+constexpr bool kLocal = PPPM_GATHER_LOCAL != 0;
+// the third tile array: normal.z (float), or normal.yz (float2) in local form
+using TileC = std::conditional_t<kLocal, float2, float>;
+
 // dynamic shared memory of a gather block with tiles of `stage` photons
-size_t gatherSmem(int stage) { return (size_t)kWarps * stage * (2 * sizeof(float4) + sizeof(float)); }
+size_t gatherSmem(int stage) { return (size_t)kWarps * stage * (2 * sizeof(float4) + sizeof(TileC)); }
 
 unsigned blocksFor(int64_t n, int bs, int cap = 152 * 32) {
     const int64_t want = (n + bs - 1) / bs;
@@ -92,7 +110,8 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
                                                        const uint32_t* __restrict__ qcount, int64_t qcap, float r,
                                                        int stageRt, float* __restrict__ out,
                                                        unsigned long long* __restrict__ work) {
-    // per warp: pos.xyz|normal.x, flux.xyz|normal.y, normal.z of `stage` photons
+    // per warp: pos.xyz|normal.x, flux.xyz|normal.y, normal.z of `stage`
+    // photons; local form: (p - c).xyz|(|p - c|^2), flux.xyz|normal.x, normal.yz
     const int stage = kStage > 0 ? kStage : stageRt;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t n = qcount ? min((int64_t)*qcount, qcap) : qcap;
@@ -100,11 +119,11 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
     if (base >= n) return;  // uniform for the warp; the kernel has no block barrier
     float4* wA;
     float4* wB;
-    float* wC;
+    TileC* wC;
     if constexpr (kStage > 0) {
         __shared__ float4 sA[kWarps][kStage > 0 ? kStage : 1];
         __shared__ float4 sB[kWarps][kStage > 0 ? kStage : 1];
-        __shared__ float sC[kWarps][kStage > 0 ? kStage : 1];
+        __shared__ TileC sC[kWarps][kStage > 0 ? kStage : 1];
         wA = sA[warp];
         wB = sB[warp];
         wC = sC[warp];
@@ -112,7 +131,7 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
         extern __shared__ float4 tileDynamic[];
         wA = tileDynamic + (size_t)warp * stage;
         wB = tileDynamic + (size_t)(kWarps + warp) * stage;
-        wC = reinterpret_cast<float*>(tileDynamic + (size_t)2 * kWarps * stage) + (size_t)warp * stage;
+        wC = reinterpret_cast<TileC*>(tileDynamic + (size_t)2 * kWarps * stage) + (size_t)warp * stage;
     }
     // position and normal of each query stay in registers; its weight and
     // pixel are read again for the final write
@@ -178,6 +197,22 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
             b0 = g.start[key];
             nc = g.start[key + 1] - b0;
         }
+        // the active queries' positions; the local form reads them again from
+        // the sorted queries, so that none stays live across the tests (kept
+        // in registers, they spilled)
+        float3 qp[kQ];
+#pragma unroll
+        for (int j = 0; j < kQ; j++) {
+            if constexpr (kLocal) {
+                qp[j] = make_float3(0.f, 0.f, 0.f);
+                if (active[j]) {
+                    const float4 a = sq[3 * (base + (int64_t)kQ * lane + j)];
+                    qp[j] = make_float3(a.x, a.y, a.z);
+                }
+            } else {
+                qp[j] = q0[j];
+            }
+        }
         // bounding box of the warp's active queries; a photon farther than r
         // from the box is farther than r from each of them (kept with a
         // margin over the rounding of the distance tests)
@@ -186,12 +221,12 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
 #pragma unroll
         for (int j = 0; j < kQ; j++)
             if (active[j]) {
-                blx = fminf(blx, q0[j].x);
-                bly = fminf(bly, q0[j].y);
-                blz = fminf(blz, q0[j].z);
-                bhx = fmaxf(bhx, q0[j].x);
-                bhy = fmaxf(bhy, q0[j].y);
-                bhz = fmaxf(bhz, q0[j].z);
+                blx = fminf(blx, qp[j].x);
+                bly = fminf(bly, qp[j].y);
+                blz = fminf(blz, qp[j].z);
+                bhx = fmaxf(bhx, qp[j].x);
+                bhy = fmaxf(bhy, qp[j].y);
+                bhz = fmaxf(bhz, qp[j].z);
             }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -203,6 +238,21 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
             bhz = fmaxf(bhz, __shfl_xor_sync(0xffffffffu, bhz, o));
         }
         const float rc2 = r2 * 1.0001f;
+        // local form: the leader's cell centre, each active query's -2 q' and
+        // its threshold r^2 - |q'|^2 (-inf for the others: no photon passes)
+        const float ccx = g.ox + ((float)lx + 0.5f) * g.cell, ccy = g.oy + ((float)ly + 0.5f) * g.cell,
+                    ccz = g.oz + ((float)lz + 0.5f) * g.cell;
+        float mx[kQ], my[kQ], mz[kQ], thr[kQ];
+        if constexpr (kLocal) {
+#pragma unroll
+            for (int j = 0; j < kQ; j++) {
+                const float x = qp[j].x - ccx, y = qp[j].y - ccy, z = qp[j].z - ccz;
+                mx[j] = -2.0f * x;
+                my[j] = -2.0f * y;
+                mz[j] = -2.0f * z;
+                thr[j] = active[j] ? r2 - (x * x + y * y + z * z) : -inf;
+            }
+        }
         // tests every query of the leader's cell against the tile's photons
         auto testTile = [&](uint32_t fill) {
             __syncwarp();
@@ -213,6 +263,31 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
                 }
 #pragma unroll 2
                 for (uint32_t t = 0; t < fill; t++) {
+                    if constexpr (kLocal) {
+                        const float4 a = wA[t];
+                        bool in[kQ];
+                        bool anyIn = false;
+#pragma unroll
+                        for (int j = 0; j < kQ; j++) {
+                            in[j] = fmaf(mz[j], a.z, fmaf(my[j], a.y, fmaf(mx[j], a.x, a.w))) < thr[j];
+                            anyIn |= in[j];
+                        }
+                        if (anyIn) {
+                            const float4 b = wB[t];
+                            const float2 c = *reinterpret_cast<const float2*>(&wC[t]);
+#pragma unroll
+                            for (int j = 0; j < kQ; j++) {
+                                if (!in[j]) continue;
+                                if (kCount) inside++;
+                                if (b.w * q1[j].x + c.x * q1[j].y + c.y * q1[j].z > 0.0f) {
+                                    sx[j] += b.x;
+                                    sy[j] += b.y;
+                                    sz[j] += b.z;
+                                }
+                            }
+                        }
+                        continue;
+                    }
                     const float4 a = wA[t];
                     bool in[kQ];
                     bool anyIn = false;
@@ -224,7 +299,7 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
                     }
                     if (anyIn) {
                         const float4 b = wB[t];
-                        const float c = wC[t];
+                        const float c = *reinterpret_cast<const float*>(&wC[t]);
 #pragma unroll
                         for (int j = 0; j < kQ; j++) {
                             if (!in[j]) continue;
@@ -269,9 +344,16 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
                     const float4 f = __ldg(&g.rec[2 * ((int64_t)sb + t) + 1]);
                     const f3 nn = unpackNormal(__float_as_uint(a.w));
                     const uint32_t k = fill + __popc(km & lt);
-                    wA[k] = make_float4(a.x, a.y, a.z, nn.x);
-                    wB[k] = make_float4(f.x, f.y, f.z, nn.y);
-                    wC[k] = nn.z;
+                    if constexpr (kLocal) {
+                        const float x = a.x - ccx, y = a.y - ccy, z = a.z - ccz;
+                        wA[k] = make_float4(x, y, z, x * x + y * y + z * z);
+                        wB[k] = make_float4(f.x, f.y, f.z, nn.x);
+                        *reinterpret_cast<float2*>(&wC[k]) = make_float2(nn.y, nn.z);
+                    } else {
+                        wA[k] = make_float4(a.x, a.y, a.z, nn.x);
+                        wB[k] = make_float4(f.x, f.y, f.z, nn.y);
+                        *reinterpret_cast<float*>(&wC[k]) = nn.z;
+                    }
                 }
                 fill += __popc(km);
             }
