@@ -25,6 +25,11 @@ constexpr int kWarps = kTileQ / 32;
 #ifndef PPPM_GATHER_MINBLOCKS
 #define PPPM_GATHER_MINBLOCKS 7
 #endif
+// photons per iteration of the tile loop
+#ifndef PPPM_GATHER_UNROLL
+#define PPPM_GATHER_UNROLL 4
+#endif
+constexpr int kUnroll = PPPM_GATHER_UNROLL;
 
 // distance tests in coordinates relative to the centre of the warp's cell:
 // the tile holds p - c and |p - c|^2, so that a test is three FMAs and a
@@ -261,7 +266,7 @@ __global__ void __launch_bounds__(kTileQ, PPPM_GATHER_MINBLOCKS) kGatherTiled(Gr
 #pragma unroll
                     for (int j = 0; j < kQ; j++) pairs += active[j] ? fill : 0;
                 }
-#pragma unroll 2
+#pragma unroll kUnroll
                 for (uint32_t t = 0; t < fill; t++) {
                     if constexpr (kLocal) {
                         const float4 a = wA[t];
