@@ -457,7 +457,8 @@ int pppm_render_skip(pppm_ctx* ctx, int32_t count);
 
 /* Launch-shape knobs of an active render, applied from the next pass on
  * (values <= 0 keep the current one): hash-grid cell factor (>= 1), photon
- * bounce and eye kernel blocks per SM (grid caps; default 64, at most 64).
+ * bounce and eye kernel blocks per SM (grid caps; bounce: default 64, at
+ * most 64; eye: default 128, at most 128).
  * None changes results beyond the order
  * of floating-point accumulation; the batch autotuner sets them. No
  * counterpart in the reference. */
@@ -470,7 +471,7 @@ int pppm_render_tune(pppm_ctx* ctx, float cell_factor, int32_t bounce_blocks_per
 typedef struct pppm_tune {
     float cell_factor;             /* hash-grid cell edge / radius, >= 1 */
     int32_t bounce_blocks_per_sm;  /* photon kernel grid cap, 1..64 */
-    int32_t eye_blocks_per_sm;     /* eye kernel grid cap, 1..64 */
+    int32_t eye_blocks_per_sm;     /* eye kernel grid cap, 1..128 */
     int32_t refill;                /* persistent photon kernel: lanes of a warp with their closest hit
                                       before the warp shades them and takes new paths, 1..32 */
     int32_t exact_batch;           /* lanes waiting for double-precision triangle tests before a
@@ -484,7 +485,7 @@ typedef struct pppm_tune {
 /* Sets the knobs of an active render from the next pass on; a field < 0
  * (cell_factor <= 0) keeps its current value, a value out of range is
  * PPPM_E_ARG and changes nothing. render_begin restores the defaults
- * (1, 64, 64, 24, 12, 128, and 3 query sub-cell bits where the query sort
+ * (1, 64, 128, 24, 12, 128, and 3 query sub-cell bits where the query sort
  * keeps 4096 cell buckets with them, 1080p and up; fewer for smaller
  * images, at least 1). No counterpart in the reference. */
 int pppm_render_tune_ex(pppm_ctx* ctx, const pppm_tune* tune);

@@ -74,8 +74,8 @@ int jobFail(pppm_batch::Job& j, int code) {
 // min(6, (P - 2) / kRounds) of them.
 // query_sub_bits -1: the render's own choice (set by the image size)
 const pppm_tune kCandidates[] = {
-    {1.0f, 64, 64, 24, 12, 128, -1}, {1.25f, 64, 64, 24, 12, 256, 2}, {1.0f, 32, 32, 16, 8, 128, 3},
-    {1.0f, 64, 64, 32, 16, 64, 1},   {1.5f, 64, 64, 24, 12, 256, 2},  {1.0f, 5, 32, 24, 12, 128, -1},
+    {1.0f, 64, 128, 24, 12, 128, -1}, {1.25f, 64, 64, 24, 12, 256, 2}, {1.0f, 32, 32, 16, 8, 128, 3},
+    {1.0f, 64, 128, 32, 16, 64, 1},   {1.5f, 64, 128, 24, 12, 256, 2}, {1.0f, 5, 32, 24, 12, 128, -1},
 };
 constexpr int kNumCandidates = (int)(sizeof(kCandidates) / sizeof(kCandidates[0]));
 constexpr int kRounds = 3;  // timed passes per candidate

@@ -318,6 +318,14 @@ int pppm_gather(pppm_ctx* c, int32_t mode, const float* photons, int64_t n, int6
     return PPPM_OK;
 }
 
+// default grid cap of the eye kernel, blocks of 128 per SM: 128 gives each
+// block one 16x8 pixel tile at 1080p, so that eye blocks leave the SMs
+// sooner to the photon kernel beside them (64: 0.9 % slower, 16: 4 %)
+#ifndef PPPM_EYE_PER_SM
+#define PPPM_EYE_PER_SM 128
+#endif
+constexpr int kEyePerSmMax = 128;
+
 int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* par) {
     if (!c || !cam || !par) return fail(c, PPPM_E_ARG, "render_begin: null argument");
     if (!c->hasScene) return fail(c, PPPM_E_STATE, "render_begin: no scene");
@@ -349,10 +357,9 @@ int pppm_render_begin(pppm_ctx* c, const pppm_camera* cam, const pppm_params* pa
     rs.par = *par;
     if (!(rs.par.cell_factor >= 1.0f)) rs.par.cell_factor = 1.0f;
     // grid caps of the trace kernels (blocks of 128 per SM): more blocks
-    // than can be resident balance the long paths better; 64 measured
-    // fastest on the 1080p workload (16: +4% pass time)
+    // than can be resident balance the long paths better
     rs.bouncePerSm = 64;
-    rs.eyePerSm = 64;
+    rs.eyePerSm = PPPM_EYE_PER_SM;
     rs.refill = kRefill;
     rs.exactBatch = kExactBatch;
     rs.qsort.stage = PPPM_GATHER_WSTAGE;  // (querySortLayout below sets the sub-cell bits)
@@ -763,7 +770,7 @@ int pppm_render_tune(pppm_ctx* c, float cell_factor, int32_t bounce_blocks_per_s
         c->rs.par.cell_factor = cell_factor;
     }
     if (bounce_blocks_per_sm > 0) c->rs.bouncePerSm = std::min(bounce_blocks_per_sm, 64);
-    if (eye_blocks_per_sm > 0) c->rs.eyePerSm = std::min(eye_blocks_per_sm, 64);
+    if (eye_blocks_per_sm > 0) c->rs.eyePerSm = std::min(eye_blocks_per_sm, kEyePerSmMax);
     return PPPM_OK;
 }
 
@@ -772,7 +779,7 @@ int pppm_render_tune_ex(pppm_ctx* c, const pppm_tune* t) {
     if (!c->rs.active) return fail(c, PPPM_E_STATE, "render_tune_ex: no render");
     auto in = [](int32_t v, int lo, int hi) { return v < 0 || (v >= lo && v <= hi); };
     if ((t->cell_factor > 0.0f && !(t->cell_factor >= 1.0f)) || !in(t->bounce_blocks_per_sm, 1, 64) ||
-        !in(t->eye_blocks_per_sm, 1, 64) || !in(t->refill, 1, 32) || !in(t->exact_batch, 1, 32) ||
+        !in(t->eye_blocks_per_sm, 1, kEyePerSmMax) || !in(t->refill, 1, 32) || !in(t->exact_batch, 1, 32) ||
         !in(t->gather_stage, 32, kGatherStageMax) || (t->gather_stage > 0 && t->gather_stage % 32 != 0) ||
         !in(t->query_sub_bits, 0, 3))
         return fail(c, PPPM_E_ARG, "render_tune_ex: a knob out of range");

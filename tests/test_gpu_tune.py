@@ -12,7 +12,7 @@ import scenes as S
 
 pytestmark = pytest.mark.gpu
 
-DEFAULTS = dict(cell_factor=1.0, bounce_blocks_per_sm=64, eye_blocks_per_sm=64, refill=24, exact_batch=12,
+DEFAULTS = dict(cell_factor=1.0, bounce_blocks_per_sm=64, eye_blocks_per_sm=128, refill=24, exact_batch=12,
                 gather_stage=128, query_sub_bits=1)
 
 
@@ -74,7 +74,8 @@ def test_knob_ranges(ctx):
     assert e.value.code in (P.E_STATE,)
     ctx.render_begin(sc.camera, par)
     for bad in (dict(refill=33), dict(exact_batch=0), dict(gather_stage=48), dict(gather_stage=288),
-                dict(query_sub_bits=4), dict(cell_factor=0.5), dict(bounce_blocks_per_sm=65)):
+                dict(query_sub_bits=4), dict(cell_factor=0.5), dict(bounce_blocks_per_sm=65),
+                dict(eye_blocks_per_sm=129)):
         with pytest.raises(P.PppmError) as e:
             ctx.render_tune(**bad)
         assert e.value.code == P.E_ARG, bad
