@@ -192,13 +192,19 @@ __device__ __forceinline__ uint32_t octCell(const f3& v, int bits) {
     return r;
 }
 
+// Emission kinds, one kernel each so that the common one carries no other
+// kind's registers: the environment with XorShift tapes, the same with the
+// learned mixture (one-sample MIS), emissive triangles, permuted Halton.
+enum EmitKind { kEmitEnv = 0, kEmitMis = 1, kEmitLights = 2, kEmitQmc = 3 };
+
+template <int kKind>
 __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restrict__ photonStates,
                             PathState* __restrict__ queue, PassCounters* ctr, uint32_t* __restrict__ sortKeys,
                             uint32_t* __restrict__ sortHist) {
     const GuideView& gv = tp.guide;
     VmfMix mix;
-    bool learned = tp.guided && gv.emitRaw != nullptr;
-    if (learned) {
+    bool learned = false;
+    if constexpr (kKind == kEmitMis) {
         vmfMixFromRaw(gv.emitRaw, &mix, gv.maxLogKappa);
         learned = vmfMixFinite(mix);  // a non-finite network output: the reference's sampling alone
     }
@@ -208,8 +214,8 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
         bool ok;
         PathState p;
         double org[3];
-        bool fromLight = false;
-        if (env.numLights > 0) {
+        const bool fromLight = kKind == kEmitLights;
+        if constexpr (kKind == kEmitLights) {
             // emissive triangles: the scene's light instead of the environment
             Tape tape;
             tape.pos = 0;
@@ -221,9 +227,8 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
                 seedCanonical(tp.seed, tp.pass, (uint64_t)g, tape.x);
             }
             ok = emitFromLights(env, tape, org, &dir, &flux, &d);
-            fromLight = true;
             storeTape(tape, p);
-        } else if (tp.qmc) {
+        } else if constexpr (kKind == kEmitQmc) {
             // photon round i of thread s draws sample i of the pass from
             // sampler s (tracePhotons, ppm_probabilistic.cc:131-135)
             const int s = (int)(g / tp.taskPerThread);
@@ -241,8 +246,11 @@ __global__ void kPhotonEmit(TraceParams tp, EnvDev env, const uint32_t* __restri
             } else {
                 seedCanonical(tp.seed, tp.pass, (uint64_t)g, tape.x);
             }
-            ok = learned ? emitPhotonMis(env, tape, mix, gv.emitFloor, gv.emitK, &d, &dir, &flux)
-                         : emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux, tp.sssPass != 0);
+            if constexpr (kKind == kEmitMis)
+                ok = learned ? emitPhotonMis(env, tape, mix, gv.emitFloor, gv.emitK, &d, &dir, &flux)
+                             : emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux, tp.sssPass != 0);
+            else
+                ok = emitPhoton(env, tape, tp.numPhotons, &d, &dir, &flux, tp.sssPass != 0);
             storeTape(tape, p);
         }
         if (!ok) atomicAdd(&ctr->undefinedEmit, 1ull);
@@ -834,8 +842,19 @@ cudaError_t launchTapeStates(const TraceParams& tp, const uint32_t* streamStates
 
 cudaError_t launchPhotonEmit(const TraceParams& tp, const EnvDev& env, const uint32_t* photonStates, PathState* queue,
                              PassCounters* ctr, cudaStream_t st, const PhotonSort* sort) {
-    kPhotonEmit<<<blocksFor(tp.numPaths, 256), 256, 0, st>>>(tp, env, photonStates, queue, ctr,
-                                                             sort ? sort->keys : nullptr, sort ? sort->hist : nullptr);
+    // the kernel's own order of precedence: lights, Halton, then XorShift
+    // tapes with the learned mixture when the network has an output
+    const unsigned blocks = blocksFor(tp.numPaths, 256);
+    uint32_t* keys = sort ? sort->keys : nullptr;
+    uint32_t* hist = sort ? sort->hist : nullptr;
+    if (env.numLights > 0)
+        kPhotonEmit<kEmitLights><<<blocks, 256, 0, st>>>(tp, env, photonStates, queue, ctr, keys, hist);
+    else if (tp.qmc)
+        kPhotonEmit<kEmitQmc><<<blocks, 256, 0, st>>>(tp, env, photonStates, queue, ctr, keys, hist);
+    else if (tp.guided && tp.guide.emitRaw != nullptr)
+        kPhotonEmit<kEmitMis><<<blocks, 256, 0, st>>>(tp, env, photonStates, queue, ctr, keys, hist);
+    else
+        kPhotonEmit<kEmitEnv><<<blocks, 256, 0, st>>>(tp, env, photonStates, queue, ctr, keys, hist);
     return cudaGetLastError();
 }
 
