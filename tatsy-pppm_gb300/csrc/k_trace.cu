@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kPhotonBounce(Trace
 constexpr bool kEyeTiles = PPPM_EYE_TILES != 0;
 
 template <bool kSss, bool kPT, class TapeT = Tape>
-__global__ void __launch_bounds__(128, PPPM_TRACE_MINBLOCKS) kEyeTrace(TraceParams tp, SceneView sc, EnvDev env, CameraDev cam,
+__global__ void __launch_bounds__(128, PPPM_EYE_MINBLOCKS) kEyeTrace(TraceParams tp, SceneView sc, EnvDev env, CameraDev cam,
                                                  OctView oct, const uint32_t* __restrict__ pixelStates,
                                                  float* __restrict__ accum, float4* __restrict__ queries,
                                                  float4* __restrict__ sssQ, int64_t sssCap, PassCounters* ctr) {

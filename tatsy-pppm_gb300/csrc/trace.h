@@ -9,6 +9,11 @@
 #ifndef PPPM_TRACE_MINBLOCKS
 #define PPPM_TRACE_MINBLOCKS 7
 #endif
+// blocks per SM the eye kernel's registers are sized for (it runs beside
+// the photon kernel in short blocks of one pixel tile)
+#ifndef PPPM_EYE_MINBLOCKS
+#define PPPM_EYE_MINBLOCKS PPPM_TRACE_MINBLOCKS
+#endif
 
 namespace pppm {
 
