@@ -272,7 +272,7 @@ def counted_passes(ctx, scene, common, warm, steps):
 
 
 def rooflines(cnt, stats, clocks):
-    """Photon-pass roofline (survey byte model against the measured HBM copy
+    """Photon-pass roofline (the pass's byte model against the measured HBM copy
     bandwidth, plus the DRAM fraction the ncu capture gives) and the gather's
     issue-rate roofline (warp instructions per second against the SMs' issue
     slots)."""
@@ -285,7 +285,7 @@ def rooflines(cnt, stats, clocks):
     photon = {"bound": "latency/divergence", "ceiling": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
               "frac": achieved / peak, "traffic": traffic, "kernel": "kPhotonPersistent (all photon bounces)",
               "peak_kind": peak_kind, "algorithmic_bytes_per_pass": alg,
-              "model": "survey byte model: 48 B per ray + 128 B per BVH node visited + 48 B per triangle tested "
+              "model": "photon-pass byte model: 48 B per ray + 128 B per BVH node visited + 48 B per triangle tested "
                        "(counted live over the timed passes); most of these bytes are L1/L2 hits"}
     if traffic:
         photon["dram_achieved"] = traffic / (ms_bounce / 1e3) / 1e9
