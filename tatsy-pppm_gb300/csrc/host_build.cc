@@ -6,7 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <deque>
+#include <map>
 
 namespace pppm {
 namespace {
@@ -25,37 +25,56 @@ struct TempNode {
     int sep;
 };
 
-// Nodes and leaf slots of a subtree, as the serial construction would lay
-// them out: the subtree's root first, then its children's subtrees in
-// child order (depth-first); leaf slots in the same order.
-struct Part {
-    std::vector<TempNode> nodes;
-    std::vector<float> slots;
-    int maxDepth = 0;
-};
-
-// Subtrees of at least this many triangles, above this depth, are built as
-// OpenMP tasks into parts of their own and appended in child order, which
-// reproduces the serial layout exactly (the sorts of disjoint ranges are
-// independent; each range is sorted by the same std::sort call).
+// The construction splits a range of n > 3 triangles into quarters of
+// fixed sizes (half, then half of each half), so the number of inner nodes
+// of a subtree depends on n alone. With those counts every subtree's place
+// in the serial depth-first layout is known before it is built: a node's
+// children follow it in child order, and a leaf's slots are its triangles'
+// positions in the sorted item array. Subtrees of at least kTaskTris
+// triangles, above kTaskDepth, are built as OpenMP tasks writing straight
+// into their places, which gives the serial layout exactly (the sorts of
+// disjoint ranges are independent; each range is sorted by the same
+// std::sort call).
 constexpr int kTaskTris = 1 << 14;
 constexpr int kTaskDepth = 6;
+
+void quarterSizes(int n, int* sz) {
+    const int mid = n / 2;
+    sz[0] = mid / 2;
+    sz[1] = mid - mid / 2;
+    sz[2] = mid / 2;
+    sz[3] = n - mid - mid / 2;
+}
 
 struct Builder {
     const float* tri9;
     std::vector<Item> items;
+    std::vector<TempNode> nodes;  // serial depth-first layout
+    float* slots = nullptr;       // 12 floats per triangle, in leaf order
+    std::map<int, int> innerNodes;  // inner nodes of a subtree of n triangles (read-only while building)
 
-    int makeLeaf(Part& P, int lo, int hi) const {
-        const int first = (int)(P.slots.size() / 12);
+    int countInner(int n) {
+        if (n <= 3) return 0;
+        const auto it = innerNodes.find(n);
+        if (it != innerNodes.end()) return it->second;
+        int sz[4];
+        quarterSizes(n, sz);
+        int c = 1;
+        for (int k = 0; k < 4; k++) c += countInner(sz[k]);
+        innerNodes[n] = c;
+        return c;
+    }
+
+    int makeLeaf(int lo, int hi) const {
         for (int i = lo; i < hi; i++) {
             const float* t = tri9 + 9 * (int64_t)items[i].id;
             float idbits;
             const int id = items[i].id;
             std::memcpy(&idbits, &id, 4);
             const float rec[12] = {t[0], t[1], t[2], idbits, t[3], t[4], t[5], 0.0f, t[6], t[7], t[8], 0.0f};
-            P.slots.insert(P.slots.end(), rec, rec + 12);
+            std::memcpy(slots + 12 * (int64_t)i, rec, sizeof(rec));
         }
-        return ~((first << 2) | (hi - lo));
+        return ~((lo << 2) | (hi - lo));
     }
 
     void box(int lo, int hi, float* mn, float* mx) const {
@@ -77,18 +96,13 @@ struct Builder {
                   [dim](const Item& x, const Item& y) { return x.g[dim] < y.g[dim]; });
     }
 
-    // a child code of a part appended at (nodeOff, slotOff) of another
-    static int shift(int code, int nodeOff, int slotOff) {
-        if (code >= 0) return code + nodeOff;
-        const int lc = ~code;
-        return ~((((lc >> 2) + slotOff) << 2) | (lc & 3));
-    }
-
-    // constructRec (qbvh_accel.cc:150-203) on items[lo, hi), into P.
-    int rec(Part& P, int lo, int hi, int dim, int depth) {
+    // constructRec (qbvh_accel.cc:150-203) on items[lo, hi): its node at
+    // nodes[at] (when inner); returns the subtree's code and, in *depthOut,
+    // the deepest inner node's depth + 1 (0 for a leaf).
+    int rec(int lo, int hi, int dim, int depth, int at, int* depthOut) {
         const int n = hi - lo;
-        if (n <= 3) return makeLeaf(P, lo, hi);
-        P.maxDepth = std::max(P.maxDepth, depth + 1);
+        *depthOut = 0;
+        if (n <= 3) return makeLeaf(lo, hi);
         sortRange(lo, hi, dim);
         const int mid = n / 2;
         const bool par = n >= kTaskTris && depth < kTaskDepth;
@@ -103,40 +117,41 @@ struct Builder {
             sortRange(lo + mid, hi, (dim + 1) % 3);
         }
         const int cut[5] = {lo, lo + mid / 2, lo + mid, lo + mid + mid / 2, hi};
-        TempNode nd;
-        for (int c = 0; c < 4; c++) {
-            float mn[3], mx[3];
-            box(cut[c], cut[c + 1], mn, mx);
-            for (int d = 0; d < 3; d++) { nd.bmin[d][c] = mn[d]; nd.bmax[d][c] = mx[d]; }
-        }
-        nd.sep = dim | (((dim + 1) % 3) << 2) | (((dim + 1) % 3) << 4);
-        const int self = (int)P.nodes.size();
-        P.nodes.push_back(nd);
-        if (!par) {
+        float mn[4][3], mx[4][3];
+        if (par) {
             for (int c = 0; c < 4; c++) {
-                const int code = rec(P, cut[c], cut[c + 1], (dim + 2) % 3, depth + 1);
-                P.nodes[self].child[c] = code;
-            }
-            return self;
-        }
-        Part sub[4];
-        int code[4];
-        for (int c = 0; c < 4; c++) {
 #pragma omp task default(shared) firstprivate(c)
-            code[c] = rec(sub[c], cut[c], cut[c + 1], (dim + 2) % 3, depth + 1);
-        }
-#pragma omp taskwait
-        for (int c = 0; c < 4; c++) {
-            const int nodeOff = (int)P.nodes.size(), slotOff = (int)(P.slots.size() / 12);
-            for (TempNode t : sub[c].nodes) {
-                for (int k = 0; k < 4; k++) t.child[k] = shift(t.child[k], nodeOff, slotOff);
-                P.nodes.push_back(t);
+                box(cut[c], cut[c + 1], mn[c], mx[c]);
             }
-            P.slots.insert(P.slots.end(), sub[c].slots.begin(), sub[c].slots.end());
-            P.nodes[self].child[c] = shift(code[c], nodeOff, slotOff);
-            P.maxDepth = std::max(P.maxDepth, sub[c].maxDepth);
+#pragma omp taskwait
+        } else {
+            for (int c = 0; c < 4; c++) box(cut[c], cut[c + 1], mn[c], mx[c]);
         }
-        return self;
+        TempNode nd;
+        for (int c = 0; c < 4; c++)
+            for (int d = 0; d < 3; d++) { nd.bmin[d][c] = mn[c][d]; nd.bmax[d][c] = mx[c][d]; }
+        nd.sep = dim | (((dim + 1) % 3) << 2) | (((dim + 1) % 3) << 4);
+        int start[4], depths[4];
+        int next = at + 1;
+        for (int c = 0; c < 4; c++) {
+            start[c] = next;
+            next += innerNodes.at(cut[c + 1] - cut[c]) ;
+        }
+        if (par) {
+            for (int c = 0; c < 4; c++) {
+#pragma omp task default(shared) firstprivate(c)
+                nd.child[c] = rec(cut[c], cut[c + 1], (dim + 2) % 3, depth + 1, start[c], &depths[c]);
+            }
+#pragma omp taskwait
+        } else {
+            for (int c = 0; c < 4; c++)
+                nd.child[c] = rec(cut[c], cut[c + 1], (dim + 2) % 3, depth + 1, start[c], &depths[c]);
+        }
+        nodes[at] = nd;
+        int md = depth + 1;
+        for (int c = 0; c < 4; c++) md = std::max(md, depths[c]);
+        *depthOut = md;
+        return at;
     }
 };
 
@@ -151,6 +166,7 @@ bool buildQbvh(const float* tri9, int64_t ntri, HostBvh* out, std::string* err) 
     b.tri9 = tri9;
     b.items.resize((size_t)ntri);
     const double third = 1.0 / 3.0;
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < ntri; i++) {
         const float* t = tri9 + 9 * i;
         for (int d = 0; d < 3; d++) {
@@ -159,40 +175,42 @@ bool buildQbvh(const float* tri9, int64_t ntri, HostBvh* out, std::string* err) 
         }
         b.items[i].id = (int)i;
     }
-    Part all;
-    int rootTemp = 0;
+    // inner-node counts of every subtree size the construction meets
+    b.innerNodes[0] = 0;
+    for (int k = 1; k <= 3; k++) b.innerNodes[k] = 0;
+    b.nodes.resize((size_t)b.countInner((int)ntri));
+    out->tris.resize((size_t)ntri * 12);
+    b.slots = out->tris.data();
+    int rootTemp = 0, depth = 0;
 #pragma omp parallel
 #pragma omp single
-    rootTemp = b.rec(all, 0, (int)ntri, 0, 0);
-    if (all.maxDepth > 20) {
+    rootTemp = b.rec(0, (int)ntri, 0, 0, 0, &depth);
+    if (depth > 20) {
         *err = "QBVH deeper than 20 levels";
         return false;
     }
-    out->tris.swap(all.slots);
-    out->depth = all.maxDepth;
+    out->depth = depth;
     out->nodes.clear();
     if (rootTemp < 0) {
         out->rootCode = rootTemp;
         return true;
     }
-    // BFS renumbering: top levels become contiguous from index 0.
-    std::vector<int> newIndex(all.nodes.size(), -1);
-    std::deque<int> q;
-    q.push_back(rootTemp);
-    int next = 0;
+    const std::vector<TempNode>& allNodes = b.nodes;
+    // BFS renumbering: top levels become contiguous from index 0 (the order
+    // list is its own queue)
+    std::vector<int> newIndex(allNodes.size(), -1);
     std::vector<int> order;
-    order.reserve(all.nodes.size());
-    while (!q.empty()) {
-        const int v = q.front();
-        q.pop_front();
-        newIndex[v] = next++;
-        order.push_back(v);
+    order.reserve(allNodes.size());
+    order.push_back(rootTemp);
+    for (size_t head = 0; head < order.size(); head++) {
+        const int v = order[head];
+        newIndex[v] = (int)head;
         for (int c = 0; c < 4; c++)
-            if (all.nodes[v].child[c] >= 0) q.push_back(all.nodes[v].child[c]);
+            if (allNodes[v].child[c] >= 0) order.push_back(allNodes[v].child[c]);
     }
     out->nodes.resize(order.size());
     for (size_t k = 0; k < order.size(); k++) {
-        const TempNode& t = all.nodes[order[k]];
+        const TempNode& t = allNodes[order[k]];
         HostQNode& h = out->nodes[k];
         std::memcpy(h.bmin, t.bmin, sizeof(h.bmin));
         std::memcpy(h.bmax, t.bmax, sizeof(h.bmax));
