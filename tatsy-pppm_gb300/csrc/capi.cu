@@ -1,6 +1,7 @@
 // C-ABI entry points: lifetime, staging, scene, env map and stage queries.
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <new>
 
 #include "context.h"
@@ -212,19 +213,11 @@ int pppm_scene_set(pppm_ctx* c, const float* tri, int64_t ntri, const int32_t* m
         // per slot the exact test's double vertex and edges, with the
         // device's operations: p0 = (double)a, e1 = (double)b - p0, e2 = (double)c - p0
         const size_t slots = bvh.tris.size() / 12;
-        std::vector<double> te(slots * 10, 0.0);
-        for (size_t k = 0; k < slots; k++) {
-            const float* t = &bvh.tris[12 * k];
-            for (int d = 0; d < 3; d++) {
-                const double p0 = (double)t[d];
-                te[10 * k + d] = p0;
-                te[10 * k + 3 + d] = (double)t[4 + d] - p0;
-                te[10 * k + 6 + d] = (double)t[8 + d] - p0;
-            }
-        }
-        PPPM_CUDA(c, c->triE.ensure(std::max<size_t>(te.size(), 10) * sizeof(double)));
-        if (!te.empty())
-            PPPM_CUDA(c, cudaMemcpy(c->triE.p, te.data(), te.size() * sizeof(double), cudaMemcpyHostToDevice));
+        std::unique_ptr<double[]> te(new double[std::max<size_t>(slots, 1) * 10]);
+        slotEdges(bvh.tris.data(), (int64_t)slots, te.get());
+        PPPM_CUDA(c, c->triE.ensure(std::max<size_t>(slots, 1) * 10 * sizeof(double)));
+        if (slots)
+            PPPM_CUDA(c, cudaMemcpy(c->triE.p, te.get(), slots * 10 * sizeof(double), cudaMemcpyHostToDevice));
     }
     PPPM_CUDA(c, c->matId.ensure((size_t)ntri * 4));
     if (ntri) PPPM_CUDA(c, cudaMemcpy(c->matId.p, matId, (size_t)ntri * 4, cudaMemcpyHostToDevice));

@@ -221,6 +221,21 @@ bool buildQbvh(const float* tri9, int64_t ntri, HostBvh* out, std::string* err) 
     return true;
 }
 
+void slotEdges(const float* slots, int64_t nslots, double* out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < nslots; k++) {
+        const float* t = slots + 12 * k;
+        double* e = out + 10 * k;
+        for (int d = 0; d < 3; d++) {
+            const double p0 = (double)t[d];
+            e[d] = p0;
+            e[3 + d] = (double)t[4 + d] - p0;
+            e[6 + d] = (double)t[8 + d] - p0;
+        }
+        e[9] = 0.0;
+    }
+}
+
 namespace {
 const double kPi = 4.0 * std::atan(1.0);  // PI (common.h:14)
 

@@ -26,7 +26,12 @@ struct HostBvh {
 // with `err` set when the tree would exceed the device stack bound.
 bool buildQbvh(const float* tri9, int64_t ntri, HostBvh* out, std::string* err);
 
-// Envmap::createImportanceMap (envmap.cc:88-163): pdf and cdf, 4096 each.
+// The exact triangle test's operands of each 12-float slot of
+// HostBvh::tris: the double vertex p0 = (double)a and the edges
+// e1 = (double)b - p0, e2 = (double)c - p0, 10 doubles per slot (the last 0),
+// the operations the device test would otherwise repeat per ray.
+void slotEdges(const float* slots, int64_t nslots, double* out);
+
 // Envmap::createImportanceMap (envmap.cc:88-163): 64x64 cell pdf/cdf over
 // super-sampled directions, cell weight luminance^exponent (2 in the
 // reference: l * l).

@@ -2,8 +2,11 @@
 // the sorts meet ties) and prints a hash of each build's nodes, leaf slots,
 // root and depth, one line per size. tests/test_host_build.py runs it with
 // one and with several OpenMP threads: the parallel construction must lay
-// the tree out exactly as the serial one.
+// the tree out exactly as the serial one. The slots' double edges
+// (slotEdges) are checked against the serial formula bit for bit; a
+// mismatch prints an error line.
 #include <cstdio>
+#include <cstring>
 #include <random>
 #include <string>
 #include <vector>
@@ -37,6 +40,21 @@ int main() {
             std::printf("%d error %s\n", n, err.c_str());
             continue;
         }
+        const size_t slots = b.tris.size() / 12;
+        std::vector<double> edges(slots * 10 + 1, -1.0);
+        pppm::slotEdges(b.tris.data(), (int64_t)slots, edges.data());
+        bool same = edges[slots * 10] == -1.0;  // nothing past the last slot
+        for (size_t k = 0; k < slots && same; k++) {
+            const float* t = &b.tris[12 * k];
+            for (int d = 0; d < 3; d++) {
+                const double p0 = (double)t[d];
+                const double want[3] = {p0, (double)t[4 + d] - p0, (double)t[8 + d] - p0};
+                for (int j = 0; j < 3; j++)
+                    same = same && std::memcmp(&edges[10 * k + 3 * j + d], &want[j], sizeof(double)) == 0;
+            }
+            same = same && edges[10 * k + 9] == 0.0;
+        }
+        if (!same) std::printf("%d error slot edges\n", n);
         unsigned long long h = 1469598103934665603ull;
         h = fnv(b.nodes.data(), b.nodes.size() * sizeof(pppm::HostQNode), h);
         h = fnv(b.tris.data(), b.tris.size() * sizeof(float), h);
